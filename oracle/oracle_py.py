@@ -1,0 +1,212 @@
+"""ctypes bindings for the CPU oracle (oracle/oracle.c) and, where it has been built, for the
+reference's own code compiled against the one-rank shims (oracle/_ref, see build_ref.sh).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline legs, never by the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF = os.path.join(HERE, "_ref")
+LIB = os.path.join(BUILD, "liboracle.so")
+
+_P = C.POINTER(C.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle.c into oracle/_build/liboracle.so (plain gcc, no FMA contraction)."""
+    src = os.path.join(HERE, "oracle.c")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        os.makedirs(BUILD, exist_ok=True)
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-shared", src,
+                               "-o", tmp, "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+class OrcGrid(C.Structure):
+    _fields_ = [("nx", C.c_long), ("ny", C.c_long), ("nz", C.c_long), ("nchem", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("gamma", C.c_double), ("bc", C.c_int * 6)]
+
+
+class OrcChem(C.Structure):
+    _fields_ = [("tables", _P), ("dbin", C.c_double), ("idbin", C.c_double),
+                ("lb", C.c_double), ("nbins", C.c_int), ("tlo", C.c_double),
+                ("thi", C.c_double), ("z", C.c_double)]
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_P)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.orc_feuler.restype = C.c_int
+        _lib.orc_block_newton_solve.restype = C.c_long
+    return _lib
+
+
+def grid(shape, nchem, bc, gamma=1.4, domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+    nx, ny, nz = shape
+    g = OrcGrid()
+    g.nx, g.ny, g.nz, g.nchem = nx, ny, nz, nchem
+    # same expression as EulerData::SetupDecomp (src/euler3D.hpp:412-414)
+    g.dx = (domain[1] - domain[0]) / nx
+    g.dy = (domain[3] - domain[2]) / ny
+    g.dz = (domain[5] - domain[4]) / nz
+    g.gamma = gamma
+    for i in range(6):
+        g.bc[i] = bc[i]
+    return g
+
+
+def feuler(fields, nchem, bc, gamma=1.4, force=None, domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+    """fields: list of 5 arrays shaped (nz,ny,nx) and, if nchem>0, chem shaped (nz,ny,nx,nchem).
+    Returns (status, list of output arrays of the same shapes)."""
+    nz, ny, nx = fields[0].shape
+    g = grid((nx, ny, nz), nchem, bc, gamma, domain)
+    ins = [np.ascontiguousarray(f, dtype=np.float64) for f in fields]
+    outs = [np.zeros_like(f) for f in ins]
+    inp = (_P * 6)(*[_ptr(a) for a in ins], *([None] * (6 - len(ins))))
+    outp = (_P * 6)(*[_ptr(a) for a in outs], *([None] * (6 - len(outs))))
+    fc = None
+    if force is not None:
+        fa = np.ascontiguousarray(force, dtype=np.float64)
+        fc = _ptr(fa)
+    st = lib().orc_feuler(C.byref(g), inp, outp, fc)
+    return st, outs
+
+
+class Chem:
+    """Oracle chemistry state: tables, per-cell scale/aux arrays and the temperature history."""
+
+    def __init__(self, tables: np.ndarray, scale: np.ndarray, z: float = -1.0):
+        self.tables = np.ascontiguousarray(tables, dtype=np.float64)
+        self.c = OrcChem()
+        lib().orc_chem_init(C.byref(self.c), _ptr(self.tables), C.c_double(z))
+        self.scale = np.ascontiguousarray(scale, dtype=np.float64).reshape(-1)
+        self.n = self.scale.size // 10
+        self.inv_scale = 1.0 / self.scale
+        self.mdens = np.zeros(self.n)
+        self.imdens = np.zeros(self.n)
+        self.cie = np.zeros(self.n)
+        self.h2 = np.zeros(self.n)
+        lib().orc_chem_aux(_ptr(self.scale), C.c_long(self.n), _ptr(self.mdens),
+                           _ptr(self.imdens), _ptr(self.cie), _ptr(self.h2))
+        self.Ts = np.full(self.n, 1000.0)
+        self.dTs_ge = np.zeros(self.n)
+
+    def rhs(self, y: np.ndarray) -> np.ndarray:
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
+        yd = np.zeros_like(y)
+        lib().orc_chem_rhs(C.byref(self.c), C.c_long(self.n), _ptr(y), _ptr(self.scale),
+                           _ptr(self.inv_scale), _ptr(self.mdens), _ptr(self.imdens),
+                           _ptr(self.cie), _ptr(self.h2), _ptr(self.Ts), _ptr(self.dTs_ge),
+                           _ptr(yd))
+        return yd
+
+    def jac(self, y: np.ndarray) -> np.ndarray:
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
+        J = np.zeros(self.n * 100)
+        lib().orc_chem_jac(C.byref(self.c), C.c_long(self.n), _ptr(y), _ptr(self.scale),
+                           _ptr(self.inv_scale), _ptr(self.mdens), _ptr(self.cie),
+                           _ptr(self.h2), _ptr(self.Ts), _ptr(self.dTs_ge), _ptr(J))
+        return J.reshape(self.n, 10, 10)  # [cell][col][row]
+
+
+def block_newton_solve(J: np.ndarray, gamma: float, b: np.ndarray):
+    J = np.ascontiguousarray(J, dtype=np.float64).reshape(-1)
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
+    x = np.zeros_like(b)
+    bad = lib().orc_block_newton_solve(C.c_long(b.size // 10), _ptr(J), C.c_double(gamma),
+                                       _ptr(b), _ptr(x))
+    return int(bad), x
+
+
+# ---------------------------------------------------------------- reference build (here only)
+
+def ref_available(nvar: int = 5) -> bool:
+    return os.path.exists(os.path.join(REF, f"libref_nvar{nvar}.so"))
+
+
+_ref_libs: dict[int, C.CDLL] = {}
+
+
+def ref_lib(nvar: int):
+    if nvar not in _ref_libs:
+        path = os.path.join(REF, f"libref_nvar{nvar}.so")
+        L = C.CDLL(path)
+        L.ref_feuler.restype = C.c_int
+        L.ref_chem_setup.restype = C.c_int
+        L.ref_chem_rhs.restype = C.c_int
+        L.ref_chem_jac.restype = C.c_int
+        _ref_libs[nvar] = L
+    return _ref_libs[nvar]
+
+
+def ref_feuler(fields, nchem, bc, gamma=1.4, force=None, domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+    nz, ny, nx = fields[0].shape
+    L = ref_lib(5 + nchem)
+    ins = [np.ascontiguousarray(f, dtype=np.float64) for f in fields]
+    outs = [np.zeros_like(f) for f in ins]
+    inp = (_P * 6)(*[_ptr(a) for a in ins], *([None] * (6 - len(ins))))
+    outp = (_P * 6)(*[_ptr(a) for a in outs], *([None] * (6 - len(outs))))
+    dom = (C.c_double * 6)(*domain)
+    bca = (C.c_int * 6)(*bc)
+    fc = None
+    if force is not None:
+        fa = np.ascontiguousarray(force, dtype=np.float64)
+        fc = _ptr(fa)
+    sec = C.c_double()
+    st = L.ref_feuler(C.c_long(nx), C.c_long(ny), C.c_long(nz), dom, bca, C.c_double(gamma),
+                      C.c_double(0.0), fc, inp, outp, C.byref(sec))
+    return st, outs
+
+
+class RefChem:
+    """The reference's chemistry network (compiled from its own source) with the same API."""
+
+    def __init__(self, table_file: str, scale: np.ndarray, z: float = -1.0, nvar: int = 15):
+        self.L = ref_lib(nvar)
+        self.scale = np.ascontiguousarray(scale, dtype=np.float64).reshape(-1)
+        self.n = self.scale.size // 10
+        st = self.L.ref_chem_setup(table_file.encode(), C.c_long(self.n), _ptr(self.scale),
+                                   C.c_double(z))
+        if st != 0:
+            raise RuntimeError("ref_chem_setup failed")
+
+    def state(self):
+        out = [np.zeros(self.n) for _ in range(5)]
+        self.L.ref_chem_get_state(*[_ptr(a) for a in out])
+        return dict(zip(["Ts", "dTs_ge", "mdens", "cie", "h2"], out))
+
+    def set_Ts(self, Ts):
+        Ts = np.ascontiguousarray(Ts, dtype=np.float64)
+        self.L.ref_chem_set_Ts(_ptr(Ts))
+
+    def rhs(self, y):
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1).copy()
+        yd = np.zeros_like(y)
+        self.L.ref_chem_rhs(C.c_double(0.0), _ptr(y), _ptr(yd), None)
+        return yd
+
+    def jac(self, y):
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1).copy()
+        J = np.zeros(self.n * 100)
+        self.L.ref_chem_jac(C.c_double(0.0), _ptr(y), _ptr(J), None)
+        return J.reshape(self.n, 10, 10)

@@ -1,0 +1,6 @@
+/* Stand-in header: forwards to the one-rank shim (test infrastructure only). */
+#ifndef GBMV_SHIM_NVECTOR_NVECTOR_MANYVECTOR_H
+#define GBMV_SHIM_NVECTOR_NVECTOR_MANYVECTOR_H
+#include <math.h>
+#include "../shim_core.h"
+#endif
