@@ -1,0 +1,354 @@
+"""Benchmark of the fused chemistry-hydrodynamics RHS step at 128^3 x (5 fluid + 10 species).
+
+One step = one pass of the hot path over the whole grid, as an IMEX / multirate stage does it:
+  1. fexpl (slow hydro RHS): Dengo scaling, et <- ge, WENO5 flux divergence of all 15
+     fields with reflecting-x / periodic-y,z ghosts, ge tendency <- et tendency, unscale;
+  2. fimpl (fast chemistry source) x TimeUnits;
+  3. Jimpl (analytic chemistry Jacobian) x TimeUnits, Newton matrix I - gamma*J, batched LU;
+  4. block-diagonal Newton solve of (I - gamma*J) x = fimpl.
+metric: Mcells/s = cells / step time.  `value` is device-resident throughput; `e2e` includes
+per-step host->device copies of the state from pinned memory and device->host copies of the
+outputs (tendency vector and Newton update) through the public Python API.
+
+  python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl gbmv|reference] [--form fp64|mixed]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "sundials-manyvector-demo_gb300")
+sys.path.insert(0, PKG)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mcells/s of fused WENO RHS+chem step at 128^3x15 vs plain FP64 GPU, at 1e-6 rel"
+N = 128
+GAMMA_NEWTON = 1e-4  # h * a_ii of the implicit stage, code time units
+TABLES = os.path.join(ROOT, "tests", "golden", "primordial_tables.h5")
+WORKLOAD = ("chem_hydro 128^3 x (5 fluid + 10 species): planar Sod-like interface along x, "
+            "random primordial mass fractions, reflecting x / periodic y,z; fused step = "
+            "fexpl WENO5 RHS + chem source + chem Jacobian + I-gamma*J LU + block solve")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gbmv", choices=["gbmv", "reference"])
+    p.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--n", type=int, default=N)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------- clocks during the timed region
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                                 else "_work", f"clocks_{os.getpid()}.csv")
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}",
+                                          f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax = float(parts[2].split()[0])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- the GB300 arm
+
+class FusedStep:
+    def __init__(self, torch, n, form):
+        import gbmv
+        import h5tables
+        import workloads as W
+        self.torch, self.gbmv = torch, gbmv
+        self.precision = gbmv.MIXED if form == "mixed" else gbmv.FP64
+        wl = W.chem_hydro(n=n)
+        self.wl = wl
+        self.n = n
+        self.ncell = n ** 3
+        self.units = wl["units"]
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        self.host = [np.ascontiguousarray(f) for f in wl["fields"]]
+        self.w = [dev(f) for f in self.host]
+        self.wdot = [torch.empty_like(f) for f in self.w]
+        self.f = torch.empty(10 * self.ncell, dtype=torch.float64, device="cuda")
+        self.J = torch.empty(100 * self.ncell, dtype=torch.float64, device="cuda")
+        self.x = torch.empty_like(self.f)
+        self.hydro = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"])
+        self.chem = gbmv.Chem(self.ncell, h5tables.load_table_block(TABLES))
+        self.chem.set_scale(dev(wl["scale"].reshape(-1)))
+        self.ls = gbmv.BlockLinearSolver(self.ncell)
+        torch.cuda.synchronize()
+
+    def step(self, t=0.0):
+        g, torch = self.gbmv, self.torch
+        EU, TU = self.units["EnergyUnits"], self.units["TimeUnits"]
+        rc = g.fexpl(self.hydro, self.chem, t, self.w, self.wdot, EU, self.precision)
+        if rc != 0:
+            raise RuntimeError(f"fexpl returned {rc}")
+        y = self.w[5].view(-1)
+        self.chem.calculate_rhs_cvklu(t, y, self.f, TU)
+        self.chem.calculate_jacobian_cvklu(t, y, self.J, TU)
+        g.form_newton_matrix(self.J, GAMMA_NEWTON)
+        if self.ls.setup(self.J) != 0:
+            raise RuntimeError("singular Newton block")
+        self.ls.solve(self.J, self.x, self.f)
+
+    def bytes_in(self):
+        return sum(a.nbytes for a in self.host)
+
+    def bytes_out(self):
+        return sum(t.numel() * 8 for t in self.wdot) + self.x.numel() * 8
+
+
+def time_steps(torch, fn, steps, warmup):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gbmv(args):
+    import torch
+    import gbmv
+    import build_lib
+    if not os.path.exists(build_lib.LIB):
+        build_lib.build()
+    gbmv.load()
+    torch.cuda.set_device(0)
+    fs = FusedStep(torch, args.n, args.form)
+    ncell = fs.ncell
+
+    # device-resident timed region (profiling events on the launching stream)
+    for _ in range(args.warmup):
+        fs.step()
+    torch.cuda.synchronize()
+    gbmv.profile_reset()
+    gbmv.profile_enable(True)
+    launches0 = gbmv.launch_count()
+    with ClockSampler(0) as clk:
+        ms = time_steps(torch, fs.step, args.steps, 0)
+    launches = gbmv.launch_count() - launches0
+    gbmv.profile_enable(False)
+    fam = {f: gbmv.profile_get(f) for f in ("face_flux", "divergence", "chem_rhs", "chem_jac",
+                                            "block_lu_factor", "block_lu_solve", "glue")}
+    value = ncell / (ms * 1e-3) / 1e6
+
+    # roofline of the dominant kernel family (largest share of the step)
+    dom = max(fam, key=lambda k: fam[k][0])
+    hbm_peak, peak_kind = measured_peaks()
+    fp64_peak = gbmv.fma_rate(True) / 1e12
+    nvar = 15
+    nf = (args.n + 1) * args.n * args.n
+    algo_bytes = {  # algorithmic bytes per launch (inputs read once, outputs written once)
+        "face_flux": 8 * nvar * (ncell + nf),
+        "divergence": 8 * nvar * (3 * nf + ncell) + 8 * 5 * ncell,
+        "chem_rhs": 368 * ncell,
+        "chem_jac": (34 * 8 + 800) * ncell,
+        "block_lu_factor": 1600 * ncell + 40 * ncell,
+        "block_lu_solve": (800 + 40 + 160) * ncell,
+        "glue": 0,
+    }
+    dt_ms, nl = fam[dom]
+    avg_ms = dt_ms / max(nl, 1)
+    achieved = algo_bytes.get(dom, 0) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mcells/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.form == "fp64" else "f64/f32 mixed",
+        "data": "synthetic (seeded numpy PCG64; rate tables from the reference's primordial_tables.h5)",
+        "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "nvar": 15, "cells": ncell,
+                   "form": args.form, "newton_gamma": GAMMA_NEWTON,
+                   "l2": "inputs larger than L2 (state 252 MB, Jacobian 1.68 GB)"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
+                     "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
+                     "peak_kind": f"{peak_kind} hbm_gbs", "traffic": None,
+                     "avg_launch_ms": round(avg_ms, 4),
+                     "fp64_peak_tflops_measured": round(fp64_peak, 4)},
+        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in fam.items()},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+
+    if not args.no_e2e:
+        # end to end through the public API: pinned host state -> device, step, results -> host
+        pin_in = [torch.from_numpy(a).pin_memory() for a in fs.host]
+        pin_out = [torch.empty(t.shape, dtype=torch.float64).pin_memory() for t in fs.wdot]
+        pin_x = torch.empty(fs.x.shape, dtype=torch.float64).pin_memory()
+
+        def e2e_step():
+            for d, h in zip(fs.w, pin_in):
+                d.copy_(h, non_blocking=True)
+            fs.step()
+            for h, d in zip(pin_out, fs.wdot):
+                h.copy_(d, non_blocking=True)
+            pin_x.copy_(fs.x, non_blocking=True)
+
+        ms_e2e = time_steps(torch, e2e_step, max(3, args.steps // 2), 1)
+        line["e2e"] = {"value": round(ncell / (ms_e2e * 1e-3) / 1e6, 3), "unit": "Mcells/s",
+                       "h2d_bytes_per_step": fs.bytes_in(), "d2h_bytes_per_step": fs.bytes_out(),
+                       "ms_per_step": round(ms_e2e, 4)}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_port(sample_n=(128, 128, 32))
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------- CPU baseline (oracle port)
+
+def _cpu_fused_step(shape, seed_offset=0):
+    """One fused step of the oracle (plain-C port of the reference path) on a sub-grid of the
+    same workload; returns (cells, seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import h5tables
+    import oracle_py as O
+    import workloads as W
+    wl = W.chem_hydro(shape=shape, seed=W.SEED_BASE + 3 + seed_offset)
+    tables = h5tables.load_table_block(TABLES)
+    u = wl["units"]
+    fields = [f.copy() for f in wl["fields"]]
+    scale = wl["scale"]
+    chem = O.Chem(tables, scale.reshape(-1))
+    t0 = time.perf_counter()
+    # fexpl: scale, et <- ge, fEuler, ge tendency <- et tendency, unscale
+    phys = fields[5] * scale
+    fields[4] = phys[..., 9] / u["EnergyUnits"] + 0.5 / fields[0] * (
+        fields[1] ** 2 + fields[2] ** 2 + fields[3] ** 2)
+    st, out = O.feuler(fields[:5] + [phys], 10, wl["bc"], wl["gamma"], None)
+    out[5][..., 9] = out[4]
+    out[4][:] = 0.0
+    y = (phys / scale).reshape(-1)
+    f = chem.rhs(y) * u["TimeUnits"]
+    J = chem.jac(y) * u["TimeUnits"]
+    bad, x = O.block_newton_solve(J, GAMMA_NEWTON, f)
+    dt = time.perf_counter() - t0
+    return int(np.prod(shape)), dt
+
+
+def cpu_baseline_port(sample_n=(32, 32, 32)):
+    cells, dt = _cpu_fused_step(sample_n)
+    return {"value": round(cells / dt / 1e6, 5), "unit": "Mcells/s", "cores": 1, "kind": "port",
+            "sample": f"one fused step on a {sample_n[0]}x{sample_n[1]}x{sample_n[2]} sub-grid of "
+                      f"the same workload ({cells} cells, {dt:.2f} s), 1 thread"}
+
+
+def _ref_worker(args):
+    shape, seed, steps = args
+    tot_cells, tot_t = 0, 0.0
+    for s in range(steps):
+        c, t = _cpu_fused_step(shape, seed * 100 + s)
+        tot_cells += c
+        tot_t += t
+    return tot_cells, tot_t
+
+
+def run_reference(args):
+    """Reference arm: the reference's path as the plain-C oracle port (the reference's own
+    build needs its source tree, which is not present where the benchmark runs), on all host
+    cores as independent z-slabs (one process per core, like the reference's MPI ranks)."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    slab = (args.n, 32, 4)  # per-core sample per step: 16K cells
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_ref_worker, [(slab, i, 1) for i in range(cores)])  # warm-up (imports, build)
+        t0 = time.perf_counter()
+        res = pool.map(_ref_worker, [(slab, i, args.steps) for i in range(cores)])
+        wall = time.perf_counter() - t0
+    cells = sum(r[0] for r in res)
+    value = cells / wall / 1e6
+    sample = (f"{args.steps} steps x {cores} processes, each one fused step on a "
+              f"{slab[0]}x{slab[1]}x{slab[2]} slab of the workload per step")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "Mcells/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(wall / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "nvar": 15,
+                       "sample_cells_per_step": cells // args.steps},
+            "cpu_baseline": {"value": round(value, 5), "unit": "Mcells/s", "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 5), "unit": "Mcells/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gbmv(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,182 @@
+/* gbmv: GB300 (sm_103a) right-hand-side hot path of the SUNDIALS ManyVector chemistry/
+ * hydrodynamics demonstration code, behind a plain C ABI.
+ *
+ * All array arguments are DEVICE pointers (cudaMalloc / torch CUDA storage) unless the comment
+ * says "host".  `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ * Return codes follow the ARKODE callback convention of the reference: 0 success, >0
+ * recoverable failure, <0 unrecoverable failure; the GBMV_E* codes below are all negative.
+ *
+ * Vector layout (the reference's MPIManyVector, one rank):
+ *   component 0..4: rho, mx, my, mz, et, each nx*ny*nz doubles, x fastest
+ *                   (INDX, src/euler3D.hpp:62)
+ *   component 5   : chemistry/tracers, nchem*nx*ny*nz doubles, species fastest
+ *                   (BUFINDX, src/euler3D.hpp:65)
+ * Dense Jacobian / Newton-matrix blocks: ncells blocks of 10x10 doubles, column-major,
+ *   element (row, col) of block i at [i*100 + col*10 + row] (DENSEIDX of
+ *   src/raja_primordial_network.cpp:40, the SUNMatrix_MagmaDenseBlock layout).
+ */
+#ifndef GBMV_H
+#define GBMV_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBMV_OK 0
+#define GBMV_ILLEGAL_STATE (-1)     /* fEuler's legal_state failure (src/utilities.cpp:83-84) */
+#define GBMV_EINVAL (-101)          /* bad argument */
+#define GBMV_ECUDA (-102)           /* CUDA runtime error */
+#define GBMV_ENOMEM (-103)          /* device allocation failed */
+#define GBMV_EUNSUPPORTED (-104)    /* NVAR / option not compiled in */
+
+/* Boundary condition codes (src/euler3D.hpp:86-89). */
+#define GBMV_BC_PERIODIC 0
+#define GBMV_BC_NEUMANN 1
+#define GBMV_BC_DIRICHLET 2
+#define GBMV_BC_REFLECTING 3
+
+/* Arithmetic of the WENO flux-divergence. */
+#define GBMV_FP64 0   /* all arithmetic in FP64 (parity form: <=1e-12 vs the reference) */
+#define GBMV_MIXED 1  /* mixed-precision form (<=1e-6 vs the FP64 oracle) */
+
+/* Grid + problem description: the fields of EulerData the RHS needs
+ * (src/euler3D.hpp:183-253).  nchem must be one of 0, 2, 4, 6, 10 (NVAR 5, 7, 9, 11, 15,
+ * the variants of src/CMakeLists.txt:29). */
+typedef struct gbmv_grid {
+  long nx, ny, nz;
+  int nchem;
+  double dx, dy, dz;
+  double gamma;
+  int bc[6]; /* x-lower, x-upper, y-lower, y-upper, z-lower, z-upper */
+} gbmv_grid;
+
+/* ------------------------------------------------------------------ hydro (part a) */
+
+typedef struct gbmv_hydro_s* gbmv_hydro;
+
+/* EulerData counterpart: validates the grid (extents >= 3, periodic faces paired, as
+ * EulerData::SetupDecomp, src/euler3D.hpp:442-489) and allocates the device scratch the
+ * RHS needs.  Replaces EulerData::SetupDecomp's flux-array allocation. */
+int gbmv_hydro_create(const gbmv_grid* grid, gbmv_hydro* out);
+int gbmv_hydro_destroy(gbmv_hydro h);
+
+/* Constant per-field body force added to every cell (host array of NVAR doubles, NULL = 0):
+ * the external_forces problem hook of the reference for constant forcings such as
+ * src/rayleigh_taylor.cpp:117-128. */
+int gbmv_hydro_set_force(gbmv_hydro h, const double* force_host);
+
+/* Flags for gbmv_feuler_async. */
+#define GBMV_FORCE_IN_WDOT 1 /* wdot already holds G(t) (a general external_forces); add to it */
+
+/* fEuler (src/utilities.cpp:17-253): wdot = G - div F(w), 5th-order WENO flux divergence with
+ * periodic / Neumann / Dirichlet / reflecting ghost synthesis in-kernel (replaces
+ * EulerData::ExchangeStart/ExchangeEnd, src/euler3D.hpp:577-1191).  Synchronous: waits on
+ * `stream` to report GBMV_ILLEGAL_STATE (-1) for a non-positive density, energy or pressure
+ * anywhere (src/euler3D.hpp:1405-1414). */
+int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
+                int precision, void* stream);
+
+/* Same, fully asynchronous and CUDA-graph capturable: the legal-state bit mask (1 density,
+ * 2 energy, 4 pressure, OR-ed over cells) is OR-ed into *d_status (device int). */
+int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
+                      int precision, int flags, int* d_status, void* stream);
+
+/* stability (src/utilities.cpp:483-528): dt_stab = cfl * min(dx,dy,dz) / max(|mx/rho| + c),
+ * including the reference's use of |mx/rho| for all three directions.  *dt_stab is host. */
+int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,
+                   void* stream);
+
+/* -------------------------------------------------------------- chemistry (part b) */
+
+typedef struct gbmv_chem_s* gbmv_chem;
+
+/* cvklu_data counterpart (cvklu_setup_data, src/raja_primordial_network.cpp:45-254):
+ * `tables_host` is the (50 x 1024) table block in the order rates k01..k22 (no k20),
+ * 25 cooling terms, 4 H2 adiabatic-index tables (see h5tables.TABLE_NAMES); Ts starts at
+ * 1000 K; scale and inv_scale start at 1. */
+int gbmv_chem_create(long ncells, const double* tables_host, double current_z,
+                     gbmv_chem* out);
+int gbmv_chem_destroy(gbmv_chem c);
+
+/* prepare_Dengo_structures (src/primordial_static.cpp:227-259): scale = chem,
+ * inv_scale = 1/chem, chem = 1, then setting_up_extra_variables
+ * (src/raja_primordial_network.cpp:1969-2018). */
+int gbmv_chem_prepare(gbmv_chem c, double* chem, void* stream);
+
+/* Sets scale (device, 10*ncells) directly, inv_scale = 1/scale, and the auxiliary arrays. */
+int gbmv_chem_set_scale(gbmv_chem c, const double* scale, void* stream);
+
+/* apply_Dengo_scaling / unapply_Dengo_scaling (src/primordial_static.cpp:264-318). */
+int gbmv_chem_apply_scaling(gbmv_chem c, double* chem, void* stream);
+int gbmv_chem_unapply_scaling(gbmv_chem c, double* chem, void* stream);
+
+/* calculate_rhs_cvklu (src/raja_primordial_network.cpp:1015-1389) followed by the
+ * N_VScale(TimeUnits) of ffast/fimpl (src/multirate_chem_hydro_main.cpp:918-920):
+ * ydot = time_units * f(y).  Updates the per-cell temperature state (Ts, dTs/dge) that the
+ * next call and the Jacobian use. */
+int gbmv_chem_rhs(gbmv_chem c, double t, const double* y, double* ydot, double time_units,
+                  void* stream);
+
+/* calculate_jacobian_cvklu (src/raja_primordial_network.cpp:1393-1965) in dense blocks,
+ * times time_units (Jfast/Jimpl, src/multirate_chem_hydro_main.cpp:976-983). */
+int gbmv_chem_jac(gbmv_chem c, double t, const double* y, double* J, double time_units,
+                  void* stream);
+
+/* Device pointers of the persistent per-cell state (for checkpoint/restart and tests):
+ * which: 0 Ts, 1 dTs_ge, 2 mdensity, 3 inv_mdensity, 4 cie optical depth, 5 h2 optical depth,
+ * 6 scale, 7 inv_scale. */
+double* gbmv_chem_state(gbmv_chem c, int which);
+
+/* ---------------------------------------------------- block-diagonal solve (part c) */
+
+/* SUNLinSolSetup of the MAGMA batched dense solver wrapped by SUNLinSol_RankLocalLS /
+ * SUNLinSol_BDMPIMV (src/multirate_chem_hydro_main.cpp:1360-1369,
+ * src/imex_chem_hydro_main.cpp:1123-1132): LU with partial pivoting of every 10x10 block of
+ * A in place; pivots: 10 ints per block.  Returns 0, or a positive value (SUNLS_LUFACT_FAIL
+ * style, recoverable) if some block is singular. */
+int gbmv_block_lu_factor(long nblocks, double* A, int* pivots, void* stream);
+
+/* SUNLinSolSolve of the same (src/multirate_chem_hydro_main.cpp:1371-1395): x = A^{-1} b
+ * on the chemistry subvector; b and x may alias. */
+int gbmv_block_lu_solve(long nblocks, const double* LU, const int* pivots, const double* b,
+                        double* x, void* stream);
+
+/* ARKLS's Newton matrix A = I - gamma*J (SUNMatScaleAddI) for dense blocks, in place. */
+int gbmv_block_form_newton(long nblocks, double* J, double gamma, void* stream);
+
+/* ------------------------------------------------------ chemistry-hydro glue */
+
+/* fslow / fexpl (src/multirate_chem_hydro_main.cpp:996-1083, src/imex_chem_hydro_main.cpp:
+ * 910-1000): apply the Dengo scaling to w[5], set et = ge/EnergyUnits + |m|^2/(2 rho) in w[4],
+ * evaluate fEuler, move the total-energy tendency into the gas-energy species of wdot[5]
+ * (etdot = 0), undo the scaling.  Synchronous like gbmv_feuler. */
+int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* const* wdot,
+               double energy_units, int precision, void* stream);
+
+/* PostprocessStep (src/imex_chem_hydro_main.cpp:1002-1051): et from ge and momenta. */
+int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double energy_units,
+                          void* stream);
+
+/* ----------------------------------------------------------------- utilities */
+
+const char* gbmv_version(void);
+const char* gbmv_last_error(void);
+/* Number of kernel launches issued by this library since load (for launch accounting). */
+long gbmv_launch_count(void);
+
+/* Per-kernel-family timing with CUDA events recorded on the launching stream (no counterpart
+ * in the reference, which times with MPI_Wtime in src/profiler.hpp).  Families:
+ * "face_flux", "divergence", "chem_rhs", "chem_jac", "block_lu_factor", "block_lu_solve",
+ * "glue".  gbmv_profile_get synchronizes on the recorded events. */
+int gbmv_profile_enable(int on);
+int gbmv_profile_reset(void);
+int gbmv_profile_get(const char* family, double* total_ms, long* launches);
+
+/* Diagnostics (no counterpart in the reference): peak FMA throughput of the SIMT pipes,
+ * FP64 (fp64=1) or FP32 (fp64=0), in flop/s (2 per FMA) -- the FP64 roofline denominator. */
+int gbmv_diag_fma_rate(int fp64, double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,426 @@
+// The C ABI (include/gbmv.h): handles mirroring EulerData / cvklu_data, argument checking,
+// dispatch to the kernels, ARKODE-convention return codes.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "chem.cuh"
+#include "weno.cuh"
+
+namespace gbmv {
+
+static thread_local char g_err[512];
+static std::atomic<long> g_launches{0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+void count_launch(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+int check_cuda(cudaError_t e, const char* where) {
+  set_error("%s: %s", where, cudaGetErrorString(e));
+  return GBMV_ECUDA;
+}
+
+// ---- per-family event profiler
+struct ProfRec {
+  const char* family;
+  cudaEvent_t e0, e1;
+};
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+static std::vector<ProfRec> g_prof;
+
+ProfScope::ProfScope(const char* family, cudaStream_t s) : slot(-1), stream(s) {
+  if (!g_prof_on) return;
+  ProfRec r{family, nullptr, nullptr};
+  if (cudaEventCreate(&r.e0) != cudaSuccess || cudaEventCreate(&r.e1) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  cudaEventRecord(r.e0, s);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  slot = (int)g_prof.size();
+  g_prof.push_back(r);
+}
+ProfScope::~ProfScope() {
+  if (slot < 0) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaEventRecord(g_prof[slot].e1, stream);
+}
+
+}  // namespace gbmv
+
+using namespace gbmv;
+
+struct gbmv_hydro_s {
+  Grid g;
+  ForceTerm force;
+  double* scratch = nullptr;
+  size_t scratch_doubles = 0;
+  int* d_status = nullptr;
+};
+
+struct gbmv_chem_s {
+  long n = 0;
+  ChemParams P{};
+  ChemState S{};
+  double* tab = nullptr;
+  double* cell = nullptr;  // one allocation for all per-cell arrays
+  int* d_info = nullptr;
+};
+
+static int check_grid(const gbmv_grid* g) {
+  if (!g) { set_error("null grid"); return GBMV_EINVAL; }
+  if (g->nx < 3 || g->ny < 3 || g->nz < 3) {
+    set_error("every extent must be >= 3 (got %ld x %ld x %ld)", g->nx, g->ny, g->nz);
+    return GBMV_EINVAL;
+  }
+  if (!(g->nchem == 0 || g->nchem == 2 || g->nchem == 4 || g->nchem == 6 || g->nchem == 10)) {
+    set_error("nchem=%d not supported (0,2,4,6,10)", g->nchem);
+    return GBMV_EUNSUPPORTED;
+  }
+  for (int a = 0; a < 3; ++a) {
+    const int lo = g->bc[2 * a], hi = g->bc[2 * a + 1];
+    if (lo < 0 || lo > 3 || hi < 0 || hi > 3) { set_error("bad boundary code"); return GBMV_EINVAL; }
+    if ((lo == GBMV_BC_PERIODIC) != (hi == GBMV_BC_PERIODIC)) {
+      set_error("axis %d: only one face periodic", a);
+      return GBMV_EINVAL;
+    }
+  }
+  if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->gamma > 1.0)) {
+    set_error("bad spacing or gamma");
+    return GBMV_EINVAL;
+  }
+  return GBMV_OK;
+}
+
+static bool fields_ok(const double* const* w, int nchem) {
+  if (!w) return false;
+  for (int v = 0; v < 5; ++v)
+    if (!w[v]) return false;
+  return nchem == 0 || w[5] != nullptr;
+}
+
+extern "C" {
+
+const char* gbmv_version(void) { return "gbmv 0.1 (sm_103a)"; }
+
+int gbmv_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_on = on != 0;
+  return GBMV_OK;
+}
+
+int gbmv_profile_reset(void) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  for (auto& r : g_prof) {
+    cudaEventDestroy(r.e0);
+    cudaEventDestroy(r.e1);
+  }
+  g_prof.clear();
+  return GBMV_OK;
+}
+
+int gbmv_profile_get(const char* family, double* total_ms, long* launches) {
+  if (!family || !total_ms || !launches) return GBMV_EINVAL;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  double tot = 0.0;
+  long n = 0;
+  for (auto& r : g_prof) {
+    if (std::string(r.family) != family) continue;
+    GBMV_CUDA_TRY(cudaEventSynchronize(r.e1));
+    float ms = 0.f;
+    GBMV_CUDA_TRY(cudaEventElapsedTime(&ms, r.e0, r.e1));
+    tot += ms;
+    ++n;
+  }
+  *total_ms = tot;
+  *launches = n;
+  return GBMV_OK;
+}
+const char* gbmv_last_error(void) { return g_err; }
+long gbmv_launch_count(void) { return g_launches.load(); }
+
+int gbmv_hydro_create(const gbmv_grid* grid, gbmv_hydro* out) {
+  if (!out) return GBMV_EINVAL;
+  *out = nullptr;
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  gbmv_hydro h = new (std::nothrow) gbmv_hydro_s();
+  if (!h) return GBMV_ENOMEM;
+  h->g = make_grid(*grid);
+  memset(&h->force, 0, sizeof h->force);
+  h->scratch_doubles = feuler_fp64_scratch_doubles(h->g);
+  if (cudaMalloc(&h->scratch, h->scratch_doubles * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("device allocation of %zu flux doubles failed", h->scratch_doubles);
+    cudaFree(h->scratch);
+    delete h;
+    return GBMV_ENOMEM;
+  }
+  *out = h;
+  return GBMV_OK;
+}
+
+int gbmv_hydro_destroy(gbmv_hydro h) {
+  if (!h) return GBMV_OK;
+  cudaFree(h->scratch);
+  cudaFree(h->d_status);
+  delete h;
+  return GBMV_OK;
+}
+
+int gbmv_hydro_set_force(gbmv_hydro h, const double* force) {
+  if (!h) return GBMV_EINVAL;
+  for (int v = 0; v < 16; ++v) h->force.c[v] = (force && v < 5 + h->g.nchem) ? force[v] : 0.0;
+  return GBMV_OK;
+}
+
+int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
+                      int precision, int flags, int* d_status, void* stream) {
+  (void)t;
+  if (!h || !fields_ok(w, h->g.nchem) || !fields_ok(wdot, h->g.nchem) || !d_status) {
+    set_error("null handle, field or status pointer");
+    return GBMV_EINVAL;
+  }
+  if (precision != GBMV_FP64 && precision != GBMV_MIXED) {
+    set_error("unknown precision %d", precision);
+    return GBMV_EINVAL;
+  }
+  Fields W, Wd;
+  for (int v = 0; v < 6; ++v) {
+    W.f[v] = const_cast<double*>(w[v]);
+    Wd.f[v] = (v < 5 || h->g.nchem) ? wdot[v] : nullptr;
+  }
+  if (!h->g.nchem) W.f[5] = nullptr;
+  ForceTerm G = h->force;
+  G.in_wdot = (flags & GBMV_FORCE_IN_WDOT) ? 1 : 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  // GBMV_MIXED falls back to the FP64 form until the mixed kernel is selected by the caller
+  return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
+}
+
+int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
+                int precision, void* stream) {
+  if (!h) return GBMV_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  GBMV_CUDA_TRY(cudaMemsetAsync(h->d_status, 0, sizeof(int), s));
+  int rc = gbmv_feuler_async(h, t, w, wdot, precision, 0, h->d_status, stream);
+  if (rc) return rc;
+  int st = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st) {
+    set_error("illegal state (mask %d: 1 density, 2 energy, 4 pressure)", st);
+    return GBMV_ILLEGAL_STATE;
+  }
+  return GBMV_OK;
+}
+
+/* ------------------------------------------------------------------ chemistry */
+
+int gbmv_chem_create(long ncells, const double* tables_host, double current_z, gbmv_chem* out) {
+  if (!out || ncells <= 0 || !tables_host) { set_error("bad chem_create arguments"); return GBMV_EINVAL; }
+  *out = nullptr;
+  gbmv_chem c = new (std::nothrow) gbmv_chem_s();
+  if (!c) return GBMV_ENOMEM;
+  c->n = ncells;
+  // bin-major re-layout of the (50 x 1024) table block
+  double* h = (double*)malloc(sizeof(double) * kNT * kTSize);
+  if (!h) { delete c; return GBMV_ENOMEM; }
+  for (int b = 0; b < kTSize; ++b)
+    for (int r = 0; r < kNT; ++r) h[b * kNT + r] = tables_host[(long)r * kTSize + b];
+  const size_t per_cell = 10 + 10 + 6;
+  if (cudaMalloc(&c->tab, sizeof(double) * kNT * kTSize) != cudaSuccess ||
+      cudaMalloc(&c->cell, sizeof(double) * per_cell * ncells) != cudaSuccess ||
+      cudaMalloc(&c->d_info, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    free(h);
+    cudaFree(c->tab);
+    cudaFree(c->cell);
+    delete c;
+    set_error("device allocation failed for %ld cells", ncells);
+    return GBMV_ENOMEM;
+  }
+  cudaMemcpy(c->tab, h, sizeof(double) * kNT * kTSize, cudaMemcpyHostToDevice);
+  free(h);
+  // constants of cvklu_setup_data (src/raja_primordial_network.cpp:190-194)
+  ChemParams& P = c->P;
+  P.tab = c->tab;
+  P.tlo = 1.0;
+  P.thi = 100000.0;
+  P.nbins = kTSize - 1;
+  P.lb = log(P.tlo);
+  P.dbin = (log(P.thi) - log(P.tlo)) / P.nbins;
+  P.idbin = (double)(1.0L / (long double)P.dbin);
+  P.z = current_z;
+  P.zp1_4 = pow(current_z + 1.0, 4);
+  ChemState& S = c->S;
+  double* p = c->cell;
+  S.scale = p; p += 10 * ncells;
+  S.inv_scale = p; p += 10 * ncells;
+  S.Ts = p; p += ncells;
+  S.dTs_ge = p; p += ncells;
+  S.mdens = p; p += ncells;
+  S.imdens = p; p += ncells;
+  S.cie = p; p += ncells;
+  S.h2 = p; p += ncells;
+  // Ts = 1000 K, scale = inv_scale = 1 (src/raja_primordial_network.cpp:185-188,
+  // src/primordial_static.cpp:193-200), aux from scale
+  double* init = (double*)malloc(sizeof(double) * per_cell * ncells);
+  if (!init) { gbmv_chem_destroy(c); return GBMV_ENOMEM; }
+  for (long i = 0; i < 20 * ncells; ++i) init[i] = 1.0;
+  for (long i = 0; i < ncells; ++i) init[20 * ncells + i] = 1000.0;
+  for (long i = 21 * ncells; i < (long)per_cell * ncells; ++i) init[i] = 0.0;
+  cudaError_t e = cudaMemcpy(c->cell, init, sizeof(double) * per_cell * ncells,
+                             cudaMemcpyHostToDevice);
+  free(init);
+  if (e != cudaSuccess) { gbmv_chem_destroy(c); return check_cuda(e, "chem_create upload"); }
+  int rc = chem_aux(S, ncells, 0);
+  if (rc) { gbmv_chem_destroy(c); return rc; }
+  GBMV_CUDA_TRY(cudaDeviceSynchronize());
+  *out = c;
+  return GBMV_OK;
+}
+
+int gbmv_chem_destroy(gbmv_chem c) {
+  if (!c) return GBMV_OK;
+  cudaFree(c->tab);
+  cudaFree(c->cell);
+  cudaFree(c->d_info);
+  delete c;
+  return GBMV_OK;
+}
+
+double* gbmv_chem_state(gbmv_chem c, int which) {
+  if (!c) return nullptr;
+  switch (which) {
+    case 0: return c->S.Ts;
+    case 1: return c->S.dTs_ge;
+    case 2: return c->S.mdens;
+    case 3: return c->S.imdens;
+    case 4: return c->S.cie;
+    case 5: return c->S.h2;
+    case 6: return c->S.scale;
+    case 7: return c->S.inv_scale;
+    default: return nullptr;
+  }
+}
+
+int gbmv_chem_prepare(gbmv_chem c, double* chem, void* stream) {
+  if (!c || !chem) return GBMV_EINVAL;
+  return chem_prepare(c->S, chem, c->n, (cudaStream_t)stream);
+}
+
+int gbmv_chem_set_scale(gbmv_chem c, const double* scale, void* stream) {
+  if (!c || !scale) return GBMV_EINVAL;
+  return chem_set_scale(c->S, scale, c->n, (cudaStream_t)stream);
+}
+
+int gbmv_chem_apply_scaling(gbmv_chem c, double* chem, void* stream) {
+  if (!c || !chem) return GBMV_EINVAL;
+  return chem_scaling(c->S, chem, c->n, 0, (cudaStream_t)stream);
+}
+
+int gbmv_chem_unapply_scaling(gbmv_chem c, double* chem, void* stream) {
+  if (!c || !chem) return GBMV_EINVAL;
+  return chem_scaling(c->S, chem, c->n, 1, (cudaStream_t)stream);
+}
+
+int gbmv_chem_rhs(gbmv_chem c, double t, const double* y, double* ydot, double time_units,
+                  void* stream) {
+  (void)t;
+  if (!c || !y || !ydot) { set_error("null argument"); return GBMV_EINVAL; }
+  return chem_rhs(c->P, c->S, c->n, y, ydot, time_units, (cudaStream_t)stream);
+}
+
+int gbmv_chem_jac(gbmv_chem c, double t, const double* y, double* J, double time_units,
+                  void* stream) {
+  (void)t;
+  if (!c || !y || !J) { set_error("null argument"); return GBMV_EINVAL; }
+  return chem_jac(c->P, c->S, c->n, y, J, time_units, (cudaStream_t)stream);
+}
+
+/* ------------------------------------------------------------------ block solve */
+
+static int* lu_info_buffer() {
+  static int* buf = nullptr;
+  static std::mutex m;
+  std::lock_guard<std::mutex> lk(m);
+  if (!buf && cudaMalloc(&buf, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return buf;
+}
+
+int gbmv_block_lu_factor(long nblocks, double* A, int* pivots, void* stream) {
+  if (nblocks <= 0 || !A || !pivots) { set_error("bad factor arguments"); return GBMV_EINVAL; }
+  int* info = lu_info_buffer();
+  if (!info) return GBMV_ENOMEM;
+  cudaStream_t s = (cudaStream_t)stream;
+  GBMV_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), s));
+  int rc = block_lu_factor(nblocks, A, pivots, info, s);
+  if (rc) return rc;
+  int h = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h) { set_error("singular block"); return 1; }
+  return GBMV_OK;
+}
+
+int gbmv_block_lu_solve(long nblocks, const double* LU, const int* pivots, const double* b,
+                        double* x, void* stream) {
+  if (nblocks <= 0 || !LU || !pivots || !b || !x) { set_error("bad solve arguments"); return GBMV_EINVAL; }
+  return block_lu_solve(nblocks, LU, pivots, b, x, (cudaStream_t)stream);
+}
+
+int gbmv_block_form_newton(long nblocks, double* J, double gamma, void* stream) {
+  if (nblocks <= 0 || !J) return GBMV_EINVAL;
+  return block_form_newton(nblocks, J, gamma, (cudaStream_t)stream);
+}
+
+/* ------------------------------------------------------------------ glue */
+
+int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* const* wdot,
+               double energy_units, int precision, void* stream) {
+  if (!h || !c || h->g.nchem != 10 || c->n != h->g.ncell) {
+    set_error("fexpl needs a 10-species hydro grid matching the chemistry cell count");
+    return GBMV_EINVAL;
+  }
+  if (!fields_ok(w, 10) || !fields_ok(wdot, 10)) return GBMV_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, 0, s);
+  if (rc) return rc;
+  rc = gbmv_feuler(h, t, (const double* const*)w, wdot, precision, stream);
+  if (rc < 0 && rc != GBMV_ILLEGAL_STATE) return rc;
+  int rc2 = energy_epilogue(c->S, w[5], wdot[5], wdot[4], c->n, 10, s);
+  if (rc2) return rc2;
+  return rc;
+}
+
+int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double energy_units,
+                          void* stream) {
+  if (!h || !c || h->g.nchem != 10 || !fields_ok(w, 10)) return GBMV_EINVAL;
+  return energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, 1, (cudaStream_t)stream);
+}
+
+int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,
+                   void* stream) {
+  (void)h; (void)w; (void)cfl; (void)dt_stab; (void)stream;
+  set_error("gbmv_stability not built yet");
+  return GBMV_EUNSUPPORTED;
+}
+
+}  // extern "C"

@@ -1,0 +1,41 @@
+// Declarations for the chemistry kernels (part b) and the block solves (part c).
+#pragma once
+
+#include "chem_net.cuh"
+#include "common.cuh"
+
+namespace gbmv {
+
+// Persistent per-cell network state (device arrays), the per-cell members of cvklu_data
+// (src/raja_primordial_network.hpp:168-270) that the source/Jacobian actually need.
+struct ChemState {
+  double* scale;      // 10 per cell
+  double* inv_scale;  // 10 per cell
+  double* Ts;         // temperature, carried from call to call
+  double* dTs_ge;     // dT/dge from the last source evaluation
+  double* mdens;
+  double* imdens;
+  double* cie;        // CIE cooling optical-depth factor
+  double* h2;         // H2 line cooling optical-depth factor
+};
+
+int chem_rhs(const ChemParams& P, const ChemState& S, long n, const double* y, double* ydot,
+             double tunit, cudaStream_t s);
+int chem_jac(const ChemParams& P, const ChemState& S, long n, const double* y, double* J,
+             double tunit, cudaStream_t s);
+int chem_aux(const ChemState& S, long n, cudaStream_t s);
+int chem_prepare(const ChemState& S, double* chem, long n, cudaStream_t s);
+int chem_set_scale(const ChemState& S, const double* scale, long n, cudaStream_t s);
+int chem_scaling(const ChemState& S, double* chem, long n, int mode, cudaStream_t s);
+int energy_sync(const ChemState& S, double* const* w, long n, int nchem, double eunit_scale,
+                int restore, cudaStream_t s);
+int energy_epilogue(const ChemState& S, double* chem, double* chemdot, double* etdot, long n,
+                    int nchem, cudaStream_t s);
+
+// batched 10x10 LU (blocklu.cu)
+int block_lu_factor(long nb, double* A, int* piv, int* d_info, cudaStream_t s);
+int block_lu_solve(long nb, const double* LU, const int* piv, const double* b, double* x,
+                   cudaStream_t s);
+int block_form_newton(long nb, double* J, double gamma, cudaStream_t s);
+
+}  // namespace gbmv

@@ -1,0 +1,279 @@
+// Primordial chemistry network (10 species: H2I, H2II, HI, HII, HM, HeI, HeII, HeIII, de, ge):
+// rate interpolation, temperature solve, species sources and the analytic Jacobian, as
+// device functions shared by the RHS, Jacobian and fused Newton kernels.
+//
+// Follows src/raja_primordial_network.cpp (the Dengo "cvklu" network): temperature
+// 908-1011, rate interpolation 1044-1248, sources 1305-1375, Jacobian 1518-1867.  The species
+// sources are written as reaction fluxes times net stoichiometry, summed in reaction order,
+// which is the reference's sum term by term.
+#pragma once
+
+#include "common.cuh"
+
+namespace gbmv {
+
+constexpr int kNT = 50;      // tables per bin
+constexpr int kNRates = 46;  // interpolated per cell (21 rates + 25 cooling terms)
+constexpr int kTSize = 1024;
+
+// table rows (order of h5tables.TABLE_NAMES)
+enum : int {
+  K01, K02, K03, K04, K05, K06, K07, K08, K09, K10, K11, K12, K13, K14, K15, K16, K17, K18, K19,
+  K21, K22,
+  BREM, CEHEI, CEHEII, CEHI, CIECO, CIHEI, CIHEII, CIHEIS, CIHI, COMPTON, GAEL, GAH2, GAHE, GAHI,
+  GAHP, H2LTE, H2MCOOL, H2MHEAT, NCRD1, NCRD2, NCRN, REHEII1, REHEII2, REHEIII, REHII,
+  GAMMAH2_1, DGAMMAH2_1, GAMMAH2_2, DGAMMAH2_2
+};
+
+struct ChemParams {
+  const double* tab;  // device, bin-major: tab[bin * kNT + row]
+  double dbin, idbin, lb, tlo, thi, z, zp1_4;
+  int nbins;
+};
+
+__device__ __forceinline__ int chem_bin(const ChemParams& P, double logT, double& t1, double& t2) {
+  int b = (int)(P.idbin * (logT - P.lb));
+  if (b <= 0) b = 0;
+  else if (b >= P.nbins) b = P.nbins - 1;
+  t1 = P.lb + b * P.dbin;
+  t2 = P.lb + (b + 1) * P.dbin;
+  return b;
+}
+
+// cvklu_calculate_temperature: ten Newton iterations from the previous T, then clamp.
+__device__ __forceinline__ void chem_temperature(const ChemParams& P, const double (&y)[10],
+                                                 double& Ts, double& dTs_ge) {
+  const double kb = 1.3806504e-16, mh = 1.67e-24, gm1 = 1.0 / (5.e0 / 3.e0 - 1);
+  const double H2_1 = y[0], H2_2 = y[1], H_1 = y[2], H_2 = y[3], H_m0 = y[4], He_1 = y[5],
+               He_2 = y[6], He_3 = y[7], de = y[8], ge = y[9];
+  const double density = 2.0 * H2_1 + 2.0 * H2_2 + 1.00794 * H_1 + 1.00794 * H_2 +
+                         1.00794 * H_m0 + 4.002602 * He_1 + 4.002602 * He_2 + 4.002602 * He_3;
+  const double dmh = density * mh;
+  double T = Ts, Tnew = 0.0, dge_dT = 0.0;
+#pragma unroll 1
+  for (int it = 0; it < 10; ++it) {
+    T = Ts;
+    double t1, t2;
+    const double logT = log(Ts);
+    const int b = chem_bin(P, logT, t1, t2);
+    const double Tdef = (logT - t1) / (t2 - t1);
+    const double* lo = P.tab + (long)b * kNT;
+    const double* hi = lo + kNT;
+    const double g2 = lo[GAMMAH2_2] + Tdef * (hi[GAMMAH2_2] - lo[GAMMAH2_2]);
+    const double dg2 = lo[DGAMMAH2_2] + Tdef * (hi[DGAMMAH2_2] - lo[DGAMMAH2_2]);
+    const double g1 = lo[GAMMAH2_1] + Tdef * (hi[GAMMAH2_1] - lo[GAMMAH2_1]);
+    const double dg1 = lo[DGAMMAH2_1] + Tdef * (hi[DGAMMAH2_1] - lo[DGAMMAH2_1]);
+    const double i1 = 1.0 / (g1 - 1.0), i2 = 1.0 / (g2 - 1.0);
+    const double nsum = H2_1 * i1 + H2_2 * i2 + H_1 * gm1 + H_2 * gm1 + H_m0 * gm1 + He_1 * gm1 +
+                        He_2 * gm1 + He_3 * gm1 + gm1 * de;
+    dge_dT = T * kb * (-H2_1 * i1 * i1 * dg1 - H2_2 * i2 * i2 * dg2) / dmh + kb * nsum / dmh;
+    const double dge = T * kb * nsum / dmh - ge;
+    Tnew = T - dge / dge_dT;
+    Ts = Tnew;
+  }
+  Ts = Tnew;
+  if (Ts < P.tlo) Ts = P.tlo;
+  else if (Ts > P.thi) Ts = P.thi;
+  dTs_ge = 1.0 / dge_dT;
+}
+
+// Rates at temperature Ts (and their T-derivatives when WithSlopes).
+template <bool WithSlopes>
+__device__ __forceinline__ void chem_rates(const ChemParams& P, double Ts, double (&k)[kNRates],
+                                           double (&dk)[kNRates]) {
+  double t1, t2;
+  const double logT = log(Ts);
+  const int b = chem_bin(P, logT, t1, t2);
+  const double Tdef = (logT - t1) / (t2 - t1);
+  const double Tfactor = (1.0 / Ts) / (t2 - t1);
+  const double* lo = P.tab + (long)b * kNT;
+  const double* hi = lo + kNT;
+#pragma unroll
+  for (int r = 0; r < kNRates; ++r) {
+    const double a = __ldg(lo + r), d = __ldg(hi + r) - a;
+    k[r] = a + Tdef * d;
+    if (WithSlopes) dk[r] = d * Tfactor;
+  }
+}
+
+// The 21 reaction fluxes (rate times reactant product).
+__device__ __forceinline__ void chem_fluxes(const double (&k)[kNRates], const double (&y)[10],
+                                            double (&r)[21]) {
+  const double H2_1 = y[0], H2_2 = y[1], H_1 = y[2], H_2 = y[3], H_m0 = y[4], He_1 = y[5],
+               He_2 = y[6], He_3 = y[7], de = y[8];
+  r[0] = k[K01] * H_1 * de;
+  r[1] = k[K02] * H_2 * de;
+  r[2] = k[K03] * He_1 * de;
+  r[3] = k[K04] * He_2 * de;
+  r[4] = k[K05] * He_2 * de;
+  r[5] = k[K06] * He_3 * de;
+  r[6] = k[K07] * H_1 * de;
+  r[7] = k[K08] * H_1 * H_m0;
+  r[8] = k[K09] * H_1 * H_2;
+  r[9] = k[K10] * H2_2 * H_1;
+  r[10] = k[K11] * H2_1 * H_2;
+  r[11] = k[K12] * H2_1 * de;
+  r[12] = k[K13] * H2_1 * H_1;
+  r[13] = k[K14] * H_m0 * de;
+  r[14] = k[K15] * H_1 * H_m0;
+  r[15] = k[K16] * H_2 * H_m0;
+  r[16] = k[K17] * H_2 * H_m0;
+  r[17] = k[K18] * H2_2 * de;
+  r[18] = k[K19] * H2_2 * H_m0;
+  r[19] = k[K21] * H2_1 * H_1 * H_1;
+  r[20] = k[K22] * H_1 * H_1 * H_1;
+}
+
+// Net species sources from reaction fluxes (net stoichiometry, reaction order).
+__device__ __forceinline__ void chem_species(const double (&r)[21], double (&s)[9]) {
+  s[0] = r[7] + r[9] - r[10] - r[11] - r[12] + r[18] + r[19] + r[20];
+  s[1] = r[8] - r[9] + r[10] + r[16] - r[17] - r[18];
+  s[2] = -r[0] + r[1] - r[6] - r[7] - r[8] - r[9] + r[10] + 2 * r[11] + 2 * r[12] + r[13] + r[14] +
+         2 * r[15] + 2 * r[17] + r[18] - 2 * r[19] - 2 * r[20];
+  s[3] = r[0] - r[1] - r[8] + r[9] - r[10] - r[15] - r[16];
+  s[4] = r[6] - r[7] - r[13] - r[14] - r[15] - r[16] - r[18];
+  s[5] = -r[2] + r[3];
+  s[6] = r[2] - r[3] - r[4] + r[5];
+  s[7] = r[4] - r[5];
+  s[8] = r[0] - r[1] + r[2] - r[3] + r[4] - r[5] - r[6] + r[7] + r[13] + r[14] + r[16] - r[17];
+}
+
+struct ChemAux {
+  double mdens, imdens, cie, h2;
+};
+
+// Gas-energy source (cooling/heating), src/raja_primordial_network.cpp:1371-1375.
+__device__ __forceinline__ double chem_ge_source(const ChemParams& P, const double (&k)[kNRates],
+                                                 const double (&y)[10], double T,
+                                                 const ChemAux& A) {
+  const double H2_1 = y[0], H_1 = y[2], H_2 = y[3], He_1 = y[5], He_2 = y[6], He_3 = y[7],
+               de = y[8];
+  const double z = P.z, cie = A.cie, h2oda = A.h2, mdens = A.mdens;
+  const double G = H2_1 * k[GAH2] + H_1 * k[GAHI] + H_2 * k[GAHP] + He_1 * k[GAHE] + de * k[GAEL];
+  const double D = k[H2LTE] / G + 1.0;
+  const double F = k[NCRN] / (H2_1 * k[NCRD2] + H_1 * k[NCRD1]) + 1.0;
+  const double H13 = H_1 * H_1 * H_1;
+  const double Hf = -H2_1 * H_1 * k[H2MCOOL] + H13 * k[H2MHEAT];
+  const double de2 = de * de;
+  return -2.01588 * H2_1 * k[CIECO] * cie * mdens - H2_1 * cie * k[H2LTE] * h2oda / D -
+         H_1 * k[CEHI] * cie * de - H_1 * k[CIHI] * cie * de - H_2 * cie * de * k[REHII] -
+         He_1 * k[CIHEI] * cie * de - He_2 * k[CEHEII] * cie * de - He_2 * k[CEHEI] * cie * de2 -
+         He_2 * k[CIHEII] * cie * de - He_2 * k[CIHEIS] * cie * de2 -
+         He_2 * cie * de * k[REHEII1] - He_2 * cie * de * k[REHEII2] -
+         He_3 * cie * de * k[REHEIII] - k[BREM] * cie * de * (H_2 + He_2 + 4.0 * He_3) -
+         cie * k[COMPTON] * de * P.zp1_4 * (T - 2.73 * z - 2.73) + 0.5 / F * Hf;
+}
+
+// Analytic Jacobian block (column-major B[col*10+row]) in physical units, before the
+// inv_scale*scale and time-unit factors; rates k and slopes dk at the cell temperature.
+__device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double (&k)[kNRates],
+                                              const double (&dk)[kNRates], const double (&y)[10],
+                                              double T, double Tge, const ChemAux& A,
+                                              double (&B)[100]) {
+  const double H2_1 = y[0], H2_2 = y[1], H_1 = y[2], H_2 = y[3], H_m0 = y[4], He_1 = y[5],
+               He_2 = y[6], He_3 = y[7], de = y[8];
+  const double z = P.z, h2oda = A.h2, md = A.mdens;
+#pragma unroll
+  for (int e = 0; e < 100; ++e) B[e] = 0.0;
+#define SETJ(row, col, expr) B[(col) * 10 + (row)] = (expr)
+  const double H1sq = H_1 * H_1;
+  SETJ(0, 0, -k[K11] * H_2 - k[K12] * de - k[K13] * H_1 + k[K21] * H1sq);
+  SETJ(0, 1, k[K10] * H_1 + k[K19] * H_m0);
+  SETJ(0, 2, k[K08] * H_m0 + k[K10] * H2_2 - k[K13] * H2_1 + 2 * k[K21] * H2_1 * H_1 +
+                 3 * k[K22] * H1sq);
+  SETJ(0, 3, -k[K11] * H2_1);
+  SETJ(0, 4, k[K08] * H_1 + k[K19] * H2_2);
+  SETJ(0, 8, -k[K12] * H2_1);
+  SETJ(1, 0, k[K11] * H_2);
+  SETJ(1, 1, -k[K10] * H_1 - k[K18] * de - k[K19] * H_m0);
+  SETJ(1, 2, k[K09] * H_2 - k[K10] * H2_2);
+  SETJ(1, 3, k[K09] * H_1 + k[K11] * H2_1 + k[K17] * H_m0);
+  SETJ(1, 4, k[K17] * H_2 - k[K19] * H2_2);
+  SETJ(1, 8, -k[K18] * H2_2);
+  SETJ(2, 0, k[K11] * H_2 + 2 * k[K12] * de + 2 * k[K13] * H_1 - 2 * k[K21] * H1sq);
+  SETJ(2, 1, -k[K10] * H_1 + 2 * k[K18] * de + k[K19] * H_m0);
+  SETJ(2, 2, -k[K01] * de - k[K07] * de - k[K08] * H_m0 - k[K09] * H_2 - k[K10] * H2_2 +
+                 2 * k[K13] * H2_1 + k[K15] * H_m0 - 4 * k[K21] * H2_1 * H_1 - 6 * k[K22] * H1sq);
+  SETJ(2, 3, k[K02] * de - k[K09] * H_1 + k[K11] * H2_1 + 2 * k[K16] * H_m0);
+  SETJ(2, 4, -k[K08] * H_1 + k[K14] * de + k[K15] * H_1 + 2 * k[K16] * H_2 + k[K19] * H2_2);
+  SETJ(2, 8, -k[K01] * H_1 + k[K02] * H_2 - k[K07] * H_1 + 2 * k[K12] * H2_1 + k[K14] * H_m0 +
+                 2 * k[K18] * H2_2);
+  SETJ(3, 0, -k[K11] * H_2);
+  SETJ(3, 1, k[K10] * H_1);
+  SETJ(3, 2, k[K01] * de - k[K09] * H_2 + k[K10] * H2_2);
+  SETJ(3, 3, -k[K02] * de - k[K09] * H_1 - k[K11] * H2_1 - k[K16] * H_m0 - k[K17] * H_m0);
+  SETJ(3, 4, -k[K16] * H_2 - k[K17] * H_2);
+  SETJ(3, 8, k[K01] * H_1 - k[K02] * H_2);
+  SETJ(4, 1, -k[K19] * H_m0);
+  SETJ(4, 2, k[K07] * de - k[K08] * H_m0 - k[K15] * H_m0);
+  SETJ(4, 3, -k[K16] * H_m0 - k[K17] * H_m0);
+  SETJ(4, 4, -k[K08] * H_1 - k[K14] * de - k[K15] * H_1 - k[K16] * H_2 - k[K17] * H_2 -
+                 k[K19] * H2_2);
+  SETJ(4, 8, k[K07] * H_1 - k[K14] * H_m0);
+  SETJ(5, 5, -k[K03] * de);
+  SETJ(5, 6, k[K04] * de);
+  SETJ(5, 8, -k[K03] * He_1 + k[K04] * He_2);
+  SETJ(6, 5, k[K03] * de);
+  SETJ(6, 6, -k[K04] * de - k[K05] * de);
+  SETJ(6, 7, k[K06] * de);
+  SETJ(6, 8, k[K03] * He_1 - k[K04] * He_2 - k[K05] * He_2 + k[K06] * He_3);
+  SETJ(7, 6, k[K05] * de);
+  SETJ(7, 7, -k[K06] * de);
+  SETJ(7, 8, k[K05] * He_2 - k[K06] * He_3);
+  SETJ(8, 1, -k[K18] * de);
+  SETJ(8, 2, k[K01] * de - k[K07] * de + k[K08] * H_m0 + k[K15] * H_m0);
+  SETJ(8, 3, -k[K02] * de + k[K17] * H_m0);
+  SETJ(8, 4, k[K08] * H_1 + k[K14] * de + k[K15] * H_1 + k[K17] * H_2);
+  SETJ(8, 5, k[K03] * de);
+  SETJ(8, 6, -k[K04] * de + k[K05] * de);
+  SETJ(8, 7, -k[K06] * de);
+  SETJ(8, 8, k[K01] * H_1 - k[K02] * H_2 + k[K03] * He_1 - k[K04] * He_2 + k[K05] * He_2 -
+                 k[K06] * He_3 - k[K07] * H_1 + k[K14] * H_m0 - k[K18] * H2_2);
+  {  // species rows by ge: sources with rates replaced by slopes, times dT/dge
+    double r[21], s[9];
+    chem_fluxes(dk, y, r);
+    chem_species(r, s);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) B[90 + q] = s[q] * Tge;
+  }
+  const double G = H2_1 * k[GAH2] + H_1 * k[GAHI] + H_2 * k[GAHP] + He_1 * k[GAHE] + de * k[GAEL];
+  const double D = k[H2LTE] / G + 1.0;
+  const double N = H2_1 * k[NCRD2] + H_1 * k[NCRD1];
+  const double F = k[NCRN] / N + 1.0;
+  const double H13 = H1sq * H_1;
+  const double Hf = -H2_1 * H_1 * k[H2MCOOL] + H13 * k[H2MHEAT];
+  const double lte2 = k[H2LTE] * k[H2LTE];
+  const double DG2 = (D * D) * (G * G);
+  const double iF2 = 1.0 / (F * F);
+  const double N2 = N * N;
+  SETJ(9, 0, -H2_1 * k[GAH2] * lte2 * h2oda / DG2 - 0.5 * H_1 * k[H2MCOOL] / F -
+                 2.01588 * k[CIECO] * md - k[H2LTE] * h2oda / D +
+                 0.5 * k[NCRD2] * k[NCRN] * iF2 * Hf / N2);
+  SETJ(9, 2, -H2_1 * k[GAHI] * lte2 * h2oda / DG2 - k[CEHI] * de - k[CIHI] * de +
+                 0.5 * k[NCRD1] * k[NCRN] * iF2 * Hf / N2 +
+                 0.5 * (-H2_1 * k[H2MCOOL] + 3 * H1sq * k[H2MHEAT]) / F);
+  SETJ(9, 3, -H2_1 * k[GAHP] * lte2 * h2oda / DG2 - k[BREM] * de - de * k[REHII]);
+  SETJ(9, 5, -H2_1 * k[GAHE] * lte2 * h2oda / DG2 - k[CIHEI] * de);
+  SETJ(9, 6, -k[BREM] * de - k[CEHEII] * de - k[CEHEI] * (de * de) - k[CIHEII] * de -
+                 k[CIHEIS] * (de * de) - de * k[REHEII1] - de * k[REHEII2]);
+  SETJ(9, 7, -4.0 * k[BREM] * de - de * k[REHEIII]);
+  SETJ(9, 8, -H2_1 * k[GAEL] * lte2 * h2oda / DG2 - H_1 * k[CEHI] - H_1 * k[CIHI] -
+                 H_2 * k[REHII] - He_1 * k[CIHEI] - He_2 * k[CEHEII] - 2 * He_2 * k[CEHEI] * de -
+                 He_2 * k[CIHEII] - 2 * He_2 * k[CIHEIS] * de - He_2 * k[REHEII1] -
+                 He_2 * k[REHEII2] - He_3 * k[REHEIII] - k[BREM] * (H_2 + He_2 + 4.0 * He_3) -
+                 k[COMPTON] * P.zp1_4 * (T - 2.73 * z - 2.73));
+  const double dGn = -H2_1 * dk[GAH2] - H_1 * dk[GAHI] - H_2 * dk[GAHP] - He_1 * dk[GAHE] -
+                     de * dk[GAEL];
+  SETJ(9, 9, -H2_1 * k[H2LTE] * h2oda * (-k[H2LTE] * dGn / (G * G) - dk[H2LTE] / G) / (D * D) -
+                 H2_1 * h2oda * dk[H2LTE] / D +
+                 0.5 * iF2 * Hf *
+                     (-1.0 * k[NCRN] * (-H2_1 * dk[NCRD2] - H_1 * dk[NCRD1]) / N2 -
+                      1.0 * dk[NCRN] / N) +
+                 0.5 / F * (-H2_1 * H_1 * dk[H2MCOOL] + H13 * dk[H2MHEAT]));
+#undef SETJ
+#pragma unroll
+  for (int col = 0; col < 10; ++col) B[col * 10 + 9] *= A.imdens;
+  B[99] *= Tge;
+}
+
+}  // namespace gbmv

@@ -1,0 +1,23 @@
+// Declarations shared between the WENO kernels and the C ABI layer.
+#pragma once
+
+#include "common.cuh"
+
+namespace gbmv {
+
+// The six ManyVector components as raw device pointers (component 5 may be null if nchem==0).
+struct Fields {
+  double* f[6];
+};
+
+// External forcing: per-field constants, or "wdot already holds G" (GBMV_FORCE_IN_WDOT).
+struct ForceTerm {
+  double c[16];
+  int in_wdot;
+};
+
+size_t feuler_fp64_scratch_doubles(const Grid& g);
+int feuler_fp64(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
+                double* scratch, int* d_status, cudaStream_t s);
+
+}  // namespace gbmv

@@ -1,0 +1,298 @@
+"""Python host mirror of the reference's RHS-path interface over the C ABI (include/gbmv.h).
+
+Names and argument meanings follow the reference so that tests read like its drivers:
+
+  EulerData-like ``Hydro``   .fEuler(t, w, wdot)          src/utilities.cpp:17
+  cvklu_data-like ``Chem``   .calculate_rhs_cvklu(...)    src/raja_primordial_network.cpp:1015
+                             .calculate_jacobian_cvklu(...) :1393
+                             .prepare_Dengo_structures(...) src/primordial_static.cpp:227
+  ``BlockLinearSolver``      .setup(A) / .solve(A, x, b)   src/multirate_chem_hydro_main.cpp:1360-1395
+  ``fexpl`` / ``PostprocessStep``                          src/imex_chem_hydro_main.cpp:910, 1002
+
+A ManyVector is a list of torch CUDA float64 tensors: [rho, mx, my, mz, et] each (nz, ny, nx)
+and, when nchem > 0, chem (nz, ny, nx, nchem).  Errors follow ARKODE conventions (int return
+codes); any negative code other than -1 (illegal state) raises GbmvError.  There is no CPU
+fallback: without the CUDA library and a GPU every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libgbmv.so")
+
+BC_PERIODIC, BC_NEUMANN, BC_DIRICHLET, BC_REFLECTING = 0, 1, 2, 3
+FP64, MIXED = 0, 1
+FORCE_IN_WDOT = 1
+
+
+class GbmvError(RuntimeError):
+    pass
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nx", C.c_long), ("ny", C.c_long), ("nz", C.c_long), ("nchem", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("gamma", C.c_double), ("bc", C.c_int * 6)]
+
+
+_P = C.POINTER(C.c_double)
+_VP = C.c_void_p
+
+# (name, restype, argtypes) for every symbol of include/gbmv.h
+SIGNATURES = [
+    ("gbmv_hydro_create", C.c_int, [C.POINTER(_Grid), C.POINTER(_VP)]),
+    ("gbmv_hydro_destroy", C.c_int, [_VP]),
+    ("gbmv_hydro_set_force", C.c_int, [_VP, _P]),
+    ("gbmv_feuler", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_int, _VP]),
+    ("gbmv_feuler_async", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_int,
+                                    C.c_int, _VP, _VP]),
+    ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
+    ("gbmv_chem_create", C.c_int, [C.c_long, _P, C.c_double, C.POINTER(_VP)]),
+    ("gbmv_chem_destroy", C.c_int, [_VP]),
+    ("gbmv_chem_prepare", C.c_int, [_VP, _VP, _VP]),
+    ("gbmv_chem_set_scale", C.c_int, [_VP, _VP, _VP]),
+    ("gbmv_chem_apply_scaling", C.c_int, [_VP, _VP, _VP]),
+    ("gbmv_chem_unapply_scaling", C.c_int, [_VP, _VP, _VP]),
+    ("gbmv_chem_rhs", C.c_int, [_VP, C.c_double, _VP, _VP, C.c_double, _VP]),
+    ("gbmv_chem_jac", C.c_int, [_VP, C.c_double, _VP, _VP, C.c_double, _VP]),
+    ("gbmv_chem_state", _VP, [_VP, C.c_int]),
+    ("gbmv_block_lu_factor", C.c_int, [C.c_long, _VP, _VP, _VP]),
+    ("gbmv_block_lu_solve", C.c_int, [C.c_long, _VP, _VP, _VP, _VP, _VP]),
+    ("gbmv_block_form_newton", C.c_int, [C.c_long, _VP, C.c_double, _VP]),
+    ("gbmv_fexpl", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
+                             C.c_int, _VP]),
+    ("gbmv_postprocess_step", C.c_int, [_VP, _VP, C.POINTER(_VP), C.c_double, _VP]),
+    ("gbmv_version", C.c_char_p, []),
+    ("gbmv_last_error", C.c_char_p, []),
+    ("gbmv_launch_count", C.c_long, []),
+    ("gbmv_diag_fma_rate", C.c_int, [C.c_int, _P]),
+    ("gbmv_profile_enable", C.c_int, [C.c_int]),
+    ("gbmv_profile_reset", C.c_int, []),
+    ("gbmv_profile_get", C.c_int, [C.c_char_p, _P, C.POINTER(C.c_long)]),
+]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libgbmv.so (built by build_lib.build()); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise GbmvError(f"{path} not built: run __graft_entry__.build()")
+        L = C.CDLL(path)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, what: str, allow=(0,)):
+    if rc in allow:
+        return rc
+    if rc < 0 and rc != -1:
+        raise GbmvError(f"{what} failed ({rc}): {load().gbmv_last_error().decode()}")
+    return rc
+
+
+def _dev_ptr(t):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise GbmvError("expected a CUDA tensor")
+    if t.dtype != torch.float64 or not t.is_contiguous():
+        raise GbmvError("expected a contiguous float64 tensor")
+    return t.data_ptr()
+
+
+def _stream_ptr(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _vec(fields):
+    arr = (_VP * 6)()
+    for i, f in enumerate(fields):
+        arr[i] = _dev_ptr(f)
+    return arr
+
+
+def grid_struct(shape, nchem, bc, gamma, domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+    nx, ny, nz = shape
+    g = _Grid()
+    g.nx, g.ny, g.nz, g.nchem = nx, ny, nz, nchem
+    g.dx = (domain[1] - domain[0]) / nx  # EulerData::SetupDecomp (src/euler3D.hpp:412-414)
+    g.dy = (domain[3] - domain[2]) / ny
+    g.dz = (domain[5] - domain[4]) / nz
+    g.gamma = gamma
+    for i in range(6):
+        g.bc[i] = bc[i]
+    return g
+
+
+class Hydro:
+    """Device-side EulerData: grid, boundary conditions, gamma, constant forcing."""
+
+    def __init__(self, shape, nchem, bc, gamma=1.4, force=None,
+                 domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+        L = load()
+        self.shape, self.nchem = tuple(shape), nchem
+        self.grid = grid_struct(shape, nchem, bc, gamma, domain)
+        h = _VP()
+        _check(L.gbmv_hydro_create(C.byref(self.grid), C.byref(h)), "gbmv_hydro_create")
+        self.h = h
+        if force is not None:
+            fa = np.ascontiguousarray(force, dtype=np.float64)
+            _check(L.gbmv_hydro_set_force(h, fa.ctypes.data_as(_P)), "gbmv_hydro_set_force")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.gbmv_hydro_destroy(self.h)
+            self.h = None
+
+    def fEuler(self, t, w, wdot, precision=FP64, stream=None) -> int:
+        """Returns 0, or -1 on an illegal state (as the reference's fEuler)."""
+        return _check(load().gbmv_feuler(self.h, t, _vec(w), _vec(wdot), precision,
+                                         _stream_ptr(stream)), "gbmv_feuler", allow=(0, -1))
+
+    def fEuler_async(self, t, w, wdot, status, precision=FP64, flags=0, stream=None) -> int:
+        return _check(load().gbmv_feuler_async(self.h, t, _vec(w), _vec(wdot), precision, flags,
+                                               status.data_ptr(), _stream_ptr(stream)),
+                      "gbmv_feuler_async")
+
+
+class Chem:
+    """Device-side cvklu_data: rate tables, scale arrays, temperature state."""
+
+    def __init__(self, ncells: int, tables: np.ndarray, current_z: float = -1.0):
+        L = load()
+        tab = np.ascontiguousarray(tables, dtype=np.float64)
+        if tab.shape != (50, 1024):
+            raise GbmvError("tables must be the (50, 1024) block of h5tables.load_table_block")
+        c = _VP()
+        _check(L.gbmv_chem_create(ncells, tab.ctypes.data_as(_P), current_z, C.byref(c)),
+               "gbmv_chem_create")
+        self.c, self.n = c, ncells
+
+    def __del__(self):
+        if getattr(self, "c", None) and _lib is not None:
+            _lib.gbmv_chem_destroy(self.c)
+            self.c = None
+
+    def state(self, which: str):
+        """Torch view of a persistent per-cell array (Ts, dTs_ge, mdensity, inv_mdensity,
+        cie_optical_depth_approx, h2_optical_depth_approx, scale, inv_scale)."""
+        import torch
+        idx = ["Ts", "dTs_ge", "mdensity", "inv_mdensity", "cie_optical_depth_approx",
+               "h2_optical_depth_approx", "scale", "inv_scale"].index(which)
+        ptr = load().gbmv_chem_state(self.c, idx)
+        n = self.n * (10 if idx >= 6 else 1)
+        return _wrap_device(ptr, n)
+
+    def prepare_Dengo_structures(self, chem, stream=None):
+        _check(load().gbmv_chem_prepare(self.c, _dev_ptr(chem), _stream_ptr(stream)), "prepare")
+
+    def set_scale(self, scale, stream=None):
+        _check(load().gbmv_chem_set_scale(self.c, _dev_ptr(scale), _stream_ptr(stream)), "set_scale")
+
+    def apply_Dengo_scaling(self, chem, stream=None):
+        _check(load().gbmv_chem_apply_scaling(self.c, _dev_ptr(chem), _stream_ptr(stream)), "apply")
+
+    def unapply_Dengo_scaling(self, chem, stream=None):
+        _check(load().gbmv_chem_unapply_scaling(self.c, _dev_ptr(chem), _stream_ptr(stream)),
+               "unapply")
+
+    def calculate_rhs_cvklu(self, t, y, ydot, time_units=1.0, stream=None):
+        return _check(load().gbmv_chem_rhs(self.c, t, _dev_ptr(y), _dev_ptr(ydot), time_units,
+                                           _stream_ptr(stream)), "gbmv_chem_rhs")
+
+    def calculate_jacobian_cvklu(self, t, y, J, time_units=1.0, stream=None):
+        return _check(load().gbmv_chem_jac(self.c, t, _dev_ptr(y), _dev_ptr(J), time_units,
+                                           _stream_ptr(stream)), "gbmv_chem_jac")
+
+
+def _wrap_device(ptr: int, n: int):
+    """Non-owning float64 CUDA tensor over library-owned device memory."""
+    import torch
+
+    class _Holder:
+        def __init__(self, p, nbytes):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8",
+                                             "data": (p, False), "version": 3,
+                                             "strides": None}
+
+    return torch.as_tensor(_Holder(ptr, n * 8), device="cuda")
+
+
+class BlockLinearSolver:
+    """Block-diagonal direct solver on the chemistry subvector (SUNLinSol_RankLocalLS /
+    SUNLinSol_BDMPIMV over the batched dense LU): setup factors A in place."""
+
+    def __init__(self, nblocks: int):
+        import torch
+        self.nb = nblocks
+        self.piv = torch.zeros(nblocks * 10, dtype=torch.int32, device="cuda")
+        self.last_flag = 0
+
+    def setup(self, A, stream=None) -> int:
+        self.last_flag = _check(load().gbmv_block_lu_factor(self.nb, _dev_ptr(A),
+                                                            self.piv.data_ptr(),
+                                                            _stream_ptr(stream)),
+                                "gbmv_block_lu_factor", allow=(0, 1))
+        return self.last_flag
+
+    def solve(self, A, x, b, tol=0.0, stream=None) -> int:
+        self.last_flag = _check(load().gbmv_block_lu_solve(self.nb, _dev_ptr(A), self.piv.data_ptr(),
+                                                           _dev_ptr(b), _dev_ptr(x),
+                                                           _stream_ptr(stream)),
+                                "gbmv_block_lu_solve")
+        return self.last_flag
+
+
+def form_newton_matrix(J, gamma, stream=None):
+    """A = I - gamma*J in place (ARKLS's SUNMatScaleAddI on the block matrix)."""
+    nb = J.numel() // 100
+    _check(load().gbmv_block_form_newton(nb, _dev_ptr(J), gamma, _stream_ptr(stream)),
+           "gbmv_block_form_newton")
+
+
+def fexpl(hydro: Hydro, chem: Chem, t, w, wdot, energy_units, precision=FP64, stream=None):
+    return _check(load().gbmv_fexpl(hydro.h, chem.c, t, _vec(w), _vec(wdot), energy_units,
+                                    precision, _stream_ptr(stream)), "gbmv_fexpl", allow=(0, -1))
+
+
+def PostprocessStep(hydro: Hydro, chem: Chem, w, energy_units, stream=None):
+    return _check(load().gbmv_postprocess_step(hydro.h, chem.c, _vec(w), energy_units,
+                                               _stream_ptr(stream)), "gbmv_postprocess_step")
+
+
+def fma_rate(fp64: bool = True) -> float:
+    """Measured peak FMA throughput (flop/s) of the FP64 or FP32 pipes."""
+    v = C.c_double()
+    _check(load().gbmv_diag_fma_rate(1 if fp64 else 0, C.byref(v)), "gbmv_diag_fma_rate")
+    return v.value
+
+
+def profile_enable(on: bool = True):
+    _check(load().gbmv_profile_enable(1 if on else 0), "gbmv_profile_enable")
+
+
+def profile_reset():
+    _check(load().gbmv_profile_reset(), "gbmv_profile_reset")
+
+
+def profile_get(family: str):
+    """(total milliseconds, launches) recorded for a kernel family since the last reset."""
+    ms, n = C.c_double(), C.c_long()
+    _check(load().gbmv_profile_get(family.encode(), C.byref(ms), C.byref(n)), "gbmv_profile_get")
+    return ms.value, n.value
+
+
+def launch_count() -> int:
+    return int(load().gbmv_launch_count())
