@@ -80,10 +80,10 @@ def test_prepare_dengo_structures(cuda, tables):
     # apply/unapply round trip: x*s/s, exactly the reference's pair of kernels
     c.apply_Dengo_scaling(chem)
     torch.cuda.synchronize()
-    assert np.array_equal(chem.cpu().numpy(), y.reshape(-1))
+    assert np.array_equal(chem.cpu().numpy().reshape(-1), y.reshape(-1))
     c.unapply_Dengo_scaling(chem)
     torch.cuda.synchronize()
-    assert np.array_equal(chem.cpu().numpy(), y.reshape(-1) / y.reshape(-1))
+    assert np.array_equal(chem.cpu().numpy().reshape(-1), y.reshape(-1) / y.reshape(-1))
 
 
 def _numpy_newton(J, gamma, b):
