@@ -81,6 +81,28 @@ int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* w
 int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
                       int precision, int flags, int* d_status, void* stream);
 
+/* fEuler without any device allocation.  This entry point has no counterpart in the
+ * reference; it exists for callers that cannot call cudaMalloc: code running under a
+ * fixed device-memory budget handed out by someone else (an integrator or application
+ * that owns every byte of HBM through its own pool), or code paths where allocating would
+ * synchronise the device at a moment the caller cannot afford.  It computes exactly what
+ * gbmv_feuler computes in the FP64 form (no handle needed: grid and the NVAR per-field force
+ * constants, host array or NULL, are passed directly), using a face-flux scratch array and a
+ * status word that are fixed-size __device__ arrays inside this library instead of
+ * cudaMalloc'ed buffers.
+ *   Limit: (5+nchem) * [(nx+1)*ny*nz + nx*(ny+1)*nz + nx*ny*(nz+1)] <= 8388608 doubles
+ *          (64 MiB, e.g. 56^3 at nchem=10, 82^3 at nchem=0); larger grids return GBMV_EINVAL
+ *          with a message, nothing is launched.  Every GPU that loads this library keeps the
+ *          64 MiB reserved until the process exits.
+ *   The first call on each device looks up the arrays' device addresses (with that device
+ *   current); make that first call before any stream capture.
+ *   All calls share the one array and status word, which keep the last call's contents: the
+ *   status word is cleared at the start of each call, but calls that overlap on the GPU
+ *   (other streams, other host threads) race on the shared scratch -- serialise them.
+ *   Synchronous on `stream` like gbmv_feuler; returns 0, GBMV_ILLEGAL_STATE, or < 0. */
+int gbmv_feuler_noalloc(const gbmv_grid* grid, const double* force_host, double t,
+                        const double* const* w, double* const* wdot, void* stream);
+
 /* stability (src/utilities.cpp:483-528): dt_stab = cfl * min(dx,dy,dz) / max(|mx/rho| + c),
  * including the reference's use of |mx/rho| for all three directions.  *dt_stab is host. */
 int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,

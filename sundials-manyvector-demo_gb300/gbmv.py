@@ -50,6 +50,8 @@ SIGNATURES = [
     ("gbmv_feuler", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_int, _VP]),
     ("gbmv_feuler_async", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_int,
                                     C.c_int, _VP, _VP]),
+    ("gbmv_feuler_noalloc", C.c_int, [C.POINTER(_Grid), _P, C.c_double, C.POINTER(_VP),
+                                      C.POINTER(_VP), _VP]),
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
     ("gbmv_chem_create", C.c_int, [C.c_long, _P, C.c_double, C.POINTER(_VP)]),
     ("gbmv_chem_destroy", C.c_int, [_VP]),
