@@ -3,79 +3,100 @@
 // reference's SUNLinSol_RankLocalLS / SUNLinSol_BDMPIMV wrappers,
 // src/multirate_chem_hydro_main.cpp:1312-1411, src/imex_chem_hydro_main.cpp:1075-1194).
 //
-// One thread owns one block; the whole 10x10 block lives in registers (fully unrolled loops
-// with compile-time indices), row interchanges are predicated selects.  Blocks are read and
-// written through shared memory so that global traffic is coalesced: a warp stages its 32
-// consecutive blocks (32 x 800 B, contiguous) with unit-stride loads.
+// One thread owns one block; the whole 10x10 block lives in registers (fully unrolled through
+// template recursion, compile-time indices), row interchanges are predicated selects.  A CTA
+// stages 128 consecutive blocks (102 KB, contiguous in HBM) through shared memory with
+// 16-byte coalesced accesses; two CTAs per SM overlap one tile's traffic with the other's
+// arithmetic.
 #include "chem.cuh"
 
 namespace gbmv {
 
-constexpr int kLuThreads = 64;
+constexpr int kLuThreads = 128;  // blocks per tile = threads per CTA
+constexpr int kLuStride = 101;   // padded per-block stride of the shared tile (doubles)
 
-// Coalesced copy of nb_here consecutive blocks between global and a shared tile laid out
-// element-major ([e][thread], conflict-free per-thread access).
-template <typename T, int NE>
-__device__ __forceinline__ void stage_in(const T* __restrict__ g, T* sh, long blk0, int nb_here) {
-  const long base = blk0 * NE;
-  for (int t = threadIdx.x; t < nb_here * NE; t += blockDim.x) {
-    const int b = t / NE, e = t % NE;
-    sh[e * kLuThreads + b] = g[base + t];
+// Coalesced copy of `nb` consecutive blocks of NE doubles between global memory and a shared
+// tile with per-block stride kLuStride (16-byte global accesses when NE is even).
+template <int NE>
+__device__ __forceinline__ void tile_in(const double* __restrict__ g, double* sh, long blk0, int nb) {
+  const double* src = g + blk0 * NE;
+  if (NE % 2 == 0) {
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    for (int c = threadIdx.x; c < nb * NE / 2; c += blockDim.x) {
+      const double2 v = s2[c];
+      const int b = (2 * c) / NE, e = (2 * c) % NE;
+      sh[b * kLuStride + e] = v.x;
+      sh[b * kLuStride + e + 1] = v.y;
+    }
+  } else {
+    for (int c = threadIdx.x; c < nb * NE; c += blockDim.x) sh[(c / NE) * kLuStride + c % NE] = src[c];
   }
 }
-template <typename T, int NE>
-__device__ __forceinline__ void stage_out(T* __restrict__ g, const T* sh, long blk0, int nb_here) {
-  const long base = blk0 * NE;
-  for (int t = threadIdx.x; t < nb_here * NE; t += blockDim.x) {
-    const int b = t / NE, e = t % NE;
-    g[base + t] = sh[e * kLuThreads + b];
+template <int NE>
+__device__ __forceinline__ void tile_out(double* __restrict__ g, const double* sh, long blk0, int nb) {
+  double* dst = g + blk0 * NE;
+  if (NE % 2 == 0) {
+    double2* d2 = reinterpret_cast<double2*>(dst);
+    for (int c = threadIdx.x; c < nb * NE / 2; c += blockDim.x) {
+      const int b = (2 * c) / NE, e = (2 * c) % NE;
+      d2[c] = make_double2(sh[b * kLuStride + e], sh[b * kLuStride + e + 1]);
+    }
+  } else {
+    for (int c = threadIdx.x; c < nb * NE; c += blockDim.x) dst[c] = sh[(c / NE) * kLuStride + c % NE];
   }
 }
 
-// In-register LU with partial pivoting (first maximal |pivot|, full-row interchanges, the
-// dgetf2 order).  Returns 0 or 1 + first zero-pivot column.
+// One elimination step KK of LU with partial pivoting (first maximal |pivot|, full-row
+// interchange, the dgetf2 order), fully unrolled through template recursion so the block
+// stays in registers.  The factor keeps 1/U(k,k) on the diagonal (the solve only multiplies);
+// the factored matrix is private to this solver, as MAGMA's is to its own getrs.
+template <int KK, typename R>
+__device__ __forceinline__ void lu_step(R (&A)[100], int (&piv)[10], int& info) {
+  int p = KK;
+  R amax = fabs(A[KK * 10 + KK]);
+#pragma unroll
+  for (int r = KK + 1; r < 10; ++r) {
+    const R v = fabs(A[KK * 10 + r]);
+    if (v > amax) { amax = v; p = r; }
+  }
+  piv[KK] = p;
+#pragma unroll
+  for (int r = KK + 1; r < 10; ++r) {
+    const bool sw = (r == p);
+#pragma unroll
+    for (int col = 0; col < 10; ++col) {
+      const R a = A[col * 10 + KK], b = A[col * 10 + r];
+      A[col * 10 + KK] = sw ? b : a;
+      A[col * 10 + r] = sw ? a : b;
+    }
+  }
+  const R d = A[KK * 10 + KK];
+  if (d == R(0)) {
+    if (!info) info = KK + 1;
+  } else {
+    const R rp = R(1) / d;
+    A[KK * 10 + KK] = rp;
+#pragma unroll
+    for (int r = KK + 1; r < 10; ++r) A[KK * 10 + r] *= rp;
+#pragma unroll
+    for (int col = KK + 1; col < 10; ++col) {
+      const R a = A[col * 10 + KK];
+#pragma unroll
+      for (int r = KK + 1; r < 10; ++r) A[col * 10 + r] -= A[KK * 10 + r] * a;
+    }
+  }
+  if constexpr (KK < 9) lu_step<KK + 1>(A, piv, info);
+}
+
 template <typename R>
 __device__ __forceinline__ int lu10_regs(R (&A)[100], int (&piv)[10]) {
   int info = 0;
-#pragma unroll
-  for (int kk = 0; kk < 10; ++kk) {
-    int p = kk;
-    R amax = fabs(A[kk * 10 + kk]);
-#pragma unroll
-    for (int r = kk + 1; r < 10; ++r) {
-      const R v = fabs(A[kk * 10 + r]);
-      if (v > amax) { amax = v; p = r; }
-    }
-    piv[kk] = p;
-    // predicated interchange of rows kk and p across all columns
-#pragma unroll
-    for (int r = kk + 1; r < 10; ++r) {
-      const bool sw = (r == p);
-#pragma unroll
-      for (int col = 0; col < 10; ++col) {
-        const R a = A[col * 10 + kk], b = A[col * 10 + r];
-        A[col * 10 + kk] = sw ? b : a;
-        A[col * 10 + r] = sw ? a : b;
-      }
-    }
-    const R d = A[kk * 10 + kk];
-    if (d == R(0)) {
-      if (!info) info = kk + 1;
-    } else {
-      const R rp = R(1) / d;
-#pragma unroll
-      for (int r = kk + 1; r < 10; ++r) A[kk * 10 + r] *= rp;
-#pragma unroll
-      for (int col = kk + 1; col < 10; ++col) {
-        const R a = A[col * 10 + kk];
-#pragma unroll
-        for (int r = kk + 1; r < 10; ++r) A[col * 10 + r] -= A[kk * 10 + r] * a;
-      }
-    }
-  }
+  lu_step<0>(A, piv, info);
   return info;
 }
 
+// Solve with the factor of lu10_regs (row interchanges, unit-lower forward substitution,
+// upper back substitution multiplying by the stored reciprocal pivots).
 template <typename R, typename X>
 __device__ __forceinline__ void lus10_regs(const R (&A)[100], const int (&piv)[10], X (&x)[10]) {
 #pragma unroll
@@ -94,72 +115,71 @@ __device__ __forceinline__ void lus10_regs(const R (&A)[100], const int (&piv)[1
     for (int r = col + 1; r < 10; ++r) x[r] -= X(A[col * 10 + r]) * x[col];
 #pragma unroll
   for (int col = 9; col >= 0; --col) {
-    x[col] /= X(A[col * 10 + col]);
+    x[col] *= X(A[col * 10 + col]);
 #pragma unroll
     for (int r = 0; r < col; ++r) x[r] -= X(A[col * 10 + r]) * x[col];
   }
 }
 
-__global__ void __launch_bounds__(kLuThreads) block_lu_factor_kernel(long nb, double* __restrict__ A,
-                                                                     int* __restrict__ piv,
-                                                                     int* __restrict__ info_out) {
-  extern __shared__ double sh[];  // [100][kLuThreads]
-  __shared__ int shp[10 * kLuThreads];
+__global__ void __launch_bounds__(kLuThreads, 2) block_lu_factor_kernel(long nb, double* __restrict__ A,
+                                                                        int* __restrict__ piv,
+                                                                        int* __restrict__ info_out) {
+  extern __shared__ double sh[];  // [kLuThreads][kLuStride]
   int bad = 0;
   for (long blk0 = (long)blockIdx.x * kLuThreads; blk0 < nb; blk0 += (long)gridDim.x * kLuThreads) {
     const int nb_here = (int)((nb - blk0) < kLuThreads ? (nb - blk0) : kLuThreads);
-    stage_in<double, 100>(A, sh, blk0, nb_here);
+    tile_in<100>(A, sh, blk0, nb_here);
     __syncthreads();
     if (threadIdx.x < nb_here) {
       double a[100];
       int p[10];
+      const double* mine = sh + threadIdx.x * kLuStride;
 #pragma unroll
-      for (int e = 0; e < 100; ++e) a[e] = sh[e * kLuThreads + threadIdx.x];
-      const int info = lu10_regs(a, p);
-      if (info && !bad) bad = 1;
+      for (int e = 0; e < 100; ++e) a[e] = mine[e];
+      if (lu10_regs(a, p)) bad = 1;
+      double* out = sh + threadIdx.x * kLuStride;
 #pragma unroll
-      for (int e = 0; e < 100; ++e) sh[e * kLuThreads + threadIdx.x] = a[e];
+      for (int e = 0; e < 100; ++e) out[e] = a[e];
+      int* pg = piv + (blk0 + threadIdx.x) * 10;
 #pragma unroll
-      for (int e = 0; e < 10; ++e) shp[e * kLuThreads + threadIdx.x] = p[e];
+      for (int e = 0; e < 10; ++e) pg[e] = p[e];
     }
     __syncthreads();
-    stage_out<double, 100>(A, sh, blk0, nb_here);
-    stage_out<int, 10>(piv, shp, blk0, nb_here);
+    tile_out<100>(A, sh, blk0, nb_here);
     __syncthreads();
   }
   if (bad) atomicMax(info_out, 1);
 }
 
-__global__ void __launch_bounds__(kLuThreads) block_lu_solve_kernel(long nb,
-                                                                    const double* __restrict__ LU,
-                                                                    const int* __restrict__ piv,
-                                                                    const double* b,
-                                                                    double* x) {
-  extern __shared__ double sh[];
-  __shared__ int shp[10 * kLuThreads];
-  __shared__ double shx[10 * kLuThreads];
+__global__ void __launch_bounds__(kLuThreads, 2) block_lu_solve_kernel(long nb,
+                                                                       const double* __restrict__ LU,
+                                                                       const int* __restrict__ piv,
+                                                                       const double* b, double* x) {
+  extern __shared__ double sh[];  // LU tile, then the right-hand sides
+  double* shb = sh + kLuThreads * kLuStride;
   for (long blk0 = (long)blockIdx.x * kLuThreads; blk0 < nb; blk0 += (long)gridDim.x * kLuThreads) {
     const int nb_here = (int)((nb - blk0) < kLuThreads ? (nb - blk0) : kLuThreads);
-    stage_in<double, 100>(LU, sh, blk0, nb_here);
-    stage_in<int, 10>(piv, shp, blk0, nb_here);
-    stage_in<double, 10>(b, shx, blk0, nb_here);
+    tile_in<100>(LU, sh, blk0, nb_here);
+    tile_in<10>(b, shb, blk0, nb_here);
     __syncthreads();
     if (threadIdx.x < nb_here) {
       double a[100], v[10];
       int p[10];
+      const double* mine = sh + threadIdx.x * kLuStride;
 #pragma unroll
-      for (int e = 0; e < 100; ++e) a[e] = sh[e * kLuThreads + threadIdx.x];
+      for (int e = 0; e < 100; ++e) a[e] = mine[e];
+      const int* pg = piv + (blk0 + threadIdx.x) * 10;
 #pragma unroll
       for (int e = 0; e < 10; ++e) {
-        p[e] = shp[e * kLuThreads + threadIdx.x];
-        v[e] = shx[e * kLuThreads + threadIdx.x];
+        p[e] = pg[e];
+        v[e] = shb[threadIdx.x * kLuStride + e];
       }
       lus10_regs(a, p, v);
 #pragma unroll
-      for (int e = 0; e < 10; ++e) shx[e * kLuThreads + threadIdx.x] = v[e];
+      for (int e = 0; e < 10; ++e) shb[threadIdx.x * kLuStride + e] = v[e];
     }
     __syncthreads();
-    stage_out<double, 10>(x, shx, blk0, nb_here);
+    tile_out<10>(x, shb, blk0, nb_here);
     __syncthreads();
   }
 }
@@ -176,13 +196,13 @@ __global__ void block_form_newton_kernel(long nel, double* __restrict__ J, doubl
 
 static int lu_grid(long nb) {
   long b = (nb + kLuThreads - 1) / kLuThreads;
-  const long cap = (long)kSM * 8;
+  const long cap = (long)kSM * 2;
   if (b < 1) b = 1;
   return (int)(b < cap ? b : cap);
 }
 
 int block_lu_factor(long nb, double* A, int* piv, int* d_info, cudaStream_t s) {
-  const size_t shm = sizeof(double) * 100 * kLuThreads;
+  const size_t shm = sizeof(double) * kLuStride * kLuThreads;
   GBMV_CUDA_TRY(cudaFuncSetAttribute(block_lu_factor_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   ProfScope ps("block_lu_factor", s);
@@ -193,7 +213,7 @@ int block_lu_factor(long nb, double* A, int* piv, int* d_info, cudaStream_t s) {
 
 int block_lu_solve(long nb, const double* LU, const int* piv, const double* b, double* x,
                    cudaStream_t s) {
-  const size_t shm = sizeof(double) * 100 * kLuThreads;
+  const size_t shm = sizeof(double) * 2 * kLuStride * kLuThreads;
   GBMV_CUDA_TRY(cudaFuncSetAttribute(block_lu_solve_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   ProfScope ps("block_lu_solve", s);
