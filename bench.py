@@ -10,7 +10,11 @@ metric: Mcells/s = cells / step time.  `value` is device-resident throughput; `e
 per-step host->device copies of the state from pinned memory and device->host copies of the
 outputs (tendency vector and Newton update) through the public Python API.
 
-  python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl gbmv|reference] [--form fp64|mixed]
+  python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl gbmv|reference]
+                  [--form best|fp64|mixed]
+--form best (default) times the plain FP64 form and the mixed-precision batched form, checks
+the mixed form's outputs against the FP64 form's (max-normalised per field), and reports the
+mixed form as the headline when that error is <= 1e-6.
 """
 from __future__ import annotations
 
@@ -43,7 +47,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gbmv", choices=["gbmv", "reference"])
-    p.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--form", default="best", choices=["best", "fp64", "mixed"])
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -107,13 +111,23 @@ class ClockSampler:
 # ----------------------------------------------------------------- the GB300 arm
 
 class FusedStep:
-    def __init__(self, torch, n, form):
+    """One fused step on device-resident state.
+
+    form "fp64" : the plain FP64 GPU form -- the drop-in entry points in the order an ARKODE
+                  IMEX/MRI stage calls them (fexpl, fimpl, Jimpl, SUNMatScaleAddI, LS setup,
+                  LS solve), every kernel in FP64;
+    form "mixed": the batched mixed-precision form -- mixed-precision WENO (FP32 flux
+                  arithmetic, float-float indicators/weights, FP64 pressure and divergence) and
+                  the fused chemistry Newton kernel (FP64 source and Jacobian, FP32 LU with two
+                  FP64-residual refinement steps, no Jacobian in HBM)."""
+
+    def __init__(self, torch, n, form, wl=None):
         import gbmv
         import h5tables
         import workloads as W
-        self.torch, self.gbmv = torch, gbmv
+        self.torch, self.gbmv, self.form = torch, gbmv, form
         self.precision = gbmv.MIXED if form == "mixed" else gbmv.FP64
-        wl = W.chem_hydro(n=n)
+        wl = wl if wl is not None else W.chem_hydro(n=n)
         self.wl = wl
         self.n = n
         self.ncell = n ** 3
@@ -123,27 +137,44 @@ class FusedStep:
         self.w = [dev(f) for f in self.host]
         self.wdot = [torch.empty_like(f) for f in self.w]
         self.f = torch.empty(10 * self.ncell, dtype=torch.float64, device="cuda")
-        self.J = torch.empty(100 * self.ncell, dtype=torch.float64, device="cuda")
         self.x = torch.empty_like(self.f)
+        self.J = (torch.empty(100 * self.ncell, dtype=torch.float64, device="cuda")
+                  if form == "fp64" else None)
         self.hydro = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"])
         self.chem = gbmv.Chem(self.ncell, h5tables.load_table_block(TABLES))
         self.chem.set_scale(dev(wl["scale"].reshape(-1)))
-        self.ls = gbmv.BlockLinearSolver(self.ncell)
+        self.ls = gbmv.BlockLinearSolver(self.ncell) if form == "fp64" else None
         torch.cuda.synchronize()
 
+    def reset(self):
+        """Back to the initial state (fields and the chemistry temperature history)."""
+        for d, h in zip(self.w, self.host):
+            d.copy_(self.torch.from_numpy(h))
+        self.chem.state("Ts").fill_(1000.0)
+        self.torch.cuda.synchronize()
+
     def step(self, t=0.0):
-        g, torch = self.gbmv, self.torch
+        g = self.gbmv
         EU, TU = self.units["EnergyUnits"], self.units["TimeUnits"]
         rc = g.fexpl(self.hydro, self.chem, t, self.w, self.wdot, EU, self.precision)
         if rc != 0:
             raise RuntimeError(f"fexpl returned {rc}")
         y = self.w[5].view(-1)
-        self.chem.calculate_rhs_cvklu(t, y, self.f, TU)
-        self.chem.calculate_jacobian_cvklu(t, y, self.J, TU)
-        g.form_newton_matrix(self.J, GAMMA_NEWTON)
-        if self.ls.setup(self.J) != 0:
-            raise RuntimeError("singular Newton block")
-        self.ls.solve(self.J, self.x, self.f)
+        if self.form == "fp64":
+            self.chem.calculate_rhs_cvklu(t, y, self.f, TU)
+            self.chem.calculate_jacobian_cvklu(t, y, self.J, TU)
+            g.form_newton_matrix(self.J, GAMMA_NEWTON)
+            if self.ls.setup(self.J) != 0:
+                raise RuntimeError("singular Newton block")
+            self.ls.solve(self.J, self.x, self.f)
+        else:
+            if self.chem.newton_iteration(t, y, self.f, self.x, GAMMA_NEWTON, TU,
+                                          lu_precision=g.MIXED, refine=2) != 0:
+                raise RuntimeError("singular Newton block")
+
+    def outputs(self):
+        outs = [t.cpu().numpy() for t in self.wdot]
+        return outs + [self.f.cpu().numpy(), self.x.cpu().numpy()]
 
     def bytes_in(self):
         return sum(a.nbytes for a in self.host)
@@ -174,72 +205,117 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def run_gbmv(args):
-    import torch
-    import gbmv
-    import build_lib
-    if not os.path.exists(build_lib.LIB):
-        build_lib.build()
-    gbmv.load()
-    torch.cuda.set_device(0)
-    fs = FusedStep(torch, args.n, args.form)
-    ncell = fs.ncell
+FAMILIES = ("face_flux", "divergence", "prims", "chem_rhs", "chem_jac", "chem_newton",
+            "block_lu_factor", "block_lu_solve", "glue")
 
-    # device-resident timed region (profiling events on the launching stream)
-    for _ in range(args.warmup):
+
+def algo_bytes(fam, n):
+    """Algorithmic bytes per launch: inputs read once, outputs written once."""
+    ncell, nvar = n ** 3, 15
+    nf = (n + 1) * n * n
+    return {
+        "face_flux": 8 * nvar * (ncell + nf),           # FP64 form: state in, fluxes out
+        "face_flux_mx": 4 * (16 * ncell + nvar * nf),   # mixed form: FP32 copies in, FP32 fluxes out
+        "divergence": 8 * nvar * (3 * nf + ncell) + 8 * 5 * ncell,
+        "prims": 8 * nvar * ncell + 4 * 16 * ncell,
+        "chem_rhs": 368 * ncell,
+        "chem_jac": (34 * 8 + 800) * ncell,
+        "chem_newton": 456 * ncell,
+        "block_lu_factor": 1640 * ncell,
+        "block_lu_solve": 1000 * ncell,
+        "glue": 0,
+    }[fam]
+
+
+def timed_form(torch, gbmv, fs, steps, warmup):
+    for _ in range(warmup):
         fs.step()
     torch.cuda.synchronize()
     gbmv.profile_reset()
     gbmv.profile_enable(True)
-    launches0 = gbmv.launch_count()
+    l0 = gbmv.launch_count()
     with ClockSampler(0) as clk:
-        ms = time_steps(torch, fs.step, args.steps, 0)
-    launches = gbmv.launch_count() - launches0
+        ms = time_steps(torch, fs.step, steps, 0)
+    launches = gbmv.launch_count() - l0
     gbmv.profile_enable(False)
-    fam = {f: gbmv.profile_get(f) for f in ("face_flux", "divergence", "chem_rhs", "chem_jac",
-                                            "block_lu_factor", "block_lu_solve", "glue")}
-    value = ncell / (ms * 1e-3) / 1e6
+    fam = {f: gbmv.profile_get(f) for f in FAMILIES}
+    return ms, fam, launches, clk.summary()
 
-    # roofline of the dominant kernel family (largest share of the step)
+
+def run_gbmv(args):
+    import torch
+    import gbmv
+    import build_lib
+    import workloads as W
+    if not os.path.exists(build_lib.LIB):
+        build_lib.build()
+    gbmv.load()
+    torch.cuda.set_device(0)
+    wl = W.chem_hydro(n=args.n)
+    forms = ["fp64", "mixed"] if args.form == "best" else [args.form]
+    res = {}
+    for form in forms:
+        fs = FusedStep(torch, args.n, form, wl)
+        ms, fam, launches, clk = timed_form(torch, gbmv, fs, args.steps, args.warmup)
+        fs.reset()
+        fs.step()
+        torch.cuda.synchronize()
+        res[form] = dict(fs=fs, ms=ms, fam=fam, launches=launches, clocks=clk, out=fs.outputs())
+        if form != forms[-1]:
+            del fs.J
+            res[form]["fs"] = None
+            torch.cuda.empty_cache()
+    ncell = args.n ** 3
+    errs = None
+    if "fp64" in res and "mixed" in res:
+        names = ["rho", "mx", "my", "mz", "et", "chem", "fimpl", "newton_x"]
+        ref, mx = res["fp64"]["out"], res["mixed"]["out"]
+        errs = {}
+        for nm, a, b in zip(names, mx, ref):
+            if nm in ("chem", "fimpl", "newton_x"):
+                a2, b2 = a.reshape(-1, 10), b.reshape(-1, 10)
+                e = max(float(np.max(np.abs(a2[:, s] - b2[:, s])) / max(np.max(np.abs(b2[:, s])), 1e-300))
+                        for s in range(10))
+            else:
+                e = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+            errs[nm] = e
+    head = "mixed" if ("mixed" in res and (errs is None or max(errs.values()) <= 1e-6)) else forms[0]
+    R = res[head]
+    ms, fam = R["ms"], R["fam"]
+    value = ncell / (ms * 1e-3) / 1e6
     dom = max(fam, key=lambda k: fam[k][0])
     hbm_peak, peak_kind = measured_peaks()
     fp64_peak = gbmv.fma_rate(True) / 1e12
-    nvar = 15
-    nf = (args.n + 1) * args.n * args.n
-    algo_bytes = {  # algorithmic bytes per launch (inputs read once, outputs written once)
-        "face_flux": 8 * nvar * (ncell + nf),
-        "divergence": 8 * nvar * (3 * nf + ncell) + 8 * 5 * ncell,
-        "chem_rhs": 368 * ncell,
-        "chem_jac": (34 * 8 + 800) * ncell,
-        "block_lu_factor": 1600 * ncell + 40 * ncell,
-        "block_lu_solve": (800 + 40 + 160) * ncell,
-        "glue": 0,
-    }
     dt_ms, nl = fam[dom]
     avg_ms = dt_ms / max(nl, 1)
-    achieved = algo_bytes.get(dom, 0) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
-
+    key = "face_flux_mx" if (dom == "face_flux" and head == "mixed") else dom
+    achieved = algo_bytes(key, args.n) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mcells/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.form == "fp64" else "f64/f32 mixed",
+        "dtype": "f64" if head == "fp64" else "f64 state; f32 + float-float WENO, f32 LU + f64 refinement",
         "data": "synthetic (seeded numpy PCG64; rate tables from the reference's primordial_tables.h5)",
         "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "nvar": 15, "cells": ncell,
-                   "form": args.form, "newton_gamma": GAMMA_NEWTON,
-                   "l2": "inputs larger than L2 (state 252 MB, Jacobian 1.68 GB)"},
+                   "form": head, "newton_gamma": GAMMA_NEWTON,
+                   "l2": "inputs larger than L2 (state 252 MB)"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
                      "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
                      "peak_kind": f"{peak_kind} hbm_gbs", "traffic": None,
                      "avg_launch_ms": round(avg_ms, 4),
                      "fp64_peak_tflops_measured": round(fp64_peak, 4)},
-        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in fam.items()},
-        "gpu_launches": int(launches),
-        "clocks": clk.summary(),
+        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in fam.items() if v[1]},
+        "gpu_launches": int(R["launches"]),
+        "clocks": R["clocks"],
+        "forms": {f: {"ms_per_step": round(r["ms"], 4),
+                      "value": round(ncell / (r["ms"] * 1e-3) / 1e6, 3)} for f, r in res.items()},
     }
+    if errs is not None:
+        line["mixed_vs_fp64_maxnorm_err"] = {k: float(f"{v:.3e}") for k, v in errs.items()}
+        line["speedup_vs_fp64_form"] = round(res["fp64"]["ms"] / res["mixed"]["ms"], 3)
 
     if not args.no_e2e:
-        # end to end through the public API: pinned host state -> device, step, results -> host
+        fs = R["fs"] if R["fs"] is not None else FusedStep(torch, args.n, head, wl)
         pin_in = [torch.from_numpy(a).pin_memory() for a in fs.host]
         pin_out = [torch.empty(t.shape, dtype=torch.float64).pin_memory() for t in fs.wdot]
         pin_x = torch.empty(fs.x.shape, dtype=torch.float64).pin_memory()

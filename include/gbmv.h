@@ -36,8 +36,10 @@ extern "C" {
 #define GBMV_BC_REFLECTING 3
 
 /* Arithmetic of the WENO flux-divergence. */
-#define GBMV_FP64 0   /* all arithmetic in FP64 (parity form: <=1e-12 vs the reference) */
-#define GBMV_MIXED 1  /* mixed-precision form (<=1e-6 vs the FP64 oracle) */
+#define GBMV_FP64 0        /* all arithmetic in FP64 (parity form: <=1e-12 vs the reference) */
+#define GBMV_MIXED 1       /* FP32 flux arithmetic, float-float smoothness indicators and
+                              weights, FP64 pressure and divergence (<=1e-6 vs the FP64 oracle) */
+#define GBMV_MIXED_F64W 2  /* as GBMV_MIXED with native FP64 indicators and weights */
 
 /* Grid + problem description: the fields of EulerData the RHS needs
  * (src/euler3D.hpp:183-253).  nchem must be one of 0, 2, 4, 6, 10 (NVAR 5, 7, 9, 11, 15,
@@ -143,6 +145,18 @@ int gbmv_chem_rhs(gbmv_chem c, double t, const double* y, double* ydot, double t
  * times time_units (Jfast/Jimpl, src/multirate_chem_hydro_main.cpp:976-983). */
 int gbmv_chem_jac(gbmv_chem c, double t, const double* y, double* J, double time_units,
                   void* stream);
+
+/* One batched Newton iteration of the implicit chemistry stage, fused (no Jacobian in HBM):
+ *   f = time_units * f_chem(y)           -- exactly gbmv_chem_rhs (temperature state updated)
+ *   x = (I - gamma * J(y))^{-1} f        -- J as gbmv_chem_jac, A as gbmv_block_form_newton,
+ *                                           solve as gbmv_block_lu_factor + _solve
+ * i.e. Jfast/Jimpl + ARKLS setup + Solve_RankLocalLS of src/multirate_chem_hydro_main.cpp:
+ * 954-1395 for one right-hand side, in one kernel.  lu_precision: GBMV_FP64 (FP64 LU) or
+ * GBMV_MIXED (FP32 LU + `refine` iterative-refinement steps against FP64 residuals, FP64
+ * fallback for blocks whose FP32 factor fails).  Returns 0, or 1 if a block is singular. */
+int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* x,
+                     double gamma, double time_units, int lu_precision, int refine,
+                     void* stream);
 
 /* Device pointers of the persistent per-cell state (for checkpoint/restart and tests):
  * which: 0 Ts, 1 dTs_ge, 2 mdensity, 3 inv_mdensity, 4 cie optical depth, 5 h2 optical depth,

@@ -67,6 +67,7 @@ struct gbmv_hydro_s {
   ForceTerm force;
   double* scratch = nullptr;
   size_t scratch_doubles = 0;
+  float* scratch32 = nullptr;  // mixed-precision form, allocated on its first use
   int* d_status = nullptr;
 };
 
@@ -176,6 +177,7 @@ int gbmv_hydro_create(const gbmv_grid* grid, gbmv_hydro* out) {
 int gbmv_hydro_destroy(gbmv_hydro h) {
   if (!h) return GBMV_OK;
   cudaFree(h->scratch);
+  cudaFree(h->scratch32);
   cudaFree(h->d_status);
   delete h;
   return GBMV_OK;
@@ -194,7 +196,7 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
     set_error("null handle, field or status pointer");
     return GBMV_EINVAL;
   }
-  if (precision != GBMV_FP64 && precision != GBMV_MIXED) {
+  if (precision != GBMV_FP64 && precision != GBMV_MIXED && precision != GBMV_MIXED_F64W) {
     set_error("unknown precision %d", precision);
     return GBMV_EINVAL;
   }
@@ -207,8 +209,17 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
   ForceTerm G = h->force;
   G.in_wdot = (flags & GBMV_FORCE_IN_WDOT) ? 1 : 0;
   cudaStream_t s = (cudaStream_t)stream;
-  // GBMV_MIXED falls back to the FP64 form until the mixed kernel is selected by the caller
-  return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
+  if (precision == GBMV_FP64) return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
+  if (!h->scratch32) {
+    const size_t nf = feuler_mixed_scratch_floats(h->g);
+    if (cudaMalloc(&h->scratch32, nf * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      h->scratch32 = nullptr;
+      set_error("device allocation of %zu mixed-precision scratch floats failed", nf);
+      return GBMV_ENOMEM;
+    }
+  }
+  return feuler_mixed(h->g, W, Wd, G, h->scratch32, d_status, precision == GBMV_MIXED_F64W, s);
 }
 
 int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
@@ -350,6 +361,27 @@ int gbmv_chem_jac(gbmv_chem c, double t, const double* y, double* J, double time
   (void)t;
   if (!c || !y || !J) { set_error("null argument"); return GBMV_EINVAL; }
   return chem_jac(c->P, c->S, c->n, y, J, time_units, (cudaStream_t)stream);
+}
+
+int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* x,
+                     double gamma, double time_units, int lu_precision, int refine,
+                     void* stream) {
+  (void)t;
+  if (!c || !y || !f || !x || refine < 0 || refine > 8 ||
+      (lu_precision != GBMV_FP64 && lu_precision != GBMV_MIXED)) {
+    set_error("bad chem_newton arguments");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  GBMV_CUDA_TRY(cudaMemsetAsync(c->d_info, 0, sizeof(int), s));
+  int rc = chem_newton(c->P, c->S, c->n, y, f, x, gamma, time_units, lu_precision == GBMV_MIXED,
+                       refine, c->d_info, s);
+  if (rc) return rc;
+  int h = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&h, c->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h) { set_error("singular Newton block"); return 1; }
+  return GBMV_OK;
 }
 
 /* ------------------------------------------------------------------ block solve */

@@ -42,25 +42,21 @@ __global__ void __launch_bounds__(128) chem_jac_kernel(ChemParams P, ChemState S
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
        i += (long)gridDim.x * blockDim.x) {
     const long j = i * 10;
-    double ya[10], sc[10], isc[10];
+    const double* __restrict__ sc = S.scale + j;
+    const double* __restrict__ isc = S.inv_scale + j;
+    double ya[10];
 #pragma unroll
-    for (int s = 0; s < 10; ++s) {
-      sc[s] = S.scale[j + s];
-      isc[s] = S.inv_scale[j + s];
-      ya[s] = y[j + s] * sc[s];
-    }
+    for (int s = 0; s < 10; ++s) ya[s] = y[j + s] * sc[s];
     const double T = S.Ts[i];
     double k[kNRates], dk[kNRates];
     chem_rates<true>(P, T, k, dk);
     const ChemAux A{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
-    double B[100];
-    chem_jacobian(P, k, dk, ya, T, S.dTs_ge[i], A, B);
     double* out = J + 100 * i;
 #pragma unroll
-    for (int col = 0; col < 10; ++col)
-#pragma unroll
-      for (int row = 0; row < 10; ++row)
-        out[col * 10 + row] = (B[col * 10 + row] * (isc[row] * sc[col])) * tunit;
+    for (int e = 0; e < 100; ++e) out[e] = 0.0;
+    chem_jacobian(P, k, dk, ya, T, S.dTs_ge[i], A, [&](int row, int col, double v) {
+      out[col * 10 + row] = (v * (isc[row] * sc[col])) * tunit;
+    });
   }
 }
 

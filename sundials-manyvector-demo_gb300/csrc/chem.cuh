@@ -32,6 +32,11 @@ int energy_sync(const ChemState& S, double* const* w, long n, int nchem, double 
 int energy_epilogue(const ChemState& S, double* chem, double* chemdot, double* etdot, long n,
                     int nchem, cudaStream_t s);
 
+// fused source + Jacobian + Newton matrix + LU solve (chem_newton.cu)
+int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
+                double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
+                cudaStream_t s);
+
 // batched 10x10 LU (blocklu.cu)
 int block_lu_factor(long nb, double* A, int* piv, int* d_info, cudaStream_t s);
 int block_lu_solve(long nb, const double* LU, const int* piv, const double* b, double* x,

@@ -164,18 +164,19 @@ __device__ __forceinline__ double chem_ge_source(const ChemParams& P, const doub
          cie * k[COMPTON] * de * P.zp1_4 * (T - 2.73 * z - 2.73) + 0.5 / F * Hf;
 }
 
-// Analytic Jacobian block (column-major B[col*10+row]) in physical units, before the
-// inv_scale*scale and time-unit factors; rates k and slopes dk at the cell temperature.
+// Analytic Jacobian in physical units, before the inv_scale*scale and time-unit factors;
+// rates k and slopes dk at the cell temperature.  Each of the 64 nonzeros is handed to
+// put(row, col, value) once, already multiplied by the factors the reference applies to that
+// entry (1/mdensity on the ge row, dT/dge on the ge column); entries never put are zero.
+template <class Put>
 __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double (&k)[kNRates],
                                               const double (&dk)[kNRates], const double (&y)[10],
-                                              double T, double Tge, const ChemAux& A,
-                                              double (&B)[100]) {
+                                              double T, double Tge, const ChemAux& A, Put&& put) {
   const double H2_1 = y[0], H2_2 = y[1], H_1 = y[2], H_2 = y[3], H_m0 = y[4], He_1 = y[5],
                He_2 = y[6], He_3 = y[7], de = y[8];
-  const double z = P.z, h2oda = A.h2, md = A.mdens;
-#pragma unroll
-  for (int e = 0; e < 100; ++e) B[e] = 0.0;
-#define SETJ(row, col, expr) B[(col) * 10 + (row)] = (expr)
+  const double z = P.z, h2oda = A.h2, md = A.mdens, imd = A.imdens;
+#define SETJ(row, col, expr) put(row, col, (expr))
+#define SETG(col, expr) put(9, col, (expr) * imd)
   const double H1sq = H_1 * H_1;
   SETJ(0, 0, -k[K11] * H_2 - k[K12] * de - k[K13] * H_1 + k[K21] * H1sq);
   SETJ(0, 1, k[K10] * H_1 + k[K19] * H_m0);
@@ -234,7 +235,7 @@ __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double 
     chem_fluxes(dk, y, r);
     chem_species(r, s);
 #pragma unroll
-    for (int q = 0; q < 9; ++q) B[90 + q] = s[q] * Tge;
+    for (int q = 0; q < 9; ++q) put(q, 9, s[q] * Tge);
   }
   const double G = H2_1 * k[GAH2] + H_1 * k[GAHI] + H_2 * k[GAHP] + He_1 * k[GAHE] + de * k[GAEL];
   const double D = k[H2LTE] / G + 1.0;
@@ -246,34 +247,33 @@ __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double 
   const double DG2 = (D * D) * (G * G);
   const double iF2 = 1.0 / (F * F);
   const double N2 = N * N;
-  SETJ(9, 0, -H2_1 * k[GAH2] * lte2 * h2oda / DG2 - 0.5 * H_1 * k[H2MCOOL] / F -
+  SETG(0, -H2_1 * k[GAH2] * lte2 * h2oda / DG2 - 0.5 * H_1 * k[H2MCOOL] / F -
                  2.01588 * k[CIECO] * md - k[H2LTE] * h2oda / D +
                  0.5 * k[NCRD2] * k[NCRN] * iF2 * Hf / N2);
-  SETJ(9, 2, -H2_1 * k[GAHI] * lte2 * h2oda / DG2 - k[CEHI] * de - k[CIHI] * de +
+  SETG(2, -H2_1 * k[GAHI] * lte2 * h2oda / DG2 - k[CEHI] * de - k[CIHI] * de +
                  0.5 * k[NCRD1] * k[NCRN] * iF2 * Hf / N2 +
                  0.5 * (-H2_1 * k[H2MCOOL] + 3 * H1sq * k[H2MHEAT]) / F);
-  SETJ(9, 3, -H2_1 * k[GAHP] * lte2 * h2oda / DG2 - k[BREM] * de - de * k[REHII]);
-  SETJ(9, 5, -H2_1 * k[GAHE] * lte2 * h2oda / DG2 - k[CIHEI] * de);
-  SETJ(9, 6, -k[BREM] * de - k[CEHEII] * de - k[CEHEI] * (de * de) - k[CIHEII] * de -
+  SETG(3, -H2_1 * k[GAHP] * lte2 * h2oda / DG2 - k[BREM] * de - de * k[REHII]);
+  SETG(5, -H2_1 * k[GAHE] * lte2 * h2oda / DG2 - k[CIHEI] * de);
+  SETG(6, -k[BREM] * de - k[CEHEII] * de - k[CEHEI] * (de * de) - k[CIHEII] * de -
                  k[CIHEIS] * (de * de) - de * k[REHEII1] - de * k[REHEII2]);
-  SETJ(9, 7, -4.0 * k[BREM] * de - de * k[REHEIII]);
-  SETJ(9, 8, -H2_1 * k[GAEL] * lte2 * h2oda / DG2 - H_1 * k[CEHI] - H_1 * k[CIHI] -
+  SETG(7, -4.0 * k[BREM] * de - de * k[REHEIII]);
+  SETG(8, -H2_1 * k[GAEL] * lte2 * h2oda / DG2 - H_1 * k[CEHI] - H_1 * k[CIHI] -
                  H_2 * k[REHII] - He_1 * k[CIHEI] - He_2 * k[CEHEII] - 2 * He_2 * k[CEHEI] * de -
                  He_2 * k[CIHEII] - 2 * He_2 * k[CIHEIS] * de - He_2 * k[REHEII1] -
                  He_2 * k[REHEII2] - He_3 * k[REHEIII] - k[BREM] * (H_2 + He_2 + 4.0 * He_3) -
                  k[COMPTON] * P.zp1_4 * (T - 2.73 * z - 2.73));
   const double dGn = -H2_1 * dk[GAH2] - H_1 * dk[GAHI] - H_2 * dk[GAHP] - He_1 * dk[GAHE] -
                      de * dk[GAEL];
-  SETJ(9, 9, -H2_1 * k[H2LTE] * h2oda * (-k[H2LTE] * dGn / (G * G) - dk[H2LTE] / G) / (D * D) -
+  put(9, 9, (-H2_1 * k[H2LTE] * h2oda * (-k[H2LTE] * dGn / (G * G) - dk[H2LTE] / G) / (D * D) -
                  H2_1 * h2oda * dk[H2LTE] / D +
                  0.5 * iF2 * Hf *
                      (-1.0 * k[NCRN] * (-H2_1 * dk[NCRD2] - H_1 * dk[NCRD1]) / N2 -
                       1.0 * dk[NCRN] / N) +
-                 0.5 / F * (-H2_1 * H_1 * dk[H2MCOOL] + H13 * dk[H2MHEAT]));
+                 0.5 / F * (-H2_1 * H_1 * dk[H2MCOOL] + H13 * dk[H2MHEAT])) * imd * Tge);
+#undef SETG
 #undef SETJ
-#pragma unroll
-  for (int col = 0; col < 10; ++col) B[col * 10 + 9] *= A.imdens;
-  B[99] *= Tge;
 }
+
 
 }  // namespace gbmv

@@ -25,7 +25,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libgbmv.so")
 
 BC_PERIODIC, BC_NEUMANN, BC_DIRICHLET, BC_REFLECTING = 0, 1, 2, 3
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_F64W = 0, 1, 2
 FORCE_IN_WDOT = 1
 
 
@@ -62,6 +62,8 @@ SIGNATURES = [
     ("gbmv_chem_rhs", C.c_int, [_VP, C.c_double, _VP, _VP, C.c_double, _VP]),
     ("gbmv_chem_jac", C.c_int, [_VP, C.c_double, _VP, _VP, C.c_double, _VP]),
     ("gbmv_chem_state", _VP, [_VP, C.c_int]),
+    ("gbmv_chem_newton", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double, C.c_double,
+                                   C.c_int, C.c_int, _VP]),
     ("gbmv_block_lu_factor", C.c_int, [C.c_long, _VP, _VP, _VP]),
     ("gbmv_block_lu_solve", C.c_int, [C.c_long, _VP, _VP, _VP, _VP, _VP]),
     ("gbmv_block_form_newton", C.c_int, [C.c_long, _VP, C.c_double, _VP]),
@@ -213,6 +215,14 @@ class Chem:
     def calculate_rhs_cvklu(self, t, y, ydot, time_units=1.0, stream=None):
         return _check(load().gbmv_chem_rhs(self.c, t, _dev_ptr(y), _dev_ptr(ydot), time_units,
                                            _stream_ptr(stream)), "gbmv_chem_rhs")
+
+    def newton_iteration(self, t, y, f, x, gamma, time_units=1.0, lu_precision=FP64, refine=2,
+                         stream=None) -> int:
+        """Fused f = TimeUnits*f(y) and x = (I - gamma*J(y))^{-1} f; 0, or 1 if singular."""
+        return _check(load().gbmv_chem_newton(self.c, t, _dev_ptr(y), _dev_ptr(f), _dev_ptr(x),
+                                              gamma, time_units, lu_precision, refine,
+                                              _stream_ptr(stream)),
+                      "gbmv_chem_newton", allow=(0, 1))
 
     def calculate_jacobian_cvklu(self, t, y, J, time_units=1.0, stream=None):
         return _check(load().gbmv_chem_jac(self.c, t, _dev_ptr(y), _dev_ptr(J), time_units,

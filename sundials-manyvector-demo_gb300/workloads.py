@@ -127,7 +127,7 @@ def chem_hydro(n=128, seed=SEED_BASE + 3, shape=None, perturb=1e-3):
 
     Density: planar Sod-like interface along x (1e2 m_H left, 0.125e2 m_H right, g/cm^3),
     temperature 2000 K left / 1600 K right (pressure ratio 0.1), random primordial mass
-    fractions per cell, small random velocities.  Returned in the reference's working
+    fractions per cell, random velocities of up to 10% of the local sound speed.  Returned in the reference's working
     representation after prepare_Dengo_structures (src/primordial_static.cpp:227-259): the
     chemistry component is ~1 (+- perturb) and `scale` holds the physical values."""
     nx, ny, nz = shape if shape is not None else (n, n, n)
@@ -143,9 +143,14 @@ def chem_hydro(n=128, seed=SEED_BASE + 3, shape=None, perturb=1e-3):
     u = derived_units(**UNITS)
     shp = (nz, ny, nx)
     rho = (dens / u["DensityUnits"]).reshape(shp)
-    vel = rng.uniform(-1e-2, 1e-2, size=(3,) + shp)
+    eint = y[:, 9].reshape(shp) / u["EnergyUnits"]
+    # velocity perturbations of 10% of the local sound speed c = sqrt(gamma p / rho) with
+    # p = (gamma - 1) * ge / EnergyUnits (the fluid energy of src/primordial_static.cpp:152)
+    gam = 5.0 / 3.0
+    cs = np.sqrt(gam * (gam - 1.0) * eint / rho)
+    vel = rng.uniform(-0.1, 0.1, size=(3,) + shp) * cs
     mx, my, mz = rho * vel[0], rho * vel[1], rho * vel[2]
-    et = y[:, 9].reshape(shp) / u["EnergyUnits"] + 0.5 / rho * (mx * mx + my * my + mz * mz)
+    et = eint + 0.5 / rho * (mx * mx + my * my + mz * mz)
     scale = y.reshape(shp + (10,)).copy()
     chem = 1.0 + rng.uniform(-perturb, perturb, size=shp + (10,))
     bc = (BC_REFLECTING, BC_REFLECTING, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC)

@@ -1,0 +1,111 @@
+"""Mixed-precision and fused forms against the FP64 oracle (GPU).
+
+Tolerance: the benchmark spec's 1e-6 relative error against the FP64 oracle, measured per field
+as max|mixed - oracle| / max|oracle| over the grid.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as O
+import workloads as W
+from conftest import maxnorm_err
+
+pytestmark = pytest.mark.gpu
+TOL_MIXED = 1e-6
+
+
+def _run(torch, wl, precision):
+    import gbmv
+    nz, ny, nx = wl["fields"][0].shape
+    h = gbmv.Hydro((nx, ny, nz), wl["nchem"], wl["bc"], wl["gamma"], wl["force"])
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    wdot = [torch.full_like(f, np.nan) for f in w]
+    st = h.fEuler(0.0, w, wdot, precision)
+    torch.cuda.synchronize()
+    return st, [x.cpu().numpy() for x in wdot]
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("case", ["rt", "chemhydro", "smooth", "sod"])
+def test_mixed_weno_within_1e6_of_oracle(cuda, precision, case):
+    if case == "rt":
+        wl = W.rayleigh_taylor(shape=(32, 24, 20), nchem=10, seed=W.SEED_BASE + 300)
+    elif case == "chemhydro":
+        wl = W.chem_hydro(shape=(24, 16, 16))
+        wl["fields"][5] = wl["fields"][5] * wl["scale"]
+    elif case == "smooth":
+        wl = W.smooth_periodic(shape=(24, 24, 24), nchem=4)
+    else:
+        wl = W.sod(64, 3, 3)
+    st0, ref = O.feuler(wl["fields"], wl["nchem"], wl["bc"], wl["gamma"], wl["force"])
+    st1, out = _run(cuda, wl, precision)
+    assert st0 == st1 == 0
+    errs = [maxnorm_err(a, b) for a, b in zip(out, ref)]
+    assert max(errs) <= TOL_MIXED, errs
+
+
+def test_mixed_illegal_state_flagged(cuda):
+    wl = W.rayleigh_taylor(shape=(6, 5, 4), nchem=0)
+    wl["fields"][4][1, 1, 1] = -1.0
+    st, _ = _run(cuda, wl, 1)
+    assert st == -1
+
+
+def _chem_setup(torch, tables, n, seed):
+    import gbmv
+    y, _ = W.primordial(n, seed=seed)
+    c = gbmv.Chem(n, tables)
+    c.set_scale(torch.from_numpy(y.reshape(-1).copy()).cuda())
+    rng = np.random.default_rng(seed)
+    state = 1.0 + rng.uniform(-1e-3, 1e-3, size=10 * n)
+    return c, y.reshape(-1), state
+
+
+@pytest.mark.parametrize("lu", [0, 1])
+def test_fused_newton_matches_separate_path(cuda, tables, lu):
+    """gbmv_chem_newton == rhs + jac + (I - gamma J) + factor + solve."""
+    torch = cuda
+    import gbmv
+    n, gamma, tu = 4096, 1e-4, 1.0e11
+    c1, y, state = _chem_setup(torch, tables, n, 401)
+    c2, _, _ = _chem_setup(torch, tables, n, 401)
+    ys = torch.from_numpy(state).cuda()
+    f1 = torch.empty_like(ys)
+    J = torch.empty(100 * n, dtype=torch.float64, device="cuda")
+    x1 = torch.empty_like(ys)
+    c1.calculate_rhs_cvklu(0.0, ys, f1, tu)
+    c1.calculate_jacobian_cvklu(0.0, ys, J, tu)
+    gbmv.form_newton_matrix(J, gamma)
+    ls = gbmv.BlockLinearSolver(n)
+    assert ls.setup(J) == 0
+    ls.solve(J, x1, f1)
+    f2, x2 = torch.empty_like(ys), torch.empty_like(ys)
+    assert c2.newton_iteration(0.0, ys, f2, x2, gamma, tu, lu_precision=lu, refine=2) == 0
+    torch.cuda.synchronize()
+    a, b = f1.cpu().numpy().reshape(n, 10), f2.cpu().numpy().reshape(n, 10)
+    for s in range(10):
+        assert maxnorm_err(b[:, s], a[:, s]) <= 1e-12, s
+    xa, xb = x1.cpu().numpy().reshape(n, 10), x2.cpu().numpy().reshape(n, 10)
+    tol = 1e-12 if lu == 0 else 1e-10
+    for s in range(10):
+        assert maxnorm_err(xb[:, s], xa[:, s]) <= tol, (s, maxnorm_err(xb[:, s], xa[:, s]))
+    assert torch.equal(c1.state("Ts"), c2.state("Ts"))
+
+
+def test_fused_newton_against_oracle(cuda, tables):
+    torch = cuda
+    n, gamma, tu = 512, 3e-5, 1.0e11
+    c, y, state = _chem_setup(torch, tables, n, 402)
+    ys = torch.from_numpy(state).cuda()
+    f, x = torch.empty_like(ys), torch.empty_like(ys)
+    assert c.newton_iteration(0.0, ys, f, x, gamma, tu, lu_precision=1, refine=2) == 0
+    torch.cuda.synchronize()
+    oc = O.Chem(tables, y)
+    fr = oc.rhs(state) * tu
+    Jr = oc.jac(state) * tu
+    bad, xr = O.block_newton_solve(Jr, gamma, fr)
+    assert bad == 0
+    fo, xo = f.cpu().numpy().reshape(n, 10), x.cpu().numpy().reshape(n, 10)
+    for s in range(10):
+        assert maxnorm_err(fo[:, s], fr.reshape(n, 10)[:, s]) <= 1e-12
+        assert maxnorm_err(xo[:, s], xr.reshape(n, 10)[:, s]) <= 1e-10
