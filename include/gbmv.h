@@ -36,10 +36,10 @@ extern "C" {
 #define GBMV_BC_REFLECTING 3
 
 /* Arithmetic of the WENO flux-divergence. */
-#define GBMV_FP64 0        /* all arithmetic in FP64 (parity form: <=1e-12 vs the reference) */
-#define GBMV_MIXED 1       /* FP32 flux arithmetic, float-float smoothness indicators and
-                              weights, FP64 pressure and divergence (<=1e-6 vs the FP64 oracle) */
-#define GBMV_MIXED_F64W 2  /* as GBMV_MIXED with native FP64 indicators and weights */
+#define GBMV_FP64 0   /* all arithmetic in FP64 (parity form: <=1e-12 vs the reference) */
+#define GBMV_MIXED 1  /* face fluxes in float-float arithmetic on the FP32 pipes (~48-bit
+                         significand, native-FP64 fallback outside the float range), divergence
+                         and conservation sums in FP64 (<=1e-6 vs the FP64 oracle) */
 
 /* Grid + problem description: the fields of EulerData the RHS needs
  * (src/euler3D.hpp:183-253).  nchem must be one of 0, 2, 4, 6, 10 (NVAR 5, 7, 9, 11, 15,

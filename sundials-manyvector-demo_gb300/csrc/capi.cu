@@ -67,7 +67,6 @@ struct gbmv_hydro_s {
   ForceTerm force;
   double* scratch = nullptr;
   size_t scratch_doubles = 0;
-  float* scratch32 = nullptr;  // mixed-precision form, allocated on its first use
   int* d_status = nullptr;
 };
 
@@ -177,7 +176,6 @@ int gbmv_hydro_create(const gbmv_grid* grid, gbmv_hydro* out) {
 int gbmv_hydro_destroy(gbmv_hydro h) {
   if (!h) return GBMV_OK;
   cudaFree(h->scratch);
-  cudaFree(h->scratch32);
   cudaFree(h->d_status);
   delete h;
   return GBMV_OK;
@@ -196,7 +194,7 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
     set_error("null handle, field or status pointer");
     return GBMV_EINVAL;
   }
-  if (precision != GBMV_FP64 && precision != GBMV_MIXED && precision != GBMV_MIXED_F64W) {
+  if (precision != GBMV_FP64 && precision != GBMV_MIXED) {
     set_error("unknown precision %d", precision);
     return GBMV_EINVAL;
   }
@@ -210,16 +208,7 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
   G.in_wdot = (flags & GBMV_FORCE_IN_WDOT) ? 1 : 0;
   cudaStream_t s = (cudaStream_t)stream;
   if (precision == GBMV_FP64) return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
-  if (!h->scratch32) {
-    const size_t nf = feuler_mixed_scratch_floats(h->g);
-    if (cudaMalloc(&h->scratch32, nf * sizeof(float)) != cudaSuccess) {
-      cudaGetLastError();
-      h->scratch32 = nullptr;
-      set_error("device allocation of %zu mixed-precision scratch floats failed", nf);
-      return GBMV_ENOMEM;
-    }
-  }
-  return feuler_mixed(h->g, W, Wd, G, h->scratch32, d_status, precision == GBMV_MIXED_F64W, s);
+  return feuler_mixed(h->g, W, Wd, G, h->scratch, d_status, s);
 }
 
 int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,

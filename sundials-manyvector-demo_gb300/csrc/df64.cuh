@@ -16,7 +16,7 @@ struct f2 {
   __host__ __device__ constexpr f2() : hi(0.f), lo(0.f) {}
   __host__ __device__ constexpr f2(float h, float l) : hi(h), lo(l) {}
   // from a double constant (split into the nearest float and the rounded remainder)
-  __host__ __device__ constexpr f2(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  __host__ __device__ constexpr explicit f2(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
   __host__ __device__ constexpr explicit f2(int i) : hi((float)i), lo(0.f) {}
   __device__ __forceinline__ static f2 from(float x) { return f2(x, 0.f); }
   __device__ __forceinline__ float to_float() const { return hi + lo; }
@@ -58,6 +58,28 @@ __device__ __forceinline__ f2 operator/(f2 x, f2 y) {
   const f2 r = x - y * f2(q1, 0.f);
   const float q2 = r.hi / y.hi;
   return quick_two_sum(q1, q2);
+}
+
+// exact split of a double into hi + lo (48 of its 53 significant bits survive)
+__device__ __forceinline__ f2 f2_from_double(double d) {
+  const float h = __double2float_rn(d);
+  return f2(h, __double2float_rn(d - (double)h));
+}
+
+__device__ __forceinline__ bool operator<(f2 a, f2 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(f2 a, f2 b) { return b < a; }
+__device__ __forceinline__ bool operator<=(f2 a, f2 b) { return !(b < a); }
+__device__ __forceinline__ bool operator==(f2 a, f2 b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ f2 f2_fabs(f2 a) { return a.hi < 0.f ? -a : a; }
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) { return a * b + c; }
+
+// square root: FP32 estimate, one Newton correction in float-float
+__device__ __forceinline__ f2 f2_sqrt(f2 a) {
+  if (!(a.hi > 0.f)) return f2(0.f, 0.f);
+  const float s = sqrtf(a.hi);
+  const f2 ss = two_prod(s, s);
+  const float r = ((a.hi - ss.hi) - ss.lo + a.lo) / (2.f * s);
+  return quick_two_sum(s, r);
 }
 
 }  // namespace gbmv

@@ -20,8 +20,7 @@ size_t feuler_fp64_scratch_doubles(const Grid& g);
 int feuler_fp64(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
                 double* scratch, int* d_status, cudaStream_t s);
 
-size_t feuler_mixed_scratch_floats(const Grid& g);
 int feuler_mixed(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
-                 float* scratch, int* d_status, int fp64_weights, cudaStream_t s);
+                 double* scratch, int* d_status, cudaStream_t s);
 
 }  // namespace gbmv

@@ -1,0 +1,231 @@
+// WENO5 characteristic face flux (the reference's face_flux, src/utilities.cpp:270-479),
+// written once for two arithmetic types:
+//   T = double : the FP64 form (parity with the reference to rounding);
+//   T = f2     : float-float arithmetic (~48-bit significand) on the FP32 pipes -- the
+//                mixed-precision form.  GB300 retires FP32 FMAs 64x faster than FP64 ones, and
+//                the reference's eigenvector basis (built with c^2 where c is expected,
+//                src/utilities.cpp:309) is ill-conditioned when c is small in code units, so
+//                plain FP32 characteristic arithmetic loses too many digits; float-float keeps
+//                FP64-class accuracy.  Any split flux beyond 1e18 in magnitude (where the
+//                float exponent range would overflow a square) falls back to native FP64.
+//
+// Arrangement (both types), chosen to spend few instructions on the slow pipe:
+//   * nonlinear weights normalised by the smallest a_k = eps + beta_k (no overflow) and one
+//     final division -- for doubles the equivalent product form with ONE division;
+//   * Lax-Friedrichs splitting folded into one FMA per value (0.5 f +- (0.5 alpha) w); tracers
+//     one multiply (c_j * 0.5 (u_j +- alpha));
+//   * the sparse rows of the eigenvector matrices applied without their zeros.
+// Results agree with the reference's to a few ulps of each face flux (FP64 form).
+#pragma once
+
+#include "common.cuh"
+#include "df64.cuh"
+
+namespace gbmv {
+
+// ---- conversions used by the type-generic code
+__device__ __forceinline__ double num_from(double d, double*) { return d; }
+__device__ __forceinline__ f2 num_from(double d, f2*) { return f2_from_double(d); }
+__device__ __forceinline__ double num_to_double(double x) { return x; }
+__device__ __forceinline__ double num_to_double(f2 x) { return x.to_double(); }
+
+__device__ __forceinline__ double num_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ f2 num_sqrt(f2 x) { return f2_sqrt(x); }
+__device__ __forceinline__ double num_fabs(double x) { return fabs(x); }
+__device__ __forceinline__ f2 num_fabs(f2 x) { return f2_fabs(x); }
+__device__ __forceinline__ double num_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ f2 num_fma(f2 a, f2 b, f2 c) { return f2_fma(a, b, c); }
+
+template <typename T>
+__device__ __forceinline__ T sqrt0(T x) {
+  return x <= T(0.0) ? T(0.0) : num_sqrt(x);
+}
+
+__device__ __forceinline__ double eos64(double gamma, double rho, double mx, double my, double mz,
+                                        double et) {
+  return (gamma - 1.0) * (et - (mx * mx + my * my + mz * mz) * 0.5 / rho);
+}
+
+template <typename T>
+__device__ __forceinline__ T eos_t(T gm, T rho, T mx, T my, T mz, T et) {
+  return gm * (et - (mx * mx + my * my + mz * mz) * T(0.5) / rho);
+}
+
+// Smoothness indicators of the three candidate stencils of f0..f4 (Jiang-Shu, as the
+// reference: beta = 13/12 (second difference)^2 + 1/4 (first-difference combination)^2).
+template <typename T>
+__device__ __forceinline__ void weno_betas(T f0, T f1, T f2_, T f3, T f4, T& bA, T& bB, T& bC) {
+  const T b13 = T(13.0 / 12.0), q = T(0.25);
+  const T dA = f2_ - T(2.0) * f3 + f4, eA = T(3.0) * f2_ - T(4.0) * f3 + f4;
+  const T dB = f1 - T(2.0) * f2_ + f3, eB = f1 - f3;
+  const T dC = f0 - T(2.0) * f1 + f2_, eC = f0 - T(4.0) * f1 + T(3.0) * f2_;
+  bA = b13 * (dA * dA) + q * (eA * eA);
+  bB = b13 * (dB * dB) + q * (eB * eB);
+  bC = b13 * (dC * dC) + q * (eC * eC);
+}
+
+// sum_k q_k d_k / a_k^2 / sum_k d_k / a_k^2 with a_k = eps + beta_k.
+__device__ __forceinline__ double weno_combine(double bA, double bB, double bC, double qA,
+                                               double qB, double qC, double dA, double dB,
+                                               double dC) {
+  // product form, one division: weights d_k * prod_{j != k} a_j^2 (a_k >= 1e-6)
+  const double eps = 1e-6;
+  double aA = eps + bA, aB = eps + bB, aC = eps + bC;
+  aA = aA * aA;
+  aB = aB * aB;
+  aC = aC * aC;
+  const double tA = dA * (aB * aC), tB = dB * (aA * aC), tC = dC * (aA * aB);
+  return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
+}
+__device__ __forceinline__ f2 weno_combine(f2 bA, f2 bB, f2 bC, f2 qA, f2 qB, f2 qC, f2 dA, f2 dB,
+                                           f2 dC) {
+  // normalised by the smallest a_k: ratios in (0, 1], nothing overflows the float range
+  const f2 eps(1e-6);
+  const f2 aA = eps + bA, aB = eps + bB, aC = eps + bC;
+  f2 m = aA < aB ? aA : aB;
+  m = m < aC ? m : aC;
+  const f2 rA = m / aA, rB = m / aB, rC = m / aC;
+  const f2 tA = dA * (rA * rA), tB = dB * (rB * rB), tC = dC * (rC * rC);
+  return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
+}
+
+// Upwind-biased reconstruction at x_{i+1/2} from f0..f4 = points i-2..i+2 (linear weights
+// 0.3, 0.6, 0.1 for candidates {f2,f3,f4}, {f1,f2,f3}, {f0,f1,f2}); mirror image for the
+// left-moving part from points i-1..i+3.
+template <bool Plus, typename T>
+__device__ __forceinline__ T weno_side(T f0, T f1, T f2_, T f3, T f4) {
+  T bA, bB, bC;
+  weno_betas(f0, f1, f2_, f3, f4, bA, bB, bC);
+  const T c13 = T(1.0 / 3.0), c56 = T(5.0 / 6.0), c16 = T(1.0 / 6.0), c76 = T(7.0 / 6.0),
+          c116 = T(11.0 / 6.0);
+  if (Plus) {
+    const T qA = c13 * f2_ + c56 * f3 - c16 * f4;
+    const T qB = -c16 * f1 + c56 * f2_ + c13 * f3;
+    const T qC = c13 * f0 - c76 * f1 + c116 * f2_;
+    return weno_combine(bA, bB, bC, qA, qB, qC, T(0.3), T(0.6), T(0.1));
+  } else {
+    const T qA = c116 * f2_ - c76 * f3 + c13 * f4;
+    const T qB = c13 * f1 + c56 * f2_ - c16 * f3;
+    const T qC = -c16 * f0 + c56 * f1 + c13 * f2_;
+    return weno_combine(bA, bB, bC, qA, qB, qC, T(0.1), T(0.6), T(0.3));
+  }
+}
+
+template <bool Plus>
+__device__ __forceinline__ double weno_safe(double f0, double f1, double f2_, double f3, double f4) {
+  return weno_side<Plus>(f0, f1, f2_, f3, f4);
+}
+// float-float with a native-FP64 fallback for values whose squares would leave the float range
+template <bool Plus>
+__device__ __forceinline__ f2 weno_safe(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
+  const float m = fmaxf(fmaxf(fmaxf(fabsf(f0.hi), fabsf(f1.hi)), fmaxf(fabsf(f2_.hi), fabsf(f3.hi))),
+                        fabsf(f4.hi));
+  if (m < 1e18f) return weno_side<Plus>(f0, f1, f2_, f3, f4);
+  const double r = weno_side<Plus>(f0.to_double(), f1.to_double(), f2_.to_double(),
+                                   f3.to_double(), f4.to_double());
+  return f2_from_double(r);
+}
+
+// Face-local data shared by the fluid and tracer parts.
+template <typename T>
+struct FaceState {
+  T hp[6], hm[6];  // 0.5 (u_j + alpha), 0.5 (u_j - alpha): tracer split-flux factors
+};
+
+// Fluid part: W[j] = (rho, m_normal, m_t1, m_t2, et) of stencil point j (after the direction
+// swap); writes the five fluxes in the same order.
+template <typename T>
+__device__ __forceinline__ void fluid_face_flux(const T (&W)[6][5], double gamma_d,
+                                                FaceState<T>& S, T (&out)[5]) {
+  T* tag = nullptr;
+  const T gamma = num_from(gamma_d, tag);
+  const T gm = num_from(gamma_d - 1.0, tag);
+  const T half(0.5), one(1.0);
+  T p[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) p[j] = eos_t(gm, W[j][0], W[j][1], W[j][2], W[j][3], W[j][4]);
+  // Roe average at the face (src/utilities.cpp:298-304)
+  const T sL = sqrt0(W[2][0]), sR = sqrt0(W[3][0]);
+  const T sbar = half * (sL + sR);
+  const T u = half * (W[2][1] / sL + W[3][1] / sR) / sbar;
+  const T v = half * (W[2][2] / sL + W[3][2] / sR) / sbar;
+  const T ww = half * (W[2][3] / sL + W[3][3] / sR) / sbar;
+  const T H = half * ((p[2] + W[2][4]) / sL + (p[3] + W[3][4]) / sR) / sbar;
+  const T qsq = u * u + v * v + ww * ww;
+  const T c = gm * (H - half * qsq);  // the reference's "csnd" (src/utilities.cpp:309)
+  const T ci = one / c;
+  // nonzero entries of the left eigenvector rows (src/utilities.cpp:342-364)
+  const T hgc = half * gm * ci, hc = half * ci;
+  const T L00 = hc * (u + half * gm * qsq), L01 = -hc * (gm * u + one), L02 = -v * hgc,
+          L03 = -ww * hgc, L04 = hgc;
+  const T gc = gm * ci;
+  const T L30 = -gc * (qsq - H), L31 = u * gc, L32 = v * gc, L33 = ww * gc, L34 = -gc;
+  const T L40 = -hc * (u - half * gm * qsq), L41 = -hc * (gm * u - one);
+
+  // point fluxes (halved) and the Lax-Friedrichs speed (src/utilities.cpp:368-380)
+  T hf[6][5];
+  T alpha(0.0);
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const T uj = W[j][1] / W[j][0];
+    hf[j][0] = half * W[j][1];
+    hf[j][1] = half * (uj * W[j][1] + p[j]);
+    hf[j][2] = half * (uj * W[j][2]);
+    hf[j][3] = half * (uj * W[j][3]);
+    hf[j][4] = half * (uj * (W[j][4] + p[j]));
+    S.hp[j] = uj;  // temporarily u_j
+    const T s = num_fabs(uj) + sqrt0(gamma * p[j] / W[j][0]);
+    alpha = (alpha < s) ? s : alpha;
+  }
+  const T ha = half * alpha;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const T uj = S.hp[j];
+    S.hp[j] = half * uj + ha;
+    S.hm[j] = half * uj - ha;
+  }
+
+  T ff[5];
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    T pr[5][5];  // projected split flux [point][characteristic component]
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const int pt = j + side;
+      const T sa = side == 0 ? ha : -ha;
+      T fs[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) fs[m] = num_fma(sa, W[pt][m], hf[pt][m]);
+      pr[j][0] = L00 * fs[0] + L01 * fs[1] + L02 * fs[2] + L03 * fs[3] + L04 * fs[4];
+      pr[j][1] = fs[2] - v * fs[0];
+      pr[j][2] = fs[3] - ww * fs[0];
+      pr[j][3] = L30 * fs[0] + L31 * fs[1] + L32 * fs[2] + L33 * fs[3] + L34 * fs[4];
+      pr[j][4] = L40 * fs[0] + L41 * fs[1] + L02 * fs[2] + L03 * fs[3] + L04 * fs[4];
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      if (side == 0)
+        ff[i] = weno_safe<true>(pr[0][i], pr[1][i], pr[2][i], pr[3][i], pr[4][i]);
+      else
+        ff[i] = ff[i] + weno_safe<false>(pr[0][i], pr[1][i], pr[2][i], pr[3][i], pr[4][i]);
+    }
+  }
+  // right eigenvector columns (src/utilities.cpp:318-340)
+  out[0] = ff[0] + ff[3] + ff[4];
+  out[1] = (u - c) * ff[0] + u * ff[3] + (u + c) * ff[4];
+  out[2] = v * ff[0] + ff[1] + v * ff[3] + v * ff[4];
+  out[3] = ww * ff[0] + ff[2] + ww * ff[3] + ww * ff[4];
+  out[4] = (H - u * c) * ff[0] + v * ff[1] + ww * ff[2] + (half * qsq) * ff[3] + (H + u * c) * ff[4];
+}
+
+// Tracer part for one advected field from its 6 stencil values.
+template <typename T>
+__device__ __forceinline__ T tracer_face_flux(const FaceState<T>& S, const T (&cv)[6]) {
+  T r = weno_safe<true>(cv[0] * S.hp[0], cv[1] * S.hp[1], cv[2] * S.hp[2], cv[3] * S.hp[3],
+                        cv[4] * S.hp[4]);
+  r = r + weno_safe<false>(cv[1] * S.hm[1], cv[2] * S.hm[2], cv[3] * S.hm[3], cv[4] * S.hm[4],
+                           cv[5] * S.hm[5]);
+  return r;
+}
+
+}  // namespace gbmv
