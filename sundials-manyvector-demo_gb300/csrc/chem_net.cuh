@@ -77,6 +77,77 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
   dTs_ge = 1.0 / dge_dT;
 }
 
+// The same ten-iteration Newton solve with the first `nfloat` iterations in FP32 (table
+// lookups on the FP64 tables, rounded) and the rest in FP64.  From the converged basin the
+// FP64 iterations restore full accuracy (Newton's quadratic convergence), so the result
+// matches chem_temperature's to rounding whenever the reference's ten iterations converge.
+__device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, const double (&y)[10],
+                                                       double& Ts, double& dTs_ge, int nfloat) {
+  const float kb = 1.3806504e-16f, mh = 1.67e-24f, gm1 = 1.5f;
+  const float H2_1 = (float)y[0], H2_2 = (float)y[1], H_1 = (float)y[2], H_2 = (float)y[3],
+              H_m0 = (float)y[4], He_1 = (float)y[5], He_2 = (float)y[6], He_3 = (float)y[7],
+              de = (float)y[8], ge = (float)y[9];
+  const float density = 2.f * H2_1 + 2.f * H2_2 + 1.00794f * H_1 + 1.00794f * H_2 +
+                        1.00794f * H_m0 + 4.002602f * He_1 + 4.002602f * He_2 + 4.002602f * He_3;
+  const float kdm = kb / (density * mh);
+  const float lb = (float)P.lb, idbin = (float)P.idbin, dbin = (float)P.dbin;
+  float T = (float)Ts;
+#pragma unroll 1
+  for (int it = 0; it < nfloat; ++it) {
+    const float logT = logf(T);
+    int b = (int)(idbin * (logT - lb));
+    b = b <= 0 ? 0 : (b >= P.nbins ? P.nbins - 1 : b);
+    const float t1 = lb + b * dbin;
+    const float Tdef = (logT - t1) / dbin;
+    const double* lo = P.tab + (long)b * kNT;
+    const double* hi = lo + kNT;
+    const float g2 = (float)lo[GAMMAH2_2] + Tdef * (float)(hi[GAMMAH2_2] - lo[GAMMAH2_2]);
+    const float dg2 = (float)lo[DGAMMAH2_2] + Tdef * (float)(hi[DGAMMAH2_2] - lo[DGAMMAH2_2]);
+    const float g1 = (float)lo[GAMMAH2_1] + Tdef * (float)(hi[GAMMAH2_1] - lo[GAMMAH2_1]);
+    const float dg1 = (float)lo[DGAMMAH2_1] + Tdef * (float)(hi[DGAMMAH2_1] - lo[DGAMMAH2_1]);
+    const float i1 = 1.f / (g1 - 1.f), i2 = 1.f / (g2 - 1.f);
+    const float nsum = H2_1 * i1 + H2_2 * i2 +
+                       gm1 * (H_1 + H_2 + H_m0 + He_1 + He_2 + He_3 + de);
+    const float dge_dT = kdm * (T * (-H2_1 * i1 * i1 * dg1 - H2_2 * i2 * i2 * dg2) + nsum);
+    const float dge = kdm * T * nsum - ge;
+    T = T - dge / dge_dT;
+  }
+  Ts = (double)T;
+  // remaining iterations (and dT/dge) in FP64: exactly chem_temperature's loop body
+  const double kbd = 1.3806504e-16, mhd = 1.67e-24, gm1d = 1.0 / (5.e0 / 3.e0 - 1);
+  const double dH2_1 = y[0], dH2_2 = y[1], dH_1 = y[2], dH_2 = y[3], dH_m0 = y[4], dHe_1 = y[5],
+               dHe_2 = y[6], dHe_3 = y[7], dde = y[8], dge0 = y[9];
+  const double ddensity = 2.0 * dH2_1 + 2.0 * dH2_2 + 1.00794 * dH_1 + 1.00794 * dH_2 +
+                          1.00794 * dH_m0 + 4.002602 * dHe_1 + 4.002602 * dHe_2 + 4.002602 * dHe_3;
+  const double dmh = ddensity * mhd;
+  double Tc = Ts, Tnew = Ts, dge_dTd = 0.0;
+#pragma unroll 1
+  for (int it = nfloat; it < 10; ++it) {
+    Tc = Ts;
+    double t1, t2;
+    const double logT = log(Ts);
+    const int b = chem_bin(P, logT, t1, t2);
+    const double Tdef = (logT - t1) / (t2 - t1);
+    const double* lo = P.tab + (long)b * kNT;
+    const double* hi = lo + kNT;
+    const double g2 = lo[GAMMAH2_2] + Tdef * (hi[GAMMAH2_2] - lo[GAMMAH2_2]);
+    const double dg2 = lo[DGAMMAH2_2] + Tdef * (hi[DGAMMAH2_2] - lo[DGAMMAH2_2]);
+    const double g1 = lo[GAMMAH2_1] + Tdef * (hi[GAMMAH2_1] - lo[GAMMAH2_1]);
+    const double dg1 = lo[DGAMMAH2_1] + Tdef * (hi[DGAMMAH2_1] - lo[DGAMMAH2_1]);
+    const double i1 = 1.0 / (g1 - 1.0), i2 = 1.0 / (g2 - 1.0);
+    const double nsum = dH2_1 * i1 + dH2_2 * i2 + dH_1 * gm1d + dH_2 * gm1d + dH_m0 * gm1d +
+                        dHe_1 * gm1d + dHe_2 * gm1d + dHe_3 * gm1d + gm1d * dde;
+    dge_dTd = Tc * kbd * (-dH2_1 * i1 * i1 * dg1 - dH2_2 * i2 * i2 * dg2) / dmh + kbd * nsum / dmh;
+    const double dgev = Tc * kbd * nsum / dmh - dge0;
+    Tnew = Tc - dgev / dge_dTd;
+    Ts = Tnew;
+  }
+  Ts = Tnew;
+  if (Ts < P.tlo) Ts = P.tlo;
+  else if (Ts > P.thi) Ts = P.thi;
+  dTs_ge = 1.0 / dge_dTd;
+}
+
 // Rates at temperature Ts (and their T-derivatives when WithSlopes).
 template <bool WithSlopes>
 __device__ __forceinline__ void chem_rates(const ChemParams& P, double Ts, double (&k)[kNRates],

