@@ -67,6 +67,7 @@ struct gbmv_hydro_s {
   ForceTerm force;
   double* scratch = nullptr;
   size_t scratch_doubles = 0;
+  float* prims = nullptr;  // float-float per-cell primitives of the mixed form (first use)
   int* d_status = nullptr;
 };
 
@@ -176,6 +177,7 @@ int gbmv_hydro_create(const gbmv_grid* grid, gbmv_hydro* out) {
 int gbmv_hydro_destroy(gbmv_hydro h) {
   if (!h) return GBMV_OK;
   cudaFree(h->scratch);
+  cudaFree(h->prims);
   cudaFree(h->d_status);
   delete h;
   return GBMV_OK;
@@ -208,7 +210,16 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
   G.in_wdot = (flags & GBMV_FORCE_IN_WDOT) ? 1 : 0;
   cudaStream_t s = (cudaStream_t)stream;
   if (precision == GBMV_FP64) return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
-  return feuler_mixed(h->g, W, Wd, G, h->scratch, d_status, s);
+  if (!h->prims) {
+    const size_t nf = feuler_f2_prims_floats(h->g);
+    if (cudaMalloc(&h->prims, nf * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      h->prims = nullptr;
+      set_error("device allocation of %zu mixed-form primitive floats failed", nf);
+      return GBMV_ENOMEM;
+    }
+  }
+  return feuler_f2(h->g, W, Wd, G, h->scratch, h->prims, d_status, s);
 }
 
 int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,

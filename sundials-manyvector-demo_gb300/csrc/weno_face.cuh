@@ -115,15 +115,25 @@ template <bool Plus>
 __device__ __forceinline__ double weno_safe(double f0, double f1, double f2_, double f3, double f4) {
   return weno_side<Plus>(f0, f1, f2_, f3, f4);
 }
-// float-float with a native-FP64 fallback for values whose squares would leave the float range
+// float-float with a native-FP64 fallback for values whose squares would leave the float
+// range.  Kept out of line: one copy of the long float-float sequence serves all 2*NVAR
+// reconstructions of a face, which keeps the kernel inside the instruction cache.
+template <bool Plus>
+__device__ __noinline__ f2 weno_side_f2(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
+  return weno_side<Plus>(f0, f1, f2_, f3, f4);
+}
+template <bool Plus>
+__device__ __noinline__ f2 weno_side_f2_fallback(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
+  const double r = weno_side<Plus>(f0.to_double(), f1.to_double(), f2_.to_double(),
+                                   f3.to_double(), f4.to_double());
+  return f2_from_double(r);
+}
 template <bool Plus>
 __device__ __forceinline__ f2 weno_safe(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
   const float m = fmaxf(fmaxf(fmaxf(fabsf(f0.hi), fabsf(f1.hi)), fmaxf(fabsf(f2_.hi), fabsf(f3.hi))),
                         fabsf(f4.hi));
-  if (m < 1e18f) return weno_side<Plus>(f0, f1, f2_, f3, f4);
-  const double r = weno_side<Plus>(f0.to_double(), f1.to_double(), f2_.to_double(),
-                                   f3.to_double(), f4.to_double());
-  return f2_from_double(r);
+  if (m < 1e18f) return weno_side_f2<Plus>(f0, f1, f2_, f3, f4);
+  return weno_side_f2_fallback<Plus>(f0, f1, f2_, f3, f4);
 }
 
 // Face-local data shared by the fluid and tracer parts.
@@ -134,23 +144,40 @@ struct FaceState {
 
 // Fluid part: W[j] = (rho, m_normal, m_t1, m_t2, et) of stencil point j (after the direction
 // swap); writes the five fluxes in the same order.
+// Per-point primitives computed once per cell (pressure, normal velocity, sound speed).
 template <typename T>
+struct PointPrims {
+  T p[6], u[6], c[6];
+};
+
+template <typename T, bool Pre = false>
 __device__ __forceinline__ void fluid_face_flux(const T (&W)[6][5], double gamma_d,
-                                                FaceState<T>& S, T (&out)[5]) {
+                                                FaceState<T>& S, T (&out)[5],
+                                                const PointPrims<T>* pre = nullptr) {
   T* tag = nullptr;
   const T gamma = num_from(gamma_d, tag);
   const T gm = num_from(gamma_d - 1.0, tag);
   const T half(0.5), one(1.0);
   T p[6];
 #pragma unroll
-  for (int j = 0; j < 6; ++j) p[j] = eos_t(gm, W[j][0], W[j][1], W[j][2], W[j][3], W[j][4]);
+  for (int j = 0; j < 6; ++j)
+    p[j] = Pre ? pre->p[j] : eos_t(gm, W[j][0], W[j][1], W[j][2], W[j][3], W[j][4]);
   // Roe average at the face (src/utilities.cpp:298-304)
   const T sL = sqrt0(W[2][0]), sR = sqrt0(W[3][0]);
   const T sbar = half * (sL + sR);
-  const T u = half * (W[2][1] / sL + W[3][1] / sR) / sbar;
-  const T v = half * (W[2][2] / sL + W[3][2] / sR) / sbar;
-  const T ww = half * (W[2][3] / sL + W[3][3] / sR) / sbar;
-  const T H = half * ((p[2] + W[2][4]) / sL + (p[3] + W[3][4]) / sR) / sbar;
+  T u, v, ww, H;
+  if (Pre) {  // three divisions instead of twelve (float-float divisions are the costly op)
+    const T isL = one / sL, isR = one / sR, hs = half / sbar;
+    u = (W[2][1] * isL + W[3][1] * isR) * hs;
+    v = (W[2][2] * isL + W[3][2] * isR) * hs;
+    ww = (W[2][3] * isL + W[3][3] * isR) * hs;
+    H = ((p[2] + W[2][4]) * isL + (p[3] + W[3][4]) * isR) * hs;
+  } else {
+    u = half * (W[2][1] / sL + W[3][1] / sR) / sbar;
+    v = half * (W[2][2] / sL + W[3][2] / sR) / sbar;
+    ww = half * (W[2][3] / sL + W[3][3] / sR) / sbar;
+    H = half * ((p[2] + W[2][4]) / sL + (p[3] + W[3][4]) / sR) / sbar;
+  }
   const T qsq = u * u + v * v + ww * ww;
   const T c = gm * (H - half * qsq);  // the reference's "csnd" (src/utilities.cpp:309)
   const T ci = one / c;
@@ -167,14 +194,14 @@ __device__ __forceinline__ void fluid_face_flux(const T (&W)[6][5], double gamma
   T alpha(0.0);
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    const T uj = W[j][1] / W[j][0];
+    const T uj = Pre ? pre->u[j] : W[j][1] / W[j][0];
     hf[j][0] = half * W[j][1];
     hf[j][1] = half * (uj * W[j][1] + p[j]);
     hf[j][2] = half * (uj * W[j][2]);
     hf[j][3] = half * (uj * W[j][3]);
     hf[j][4] = half * (uj * (W[j][4] + p[j]));
     S.hp[j] = uj;  // temporarily u_j
-    const T s = num_fabs(uj) + sqrt0(gamma * p[j] / W[j][0]);
+    const T s = num_fabs(uj) + (Pre ? pre->c[j] : sqrt0(gamma * p[j] / W[j][0]));
     alpha = (alpha < s) ? s : alpha;
   }
   const T ha = half * alpha;
