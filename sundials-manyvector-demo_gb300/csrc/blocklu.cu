@@ -12,37 +12,39 @@
 
 namespace gbmv {
 
-constexpr int kLuThreads = 128;  // blocks per tile = threads per CTA
+constexpr int kLuThreads = 64;   // blocks per tile = threads per CTA
 constexpr int kLuStride = 101;   // padded per-block stride of the shared tile (doubles)
+constexpr int kVecStride = 11;   // the same for the right-hand-side tile
 
 // Coalesced copy of `nb` consecutive blocks of NE doubles between global memory and a shared
-// tile with per-block stride kLuStride (16-byte global accesses when NE is even).
-template <int NE>
+// tile with per-block stride SS (16-byte global accesses when NE is even and the address is
+// 16-byte aligned -- caller arrays need only be 8-byte aligned).
+template <int NE, int SS = kLuStride>
 __device__ __forceinline__ void tile_in(const double* __restrict__ g, double* sh, long blk0, int nb) {
   const double* src = g + blk0 * NE;
-  if (NE % 2 == 0) {
+  if (NE % 2 == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
     const double2* s2 = reinterpret_cast<const double2*>(src);
     for (int c = threadIdx.x; c < nb * NE / 2; c += blockDim.x) {
       const double2 v = s2[c];
       const int b = (2 * c) / NE, e = (2 * c) % NE;
-      sh[b * kLuStride + e] = v.x;
-      sh[b * kLuStride + e + 1] = v.y;
+      sh[b * SS + e] = v.x;
+      sh[b * SS + e + 1] = v.y;
     }
   } else {
-    for (int c = threadIdx.x; c < nb * NE; c += blockDim.x) sh[(c / NE) * kLuStride + c % NE] = src[c];
+    for (int c = threadIdx.x; c < nb * NE; c += blockDim.x) sh[(c / NE) * SS + c % NE] = src[c];
   }
 }
-template <int NE>
+template <int NE, int SS = kLuStride>
 __device__ __forceinline__ void tile_out(double* __restrict__ g, const double* sh, long blk0, int nb) {
   double* dst = g + blk0 * NE;
-  if (NE % 2 == 0) {
+  if (NE % 2 == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
     double2* d2 = reinterpret_cast<double2*>(dst);
     for (int c = threadIdx.x; c < nb * NE / 2; c += blockDim.x) {
       const int b = (2 * c) / NE, e = (2 * c) % NE;
-      d2[c] = make_double2(sh[b * kLuStride + e], sh[b * kLuStride + e + 1]);
+      d2[c] = make_double2(sh[b * SS + e], sh[b * SS + e + 1]);
     }
   } else {
-    for (int c = threadIdx.x; c < nb * NE; c += blockDim.x) dst[c] = sh[(c / NE) * kLuStride + c % NE];
+    for (int c = threadIdx.x; c < nb * NE; c += blockDim.x) dst[c] = sh[(c / NE) * SS + c % NE];
   }
 }
 
@@ -121,7 +123,7 @@ __device__ __forceinline__ void lus10_regs(const R (&A)[100], const int (&piv)[1
   }
 }
 
-__global__ void __launch_bounds__(kLuThreads, 2) block_lu_factor_kernel(long nb, double* __restrict__ A,
+__global__ void __launch_bounds__(kLuThreads, 4) block_lu_factor_kernel(long nb, double* __restrict__ A,
                                                                         int* __restrict__ piv,
                                                                         int* __restrict__ info_out) {
   extern __shared__ double sh[];  // [kLuThreads][kLuStride]
@@ -151,16 +153,16 @@ __global__ void __launch_bounds__(kLuThreads, 2) block_lu_factor_kernel(long nb,
   if (bad) atomicMax(info_out, 1);
 }
 
-__global__ void __launch_bounds__(kLuThreads, 2) block_lu_solve_kernel(long nb,
+__global__ void __launch_bounds__(kLuThreads, 4) block_lu_solve_kernel(long nb,
                                                                        const double* __restrict__ LU,
                                                                        const int* __restrict__ piv,
                                                                        const double* b, double* x) {
   extern __shared__ double sh[];  // LU tile, then the right-hand sides
-  double* shb = sh + kLuThreads * kLuStride;
+  double* shb = sh + kLuThreads * kLuStride;  // [kLuThreads][kVecStride]
   for (long blk0 = (long)blockIdx.x * kLuThreads; blk0 < nb; blk0 += (long)gridDim.x * kLuThreads) {
     const int nb_here = (int)((nb - blk0) < kLuThreads ? (nb - blk0) : kLuThreads);
     tile_in<100>(LU, sh, blk0, nb_here);
-    tile_in<10>(b, shb, blk0, nb_here);
+    tile_in<10, kVecStride>(b, shb, blk0, nb_here);
     __syncthreads();
     if (threadIdx.x < nb_here) {
       double a[100], v[10];
@@ -172,14 +174,14 @@ __global__ void __launch_bounds__(kLuThreads, 2) block_lu_solve_kernel(long nb,
 #pragma unroll
       for (int e = 0; e < 10; ++e) {
         p[e] = pg[e];
-        v[e] = shb[threadIdx.x * kLuStride + e];
+        v[e] = shb[threadIdx.x * kVecStride + e];
       }
       lus10_regs(a, p, v);
 #pragma unroll
-      for (int e = 0; e < 10; ++e) shb[threadIdx.x * kLuStride + e] = v[e];
+      for (int e = 0; e < 10; ++e) shb[threadIdx.x * kVecStride + e] = v[e];
     }
     __syncthreads();
-    tile_out<10>(x, shb, blk0, nb_here);
+    tile_out<10, kVecStride>(x, shb, blk0, nb_here);
     __syncthreads();
   }
 }
@@ -196,7 +198,7 @@ __global__ void block_form_newton_kernel(long nel, double* __restrict__ J, doubl
 
 static int lu_grid(long nb) {
   long b = (nb + kLuThreads - 1) / kLuThreads;
-  const long cap = (long)kSM * 2;
+  const long cap = (long)kSM * 4;
   if (b < 1) b = 1;
   return (int)(b < cap ? b : cap);
 }
@@ -213,7 +215,7 @@ int block_lu_factor(long nb, double* A, int* piv, int* d_info, cudaStream_t s) {
 
 int block_lu_solve(long nb, const double* LU, const int* piv, const double* b, double* x,
                    cudaStream_t s) {
-  const size_t shm = sizeof(double) * 2 * kLuStride * kLuThreads;
+  const size_t shm = sizeof(double) * (kLuStride + kVecStride) * kLuThreads;
   GBMV_CUDA_TRY(cudaFuncSetAttribute(block_lu_solve_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   ProfScope ps("block_lu_solve", s);

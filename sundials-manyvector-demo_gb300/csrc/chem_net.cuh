@@ -308,40 +308,45 @@ __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double 
 #pragma unroll
     for (int q = 0; q < 9; ++q) put(q, 9, s[q] * Tge);
   }
+  // four reciprocals serve every ge-row entry (the reference divides ~20 times)
   const double G = H2_1 * k[GAH2] + H_1 * k[GAHI] + H_2 * k[GAHP] + He_1 * k[GAHE] + de * k[GAEL];
-  const double D = k[H2LTE] / G + 1.0;
+  const double iG = 1.0 / G;
+  const double D = k[H2LTE] * iG + 1.0;
+  const double iD = 1.0 / D;
   const double N = H2_1 * k[NCRD2] + H_1 * k[NCRD1];
-  const double F = k[NCRN] / N + 1.0;
+  const double iN = 1.0 / N;
+  const double F = k[NCRN] * iN + 1.0;
+  const double iF = 1.0 / F;
   const double H13 = H1sq * H_1;
   const double Hf = -H2_1 * H_1 * k[H2MCOOL] + H13 * k[H2MHEAT];
   const double lte2 = k[H2LTE] * k[H2LTE];
-  const double DG2 = (D * D) * (G * G);
-  const double iF2 = 1.0 / (F * F);
-  const double N2 = N * N;
-  SETG(0, -H2_1 * k[GAH2] * lte2 * h2oda / DG2 - 0.5 * H_1 * k[H2MCOOL] / F -
-                 2.01588 * k[CIECO] * md - k[H2LTE] * h2oda / D +
-                 0.5 * k[NCRD2] * k[NCRN] * iF2 * Hf / N2);
-  SETG(2, -H2_1 * k[GAHI] * lte2 * h2oda / DG2 - k[CEHI] * de - k[CIHI] * de +
-                 0.5 * k[NCRD1] * k[NCRN] * iF2 * Hf / N2 +
-                 0.5 * (-H2_1 * k[H2MCOOL] + 3 * H1sq * k[H2MHEAT]) / F);
-  SETG(3, -H2_1 * k[GAHP] * lte2 * h2oda / DG2 - k[BREM] * de - de * k[REHII]);
-  SETG(5, -H2_1 * k[GAHE] * lte2 * h2oda / DG2 - k[CIHEI] * de);
+  const double iDG2 = (iD * iD) * (iG * iG);
+  const double iF2 = iF * iF;
+  const double iN2 = iN * iN;
+  const double lteh = lte2 * h2oda * iDG2;  // h2lte^2 * h2oda / (D^2 G^2)
+  SETG(0, -H2_1 * k[GAH2] * lteh - 0.5 * H_1 * k[H2MCOOL] * iF - 2.01588 * k[CIECO] * md -
+              k[H2LTE] * h2oda * iD + 0.5 * k[NCRD2] * k[NCRN] * iF2 * Hf * iN2);
+  SETG(2, -H2_1 * k[GAHI] * lteh - k[CEHI] * de - k[CIHI] * de +
+              0.5 * k[NCRD1] * k[NCRN] * iF2 * Hf * iN2 +
+              0.5 * (-H2_1 * k[H2MCOOL] + 3 * H1sq * k[H2MHEAT]) * iF);
+  SETG(3, -H2_1 * k[GAHP] * lteh - k[BREM] * de - de * k[REHII]);
+  SETG(5, -H2_1 * k[GAHE] * lteh - k[CIHEI] * de);
   SETG(6, -k[BREM] * de - k[CEHEII] * de - k[CEHEI] * (de * de) - k[CIHEII] * de -
-                 k[CIHEIS] * (de * de) - de * k[REHEII1] - de * k[REHEII2]);
+              k[CIHEIS] * (de * de) - de * k[REHEII1] - de * k[REHEII2]);
   SETG(7, -4.0 * k[BREM] * de - de * k[REHEIII]);
-  SETG(8, -H2_1 * k[GAEL] * lte2 * h2oda / DG2 - H_1 * k[CEHI] - H_1 * k[CIHI] -
-                 H_2 * k[REHII] - He_1 * k[CIHEI] - He_2 * k[CEHEII] - 2 * He_2 * k[CEHEI] * de -
-                 He_2 * k[CIHEII] - 2 * He_2 * k[CIHEIS] * de - He_2 * k[REHEII1] -
-                 He_2 * k[REHEII2] - He_3 * k[REHEIII] - k[BREM] * (H_2 + He_2 + 4.0 * He_3) -
-                 k[COMPTON] * P.zp1_4 * (T - 2.73 * z - 2.73));
+  SETG(8, -H2_1 * k[GAEL] * lteh - H_1 * k[CEHI] - H_1 * k[CIHI] - H_2 * k[REHII] -
+              He_1 * k[CIHEI] - He_2 * k[CEHEII] - 2 * He_2 * k[CEHEI] * de - He_2 * k[CIHEII] -
+              2 * He_2 * k[CIHEIS] * de - He_2 * k[REHEII1] - He_2 * k[REHEII2] -
+              He_3 * k[REHEIII] - k[BREM] * (H_2 + He_2 + 4.0 * He_3) -
+              k[COMPTON] * P.zp1_4 * (T - 2.73 * z - 2.73));
   const double dGn = -H2_1 * dk[GAH2] - H_1 * dk[GAHI] - H_2 * dk[GAHP] - He_1 * dk[GAHE] -
                      de * dk[GAEL];
-  put(9, 9, (-H2_1 * k[H2LTE] * h2oda * (-k[H2LTE] * dGn / (G * G) - dk[H2LTE] / G) / (D * D) -
-                 H2_1 * h2oda * dk[H2LTE] / D +
-                 0.5 * iF2 * Hf *
-                     (-1.0 * k[NCRN] * (-H2_1 * dk[NCRD2] - H_1 * dk[NCRD1]) / N2 -
-                      1.0 * dk[NCRN] / N) +
-                 0.5 / F * (-H2_1 * H_1 * dk[H2MCOOL] + H13 * dk[H2MHEAT])) * imd * Tge);
+  put(9, 9, (-H2_1 * k[H2LTE] * h2oda * (-k[H2LTE] * dGn * (iG * iG) - dk[H2LTE] * iG) * (iD * iD) -
+             H2_1 * h2oda * dk[H2LTE] * iD +
+             0.5 * iF2 * Hf *
+                 (-1.0 * k[NCRN] * (-H2_1 * dk[NCRD2] - H_1 * dk[NCRD1]) * iN2 -
+                  1.0 * dk[NCRN] * iN) +
+             0.5 * iF * (-H2_1 * H_1 * dk[H2MCOOL] + H13 * dk[H2MHEAT])) * imd * Tge);
 #undef SETG
 #undef SETJ
 }

@@ -9,13 +9,23 @@
 //                with FP64 residuals r = f - A x against the FP64 matrix (the benchmark spec's
 //                mixed-precision Newton solve); a non-finite FP32 factor falls back to FP64.
 // The temperature state (Ts, dTs/dge) is updated as by gbmv_chem_rhs (LU = double: exactly;
-// LU = float: the ten Newton iterations run 8 in FP32 and the last 2 in FP64).
+// LU = float: the ten Newton iterations run 9 in FP32 and the last in FP64).
 #include "chem.cuh"
 #include "chem_net.cuh"
 
 namespace gbmv {
 
 constexpr int kNtThreads = 64;
+
+// Structural nonzeros (row, col) of the network Jacobian (the CSR pattern of
+// src/raja_primordial_network.cpp:1869-1948); every diagonal entry is among them.
+__device__ constexpr int kJacPattern[64][2] = {
+    {0, 0}, {0, 1}, {0, 2}, {0, 3}, {0, 4}, {0, 8}, {0, 9}, {1, 0}, {1, 1}, {1, 2}, {1, 3},
+    {1, 4}, {1, 8}, {1, 9}, {2, 0}, {2, 1}, {2, 2}, {2, 3}, {2, 4}, {2, 8}, {2, 9}, {3, 0},
+    {3, 1}, {3, 2}, {3, 3}, {3, 4}, {3, 8}, {3, 9}, {4, 1}, {4, 2}, {4, 3}, {4, 4}, {4, 8},
+    {4, 9}, {5, 5}, {5, 6}, {5, 8}, {5, 9}, {6, 5}, {6, 6}, {6, 7}, {6, 8}, {6, 9}, {7, 6},
+    {7, 7}, {7, 8}, {7, 9}, {8, 1}, {8, 2}, {8, 3}, {8, 4}, {8, 5}, {8, 6}, {8, 7}, {8, 8},
+    {8, 9}, {9, 0}, {9, 2}, {9, 3}, {9, 5}, {9, 6}, {9, 7}, {9, 8}, {9, 9}};
 
 // In-place LU with partial pivoting on a strided per-thread slice A[e*stride] (column-major
 // 10x10), reciprocal pivots on the diagonal; returns 0 or 1 + first zero pivot.
@@ -101,7 +111,7 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
     for (int s = 0; s < 10; ++s) ya[s] = y[j + s] * sc[s];
     double Ts = S.Ts[i], dTs = 0.0;
     if (sizeof(LU) == 4)
-      chem_temperature_mixed(P, ya, Ts, dTs, 8);  // mixed form: 8 FP32 + 2 FP64 iterations
+      chem_temperature_mixed(P, ya, Ts, dTs, 9);  // mixed form: 9 FP32 + 1 FP64 iterations
     else
       chem_temperature(P, ya, Ts, dTs);
     S.Ts[i] = Ts;
@@ -122,18 +132,25 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
     }
 #pragma unroll
     for (int s = 0; s < 10; ++s) fout[j + s] = f[s];
-    {  // A = I - gamma * (J * inv_scale[row] * scale[col] * tunit), FP64, in shared memory
+    {  // A = I - gamma * (J * inv_scale[row] * scale[col] * tunit), FP64 and a float copy
       double k[kNRates], dk[kNRates];
       chem_rates<true>(P, Ts, k, dk);
+      double rf[10];  // -gamma * tunit * inv_scale[row]
 #pragma unroll
-      for (int e = 0; e < 100; ++e) A[e * kNtThreads] = (e % 11 == 0) ? 1.0 : 0.0;
+      for (int r = 0; r < 10; ++r) rf[r] = (-gamma * tunit) * isc[r];
+#pragma unroll
+      for (int e = 0; e < 100; ++e) {
+        A[e * kNtThreads] = (e % 11 == 0) ? 1.0 : 0.0;
+        L[e * kNtThreads] = (e % 11 == 0) ? LU(1) : LU(0);
+      }
       chem_jacobian(P, k, dk, ya, Ts, dTs, Ax, [&](int row, int col, double v) {
-        const double Jv = (v * (isc[row] * sc[col])) * tunit;
-        A[(col * 10 + row) * kNtThreads] = -gamma * Jv + (row == col ? 1.0 : 0.0);
+        const double a = (v * rf[row]) * sc[col] + (row == col ? 1.0 : 0.0);
+        A[(col * 10 + row) * kNtThreads] = a;
+        L[(col * 10 + row) * kNtThreads] = (LU)a;
       });
     }
 #pragma unroll
-    for (int e = 0; e < 100; ++e) L[e * kNtThreads] = (LU)A[e * kNtThreads];
+    for (int s = 0; s < 10; ++s) f[s] = fout[j + s];
 
     int piv[10];
     double x[10];
@@ -152,9 +169,10 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
 #pragma unroll
           for (int row = 0; row < 10; ++row) rr[row] = f[row];
 #pragma unroll
-          for (int col = 0; col < 10; ++col)
-#pragma unroll
-            for (int row = 0; row < 10; ++row) rr[row] -= A[(col * 10 + row) * kNtThreads] * x[col];
+          for (int e = 0; e < 64; ++e) {  // the 64 structural nonzeros (diagonal included)
+            const int row = kJacPattern[e][0], col = kJacPattern[e][1];
+            rr[row] -= A[(col * 10 + row) * kNtThreads] * x[col];
+          }
           LU ds[10];
 #pragma unroll
           for (int s = 0; s < 10; ++s) ds[s] = (LU)rr[s];
