@@ -87,8 +87,10 @@ def test_fused_newton_matches_separate_path(cuda, tables, lu):
     for s in range(10):
         assert maxnorm_err(b[:, s], a[:, s]) <= ftol, (s, maxnorm_err(b[:, s], a[:, s]))
     xa, xb = x1.cpu().numpy().reshape(n, 10), x2.cpu().numpy().reshape(n, 10)
-    # FP32 LU + two FP64-residual refinements: ~(kappa * 6e-8)^3 relative, far inside 1e-6
-    tol = 1e-12 if lu == 0 else 1e-8
+    # the fused kernel forms I - gamma*J with a different rounding order (row factors), so
+    # even the FP64 LU differs by conditioning x 1e-16; FP32 LU + two FP64-residual
+    # refinements: ~(kappa * 6e-8)^3 relative -- both far inside the 1e-6 budget
+    tol = 1e-10 if lu == 0 else 1e-8
     for s in range(10):
         assert maxnorm_err(xb[:, s], xa[:, s]) <= tol, (s, maxnorm_err(xb[:, s], xa[:, s]))
     if lu == 0:
