@@ -53,11 +53,25 @@ __device__ __forceinline__ f2 operator*(f2 x, f2 y) {
   return quick_two_sum(p.hi, e);
 }
 
+// Division: q1 from a fast approximate reciprocal, the remainder x - y*q1 formed in
+// float-float, one correction q2 -- the correction absorbs q1's few-ulp error, so the result
+// keeps the float-float precision.
 __device__ __forceinline__ f2 operator/(f2 x, f2 y) {
-  const float q1 = x.hi / y.hi;
+  const float ry = __fdividef(1.f, y.hi);
+  const float q1 = x.hi * ry;
   const f2 r = x - y * f2(q1, 0.f);
-  const float q2 = r.hi / y.hi;
+  const float q2 = r.hi * ry;
   return quick_two_sum(q1, q2);
+}
+
+// exact scaling by a power of two
+__device__ __forceinline__ f2 f2_scale(f2 x, float p2) { return f2(x.hi * p2, x.lo * p2); }
+
+// x^2 with the exact square of the high part
+__device__ __forceinline__ f2 f2_sqr(f2 x) {
+  f2 p = two_prod(x.hi, x.hi);
+  const float e = fmaf(2.f * x.hi, x.lo, p.lo);
+  return quick_two_sum(p.hi, e);
 }
 
 // exact split of a double into hi + lo (48 of its 53 significant bits survive)

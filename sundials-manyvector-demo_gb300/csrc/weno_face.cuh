@@ -118,9 +118,40 @@ __device__ __forceinline__ double weno_safe(double f0, double f1, double f2_, do
 // float-float with a native-FP64 fallback for values whose squares would leave the float
 // range.  Kept out of line: one copy of the long float-float sequence serves all 2*NVAR
 // reconstructions of a face, which keeps the kernel inside the instruction cache.
+// Float-float reconstruction arranged for fewer float-float operations than the reference's
+// literal formula (same mathematics, ~48-bit arithmetic):
+//   * the four neighbour differences D01..D34 serve all six indicator terms and all three
+//     candidate polynomials;
+//   * the weights are d_k (a_min / a_k)^2 with a_k = eps + beta_k, ratios in (0, 1], so
+//     nothing leaves the float exponent range.
 template <bool Plus>
 __device__ __noinline__ f2 weno_side_f2(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
-  return weno_side<Plus>(f0, f1, f2_, f3, f4);
+  const f2 D01 = f0 - f1, D12 = f1 - f2_, D23 = f2_ - f3, D34 = f3 - f4;
+  const f2 dA = D23 - D34, dB = D12 - D23, dC = D01 - D12;       // second differences
+  const f2 eA = dA + f2_scale(D23, 2.f), eB = D12 + D23, eC = dC - f2_scale(D12, 2.f);
+  const f2 b13(13.0 / 12.0), sixth(1.0 / 6.0), eps(1e-6);
+  f2 aA = eps + (b13 * f2_sqr(dA) + f2_scale(f2_sqr(eA), 0.25f));
+  f2 aB = eps + (b13 * f2_sqr(dB) + f2_scale(f2_sqr(eB), 0.25f));
+  f2 aC = eps + (b13 * f2_sqr(dC) + f2_scale(f2_sqr(eC), 0.25f));
+  // candidates: (2f2+5f3-f4)/6 etc. written around their central value
+  f2 qA, qB, qC, wA, wB, wC;
+  if (Plus) {
+    qA = f3 + sixth * (f2_scale(D23, 2.f) + D34);
+    qB = f2_ - sixth * (D12 + f2_scale(D23, 2.f));
+    qC = f2_ + sixth * (f2_scale(D01, 2.f) - f2(5.0) * D12);
+    wA = f2(0.3); wB = f2(0.6); wC = f2(0.1);
+  } else {
+    qA = f2_ + sixth * (f2(5.0) * D23 - f2_scale(D34, 2.f));
+    qB = f2_ + sixth * (f2_scale(D12, 2.f) + D23);
+    qC = f1 - sixth * (D01 + f2_scale(D12, 2.f));
+    wA = f2(0.1); wB = f2(0.6); wC = f2(0.3);
+  }
+  // weights relative to the smallest a: ratios in (0, 1], nothing leaves the float range
+  f2 m = aA < aB ? aA : aB;
+  m = m < aC ? m : aC;
+  const f2 rA = m / aA, rB = m / aB, rC = m / aC;
+  const f2 tA = wA * f2_sqr(rA), tB = wB * f2_sqr(rB), tC = wC * f2_sqr(rC);
+  return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
 }
 template <bool Plus>
 __device__ __noinline__ f2 weno_side_f2_fallback(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
