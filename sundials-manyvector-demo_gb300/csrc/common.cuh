@@ -44,7 +44,7 @@ struct Grid {
   int nchem;
   int bc[6];
   double gamma;
-  double inv_d[3]; // unused by the FP64 parity form (which divides, as the reference does)
+  double inv_d[3]; // 1/dx, 1/dy, 1/dz
   double d[3];
 };
 
