@@ -169,7 +169,7 @@ class FusedStep:
             self.ls.solve(self.J, self.x, self.f)
         else:
             if self.chem.newton_iteration(t, y, self.f, self.x, GAMMA_NEWTON, TU,
-                                          lu_precision=g.MIXED, refine=2) != 0:
+                                          lu_precision=g.MIXED, refine=4) != 0:
                 raise RuntimeError("singular Newton block")
 
     def outputs(self):

@@ -437,7 +437,7 @@ int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* co
   if (rc) return rc;
   rc = gbmv_feuler(h, t, (const double* const*)w, wdot, precision, stream);
   if (rc < 0 && rc != GBMV_ILLEGAL_STATE) return rc;
-  int rc2 = energy_epilogue(c->S, w[5], wdot[5], wdot[4], c->n, 10, s);
+  int rc2 = energy_epilogue(c->S, w[5], wdot[5], wdot[4], c->n, 10, precision == GBMV_FP64, s);
   if (rc2) return rc2;
   return rc;
 }

@@ -138,16 +138,24 @@ __global__ void energy_sync_kernel(const double* __restrict__ scale, double* __r
 
 // fslow/fexpl epilogue: chemdot[ge] = etdot, etdot = 0, chem /= scale
 // (src/multirate_chem_hydro_main.cpp:1061-1077).
-__global__ void energy_epilogue_kernel(const double* __restrict__ scale, double* __restrict__ chem,
-                                       double* __restrict__ chemdot, double* __restrict__ etdot,
-                                       long n, int nchem) {
+// exact = 1 divides by scale as the reference's unapply does; exact = 0 multiplies by
+// inv_scale (one rounding apart, and no FP64 division: the mixed-precision form).
+__global__ void energy_epilogue_kernel(const double* __restrict__ scale,
+                                       const double* __restrict__ inv_scale,
+                                       double* __restrict__ chem, double* __restrict__ chemdot,
+                                       double* __restrict__ etdot, long n, int nchem, int exact) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
        i += (long)gridDim.x * blockDim.x) {
     chemdot[(long)nchem * i + nchem - 1] = etdot[i];
     etdot[i] = 0.0;
     double* c = chem + (long)nchem * i;
-    const double* s = scale + (long)nchem * i;
-    for (int v = 0; v < nchem; ++v) c[v] /= s[v];
+    if (exact) {
+      const double* s = scale + (long)nchem * i;
+      for (int v = 0; v < nchem; ++v) c[v] /= s[v];
+    } else {
+      const double* s = inv_scale + (long)nchem * i;
+      for (int v = 0; v < nchem; ++v) c[v] *= s[v];
+    }
   }
 }
 
@@ -208,9 +216,10 @@ int energy_sync(const ChemState& S, double* const* w, long n, int nchem, double 
 }
 
 int energy_epilogue(const ChemState& S, double* chem, double* chemdot, double* etdot, long n,
-                    int nchem, cudaStream_t s) {
+                    int nchem, int exact, cudaStream_t s) {
   ProfScope ps("glue", s);
-  energy_epilogue_kernel<<<grid_for(n, 256), 256, 0, s>>>(S.scale, chem, chemdot, etdot, n, nchem);
+  energy_epilogue_kernel<<<grid_for(n, 256), 256, 0, s>>>(S.scale, S.inv_scale, chem, chemdot,
+                                                           etdot, n, nchem, exact);
   GBMV_LAUNCH_CHECK("energy_epilogue_kernel");
   return GBMV_OK;
 }

@@ -30,7 +30,7 @@ int chem_scaling(const ChemState& S, double* chem, long n, int mode, cudaStream_
 int energy_sync(const ChemState& S, double* const* w, long n, int nchem, double eunit_scale,
                 int restore, cudaStream_t s);
 int energy_epilogue(const ChemState& S, double* chem, double* chemdot, double* etdot, long n,
-                    int nchem, cudaStream_t s);
+                    int nchem, int exact, cudaStream_t s);
 
 // fused source + Jacobian + Newton matrix + LU solve (chem_newton.cu)
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,

@@ -118,23 +118,22 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
     S.dTs_ge[i] = dTs;
     const ChemAux Ax{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
     double f[10];
-    {  // source (the rates are evaluated again for the Jacobian: fewer live registers)
-      double k[kNRates], dk[kNRates];
-      chem_rates<false>(P, Ts, k, dk);
-      double r[21], sp[9];
-      chem_fluxes(k, ya, r);
-      chem_species(r, sp);
-#pragma unroll
-      for (int s = 0; s < 9; ++s) f[s] = (sp[s] * isc[s]) * tunit;
-      double ge = chem_ge_source(P, k, ya, Ts, Ax) * isc[9];
-      ge *= Ax.imdens;
-      f[9] = ge * tunit;
-    }
-#pragma unroll
-    for (int s = 0; s < 10; ++s) fout[j + s] = f[s];
-    {  // A = I - gamma * (J * inv_scale[row] * scale[col] * tunit), FP64 and a float copy
+    {  // source and Newton matrix from one rate evaluation (rates and T slopes)
       double k[kNRates], dk[kNRates];
       chem_rates<true>(P, Ts, k, dk);
+      {
+        double r[21], sp[9];
+        chem_fluxes(k, ya, r);
+        chem_species(r, sp);
+#pragma unroll
+        for (int s = 0; s < 9; ++s) f[s] = (sp[s] * isc[s]) * tunit;
+        double ge = chem_ge_source(P, k, ya, Ts, Ax) * isc[9];
+        ge *= Ax.imdens;
+        f[9] = ge * tunit;
+      }
+#pragma unroll
+      for (int s = 0; s < 10; ++s) fout[j + s] = f[s];
+      // A = I - gamma * (J * inv_scale[row] * scale[col] * tunit), FP64 and a float copy
       double rf[10];  // -gamma * tunit * inv_scale[row]
 #pragma unroll
       for (int r = 0; r < 10; ++r) rf[r] = (-gamma * tunit) * isc[r];
@@ -164,6 +163,9 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
 #pragma unroll
       for (int s = 0; s < 10; ++s) x[s] = (double)xs[s];
       if (sizeof(LU) == 4) {
+        // iterative refinement against FP64 residuals; a cell stops as soon as its correction
+        // is below 1e-13 of the solution (well-conditioned cells need one step, the
+        // ill-conditioned ones use up to `refine`)
         for (int it = 0; it < refine; ++it) {
           double rr[10];
 #pragma unroll
@@ -177,8 +179,14 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
 #pragma unroll
           for (int s = 0; s < 10; ++s) ds[s] = (LU)rr[s];
           lus10_strided<LU, LU>(L, kNtThreads, piv, ds);
+          float dmax = 0.f, xmax = 0.f;
 #pragma unroll
-          for (int s = 0; s < 10; ++s) x[s] += (double)ds[s];
+          for (int s = 0; s < 10; ++s) {
+            x[s] += (double)ds[s];
+            dmax = fmaxf(dmax, fabsf((float)ds[s]));
+            xmax = fmaxf(xmax, fabsf((float)x[s]));
+          }
+          if (dmax <= 1e-13f * xmax) break;
         }
         bool finite = true;
 #pragma unroll

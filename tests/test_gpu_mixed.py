@@ -80,7 +80,7 @@ def test_fused_newton_matches_separate_path(cuda, tables, lu):
     assert ls.setup(J) == 0
     ls.solve(J, x1, f1)
     f2, x2 = torch.empty_like(ys), torch.empty_like(ys)
-    assert c2.newton_iteration(0.0, ys, f2, x2, gamma, tu, lu_precision=lu, refine=2) == 0
+    assert c2.newton_iteration(0.0, ys, f2, x2, gamma, tu, lu_precision=lu, refine=4) == 0
     torch.cuda.synchronize()
     a, b = f1.cpu().numpy().reshape(n, 10), f2.cpu().numpy().reshape(n, 10)
     ftol = 1e-12 if lu == 0 else 1e-9  # mixed: temperature iterations 1-8 in FP32
@@ -106,7 +106,7 @@ def test_fused_newton_against_oracle(cuda, tables):
     c, y, state = _chem_setup(torch, tables, n, 402)
     ys = torch.from_numpy(state).cuda()
     f, x = torch.empty_like(ys), torch.empty_like(ys)
-    assert c.newton_iteration(0.0, ys, f, x, gamma, tu, lu_precision=1, refine=2) == 0
+    assert c.newton_iteration(0.0, ys, f, x, gamma, tu, lu_precision=1, refine=4) == 0
     torch.cuda.synchronize()
     oc = O.Chem(tables, y)
     fr = oc.rhs(state) * tu
