@@ -227,6 +227,20 @@ def algo_bytes(fam, n):
     }[fam]
 
 
+# Arithmetic per unit of each kernel family, counted by ncu on these kernels
+# (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma} or {fadd,fmul,ffma}: adds + muls +
+# 2 x FMAs, per face or cell; profiles/fp_counts_112cube.md) -- the numerator of the compute
+# roofline; the denominator is the FMA rate measured by gbmv_diag_fma_rate.
+FP_COUNTS = {
+    ("fp64", "face_flux"): ("fp64", 3841.3, "face"),
+    ("fp64", "chem_rhs"): ("fp64", 2527.0, "cell"),
+    ("fp64", "chem_jac"): ("fp64", 1003.0, "cell"),
+    ("fp64", "block_lu_factor"): ("fp64", 759.0, "cell"),
+    ("mixed", "face_flux"): ("fp32", 25990.0, "face"),
+    ("mixed", "chem_newton"): ("fp64", 2151.1, "cell"),
+}
+
+
 def timed_form(torch, gbmv, fs, steps, warmup):
     for _ in range(warmup):
         fs.step()
@@ -290,6 +304,16 @@ def run_gbmv(args):
     avg_ms = dt_ms / max(nl, 1)
     key = "face_flux_mx" if (dom == "face_flux" and head == "mixed") else dom
     achieved = algo_bytes(key, args.n) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    pipe = None
+    if (head, dom) in FP_COUNTS:
+        pname, per_unit, unit = FP_COUNTS[(head, dom)]
+        units = (args.n + 1) * args.n * args.n if unit == "face" else ncell
+        peak_pipe = gbmv.fma_rate(pname == "fp64") / 1e12
+        ach = per_unit * units / (avg_ms * 1e-3) / 1e12
+        pipe = {"name": pname, "achieved": round(ach, 4), "peak": round(peak_pipe, 4),
+                "unit": "TFLOP/s", "frac": round(ach / peak_pipe, 4),
+                "flops_per_unit": per_unit, "per": unit,
+                "peak_kind": "measured (gbmv_diag_fma_rate FMA probe)"}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mcells/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
@@ -303,8 +327,12 @@ def run_gbmv(args):
                      "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
                      "peak_kind": f"{peak_kind} hbm_gbs", "traffic": None,
                      "avg_launch_ms": round(avg_ms, 4),
-                     "fp64_peak_tflops_measured": round(fp64_peak, 4)},
+                     "fp64_peak_tflops_measured": round(fp64_peak, 4),
+                     "pipe": pipe},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in fam.items() if v[1]},
+        "kernel_ms_per_step_fp64_form": ({k: round(v[0] / args.steps, 4)
+                                          for k, v in res["fp64"]["fam"].items() if v[1]}
+                                         if "fp64" in res else None),
         "gpu_launches": int(R["launches"]),
         "clocks": R["clocks"],
         "forms": {f: {"ms_per_step": round(r["ms"], 4),

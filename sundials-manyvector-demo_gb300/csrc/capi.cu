@@ -163,7 +163,7 @@ int gbmv_hydro_create(const gbmv_grid* grid, gbmv_hydro* out) {
   memset(&h->force, 0, sizeof h->force);
   h->scratch_doubles = feuler_fp64_scratch_doubles(h->g);
   if (cudaMalloc(&h->scratch, h->scratch_doubles * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&h->d_status, 2 * sizeof(double)) != cudaSuccess) {
     cudaGetLastError();
     set_error("device allocation of %zu flux doubles failed", h->scratch_doubles);
     cudaFree(h->scratch);
@@ -450,9 +450,21 @@ int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double en
 
 int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,
                    void* stream) {
-  (void)h; (void)w; (void)cfl; (void)dt_stab; (void)stream;
-  set_error("gbmv_stability not built yet");
-  return GBMV_EUNSUPPORTED;
+  if (!h || !fields_ok(w, 0) || !dt_stab) return GBMV_EINVAL;
+  Fields W;
+  for (int v = 0; v < 6; ++v) W.f[v] = (v < 5) ? const_cast<double*>(w[v]) : nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(h->d_status);  // 8-byte slot
+  int rc = wave_speed_max(h->g, W, d, s);
+  if (rc) return rc;
+  unsigned long long bits = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&bits, d, sizeof bits, cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  double alpha;
+  memcpy(&alpha, &bits, sizeof alpha);
+  const double dmin = fmin(fmin(h->g.d[0], h->g.d[1]), h->g.d[2]);
+  *dt_stab = cfl * dmin / alpha;
+  return GBMV_OK;
 }
 
 }  // extern "C"

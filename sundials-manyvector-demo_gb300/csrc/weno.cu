@@ -401,4 +401,42 @@ int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTer
   }
 }
 
+// ------------------------------------------------------------------ CFL-stable step (stability)
+//
+// stability (src/utilities.cpp:483-528): alpha = max over cells of |mx/rho| + sqrt(gamma p/rho)
+// -- the reference takes |mx/rho| for all three directions -- and
+// dt = cfl * min(dx, dy, dz) / alpha.  Non-negative doubles order like their bit patterns, so
+// the grid maximum is an atomicMax on the 64-bit integer view; NaN cells are skipped, as the
+// reference's std::max(alpha, NaN) keeps alpha.
+
+__global__ void __launch_bounds__(256) wave_speed_max_kernel(Grid g, Fields w,
+                                                            unsigned long long* __restrict__ out) {
+  double m = 0.0;
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < g.ncell;
+       c += (long)gridDim.x * blockDim.x) {
+    const double rho = w.f[0][c], mx = w.f[1][c];
+    const double u = fabs(mx / rho);
+    const double p = eos64(g.gamma, rho, mx, w.f[2][c], w.f[3][c], w.f[4][c]);
+    const double cs = sqrt0(g.gamma * p / rho);
+    const double a = fabs(u + cs);
+    m = (m < a) ? a : m;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const double o = __shfl_xor_sync(0xffffffffu, m, off);
+    m = (m < o) ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s) {
+  long b = (g.ncell + 255) / 256;
+  if (b > (long)kSM * 8) b = (long)kSM * 8;
+  if (b < 1) b = 1;
+  GBMV_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(unsigned long long), s));
+  wave_speed_max_kernel<<<(int)b, 256, 0, s>>>(g, w, d_out);
+  GBMV_LAUNCH_CHECK("wave_speed_max_kernel");
+  return GBMV_OK;
+}
+
 }  // namespace gbmv

@@ -23,6 +23,8 @@ int feuler_fp64(const Grid& g, const Fields& w, const Fields& wdot, const ForceT
 int feuler_mixed(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
                  double* scratch, int* d_status, cudaStream_t s);
 
+int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s);
+
 size_t feuler_f2_prims_floats(const Grid& g);
 int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
               double* scratch, float* prims, int* d_status, cudaStream_t s);

@@ -165,6 +165,13 @@ class Hydro:
         return _check(load().gbmv_feuler(self.h, t, _vec(w), _vec(wdot), precision,
                                          _stream_ptr(stream)), "gbmv_feuler", allow=(0, -1))
 
+    def stability(self, w, cfl, stream=None) -> float:
+        """CFL-limited step (the reference's ARKStabilityFn `stability`)."""
+        dt = C.c_double()
+        _check(load().gbmv_stability(self.h, _vec(w[:5]), cfl, C.byref(dt), _stream_ptr(stream)),
+               "gbmv_stability")
+        return dt.value
+
     def fEuler_async(self, t, w, wdot, status, precision=FP64, flags=0, stream=None) -> int:
         return _check(load().gbmv_feuler_async(self.h, t, _vec(w), _vec(wdot), precision, flags,
                                                status.data_ptr(), _stream_ptr(stream)),

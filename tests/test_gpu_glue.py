@@ -1,0 +1,90 @@
+"""Chemistry-hydrodynamics glue on the GPU: fexpl / fslow, PostprocessStep and the CFL
+stability function, against the oracle composition of the reference's steps
+(src/multirate_chem_hydro_main.cpp:996-1083, src/imex_chem_hydro_main.cpp:910-1051,
+src/utilities.cpp:483-528)."""
+import numpy as np
+import pytest
+
+import oracle_py as O
+import workloads as W
+from conftest import maxnorm_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _oracle_fexpl(wl, energy_units):
+    f = [x.copy() for x in wl["fields"]]
+    scale = wl["scale"]
+    phys = f[5] * scale                                      # apply_Dengo_scaling
+    f[4] = phys[..., 9] * (1.0 / energy_units) + 0.5 / f[0] * (f[1] * f[1] + f[2] * f[2] + f[3] * f[3])
+    st, out = O.feuler(f[:5] + [phys], 10, wl["bc"], wl["gamma"], None)
+    out[5][..., 9] = out[4]                                  # chemdot[ge] = etdot
+    out[4][:] = 0.0
+    f[5] = phys / scale                                      # unapply_Dengo_scaling
+    return st, out, f
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fexpl_matches_oracle_composition(cuda, tables, precision):
+    torch = cuda
+    import gbmv
+    wl = W.chem_hydro(shape=(16, 12, 10))
+    eu = wl["units"]["EnergyUnits"]
+    st0, ref, wref = _oracle_fexpl(wl, eu)
+    nz, ny, nx = wl["fields"][0].shape
+    h = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"])
+    c = gbmv.Chem(nx * ny * nz, tables)
+    c.set_scale(_dev(torch, wl["scale"].reshape(-1)))
+    w = [_dev(torch, f) for f in wl["fields"]]
+    wdot = [torch.full_like(f, np.nan) for f in w]
+    st = gbmv.fexpl(h, c, 0.0, w, wdot, eu, precision)
+    torch.cuda.synchronize()
+    assert st == st0 == 0
+    tol = 1e-12 if precision == 0 else 1e-6
+    for i, (a, b) in enumerate(zip(wdot, ref)):
+        if i == 5:
+            a2, b2 = a.cpu().numpy().reshape(-1, 10), b.reshape(-1, 10)
+            for s in range(10):
+                assert maxnorm_err(a2[:, s], b2[:, s]) <= tol, (i, s)
+        else:
+            assert maxnorm_err(a.cpu().numpy(), b) <= tol, i
+    # the state is updated as the reference updates it: et from ge, chem*scale/scale
+    assert maxnorm_err(w[4].cpu().numpy(), wref[4]) <= 1e-15
+    assert maxnorm_err(w[5].cpu().numpy(), wref[5]) <= 1e-15
+
+
+def test_postprocess_step(cuda, tables):
+    torch = cuda
+    import gbmv
+    wl = W.chem_hydro(shape=(8, 6, 5))
+    eu = wl["units"]["EnergyUnits"]
+    nz, ny, nx = wl["fields"][0].shape
+    h = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"])
+    c = gbmv.Chem(nx * ny * nz, tables)
+    c.set_scale(_dev(torch, wl["scale"].reshape(-1)))
+    w = [_dev(torch, f) for f in wl["fields"]]
+    gbmv.PostprocessStep(h, c, w, eu)
+    torch.cuda.synchronize()
+    f = wl["fields"]
+    phys = f[5] * wl["scale"]
+    et = phys[..., 9] * (1.0 / eu) + 0.5 / f[0] * (f[1] ** 2 + f[2] ** 2 + f[3] ** 2)
+    assert maxnorm_err(w[4].cpu().numpy(), et) <= 1e-15
+
+
+def test_stability_cfl(cuda):
+    torch = cuda
+    import gbmv
+    wl = W.rayleigh_taylor(shape=(20, 18, 16), nchem=0)
+    nz, ny, nx = wl["fields"][0].shape
+    h = gbmv.Hydro((nx, ny, nz), 0, wl["bc"], wl["gamma"])
+    w = [_dev(torch, f) for f in wl["fields"]]
+    dt = h.stability(w, 0.5)
+    rho, mx, my, mz, et = wl["fields"]
+    p = (wl["gamma"] - 1.0) * (et - (mx * mx + my * my + mz * mz) * 0.5 / rho)
+    alpha = np.max(np.abs(mx / rho) + np.sqrt(wl["gamma"] * p / rho))  # |mx/rho| for all axes
+    ref = 0.5 * min(1.0 / nx, 1.0 / ny, 1.0 / nz) / alpha
+    assert abs(dt - ref) <= 1e-14 * ref
