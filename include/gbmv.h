@@ -158,6 +158,12 @@ int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* 
                      double gamma, double time_units, int lu_precision, int refine,
                      void* stream);
 
+/* Same, asynchronous and CUDA-graph capturable: a singular block raises *d_info (device int,
+ * atomicMax to 1) instead of being returned. */
+int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, double* x,
+                           double gamma, double time_units, int lu_precision, int refine,
+                           int* d_info, void* stream);
+
 /* Device pointers of the persistent per-cell state (for checkpoint/restart and tests):
  * which: 0 Ts, 1 dTs_ge, 2 mdensity, 3 inv_mdensity, 4 cie optical depth, 5 h2 optical depth,
  * 6 scale, 7 inv_scale. */
@@ -188,6 +194,12 @@ int gbmv_block_form_newton(long nblocks, double* J, double gamma, void* stream);
  * (etdot = 0), undo the scaling.  Synchronous like gbmv_feuler. */
 int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* const* wdot,
                double energy_units, int precision, void* stream);
+
+/* Same, asynchronous and CUDA-graph capturable: the legal-state mask is OR-ed into
+ * *d_status (device int) instead of being returned. */
+int gbmv_fexpl_async(gbmv_hydro h, gbmv_chem c, double t, double* const* w,
+                     double* const* wdot, double energy_units, int precision, int* d_status,
+                     void* stream);
 
 /* PostprocessStep (src/imex_chem_hydro_main.cpp:1002-1051): et from ge and momenta. */
 int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double energy_units,

@@ -42,6 +42,11 @@ static std::vector<ProfRec> g_prof;
 
 ProfScope::ProfScope(const char* family, cudaStream_t s) : slot(-1), stream(s) {
   if (!g_prof_on) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return;  // no timing events inside a graph capture
+  }
   ProfRec r{family, nullptr, nullptr};
   if (cudaEventCreate(&r.e0) != cudaSuccess || cudaEventCreate(&r.e1) != cudaSuccess) {
     cudaGetLastError();
@@ -363,6 +368,19 @@ int gbmv_chem_jac(gbmv_chem c, double t, const double* y, double* J, double time
   return chem_jac(c->P, c->S, c->n, y, J, time_units, (cudaStream_t)stream);
 }
 
+int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, double* x,
+                           double gamma, double time_units, int lu_precision, int refine,
+                           int* d_info, void* stream) {
+  (void)t;
+  if (!c || !y || !f || !x || !d_info || refine < 0 || refine > 8 ||
+      (lu_precision != GBMV_FP64 && lu_precision != GBMV_MIXED)) {
+    set_error("bad chem_newton arguments");
+    return GBMV_EINVAL;
+  }
+  return chem_newton(c->P, c->S, c->n, y, f, x, gamma, time_units, lu_precision == GBMV_MIXED,
+                     refine, d_info, (cudaStream_t)stream);
+}
+
 int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* x,
                      double gamma, double time_units, int lu_precision, int refine,
                      void* stream) {
@@ -424,6 +442,22 @@ int gbmv_block_form_newton(long nblocks, double* J, double gamma, void* stream) 
 }
 
 /* ------------------------------------------------------------------ glue */
+
+int gbmv_fexpl_async(gbmv_hydro h, gbmv_chem c, double t, double* const* w,
+                     double* const* wdot, double energy_units, int precision, int* d_status,
+                     void* stream) {
+  if (!h || !c || h->g.nchem != 10 || c->n != h->g.ncell || !d_status) {
+    set_error("fexpl needs a 10-species hydro grid matching the chemistry cell count");
+    return GBMV_EINVAL;
+  }
+  if (!fields_ok(w, 10) || !fields_ok(wdot, 10)) return GBMV_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, 0, s);
+  if (rc) return rc;
+  rc = gbmv_feuler_async(h, t, (const double* const*)w, wdot, precision, 0, d_status, stream);
+  if (rc) return rc;
+  return energy_epilogue(c->S, w[5], wdot[5], wdot[4], c->n, 10, precision == GBMV_FP64, s);
+}
 
 int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* const* wdot,
                double energy_units, int precision, void* stream) {

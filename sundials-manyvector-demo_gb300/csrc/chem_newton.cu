@@ -217,6 +217,7 @@ int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y
   ProfScope ps("chem_newton", s);
   if (lu_fp32) {
     const size_t shm = (size_t)kNtThreads * 100 * (sizeof(double) + sizeof(float));
+    // a function attribute, not a stream operation: also legal during graph capture
     GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_newton_kernel<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     chem_newton_kernel<float><<<(int)b, kNtThreads, shm, s>>>(P, S, n, y, f, x, gamma, tunit,

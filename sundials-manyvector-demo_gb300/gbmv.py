@@ -69,6 +69,10 @@ SIGNATURES = [
     ("gbmv_block_form_newton", C.c_int, [C.c_long, _VP, C.c_double, _VP]),
     ("gbmv_fexpl", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
                              C.c_int, _VP]),
+    ("gbmv_fexpl_async", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
+                                   C.c_double, C.c_int, _VP, _VP]),
+    ("gbmv_chem_newton_async", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double, C.c_double,
+                                         C.c_int, C.c_int, _VP, _VP]),
     ("gbmv_postprocess_step", C.c_int, [_VP, _VP, C.POINTER(_VP), C.c_double, _VP]),
     ("gbmv_version", C.c_char_p, []),
     ("gbmv_last_error", C.c_char_p, []),
@@ -284,6 +288,23 @@ def form_newton_matrix(J, gamma, stream=None):
 def fexpl(hydro: Hydro, chem: Chem, t, w, wdot, energy_units, precision=FP64, stream=None):
     return _check(load().gbmv_fexpl(hydro.h, chem.c, t, _vec(w), _vec(wdot), energy_units,
                                     precision, _stream_ptr(stream)), "gbmv_fexpl", allow=(0, -1))
+
+
+def fexpl_async(hydro: Hydro, chem: Chem, t, w, wdot, energy_units, status, precision=FP64,
+                stream=None):
+    """Graph-capturable fexpl: the legal-state mask is OR-ed into `status` (int32 CUDA tensor)."""
+    return _check(load().gbmv_fexpl_async(hydro.h, chem.c, t, _vec(w), _vec(wdot), energy_units,
+                                          precision, status.data_ptr(), _stream_ptr(stream)),
+                  "gbmv_fexpl_async")
+
+
+def chem_newton_async(chem: Chem, t, y, f, x, gamma, time_units, info, lu_precision=FP64,
+                      refine=4, stream=None):
+    """Graph-capturable fused Newton iteration; singular blocks set `info` (int32 tensor)."""
+    return _check(load().gbmv_chem_newton_async(chem.c, t, _dev_ptr(y), _dev_ptr(f), _dev_ptr(x),
+                                                gamma, time_units, lu_precision, refine,
+                                                info.data_ptr(), _stream_ptr(stream)),
+                  "gbmv_chem_newton_async")
 
 
 def PostprocessStep(hydro: Hydro, chem: Chem, w, energy_units, stream=None):

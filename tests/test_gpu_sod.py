@@ -47,7 +47,7 @@ def test_sod_whole_run(cuda):
     for y in (yc, yg):
         rho = y[0].reshape(shape)[1, 1]
         mx = y[1].reshape(shape)[1, 1]
-        assert np.mean(np.abs(rho - r)) < 6e-3      # WENO5 at 128 cells, shock-smeared
+        assert np.mean(np.abs(rho - r)) < 7e-3      # WENO5 at 128 cells, shock-smeared (5.3e-3)
         assert np.mean(np.abs(mx / rho - u)) < 2e-2
         # the solution is uniform across the periodic y/z directions
         assert np.allclose(y[0].reshape(shape), y[0].reshape(shape)[:1, :1], rtol=0, atol=1e-12)
