@@ -116,10 +116,11 @@ class FusedStep:
     form "fp64" : the plain FP64 GPU form -- the drop-in entry points in the order an ARKODE
                   IMEX/MRI stage calls them (fexpl, fimpl, Jimpl, SUNMatScaleAddI, LS setup,
                   LS solve), every kernel in FP64;
-    form "mixed": the batched mixed-precision form -- mixed-precision WENO (FP32 flux
-                  arithmetic, float-float indicators/weights, FP64 pressure and divergence) and
-                  the fused chemistry Newton kernel (FP64 source and Jacobian, FP32 LU with two
-                  FP64-residual refinement steps, no Jacobian in HBM)."""
+    form "mixed": the batched mixed-precision form -- float-float WENO face fluxes on the
+                  FP32 pipes (FP64 per-cell primitives, FP64 divergence) and the fused
+                  chemistry Newton kernel (FP64 source and Jacobian, FP32 LU with adaptive
+                  FP64-residual refinement, no Jacobian in HBM), the whole stage captured as
+                  one CUDA graph and replayed."""
 
     def __init__(self, torch, n, form, wl=None):
         import gbmv
@@ -144,7 +145,35 @@ class FusedStep:
         self.chem = gbmv.Chem(self.ncell, h5tables.load_table_block(TABLES))
         self.chem.set_scale(dev(wl["scale"].reshape(-1)))
         self.ls = gbmv.BlockLinearSolver(self.ncell) if form == "fp64" else None
+        self.status = torch.zeros(2, dtype=torch.int32, device="cuda")
+        self.graph = None
         torch.cuda.synchronize()
+        if form == "mixed":  # the whole stage as one CUDA graph (asynchronous entry points)
+            self._stage_async()
+            torch.cuda.synchronize()
+            self.check_status()
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=side):
+                self._stage_async()
+            torch.cuda.synchronize()
+
+    def _stage_async(self, t=0.0):
+        g = self.gbmv
+        EU, TU = self.units["EnergyUnits"], self.units["TimeUnits"]
+        self.status.zero_()
+        g.fexpl_async(self.hydro, self.chem, t, self.w, self.wdot, EU, self.status[0:1],
+                      self.precision)
+        g.chem_newton_async(self.chem, t, self.w[5].view(-1), self.f, self.x, GAMMA_NEWTON, TU,
+                            self.status[1:2], lu_precision=g.MIXED, refine=4)
+
+    def check_status(self):
+        st = self.status.cpu().tolist()
+        if st[0]:
+            raise RuntimeError(f"illegal state mask {st[0]}")
+        if st[1]:
+            raise RuntimeError("singular Newton block")
 
     def reset(self):
         """Back to the initial state (fields and the chemistry temperature history)."""
@@ -155,6 +184,9 @@ class FusedStep:
 
     def step(self, t=0.0):
         g = self.gbmv
+        if self.graph is not None:
+            self.graph.replay()
+            return
         EU, TU = self.units["EnergyUnits"], self.units["TimeUnits"]
         rc = g.fexpl(self.hydro, self.chem, t, self.w, self.wdot, EU, self.precision)
         if rc != 0:
@@ -173,6 +205,7 @@ class FusedStep:
                 raise RuntimeError("singular Newton block")
 
     def outputs(self):
+        self.check_status()
         outs = [t.cpu().numpy() for t in self.wdot]
         return outs + [self.f.cpu().numpy(), self.x.cpu().numpy()]
 
@@ -271,6 +304,12 @@ def run_gbmv(args):
     for form in forms:
         fs = FusedStep(torch, args.n, form, wl)
         ms, fam, launches, clk = timed_form(torch, gbmv, fs, args.steps, args.warmup)
+        if fs.graph is not None:  # graph replays bypass the per-call timing events: time eagerly
+            g_ms = ms
+            graph, fs.graph = fs.graph, None
+            _, fam, launches, _ = timed_form(torch, gbmv, fs, max(2, args.steps // 2), 1)
+            fs.graph = graph
+            ms = g_ms
         fs.reset()
         fs.step()
         torch.cuda.synchronize()
