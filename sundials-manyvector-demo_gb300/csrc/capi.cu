@@ -216,6 +216,12 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
   cudaStream_t s = (cudaStream_t)stream;
   if (precision == GBMV_FP64) return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
   if (!h->prims) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      set_error("the first GBMV_MIXED call on a handle allocates its buffers: make it before "
+                "any stream capture");
+      return GBMV_EINVAL;
+    }
     const size_t nf = feuler_f2_prims_floats(h->g);
     if (cudaMalloc(&h->prims, nf * sizeof(float)) != cudaSuccess) {
       cudaGetLastError();
