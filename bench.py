@@ -23,6 +23,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -63,8 +64,7 @@ class ClockSampler:
 
     def __init__(self, gpu_index: int = 0):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                                 else "_work", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"gbmv_clocks_{os.getpid()}.csv")
         self.gpu = gpu_index
 
     def __enter__(self):
@@ -73,7 +73,7 @@ class ClockSampler:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}",
                                           f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
-                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -304,16 +304,21 @@ def run_gbmv(args):
     for form in forms:
         fs = FusedStep(torch, args.n, form, wl)
         ms, fam, launches, clk = timed_form(torch, gbmv, fs, args.steps, args.warmup)
+        fam_steps = args.steps
         if fs.graph is not None:  # graph replays bypass the per-call timing events: time eagerly
             g_ms = ms
             graph, fs.graph = fs.graph, None
-            _, fam, launches, _ = timed_form(torch, gbmv, fs, max(2, args.steps // 2), 1)
+            fam_steps = max(2, args.steps // 2)
+            _, fam, el, _ = timed_form(torch, gbmv, fs, fam_steps, 1)
+            # replays launch the captured kernels: the eager count per step times the steps
+            launches = el // fam_steps * args.steps
             fs.graph = graph
             ms = g_ms
         fs.reset()
         fs.step()
         torch.cuda.synchronize()
-        res[form] = dict(fs=fs, ms=ms, fam=fam, launches=launches, clocks=clk, out=fs.outputs())
+        res[form] = dict(fs=fs, ms=ms, fam=fam, fam_steps=fam_steps, launches=launches, clocks=clk,
+                         out=fs.outputs())
         if form != forms[-1]:
             del fs.J
             res[form]["fs"] = None
@@ -368,8 +373,8 @@ def run_gbmv(args):
                      "avg_launch_ms": round(avg_ms, 4),
                      "fp64_peak_tflops_measured": round(fp64_peak, 4),
                      "pipe": pipe},
-        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in fam.items() if v[1]},
-        "kernel_ms_per_step_fp64_form": ({k: round(v[0] / args.steps, 4)
+        "kernel_ms_per_step": {k: round(v[0] / R["fam_steps"], 4) for k, v in fam.items() if v[1]},
+        "kernel_ms_per_step_fp64_form": ({k: round(v[0] / res["fp64"]["fam_steps"], 4)
                                           for k, v in res["fp64"]["fam"].items() if v[1]}
                                          if "fp64" in res else None),
         "gpu_launches": int(R["launches"]),

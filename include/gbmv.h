@@ -164,6 +164,57 @@ int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, do
                            double gamma, double time_units, int lu_precision, int refine,
                            int* d_info, void* stream);
 
+/* Options of the persistent DIRK chemistry integrator (gbmv_chem_dirk_evolve). */
+typedef struct {
+  double rtol, atol; /* WRMS weights 1 / (rtol |z| + atol) on the scaled variables */
+  double nlscoef;    /* Newton convergence factor (ARKODE's nlscoef; default 0.1) */
+  double h0;         /* first step in time units of t; <= 0: from ||F(z0)|| (default 0) */
+  double safety;     /* step-size safety factor (default 0.9) */
+  double dgmax;      /* refactor when |gamma / gamma_p - 1| > dgmax (default 0.2) */
+  double growth;     /* largest step growth after the first step (default 20) */
+  double etamx1;     /* largest growth on the first step (default 10000) */
+  double hmax;       /* largest step, <= 0: none (default 0) */
+  int maxcor;        /* Newton iterations per stage (default 3) */
+  int max_steps;     /* steps per cell before it counts as failed (default 5000) */
+  int msbp;          /* refactor the Newton matrix at least every msbp steps (default 20) */
+  int msbj;          /* new Jacobian at least every msbj steps (default 50) */
+  int maxnef;        /* error-test failures per step (default 7) */
+  int maxncf;        /* Newton failures per step (default 10) */
+  int precision;     /* GBMV_FP64: FP64 LU and temperature; GBMV_MIXED: FP32 LU (+ refine),
+                        temperature iterations 1-8 in FP32 (default GBMV_FP64) */
+  int refine;        /* GBMV_MIXED: FP64-residual refinement steps per solve, 0-8 (default 1) */
+  int block;         /* threads per block: 32, 64 or 128; 0 = autotuned (default 0) */
+} gbmv_dirk_opts;
+
+/* Fill *o with the defaults above (rtol 1e-6, atol 1e-10). */
+void gbmv_dirk_opts_default(gbmv_dirk_opts* o);
+
+/* Integrate every cell's chemistry dz/dt = time_units * f_chem(z) (scaled variables, as
+ * gbmv_chem_rhs) from t0 to tout with an adaptive TR-BDF2 ESDIRK and modified Newton on
+ * per-cell 10x10 systems, each cell on its own step sequence, in one persistent launch that
+ * retires finished cells and pulls new ones.  It replaces the fast-stage integration of the
+ * chemistry drivers: ARKStep DIRK + Jfast/Jimpl + the block solver
+ * (src/primordial_ode_main.cpp) and the rank-local MRI inner stepper's evolve
+ * (src/multirate_chem_hydro_main.cpp:1114-1224), with per-cell instead of rank-wide step
+ * control.  y: 10 * ncells device doubles, updated in place; the temperature state is
+ * carried.  stats: NULL or 8 device ints per cell (steps, Newton iterations, error-test
+ * failures, Newton failures, matrix setups, Jacobian evaluations, F evaluations, failed).
+ * With opts->block == 0 the first call per precision times each block size on a sample of
+ * the cells (state restored) and keeps the fastest: make that call before any stream capture.
+ * Returns the number of failed cells (>= 0; their y holds the last accepted step) or a
+ * negative GBMV_E* code.  Synchronous. */
+int gbmv_chem_dirk_evolve(gbmv_chem c, double t0, double tout, double* y, double time_units,
+                          const gbmv_dirk_opts* opts, int* stats, void* stream);
+
+/* Same, asynchronous and graph-capturable (opts->block must be set, or tuned by an earlier
+ * call): the failed-cell count is added to *d_nfail (device int, caller-zeroed). */
+int gbmv_chem_dirk_evolve_async(gbmv_chem c, double t0, double tout, double* y,
+                                double time_units, const gbmv_dirk_opts* opts, int* stats,
+                                int* d_nfail, void* stream);
+
+/* Block size the autotuner chose for a precision (0 = not tuned yet). */
+int gbmv_chem_dirk_block(gbmv_chem c, int precision);
+
 /* Device pointers of the persistent per-cell state (for checkpoint/restart and tests):
  * which: 0 Ts, 1 dTs_ge, 2 mdensity, 3 inv_mdensity, 4 cie optical depth, 5 h2 optical depth,
  * 6 scale, 7 inv_scale. */

@@ -623,3 +623,201 @@ long orc_block_newton_solve(long n, const double* J, double gamma, const double*
   }
   return first_bad;
 }
+
+/* ------------------------------------------------------------------------------------------
+ * Per-cell adaptive DIRK integration of the scaled chemistry system dz/dt = tunit * f(z):
+ * the CPU restatement of the persistent GPU integrator (gbmv_chem_dirk_evolve), FP64
+ * throughout.  The reference integrates the same system with ARKStep (DIRK + Newton +
+ * block-diagonal direct solver, src/primordial_ode_main.cpp) over all cells at once; this
+ * restatement applies ARKODE's Newton and step rules per cell (see oracle.h).
+ * TR-BDF2 ESDIRK pair: A = [[0,0,0],[gd,gd,0],[w,w,gd]], b = (w,w,gd),
+ * bhat = ((1-w)/3, (3w+1)/3, gd/3) (Hosea & Shampine 1996). */
+#define DK_SQRT2 1.4142135623730951
+static const double dk_gd = (2.0 - DK_SQRT2) / 2.0;
+static const double dk_w = DK_SQRT2 / 4.0;
+
+static void dirk_F(const orc_chem* c, const double* X, const double* sc, const double* isc,
+                   double md, double imd, double cie, double h2, double tunit, double* Ts,
+                   double* dTs, double* f) {
+  double ya[10], k[NRATES], dk[NRATES], r[21];
+  for (int s = 0; s < 10; ++s) ya[s] = X[s] * sc[s];
+  temperature(c, ya, Ts, dTs);
+  rates_at(c, *Ts, k, dk);
+  reaction_fluxes(k, ya, r);
+  for (int s = 0; s < 9; ++s) f[s] = (species_sum(s, r) * isc[s]) * tunit;
+  double ge = ge_source(c, k, ya, *Ts, md, cie, h2) * isc[9];
+  ge *= imd;
+  f[9] = ge * tunit;
+}
+
+static double dk_wrms(const double* v, const double* ew) {
+  double s2 = 0.0;
+  for (int s = 0; s < 10; ++s) {
+    const double q = v[s] * ew[s];
+    s2 += q * q;
+  }
+  return sqrt(s2 / 10.0);
+}
+
+long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* scale,
+                          const double* inv_scale, const double* mdens, const double* imdens,
+                          const double* cie_oda, const double* h2_oda, double* Ts, double* dTs_ge,
+                          const orc_dirk_opts* O, int* stats) {
+  const double e1 = dk_w - (1.0 - dk_w) / 3.0, e2 = dk_w - (3.0 * dk_w + 1.0) / 3.0,
+               e3 = dk_gd - dk_gd / 3.0;
+  long nfail = 0;
+  for (long i = 0; i < n; ++i) {
+    const long j = i * 10;
+    const double *sc = scale + j, *isc = inv_scale + j;
+    const double md = mdens[i], imd = imdens[i], cie = cie_oda[i], h2 = h2_oda[i];
+    double Y[10], K1[10], K2[10], Z[10], EW[10], f[10], J[100], A[100];
+    int piv[10];
+    for (int s = 0; s < 10; ++s) Y[s] = y[j + s];
+    double Tsc = Ts[i], dTsc = dTs_ge[i], Tsy, dTsy;
+    double t = O->t0, h = O->h0, gp = 0.0, crate = 1.0, delp = 0.0;
+    int nst = 0, nst_lp = 0, nst_lj = 0, nef_s = 0, ncf_s = 0;
+    int nni = 0, netf = 0, ncf = 0, nsetup = 0, nje = 0, nfe = 0;
+    int jcur = 0, need_jac = 1, last = 0, failed = 0;
+    dirk_F(c, Y, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, K1);
+    ++nfe;
+    Tsy = Tsc;
+    dTsy = dTsc;
+    if (h <= 0.0) {
+      double s2 = 0.0;
+      for (int s = 0; s < 10; ++s) {
+        const double v = K1[s] / (O->rtol * fabs(Y[s]) + O->atol);
+        s2 += v * v;
+      }
+      const double fn = sqrt(s2 / 10.0);
+      h = (fn > 0.0) ? O->h0fac / fn : O->tout - t;
+    }
+    if (O->hmax > 0.0 && h > O->hmax) h = O->hmax;
+    for (;;) {
+      /* step setup: weights, predictor, Jacobian / Newton matrix as needed */
+      for (;;) {
+        last = (t + h >= O->tout);
+        if (last) h = O->tout - t;
+        Tsc = Tsy;
+        dTsc = dTsy;
+        for (int s = 0; s < 10; ++s) {
+          EW[s] = 1.0 / (O->rtol * fabs(Y[s]) + O->atol);
+          Z[s] = Y[s];
+        }
+        const double gam = h * dk_gd;
+        int refactor = 0;
+        if (need_jac || nst >= nst_lj + O->msbj) {
+          double B[100];
+          orc_chem_jac(c, 1, Y, sc, isc, &mdens[i], &cie_oda[i], &h2_oda[i], &Tsy, &dTsy, B);
+          for (int e = 0; e < 100; ++e) J[e] = B[e] * O->tunit;
+          ++nje;
+          nst_lj = nst;
+          jcur = 1;
+          need_jac = 0;
+          refactor = 1;
+        }
+        if (refactor || nst >= nst_lp + O->msbp || !(fabs(gam / gp - 1.0) <= O->dgmax)) {
+          for (int col = 0; col < 10; ++col)
+            for (int r = 0; r < 10; ++r)
+              A[col * 10 + r] = (r == col ? 1.0 : 0.0) - gam * J[col * 10 + r];
+          const int info = lu10(A, piv);
+          gp = gam;
+          nst_lp = nst;
+          crate = 1.0;
+          ++nsetup;
+          if (info) {
+            ++ncf_s;
+            ++ncf;
+            if (ncf_s >= O->maxncf) { failed = 1; break; }
+            h *= 0.25;
+            if (!jcur) need_jac = 1;
+            gp = 0.0;
+            continue;
+          }
+        }
+        break;
+      }
+      if (failed) break;
+      /* stages 2 and 3 by modified Newton */
+      int conv = 1;
+      for (int stage = 2; stage <= 3 && conv; ++stage) {
+        const double gam = h * dk_gd, hw = h * dk_w;
+        int m = 0;
+        conv = 0;
+        for (;;) {
+          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, f);
+          ++nfe;
+          double dl[10];
+          for (int s = 0; s < 10; ++s)
+            dl[s] = (stage == 2) ? (Y[s] + gam * K1[s]) + gam * f[s] - Z[s]
+                                 : (Y[s] + hw * (K1[s] + K2[s])) + gam * f[s] - Z[s];
+          lus10(A, piv, dl);
+          if (gam != gp) {
+            const double scl = 2.0 / (1.0 + gam / gp);
+            for (int s = 0; s < 10; ++s) dl[s] *= scl;
+          }
+          for (int s = 0; s < 10; ++s) Z[s] += dl[s];
+          const double del = dk_wrms(dl, EW);
+          ++m;
+          ++nni;
+          if (m > 1) crate = fmax(0.3 * crate, del / delp);
+          if (fmin(crate, 1.0) * del / O->nlscoef <= 1.0) { conv = 1; break; }
+          if ((m > 1 && del > 2.3 * delp) || m >= O->maxcor || !(del == del)) break;
+          delp = del;
+        }
+        if (conv && stage == 2) {
+          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, K2);
+          ++nfe;
+        }
+      }
+      if (!conv) {
+        ++ncf_s;
+        ++ncf;
+        if (ncf_s >= O->maxncf) { failed = 1; break; }
+        if (jcur) h *= 0.25;
+        else need_jac = 1;
+        continue;
+      }
+      dirk_F(c, Z, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, f);
+      ++nfe;
+      double err[10];
+      for (int s = 0; s < 10; ++s) err[s] = h * ((e1 * K1[s] + e2 * K2[s]) + e3 * f[s]);
+      const double dsm = dk_wrms(err, EW);
+      if (dsm <= 1.0) {
+        ++nst;
+        t = last ? O->tout : t + h;
+        for (int s = 0; s < 10; ++s) {
+          Y[s] = Z[s];
+          K1[s] = f[s];
+        }
+        Tsy = Tsc;
+        dTsy = dTsc;
+        jcur = 0;
+        double eta = (dsm > 0.0) ? O->safety / cbrt(dsm) : 1.0e300;
+        eta = fmin(eta, nst == 1 ? O->etamx1 : O->growth);
+        if (nef_s > 0 || ncf_s > 0) eta = fmin(eta, 1.0);
+        h *= eta;
+        if (O->hmax > 0.0 && h > O->hmax) h = O->hmax;
+        nef_s = ncf_s = 0;
+        if (last) break;
+        if (nst >= O->max_steps) { failed = 1; break; }
+      } else {
+        ++nef_s;
+        ++netf;
+        if (nef_s >= O->maxnef) { failed = 1; break; }
+        double eta = fmax(0.1, O->safety / cbrt(dsm));
+        if (nef_s >= 2) eta = fmin(eta, 0.3);
+        h *= eta;
+      }
+    }
+    for (int s = 0; s < 10; ++s) y[j + s] = Y[s];
+    Ts[i] = Tsy;
+    dTs_ge[i] = dTsy;
+    if (stats) {
+      int* st = stats + i * 8;
+      st[0] = nst; st[1] = nni; st[2] = netf; st[3] = ncf;
+      st[4] = nsetup; st[5] = nje; st[6] = nfe; st[7] = failed;
+    }
+    nfail += failed;
+  }
+  return nfail;
+}

@@ -79,6 +79,24 @@ void orc_chem_jac(const orc_chem* c, long n, const double* y, const double* scal
  * pivoting, then solve A_i x_i = b_i.  Returns 0 or (1 + first singular block index). */
 long orc_block_newton_solve(long n, const double* J, double gamma, const double* b, double* x);
 
+/* Options of orc_chem_dirk_evolve (the fields of gbmv_dirk_opts plus the resolved times). */
+typedef struct {
+  double t0, tout, tunit;
+  double rtol, atol, nlscoef, h0, h0fac, safety, dgmax, growth, etamx1, hmax;
+  int maxcor, max_steps, msbp, msbj, maxnef, maxncf;
+} orc_dirk_opts;
+
+/* Per-cell adaptive TR-BDF2 ESDIRK integration of dz/dt = tunit * f_chem(z) (scaled
+ * variables, as orc_chem_rhs x tunit) from t0 to tout, modified Newton with ARKODE's
+ * convergence, reuse and step rules, FP64 LU; the algorithm of the GPU integrator
+ * (gbmv_chem_dirk_evolve).  y, Ts, dTs_ge updated in place; stats (8 ints per cell, or NULL):
+ * steps, Newton iterations, error-test failures, Newton failures, matrix setups, Jacobians,
+ * F evaluations, failed.  Returns the number of failed cells. */
+long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* scale,
+                          const double* inv_scale, const double* mdens, const double* imdens,
+                          const double* cie_oda, const double* h2_oda, double* Ts, double* dTs_ge,
+                          const orc_dirk_opts* O, int* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,6 +44,19 @@ class OrcChem(C.Structure):
                 ("thi", C.c_double), ("z", C.c_double)]
 
 
+class OrcDirkOpts(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("t0", "tout", "tunit", "rtol", "atol", "nlscoef", "h0",
+                                          "h0fac", "safety", "dgmax", "growth", "etamx1",
+                                          "hmax")] + \
+               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "msbj", "maxnef", "maxncf")]
+
+
+# defaults of gbmv_dirk_opts_default (include/gbmv.h)
+DIRK_DEFAULTS = dict(rtol=1e-6, atol=1e-10, nlscoef=0.1, h0=0.0, safety=0.9, dgmax=0.2,
+                     growth=20.0, etamx1=10000.0, hmax=0.0, maxcor=3, max_steps=5000, msbp=20,
+                     msbj=50, maxnef=7, maxncf=10)
+
+
 def _ptr(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_P)
@@ -58,6 +71,7 @@ def lib():
         _lib = C.CDLL(build())
         _lib.orc_feuler.restype = C.c_int
         _lib.orc_block_newton_solve.restype = C.c_long
+        _lib.orc_chem_dirk_evolve.restype = C.c_long
     return _lib
 
 
@@ -127,6 +141,23 @@ class Chem:
                            _ptr(self.inv_scale), _ptr(self.mdens), _ptr(self.cie),
                            _ptr(self.h2), _ptr(self.Ts), _ptr(self.dTs_ge), _ptr(J))
         return J.reshape(self.n, 10, 10)  # [cell][col][row]
+
+    def dirk_evolve(self, y: np.ndarray, t0: float, tout: float, tunit: float, **opts):
+        """Per-cell adaptive TR-BDF2 integration from t0 to tout (orc_chem_dirk_evolve).
+        Returns (y(tout), stats[n, 8], number of failed cells); Ts / dTs_ge carried."""
+        o = dict(DIRK_DEFAULTS, **opts)
+        O = OrcDirkOpts()
+        O.t0, O.tout, O.tunit = t0, tout, tunit
+        for k, v in o.items():
+            setattr(O, k, v)
+        O.h0fac = 0.5 * o["rtol"] ** (-2.0 / 3.0)
+        y = np.array(y, dtype=np.float64).reshape(-1)
+        stats = np.zeros((self.n, 8), dtype=np.int32)
+        nf = lib().orc_chem_dirk_evolve(
+            C.byref(self.c), C.c_long(self.n), _ptr(y), _ptr(self.scale), _ptr(self.inv_scale),
+            _ptr(self.mdens), _ptr(self.imdens), _ptr(self.cie), _ptr(self.h2), _ptr(self.Ts),
+            _ptr(self.dTs_ge), C.byref(O), stats.ctypes.data_as(C.POINTER(C.c_int)))
+        return y, stats, int(nf)
 
 
 def block_newton_solve(J: np.ndarray, gamma: float, b: np.ndarray):

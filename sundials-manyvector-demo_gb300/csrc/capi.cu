@@ -82,7 +82,10 @@ struct gbmv_chem_s {
   ChemState S{};
   double* tab = nullptr;
   double* cell = nullptr;  // one allocation for all per-cell arrays
-  int* d_info = nullptr;
+  int* d_info = nullptr;               // first word of a 64-byte control block:
+  int* d_nfail = nullptr;              //   [0] info, [1] failed cells,
+  unsigned long long* d_next = nullptr;  //   [16] DIRK work counter
+  int dirk_block[2] = {0, 0};          // autotuned block size per precision (0 = not yet)
 };
 
 static int check_grid(const gbmv_grid* g) {
@@ -266,7 +269,7 @@ int gbmv_chem_create(long ncells, const double* tables_host, double current_z, g
   const size_t per_cell = 10 + 10 + 6;
   if (cudaMalloc(&c->tab, sizeof(double) * kNT * kTSize) != cudaSuccess ||
       cudaMalloc(&c->cell, sizeof(double) * per_cell * ncells) != cudaSuccess ||
-      cudaMalloc(&c->d_info, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&c->d_info, 64) != cudaSuccess) {
     cudaGetLastError();
     free(h);
     cudaFree(c->tab);
@@ -275,6 +278,8 @@ int gbmv_chem_create(long ncells, const double* tables_host, double current_z, g
     set_error("device allocation failed for %ld cells", ncells);
     return GBMV_ENOMEM;
   }
+  c->d_nfail = c->d_info + 1;
+  c->d_next = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(c->d_info) + 16);
   cudaMemcpy(c->tab, h, sizeof(double) * kNT * kTSize, cudaMemcpyHostToDevice);
   free(h);
   // constants of cvklu_setup_data (src/raja_primordial_network.cpp:190-194)
@@ -406,6 +411,176 @@ int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* 
   GBMV_CUDA_TRY(cudaStreamSynchronize(s));
   if (h) { set_error("singular Newton block"); return 1; }
   return GBMV_OK;
+}
+
+/* ------------------------------------------------------------------ DIRK integrator */
+
+void gbmv_dirk_opts_default(gbmv_dirk_opts* o) {
+  if (!o) return;
+  o->rtol = 1e-6;
+  o->atol = 1e-10;
+  o->nlscoef = 0.1;
+  o->h0 = 0.0;
+  o->safety = 0.9;
+  o->dgmax = 0.2;
+  o->growth = 20.0;
+  o->etamx1 = 10000.0;
+  o->hmax = 0.0;
+  o->maxcor = 3;
+  o->max_steps = 5000;
+  o->msbp = 20;
+  o->msbj = 50;
+  o->maxnef = 7;
+  o->maxncf = 10;
+  o->precision = GBMV_FP64;
+  o->refine = 1;
+  o->block = 0;
+}
+
+static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tunit, DirkOpts* O) {
+  if (!o || !(o->rtol > 0.0) || !(o->atol > 0.0) || !(o->nlscoef > 0.0) || !(o->safety > 0.0) ||
+      !(o->dgmax >= 0.0) || !(o->growth >= 1.0) || !(o->etamx1 >= 1.0) || !(o->hmax >= 0.0) ||
+      o->maxcor < 1 || o->max_steps < 1 || o->msbp < 1 || o->msbj < 1 ||
+      o->maxnef < 1 || o->maxncf < 1 || o->refine < 0 || o->refine > 8 ||
+      (o->precision != GBMV_FP64 && o->precision != GBMV_MIXED) ||
+      (o->block != 0 && o->block != 32 && o->block != 64 && o->block != 128) ||
+      !(tout > t0) || !(tunit > 0.0)) {
+    set_error("bad DIRK options (tolerances > 0, growth >= 1, hmax >= 0, counts >= 1, refine 0-8, "
+              "block 0/32/64/128, tout > t0, time_units > 0)");
+    return GBMV_EINVAL;
+  }
+  O->t0 = t0;
+  O->tout = tout;
+  O->tunit = tunit;
+  O->rtol = o->rtol;
+  O->atol = o->atol;
+  O->nlscoef = o->nlscoef;
+  O->h0 = o->h0;
+  O->h0fac = 0.5 * pow(o->rtol, -2.0 / 3.0);  // h0 = rtol^(1/3) x (time scale |z|/|F|) / 2
+  O->safety = o->safety;
+  O->dgmax = o->dgmax;
+  O->growth = o->growth;
+  O->etamx1 = o->etamx1;
+  O->hmax = o->hmax;
+  O->maxcor = o->maxcor;
+  O->max_steps = o->max_steps;
+  O->msbp = o->msbp;
+  O->msbj = o->msbj;
+  O->maxnef = o->maxnef;
+  O->maxncf = o->maxncf;
+  O->refine = o->precision == GBMV_MIXED ? o->refine : 0;
+  O->mixed_temp = o->precision == GBMV_MIXED;
+  return GBMV_OK;
+}
+
+static int ck(cudaError_t e, const char* where) {
+  return e == cudaSuccess ? GBMV_OK : check_cuda(e, where);
+}
+
+// Block-size autotuner: integrates a sample of the cells (the first min(n, 65536), their
+// temperature state saved and restored) once per candidate and keeps the fastest.
+static int dirk_autotune(gbmv_chem c, const double* y, const DirkOpts& O, int mixed,
+                         cudaStream_t s) {
+  const long ns = c->n < 65536 ? c->n : 65536;
+  double *ybuf = nullptr, *tsave = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int best = 64;
+  float best_ms = 0.f;
+  int rc = GBMV_OK;
+  if (cudaMalloc(&ybuf, sizeof(double) * 10 * ns) != cudaSuccess ||
+      cudaMalloc(&tsave, sizeof(double) * 2 * ns) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    rc = check_cuda(cudaErrorMemoryAllocation, "DIRK autotune buffers");
+  }
+  if (!rc) rc = ck(cudaMemcpyAsync(tsave, c->S.Ts, sizeof(double) * ns,
+                                           cudaMemcpyDeviceToDevice, s), "autotune save");
+  if (!rc) rc = ck(cudaMemcpyAsync(tsave + ns, c->S.dTs_ge, sizeof(double) * ns,
+                                           cudaMemcpyDeviceToDevice, s), "autotune save");
+  const int cand[3] = {32, 64, 128};
+  for (int k = 0; k < 3 && !rc; ++k) {
+    rc = ck(cudaMemcpyAsync(ybuf, y, sizeof(double) * 10 * ns, cudaMemcpyDeviceToDevice, s),
+                    "autotune sample");
+    if (!rc) rc = ck(cudaMemcpyAsync(c->S.Ts, tsave, sizeof(double) * ns,
+                                             cudaMemcpyDeviceToDevice, s), "autotune restore");
+    if (!rc) rc = ck(cudaMemcpyAsync(c->S.dTs_ge, tsave + ns, sizeof(double) * ns,
+                                             cudaMemcpyDeviceToDevice, s), "autotune restore");
+    if (!rc) rc = ck(cudaEventRecord(e0, s), "autotune event");
+    if (rc) break;
+    const int r = chem_dirk(c->P, c->S, ns, ybuf, O, mixed, cand[k], c->d_next, nullptr,
+                            c->d_info, s);  // failures of the sample land in a scratch word
+    if (r == GBMV_EUNSUPPORTED) continue;  // does not fit on an SM
+    if (r) { rc = r; break; }
+    rc = ck(cudaEventRecord(e1, s), "autotune event");
+    if (!rc) rc = ck(cudaEventSynchronize(e1), "autotune run");
+    float ms = 0.f;
+    if (!rc) rc = ck(cudaEventElapsedTime(&ms, e0, e1), "autotune time");
+    if (!rc && (best_ms == 0.f || ms < best_ms)) { best_ms = ms; best = cand[k]; }
+  }
+  if (!rc) {
+    rc = ck(cudaMemcpyAsync(c->S.Ts, tsave, sizeof(double) * ns, cudaMemcpyDeviceToDevice, s),
+                    "autotune restore");
+    if (!rc) rc = ck(cudaMemcpyAsync(c->S.dTs_ge, tsave + ns, sizeof(double) * ns,
+                                             cudaMemcpyDeviceToDevice, s), "autotune restore");
+    if (!rc) rc = ck(cudaStreamSynchronize(s), "autotune restore");
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(ybuf);
+  cudaFree(tsave);
+  if (rc) return rc;
+  c->dirk_block[mixed] = best;
+  return GBMV_OK;
+}
+
+static int dirk_launch(gbmv_chem c, double t0, double tout, double* y, double time_units,
+                       const gbmv_dirk_opts* opts, int* stats, int* d_nfail, cudaStream_t s,
+                       bool may_tune) {
+  if (!c || !y || !d_nfail) { set_error("null argument"); return GBMV_EINVAL; }
+  DirkOpts O;
+  int rc = dirk_opts(opts, t0, tout, time_units, &O);
+  if (rc) return rc;
+  const int mixed = opts->precision == GBMV_MIXED;
+  int block = opts->block ? opts->block : c->dirk_block[mixed];
+  if (!block) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (!may_tune ||
+        (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)) {
+      set_error("DIRK block size not tuned yet: set opts->block or make a synchronous call first");
+      return GBMV_EINVAL;
+    }
+    rc = dirk_autotune(c, y, O, mixed, s);
+    if (rc) return rc;
+    block = c->dirk_block[mixed];
+  }
+  rc = chem_dirk(c->P, c->S, c->n, y, O, mixed, block, c->d_next, stats, d_nfail, s);
+  if (rc == GBMV_EUNSUPPORTED) set_error("DIRK block of %d threads does not fit on an SM", block);
+  return rc;
+}
+
+int gbmv_chem_dirk_evolve(gbmv_chem c, double t0, double tout, double* y, double time_units,
+                          const gbmv_dirk_opts* opts, int* stats, void* stream) {
+  if (!c) { set_error("null handle"); return GBMV_EINVAL; }
+  cudaStream_t s = (cudaStream_t)stream;
+  GBMV_CUDA_TRY(cudaMemsetAsync(c->d_nfail, 0, sizeof(int), s));
+  int rc = dirk_launch(c, t0, tout, y, time_units, opts, stats, c->d_nfail, s, true);
+  if (rc) return rc;
+  int h = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&h, c->d_nfail, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  return h;
+}
+
+int gbmv_chem_dirk_evolve_async(gbmv_chem c, double t0, double tout, double* y,
+                                double time_units, const gbmv_dirk_opts* opts, int* stats,
+                                int* d_nfail, void* stream) {
+  return dirk_launch(c, t0, tout, y, time_units, opts, stats, d_nfail, (cudaStream_t)stream,
+                     false);
+}
+
+int gbmv_chem_dirk_block(gbmv_chem c, int precision) {
+  if (!c || (precision != GBMV_FP64 && precision != GBMV_MIXED)) return 0;
+  return c->dirk_block[precision == GBMV_MIXED];
 }
 
 /* ------------------------------------------------------------------ block solve */

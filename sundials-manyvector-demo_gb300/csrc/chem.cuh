@@ -37,6 +37,26 @@ int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
                 cudaStream_t s);
 
+// persistent per-cell DIRK integration from t0 to tout (chem_dirk.cu)
+struct DirkOpts {
+  double t0, tout, tunit;
+  double rtol, atol;  // WRMS weights 1 / (rtol |z| + atol) on the scaled variables
+  double nlscoef;     // Newton tolerance factor
+  double h0;          // first step; <= 0: h0fac / ||F(z0)||_WRMS
+  double h0fac;
+  double safety;      // step-size safety factor
+  double dgmax;       // refactor when |gamma / gamma_p - 1| > dgmax
+  double growth, etamx1, hmax;  // step growth bounds (after the first step / on it); hmax <= 0: none
+  int maxcor, max_steps, msbp, msbj, maxnef, maxncf;
+  int refine;      // FP32 LU: refinement steps per Newton solve
+  int mixed_temp;  // temperature iterations 1-8 in FP32
+};
+constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
+                               // matrix setups, Jacobians, F evaluations, failed
+int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,
+              int lu_fp32, int block, unsigned long long* d_next, int* stats, int* d_nfail,
+              cudaStream_t s);
+
 // batched 10x10 LU (blocklu.cu)
 int block_lu_factor(long nb, double* A, int* piv, int* d_info, cudaStream_t s);
 int block_lu_solve(long nb, const double* LU, const int* piv, const double* b, double* x,

@@ -39,6 +39,14 @@ class _Grid(C.Structure):
                 ("gamma", C.c_double), ("bc", C.c_int * 6)]
 
 
+class _DirkOpts(C.Structure):
+    """gbmv_dirk_opts (include/gbmv.h)."""
+    _fields_ = [(k, C.c_double) for k in ("rtol", "atol", "nlscoef", "h0", "safety", "dgmax",
+                                          "growth", "etamx1", "hmax")] + \
+               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "msbj", "maxnef", "maxncf",
+                                       "precision", "refine", "block")]
+
+
 _P = C.POINTER(C.c_double)
 _VP = C.c_void_p
 
@@ -73,6 +81,12 @@ SIGNATURES = [
                                    C.c_double, C.c_int, _VP, _VP]),
     ("gbmv_chem_newton_async", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double, C.c_double,
                                          C.c_int, C.c_int, _VP, _VP]),
+    ("gbmv_dirk_opts_default", None, [C.POINTER(_DirkOpts)]),
+    ("gbmv_chem_dirk_evolve", C.c_int, [_VP, C.c_double, C.c_double, _VP, C.c_double,
+                                        C.POINTER(_DirkOpts), _VP, _VP]),
+    ("gbmv_chem_dirk_evolve_async", C.c_int, [_VP, C.c_double, C.c_double, _VP, C.c_double,
+                                              C.POINTER(_DirkOpts), _VP, _VP, _VP]),
+    ("gbmv_chem_dirk_block", C.c_int, [_VP, C.c_int]),
     ("gbmv_postprocess_step", C.c_int, [_VP, _VP, C.POINTER(_VP), C.c_double, _VP]),
     ("gbmv_version", C.c_char_p, []),
     ("gbmv_last_error", C.c_char_p, []),
@@ -238,6 +252,51 @@ class Chem:
     def calculate_jacobian_cvklu(self, t, y, J, time_units=1.0, stream=None):
         return _check(load().gbmv_chem_jac(self.c, t, _dev_ptr(y), _dev_ptr(J), time_units,
                                            _stream_ptr(stream)), "gbmv_chem_jac")
+
+    def dirk_evolve(self, t0, tout, y, time_units=1.0, stats=None, stream=None, **opts) -> int:
+        """Evolve every cell's chemistry from t0 to tout in place (persistent batched DIRK +
+        Newton, gbmv_chem_dirk_evolve): the fast-stage integration of the chemistry drivers.
+        opts: fields of gbmv_dirk_opts (rtol, atol, nlscoef, maxcor, precision, refine,
+        block, ...).  stats: None or a CUDA int32 tensor of 8 * ncells.  Returns the number of
+        failed cells."""
+        o = dirk_opts(**opts)
+        sp = None
+        if stats is not None:
+            import torch
+            if stats.dtype != torch.int32 or not stats.is_cuda or stats.numel() != 8 * self.n:
+                raise GbmvError("stats must be a CUDA int32 tensor of 8 * ncells")
+            sp = stats.data_ptr()
+        return _check(load().gbmv_chem_dirk_evolve(self.c, t0, tout, _dev_ptr(y), time_units,
+                                                   C.byref(o), sp, _stream_ptr(stream)),
+                      "gbmv_chem_dirk_evolve", allow=range(0, self.n + 1))
+
+    def dirk_evolve_async(self, t0, tout, y, nfail, time_units=1.0, stats=None, stream=None,
+                          **opts):
+        """Same, asynchronous and graph-capturable; failures are added to nfail (CUDA int32)."""
+        o = dirk_opts(**opts)
+        return _check(load().gbmv_chem_dirk_evolve_async(
+            self.c, t0, tout, _dev_ptr(y), time_units, C.byref(o),
+            stats.data_ptr() if stats is not None else None, nfail.data_ptr(),
+            _stream_ptr(stream)), "gbmv_chem_dirk_evolve_async")
+
+    def dirk_block(self, precision=FP64) -> int:
+        """Block size the autotuner picked for a precision (0 = not tuned yet)."""
+        return load().gbmv_chem_dirk_block(self.c, precision)
+
+
+DIRK_STATS = ("steps", "newton_iters", "error_fails", "newton_fails", "setups", "jacobians",
+              "f_evals", "failed")
+
+
+def dirk_opts(**kw) -> _DirkOpts:
+    """gbmv_dirk_opts with the library defaults, overridden by keyword."""
+    o = _DirkOpts()
+    load().gbmv_dirk_opts_default(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise GbmvError(f"unknown DIRK option {k}")
+        setattr(o, k, v)
+    return o
 
 
 def _wrap_device(ptr: int, n: int):

@@ -1,6 +1,6 @@
 """Mixed-precision and fused forms against the FP64 oracle (GPU).
 
-Tolerance: the benchmark spec's 1e-6 relative error against the FP64 oracle, measured per field
+Tolerance: the 1e-6 relative error budget against the FP64 oracle, measured per field
 as max|mixed - oracle| / max|oracle| over the grid.
 """
 import numpy as np
