@@ -176,13 +176,15 @@ typedef struct {
   double hmax;       /* largest step, <= 0: none (default 0) */
   int maxcor;        /* Newton iterations per stage (default 3) */
   int max_steps;     /* steps per cell before it counts as failed (default 5000) */
-  int msbp;          /* refactor the Newton matrix at least every msbp steps (default 20) */
-  int msbj;          /* new Jacobian at least every msbj steps (default 50) */
+  int msbp;          /* new Newton matrix (fresh J, refactored) at least every msbp steps
+                        (default 20) */
   int maxnef;        /* error-test failures per step (default 7) */
   int maxncf;        /* Newton failures per step (default 10) */
   int precision;     /* GBMV_FP64: FP64 LU and temperature; GBMV_MIXED: FP32 LU (+ refine),
                         temperature iterations 1-8 in FP32 (default GBMV_FP64) */
-  int refine;        /* GBMV_MIXED: FP64-residual refinement steps per solve, 0-8 (default 1) */
+  int refine;        /* GBMV_MIXED: FP64-residual refinement steps per linear solve, 0-8;
+                        > 0 keeps an FP64 copy of the matrix (default 0: each Newton
+                        iteration already refines against the FP64 nonlinear residual) */
   int block;         /* threads per block: 32, 64 or 128; 0 = autotuned (default 0) */
 } gbmv_dirk_opts;
 

@@ -629,7 +629,9 @@ long orc_block_newton_solve(long n, const double* J, double gamma, const double*
  * the CPU restatement of the persistent GPU integrator (gbmv_chem_dirk_evolve), FP64
  * throughout.  The reference integrates the same system with ARKStep (DIRK + Newton +
  * block-diagonal direct solver, src/primordial_ode_main.cpp) over all cells at once; this
- * restatement applies ARKODE's Newton and step rules per cell (see oracle.h).
+ * restatement applies ARKODE's Newton and step rules per cell (see oracle.h), except that no
+ * Jacobian is kept between Newton-matrix setups (each setup evaluates J at the step's state)
+ * and the WRMS weights are rounded to float, as the GPU kernel stores them.
  * TR-BDF2 ESDIRK pair: A = [[0,0,0],[gd,gd,0],[w,w,gd]], b = (w,w,gd),
  * bhat = ((1-w)/3, (3w+1)/3, gd/3) (Hosea & Shampine 1996). */
 #define DK_SQRT2 1.4142135623730951
@@ -670,14 +672,14 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
     const long j = i * 10;
     const double *sc = scale + j, *isc = inv_scale + j;
     const double md = mdens[i], imd = imdens[i], cie = cie_oda[i], h2 = h2_oda[i];
-    double Y[10], K1[10], K2[10], Z[10], EW[10], f[10], J[100], A[100];
+    double Y[10], K1[10], K2[10], Z[10], EW[10], f[10], A[100];
     int piv[10];
     for (int s = 0; s < 10; ++s) Y[s] = y[j + s];
     double Tsc = Ts[i], dTsc = dTs_ge[i], Tsy, dTsy;
     double t = O->t0, h = O->h0, gp = 0.0, crate = 1.0, delp = 0.0;
-    int nst = 0, nst_lp = 0, nst_lj = 0, nef_s = 0, ncf_s = 0;
-    int nni = 0, netf = 0, ncf = 0, nsetup = 0, nje = 0, nfe = 0;
-    int jcur = 0, need_jac = 1, last = 0, failed = 0;
+    int nst = 0, nst_lp = 0, nef_s = 0, ncf_s = 0;
+    int nni = 0, netf = 0, ncf = 0, nsetup = 0, nfe = 0;
+    int jcur = 0, force_setup = 1, last = 0, failed = 0;
     dirk_F(c, Y, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, K1);
     ++nfe;
     Tsy = Tsc;
@@ -700,37 +702,31 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
         Tsc = Tsy;
         dTsc = dTsy;
         for (int s = 0; s < 10; ++s) {
-          EW[s] = 1.0 / (O->rtol * fabs(Y[s]) + O->atol);
+          EW[s] = (double)(float)(1.0 / (O->rtol * fabs(Y[s]) + O->atol)); /* float weights */
           Z[s] = Y[s];
         }
         const double gam = h * dk_gd;
-        int refactor = 0;
-        if (need_jac || nst >= nst_lj + O->msbj) {
+        if (force_setup || nst >= nst_lp + O->msbp || !(fabs(gam / gp - 1.0) <= O->dgmax)) {
+          /* no Jacobian is kept between setups: J at (Y, Ts(Y)) for every Newton matrix */
           double B[100];
           orc_chem_jac(c, 1, Y, sc, isc, &mdens[i], &cie_oda[i], &h2_oda[i], &Tsy, &dTsy, B);
-          for (int e = 0; e < 100; ++e) J[e] = B[e] * O->tunit;
-          ++nje;
-          nst_lj = nst;
-          jcur = 1;
-          need_jac = 0;
-          refactor = 1;
-        }
-        if (refactor || nst >= nst_lp + O->msbp || !(fabs(gam / gp - 1.0) <= O->dgmax)) {
+          const double mg = -gam * O->tunit;
           for (int col = 0; col < 10; ++col)
             for (int r = 0; r < 10; ++r)
-              A[col * 10 + r] = (r == col ? 1.0 : 0.0) - gam * J[col * 10 + r];
+              A[col * 10 + r] = (r == col ? 1.0 : 0.0) + mg * B[col * 10 + r];
           const int info = lu10(A, piv);
           gp = gam;
           nst_lp = nst;
           crate = 1.0;
+          jcur = 1;
+          force_setup = 0;
           ++nsetup;
           if (info) {
             ++ncf_s;
             ++ncf;
             if (ncf_s >= O->maxncf) { failed = 1; break; }
             h *= 0.25;
-            if (!jcur) need_jac = 1;
-            gp = 0.0;
+            force_setup = 1;
             continue;
           }
         }
@@ -774,7 +770,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
         ++ncf;
         if (ncf_s >= O->maxncf) { failed = 1; break; }
         if (jcur) h *= 0.25;
-        else need_jac = 1;
+        else force_setup = 1;
         continue;
       }
       dirk_F(c, Z, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, f);
@@ -815,7 +811,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
     if (stats) {
       int* st = stats + i * 8;
       st[0] = nst; st[1] = nni; st[2] = netf; st[3] = ncf;
-      st[4] = nsetup; st[5] = nje; st[6] = nfe; st[7] = failed;
+      st[4] = nsetup; st[5] = nsetup; st[6] = nfe; st[7] = failed;
     }
     nfail += failed;
   }

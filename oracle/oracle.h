@@ -83,12 +83,12 @@ long orc_block_newton_solve(long n, const double* J, double gamma, const double*
 typedef struct {
   double t0, tout, tunit;
   double rtol, atol, nlscoef, h0, h0fac, safety, dgmax, growth, etamx1, hmax;
-  int maxcor, max_steps, msbp, msbj, maxnef, maxncf;
+  int maxcor, max_steps, msbp, maxnef, maxncf;
 } orc_dirk_opts;
 
 /* Per-cell adaptive TR-BDF2 ESDIRK integration of dz/dt = tunit * f_chem(z) (scaled
  * variables, as orc_chem_rhs x tunit) from t0 to tout, modified Newton with ARKODE's
- * convergence, reuse and step rules, FP64 LU; the algorithm of the GPU integrator
+ * convergence, reuse and step rules (a fresh J at every Newton-matrix setup), FP64 LU; the algorithm of the GPU integrator
  * (gbmv_chem_dirk_evolve).  y, Ts, dTs_ge updated in place; stats (8 ints per cell, or NULL):
  * steps, Newton iterations, error-test failures, Newton failures, matrix setups, Jacobians,
  * F evaluations, failed.  Returns the number of failed cells. */

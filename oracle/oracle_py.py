@@ -48,13 +48,13 @@ class OrcDirkOpts(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("t0", "tout", "tunit", "rtol", "atol", "nlscoef", "h0",
                                           "h0fac", "safety", "dgmax", "growth", "etamx1",
                                           "hmax")] + \
-               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "msbj", "maxnef", "maxncf")]
+               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf")]
 
 
 # defaults of gbmv_dirk_opts_default (include/gbmv.h)
 DIRK_DEFAULTS = dict(rtol=1e-6, atol=1e-10, nlscoef=0.1, h0=0.0, safety=0.9, dgmax=0.2,
                      growth=20.0, etamx1=10000.0, hmax=0.0, maxcor=3, max_steps=5000, msbp=20,
-                     msbj=50, maxnef=7, maxncf=10)
+                     maxnef=7, maxncf=10)
 
 
 def _ptr(a: np.ndarray):

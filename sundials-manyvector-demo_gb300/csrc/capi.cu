@@ -429,18 +429,17 @@ void gbmv_dirk_opts_default(gbmv_dirk_opts* o) {
   o->maxcor = 3;
   o->max_steps = 5000;
   o->msbp = 20;
-  o->msbj = 50;
   o->maxnef = 7;
   o->maxncf = 10;
   o->precision = GBMV_FP64;
-  o->refine = 1;
+  o->refine = 0;
   o->block = 0;
 }
 
 static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tunit, DirkOpts* O) {
   if (!o || !(o->rtol > 0.0) || !(o->atol > 0.0) || !(o->nlscoef > 0.0) || !(o->safety > 0.0) ||
       !(o->dgmax >= 0.0) || !(o->growth >= 1.0) || !(o->etamx1 >= 1.0) || !(o->hmax >= 0.0) ||
-      o->maxcor < 1 || o->max_steps < 1 || o->msbp < 1 || o->msbj < 1 ||
+      o->maxcor < 1 || o->max_steps < 1 || o->msbp < 1 ||
       o->maxnef < 1 || o->maxncf < 1 || o->refine < 0 || o->refine > 8 ||
       (o->precision != GBMV_FP64 && o->precision != GBMV_MIXED) ||
       (o->block != 0 && o->block != 32 && o->block != 64 && o->block != 128) ||
@@ -465,7 +464,6 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
   O->maxcor = o->maxcor;
   O->max_steps = o->max_steps;
   O->msbp = o->msbp;
-  O->msbj = o->msbj;
   O->maxnef = o->maxnef;
   O->maxncf = o->maxncf;
   O->refine = o->precision == GBMV_MIXED ? o->refine : 0;

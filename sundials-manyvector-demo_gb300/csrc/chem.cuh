@@ -47,12 +47,12 @@ struct DirkOpts {
   double safety;      // step-size safety factor
   double dgmax;       // refactor when |gamma / gamma_p - 1| > dgmax
   double growth, etamx1, hmax;  // step growth bounds (after the first step / on it); hmax <= 0: none
-  int maxcor, max_steps, msbp, msbj, maxnef, maxncf;
+  int maxcor, max_steps, msbp, maxnef, maxncf;
   int refine;      // FP32 LU: refinement steps per Newton solve
   int mixed_temp;  // temperature iterations 1-8 in FP32
 };
 constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
-                               // matrix setups, Jacobians, F evaluations, failed
+                               // matrix setups, Jacobians (= setups), F evaluations, failed
 int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,
               int lu_fp32, int block, unsigned long long* d_next, int* stats, int* d_nfail,
               cudaStream_t s);

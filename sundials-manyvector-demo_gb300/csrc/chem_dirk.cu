@@ -10,8 +10,8 @@
 // stiffly accurate, L-stable), its order-3 companion weights giving the embedded error
 // estimate (M. E. Hosea and L. F. Shampine, Appl. Numer. Math. 20 (1996) 21-37).  Each implicit
 // stage is solved by modified Newton with ARKODE's rules: Newton matrix A = I - gamma J reused
-// across steps (refactored when gamma moved by more than dgmax or after msbp steps, J
-// re-evaluated after msbj steps or a Newton failure with a stale J), correction scaled by
+// across steps (set up again when gamma moved by more than dgmax, after msbp steps, or after a
+// Newton failure with a matrix from an earlier step), correction scaled by
 // 2/(1 + gamma/gamma_p) when gamma differs from the factored one, WRMS convergence test with
 // rate estimate crate = max(0.3 crate, del/del_p), success when min(1, crate) del / nlscoef
 // <= 1, divergence when del > 2.3 del_p, at most maxcor iterations.  Step control: the error
@@ -25,9 +25,14 @@
 // temperature solve and 46 rate interpolations) and then acts on its own phase.  A lane whose
 // cell reached tout (or failed) retires it and pulls the next cell index from a global counter
 // (one warp-aggregated atomic per refill), so warps stay full until the queue drains.
-// Precision: LU = float factors the Newton matrix in FP32 and (with refine > 0) refines the
-// correction against FP64 residuals of A computed from the FP64 Jacobian; residuals G(z),
-// norms and error estimates are FP64 in both forms.
+// Unlike ARKODE no Jacobian is kept between matrix setups: each setup evaluates J at the
+// step's state (one Jacobian per setup, a few per cent of the F work), which frees 512 bytes
+// of shared memory per cell for occupancy.  WRMS weights are kept as floats (the oracle rounds
+// them the same way).
+// Precision: LU = float factors the Newton matrix in FP32 after power-of-two row and column
+// equilibration (the scaled Jacobian spans ~20 decades); REF additionally keeps A in FP64 and
+// refines each correction against FP64 residuals.  The residuals G(z), norms and error
+// estimates are FP64 in every form, so Newton itself refines against the FP64 equations.
 #include "chem.cuh"
 #include "chem_lu.cuh"
 #include "chem_net.cuh"
@@ -75,25 +80,58 @@ __device__ __forceinline__ void dirk_F(const ChemParams& P, const ChemState& S, 
 
 }  // namespace
 
-template <typename LU, int BS>
+// 2^e as a double (|e| <= 1022): exact power-of-two scaling for the equilibration.
+__device__ __forceinline__ double pow2(int e) {
+  return __longlong_as_double((long long)(1023 + e) << 52);
+}
+
+// Equilibration exponent: -e with m * 2^e = x, m in [0.5, 1) (0 for zero or non-finite x),
+// limited so that the combined row + column scale stays a normal double.
+__device__ __forceinline__ int eq_exponent(double x) {
+  if (!(x > 0.0) || !isfinite(x)) return 0;
+  int ex = 0;
+  frexp(x, &ex);
+  return max(-500, min(500, -ex));
+}
+
+template <typename LU, bool REF, int BS>
+struct DirkLayout {
+  // per-lane slices, element-major [element][BS]
+  static constexpr size_t kVec = 40 * sizeof(double);                   // Y, K1, K2, Z
+  static constexpr size_t kEw = 10 * sizeof(float);                     // weights
+  static constexpr size_t kL = 100 * sizeof(LU);                        // factor
+  static constexpr size_t kA = REF ? 100 * sizeof(double) : 0;          // FP64 matrix
+  static constexpr size_t kEq = sizeof(LU) == 4 ? 20 * sizeof(short) : 0;  // row/col exponents
+  static constexpr size_t kPiv = 10;                                    // pivots (bytes)
+  static constexpr size_t per_lane = kVec + kEw + kL + kA + kEq + kPiv;
+  static constexpr size_t bytes = per_lane * BS;
+};
+
+template <typename LU, bool REF, int BS>
 __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S, long n,
                                                        double* __restrict__ y_io, DirkOpts O,
                                                        unsigned long long* __restrict__ next,
                                                        int* __restrict__ stats,
                                                        int* __restrict__ nfail) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  using Lay = DirkLayout<LU, REF, BS>;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
-  double* const dbase = reinterpret_cast<double*>(smem_raw);
-  double* const Jm = dbase + tid;            // [64][BS] scaled Jacobian dF/dz (pattern order)
-  double* const Y = dbase + 64 * BS + tid;   // [10][BS] state at the step start
-  double* const K1 = Y + 10 * BS;            // F(Y)
-  double* const K2 = K1 + 10 * BS;           // F(stage 2)
-  double* const EW = K2 + 10 * BS;           // WRMS weights 1 / (rtol |Y| + atol)
-  double* const Z = EW + 10 * BS;            // current stage iterate
-  LU* const L = reinterpret_cast<LU*>(dbase + 114 * BS) + tid;  // [100][BS] factor
-  int* const PV = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(dbase + 114 * BS) +
-                                         sizeof(LU) * 100 * BS) + tid;  // [10][BS] pivots
+  unsigned char* p = smem_raw;
+  double* const Y = reinterpret_cast<double*>(p) + tid;  // state at the step start
+  double* const K1 = Y + 10 * BS;                         // F(Y)
+  double* const K2 = K1 + 10 * BS;                        // F(stage 2)
+  double* const Z = K2 + 10 * BS;                         // current stage iterate
+  p += Lay::kVec * BS;
+  double* const A = reinterpret_cast<double*>(p) + tid;   // REF: FP64 Newton matrix
+  p += Lay::kA * BS;
+  LU* const L = reinterpret_cast<LU*>(p) + tid;           // factor
+  p += Lay::kL * BS;
+  float* const EW = reinterpret_cast<float*>(p) + tid;    // WRMS weights
+  p += Lay::kEw * BS;
+  short* const EQ = reinterpret_cast<short*>(p) + tid;    // row exponents [0,10), col [10,20)
+  p += Lay::kEq * BS;
+  signed char* const PV = reinterpret_cast<signed char*>(p) + tid;  // pivots
   const unsigned full = 0xffffffffu;
   const bool mixed_temp = O.mixed_temp != 0;
 
@@ -102,9 +140,9 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
   int phase = kPhK1, stage = 2, m = 0;
   double t = 0.0, h = 0.0, gp = 0.0, crate = 1.0, delp = 0.0;
   double Tsy = 0.0, dTsy = 0.0, Tsc = 0.0, dTsc = 0.0;
-  int nst = 0, nst_lp = 0, nst_lj = 0, nef_s = 0, ncf_s = 0;
-  int c_nni = 0, c_netf = 0, c_ncf = 0, c_nsetup = 0, c_nje = 0, c_nfe = 0;
-  bool jcur = false, need_jac = true, last = false;
+  int nst = 0, nst_lp = 0, nef_s = 0, ncf_s = 0;
+  int c_nni = 0, c_netf = 0, c_ncf = 0, c_nsetup = 0, c_nfe = 0;
+  bool jcur = false, force_setup = true, last = false;
 
   while (true) {
     // ---- refill: lanes without a cell take the next indices (one atomic per warp)
@@ -129,10 +167,10 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           h = O.h0;
           gp = 0.0;
           phase = kPhK1;
-          nst = nst_lp = nst_lj = nef_s = ncf_s = 0;
-          c_nni = c_netf = c_ncf = c_nsetup = c_nje = c_nfe = 0;
+          nst = nst_lp = nef_s = ncf_s = 0;
+          c_nni = c_netf = c_ncf = c_nsetup = c_nfe = 0;
           jcur = false;
-          need_jac = true;
+          force_setup = true;
           last = false;
         } else {
           exhausted = true;
@@ -182,27 +220,34 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) piv[s] = PV[s * BS];
       double dl[10];
-      {
-        LU xs[10];
+      if (sizeof(LU) == 8) {
 #pragma unroll
-        for (int s = 0; s < 10; ++s) xs[s] = (LU)g[s];
-        lus10_strided<LU, LU>(L, BS, piv, xs);
+        for (int s = 0; s < 10; ++s) dl[s] = g[s];
+        lus10_strided<LU, double>(L, BS, piv, dl);
+      } else {
+        // equilibrated FP32 solve: (R A C) u = R g, dl = C u
+        LU u[10];
 #pragma unroll
-        for (int s = 0; s < 10; ++s) dl[s] = (double)xs[s];
-      }
-      if (sizeof(LU) == 4) {
-        for (int it = 0; it < O.refine; ++it) {  // residual of A_p dl = g in FP64
-          double r[10];
+        for (int s = 0; s < 10; ++s) u[s] = (LU)(g[s] * pow2(EQ[s * BS]));
+        lus10_strided<LU, LU>(L, BS, piv, u);
 #pragma unroll
-          for (int s = 0; s < 10; ++s) r[s] = 0.0;
+        for (int s = 0; s < 10; ++s) dl[s] = (double)u[s] * pow2(EQ[(10 + s) * BS]);
+        if (REF) {
+          for (int it = 0; it < O.refine; ++it) {  // r = g - A dl in FP64, solve, update
+            double r[10];
 #pragma unroll
-          for (int e = 0; e < 64; ++e) r[kJacPattern[e][0]] += Jm[e * BS] * dl[kJacPattern[e][1]];
-          LU ds[10];
+            for (int s = 0; s < 10; ++s) r[s] = g[s];
 #pragma unroll
-          for (int s = 0; s < 10; ++s) ds[s] = (LU)(g[s] - (dl[s] - gp * r[s]));
-          lus10_strided<LU, LU>(L, BS, piv, ds);
+            for (int e = 0; e < 64; ++e) {
+              const int row = kJacPattern[e][0], col = kJacPattern[e][1];
+              r[row] -= A[(col * 10 + row) * BS] * dl[col];
+            }
 #pragma unroll
-          for (int s = 0; s < 10; ++s) dl[s] += (double)ds[s];
+            for (int s = 0; s < 10; ++s) u[s] = (LU)(r[s] * pow2(EQ[s * BS]));
+            lus10_strided<LU, LU>(L, BS, piv, u);
+#pragma unroll
+            for (int s = 0; s < 10; ++s) dl[s] += (double)u[s] * pow2(EQ[(10 + s) * BS]);
+          }
         }
       }
       if (gam != gp) {
@@ -214,7 +259,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         Z[s * BS] += dl[s];
-        const double v = dl[s] * EW[s * BS];
+        const double v = dl[s] * (double)EW[s * BS];
         s2 += v * v;
       }
       const double del = sqrt(s2 / 10.0);
@@ -225,15 +270,15 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       if (dcon <= 1.0) {
         phase = (stage == 2) ? kPhK2 : kPhK3;
       } else if ((m > 1 && del > 2.3 * delp) || m >= O.maxcor || !(del == del)) {
-        // Newton failure: with a stale Jacobian retry at the same h with a fresh one, else
-        // cut the step
+        // Newton failure: with a matrix from an earlier step set up a current one at the
+        // same h, else cut the step
         ++ncf_s;
         ++c_ncf;
         if (ncf_s >= O.maxncf) {
           retire = failed = true;
         } else {
           if (jcur) h *= 0.25;
-          else need_jac = true;
+          else force_setup = true;
           setup = true;
         }
       } else {
@@ -250,7 +295,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         const double e = h * ((kE1 * K1[s * BS] + kE2 * K2[s * BS]) + kE3 * f[s]);
-        const double v = e * EW[s * BS];
+        const double v = e * (double)EW[s * BS];
         s2 += v * v;
       }
       const double dsm = sqrt(s2 / 10.0);
@@ -297,12 +342,12 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         const double ys = Y[s * BS];
-        EW[s * BS] = 1.0 / (O.rtol * fabs(ys) + O.atol);
+        EW[s * BS] = (float)(1.0 / (O.rtol * fabs(ys) + O.atol));
         Z[s * BS] = ys;  // trivial predictor
       }
       const double gam = h * kGd;
-      bool refactor = false;
-      if (need_jac || nst >= nst_lj + O.msbj) {
+      if (force_setup || nst >= nst_lp + O.msbp || !(fabs(gam / gp - 1.0) <= O.dgmax)) {
+        // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored
         const long j = i * 10;
         double ya[10];
 #pragma unroll
@@ -312,32 +357,76 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         const ChemAux Ax{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
         const double* __restrict__ sc = S.scale + j;
         const double* __restrict__ isc = S.inv_scale + j;
-        const double tu = O.tunit;
-        chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-          const int e = kJacIndex[row][col];  // every entry put is structural (folded)
-          if (e >= 0) Jm[e * BS] = ((v * isc[row]) * sc[col]) * tu;
-        });
-        ++c_nje;
-        nst_lj = nst;
-        jcur = true;
-        need_jac = false;
-        refactor = true;
-      }
-      if (refactor || nst >= nst_lp + O.msbp || !(fabs(gam / gp - 1.0) <= O.dgmax)) {
+        const double mg = -gam * O.tunit;
 #pragma unroll
-        for (int e = 0; e < 100; ++e) L[e * BS] = (e % 11 == 0) ? LU(1) : LU(0);
+        for (int e = 0; e < 100; ++e) L[e * BS] = LU(0);  // off-pattern entries
+        // A = I - gamma * tunit * (isc_r J_rc sc_c): every structural entry is put once
+        auto entry = [&](int row, int col, double v) {
+          return (row == col ? 1.0 : 0.0) + mg * ((v * isc[row]) * sc[col]);
+        };
+        if (sizeof(LU) == 8) {
+          chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+            L[(col * 10 + row) * BS] = (LU)entry(row, col, v);
+          });
+        } else {
+          // FP32 factor of R A C with power-of-two row scales R (row maxima to [0.5, 1)) and
+          // column scales C (then column maxima to [0.5, 1)), from the FP64 entries
+          double rmax[10], cmax[10];
+          int er[10], ec[10];
 #pragma unroll
-        for (int e = 0; e < 64; ++e) {
-          const int row = kJacPattern[e][0], col = kJacPattern[e][1];
-          L[(col * 10 + row) * BS] = (LU)((row == col ? 1.0 : 0.0) - gam * Jm[e * BS]);
+          for (int s = 0; s < 10; ++s) rmax[s] = cmax[s] = 0.0;
+          if (REF) {
+            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+              const double a = entry(row, col, v);
+              A[(col * 10 + row) * BS] = a;
+              rmax[row] = fmax(rmax[row], fabs(a));
+            });
+          } else {
+            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+              rmax[row] = fmax(rmax[row], fabs(entry(row, col, v)));
+            });
+          }
+#pragma unroll
+          for (int s = 0; s < 10; ++s) er[s] = eq_exponent(rmax[s]);
+          if (REF) {
+#pragma unroll
+            for (int e = 0; e < 64; ++e) {
+              const int row = kJacPattern[e][0], col = kJacPattern[e][1];
+              cmax[col] = fmax(cmax[col], fabs(A[(col * 10 + row) * BS] * pow2(er[row])));
+            }
+          } else {
+            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+              cmax[col] = fmax(cmax[col], fabs(entry(row, col, v) * pow2(er[row])));
+            });
+          }
+#pragma unroll
+          for (int s = 0; s < 10; ++s) {
+            ec[s] = eq_exponent(cmax[s]);
+            EQ[s * BS] = (short)er[s];
+            EQ[(10 + s) * BS] = (short)ec[s];
+          }
+          if (REF) {
+#pragma unroll
+            for (int e = 0; e < 64; ++e) {
+              const int row = kJacPattern[e][0], col = kJacPattern[e][1];
+              L[(col * 10 + row) * BS] =
+                  (LU)(A[(col * 10 + row) * BS] * pow2(er[row] + ec[col]));
+            }
+          } else {
+            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+              L[(col * 10 + row) * BS] = (LU)(entry(row, col, v) * pow2(er[row] + ec[col]));
+            });
+          }
         }
         int piv[10];
         const int info = lu10_strided<LU>(L, BS, piv);
 #pragma unroll
-        for (int s = 0; s < 10; ++s) PV[s * BS] = piv[s];
+        for (int s = 0; s < 10; ++s) PV[s * BS] = (signed char)piv[s];
         gp = gam;
         nst_lp = nst;
         crate = 1.0;
+        jcur = true;
+        force_setup = false;
         ++c_nsetup;
         if (info) {  // singular Newton matrix: a recoverable failure, cut the step and retry
           ++ncf_s;
@@ -346,8 +435,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
             retire = failed = true;
           } else {
             h *= 0.25;
-            if (!jcur) need_jac = true;
-            gp = 0.0;  // forces a refactor
+            force_setup = true;
             setup = true;
           }
         }
@@ -370,7 +458,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         st[2] = c_netf;
         st[3] = c_ncf;
         st[4] = c_nsetup;
-        st[5] = c_nje;
+        st[5] = c_nsetup;  // every setup evaluates the Jacobian
         st[6] = c_nfe;
         st[7] = failed ? 1 : 0;
       }
@@ -380,23 +468,36 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
   }
 }
 
-template <typename LU, int BS>
+template <typename LU, bool REF, int BS>
 static int launch_dirk(const ChemParams& P, const ChemState& S, long n, double* y,
                        const DirkOpts& O, unsigned long long* d_next, int* stats, int* d_nfail,
                        int nsm, cudaStream_t s) {
-  const size_t shm = (size_t)BS * (114 * sizeof(double) + 100 * sizeof(LU) + 10 * sizeof(int));
-  GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_dirk_kernel<LU, BS>,
+  const size_t shm = DirkLayout<LU, REF, BS>::bytes;
+  GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_dirk_kernel<LU, REF, BS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   int per_sm = 0;
-  GBMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chem_dirk_kernel<LU, BS>,
-                                                              BS, shm));
+  GBMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, chem_dirk_kernel<LU, REF, BS>, BS, shm));
   if (per_sm < 1) return GBMV_EUNSUPPORTED;
   long blocks = (long)nsm * per_sm;
   const long need = (n + BS - 1) / BS;
   if (blocks > need) blocks = need;
-  chem_dirk_kernel<LU, BS><<<(int)blocks, BS, shm, s>>>(P, S, n, y, O, d_next, stats, d_nfail);
+  chem_dirk_kernel<LU, REF, BS><<<(int)blocks, BS, shm, s>>>(P, S, n, y, O, d_next, stats,
+                                                             d_nfail);
   GBMV_LAUNCH_CHECK("chem_dirk_kernel");
   return GBMV_OK;
+}
+
+template <typename LU, bool REF>
+static int launch_dirk_bs(int block, const ChemParams& P, const ChemState& S, long n, double* y,
+                          const DirkOpts& O, unsigned long long* d_next, int* stats,
+                          int* d_nfail, int nsm, cudaStream_t s) {
+  switch (block) {
+    case 32: return launch_dirk<LU, REF, 32>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
+    case 64: return launch_dirk<LU, REF, 64>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
+    case 128: return launch_dirk<LU, REF, 128>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
+    default: return GBMV_EINVAL;
+  }
 }
 
 int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,
@@ -407,15 +508,11 @@ int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const 
   GBMV_CUDA_TRY(cudaGetDevice(&dev));
   GBMV_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   ProfScope ps("chem_dirk", s);
-  switch ((lu_fp32 ? 1000 : 0) + block) {
-    case 32: return launch_dirk<double, 32>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
-    case 64: return launch_dirk<double, 64>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
-    case 128: return launch_dirk<double, 128>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
-    case 1032: return launch_dirk<float, 32>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
-    case 1064: return launch_dirk<float, 64>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
-    case 1128: return launch_dirk<float, 128>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
-    default: return GBMV_EINVAL;
-  }
+  if (!lu_fp32)
+    return launch_dirk_bs<double, false>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
+  if (O.refine > 0)
+    return launch_dirk_bs<float, true>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
+  return launch_dirk_bs<float, false>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
 }
 
 }  // namespace gbmv

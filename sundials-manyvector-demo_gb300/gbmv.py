@@ -43,7 +43,7 @@ class _DirkOpts(C.Structure):
     """gbmv_dirk_opts (include/gbmv.h)."""
     _fields_ = [(k, C.c_double) for k in ("rtol", "atol", "nlscoef", "h0", "safety", "dgmax",
                                           "growth", "etamx1", "hmax")] + \
-               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "msbj", "maxnef", "maxncf",
+               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf",
                                        "precision", "refine", "block")]
 
 
