@@ -52,6 +52,11 @@ def parse():
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--dirk-n", type=int, default=64,
+                   help="static-chemistry DIRK measurement on dirk_n^3 cells (0 = skip)")
+    p.add_argument("--dirk-only", action="store_true",
+                   help="run only the DIRK measurement (prints its object)")
+    p.add_argument("--dirk-form", default="both", choices=["both", "fp64", "mixed"])
     return p.parse_args()
 
 
@@ -406,7 +411,102 @@ def run_gbmv(args):
                        "ms_per_step": round(ms_e2e, 4)}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(sample_n=(128, 128, 32))
+    if args.dirk_n > 0:
+        for k in ("fs",):
+            for r in res.values():
+                r[k] = None
+        fs = None
+        torch.cuda.empty_cache()
+        line["chem_dirk"] = run_dirk(torch, gbmv, args.dirk_n, not args.no_cpu_baseline,
+                                     args.dirk_form)
     print(json.dumps(line))
+
+
+# ----------------------------------------------------------------- static chemistry (DIRK)
+
+DIRK_TOUT = 1e-3      # code time units (TimeUnits = 1e11 s): 1e8 s of chemistry
+DIRK_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01)  # Newton settings of the inputs
+
+
+def _dirk_summary(st):
+    nni = st[:, 1]
+    q = np.percentile(nni, [50, 90, 99])
+    edges = np.unique(np.round(np.geomspace(max(nni.min(), 1), nni.max() + 1, 13)).astype(int))
+    cnt, _ = np.histogram(nni, bins=edges)
+    return {"steps_mean": round(float(st[:, 0].mean()), 2), "steps_max": int(st[:, 0].max()),
+            "newton_iters": {"mean": round(float(nni.mean()), 2), "p50": float(q[0]),
+                             "p90": float(q[1]), "p99": float(q[2]), "max": int(nni.max())},
+            "newton_iters_hist": {"edges": edges.tolist(), "counts": cnt.tolist()},
+            "error_test_fails_mean": round(float(st[:, 2].mean()), 3),
+            "newton_fails_mean": round(float(st[:, 3].mean()), 3),
+            "setups_mean": round(float(st[:, 4].mean()), 2),
+            "f_evals_mean": round(float(st[:, 6].mean()), 2), "failed": int(st[:, 7].sum())}
+
+
+def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
+    """Static primordial chemistry on n1^3 cells integrated to DIRK_TOUT by the persistent
+    batched DIRK kernel, FP64 form and mixed form (equilibrated FP32 LU, FP32 temperature
+    iterations); per-cell Newton-iteration histograms; oracle port timed on a sample."""
+    import h5tables
+    import workloads as W
+    tables = h5tables.load_table_block(TABLES)
+    n = n1 ** 3
+    y, _ = W.primordial(n, seed=W.SEED_BASE + 2)
+    scale = torch.from_numpy(y.reshape(-1).copy()).cuda()
+    out = {"workload": (f"static primordial chemistry {n1}^3: uniform rho = 1e2 m_H, log-uniform "
+                        "mass fractions in [1e-10, 1], log-uniform T in [10, 1e4] K; per-cell "
+                        "adaptive TR-BDF2 ESDIRK + modified Newton, rtol 1e-6, atol 1e-10, "
+                        f"maxcor 10, nlscoef 0.01, t in [0, {DIRK_TOUT}] x 1e11 s"),
+           "cells": n, "tout": DIRK_TOUT, "forms": {}}
+    finals = {}
+    for name, prec in (("fp64", gbmv.FP64), ("mixed", gbmv.MIXED)):
+        if forms not in ("both", name):
+            continue
+        c = gbmv.Chem(n, tables)
+        c.set_scale(scale)
+        z = torch.ones(10 * n, dtype=torch.float64, device="cuda")
+        st = torch.zeros(8 * n, dtype=torch.int32, device="cuda")
+        c.dirk_evolve(0.0, DIRK_TOUT * 0.01, z, 1e11, precision=prec, **DIRK_OPTS)  # + autotune
+        z.fill_(1.0)
+        c.state("Ts").fill_(1000.0)
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record(s)
+            nf = c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, stats=st, precision=prec, **DIRK_OPTS)
+            e1.record(s)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        stn = st.view(n, 8).cpu().numpy().astype(np.int64)
+        finals[name] = z.view(n, 10).cpu().numpy()
+        out["forms"][name] = {"ms": round(ms, 2), "value": round(n / (ms * 1e-3) / 1e6, 4),
+                              "unit": "Mcells/s (cells integrated to tout per second)",
+                              "block": c.dirk_block(prec), "failed_cells": int(nf),
+                              "clocks": clk.summary(), **_dirk_summary(stn)}
+        del c
+        torch.cuda.empty_cache()
+    if len(finals) == 2:
+        a, b = finals["mixed"], finals["fp64"]
+        e = np.abs(a - b) / (np.abs(b) + DIRK_OPTS["atol"] / DIRK_OPTS["rtol"])
+        out["mixed_vs_fp64_relerr"] = {"median": float(f"{np.median(e):.3e}"),
+                                       "p99": float(f"{np.percentile(e, 99):.3e}"),
+                                       "max": float(f"{e.max():.3e}")}
+        out["speedup_mixed_vs_fp64"] = round(out["forms"]["fp64"]["ms"] /
+                                             out["forms"]["mixed"]["ms"], 3)
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py as O
+        ns = 256
+        oc = O.Chem(tables, y[:ns].reshape(-1))
+        t0 = time.perf_counter()
+        oc.dirk_evolve(np.ones(10 * ns), 0.0, DIRK_TOUT, 1e11, **DIRK_OPTS)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(ns / dt / 1e6, 6), "unit": "Mcells/s", "cores": 1,
+                               "kind": "port",
+                               "sample": f"the first {ns} cells of the same inputs ({dt:.2f} s), "
+                                         "1 thread, FP64 LU"}
+    return out
 
 
 # ----------------------------------------------------------------- CPU baseline (oracle port)
@@ -494,6 +594,15 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.dirk_only:
+        import torch
+        import gbmv
+        import build_lib
+        if not os.path.exists(build_lib.LIB):
+            build_lib.build()
+        gbmv.load()
+        print(json.dumps({"chem_dirk": run_dirk(torch, gbmv, args.dirk_n,
+                                                not args.no_cpu_baseline, args.dirk_form)}))
     else:
         run_gbmv(args)
 
