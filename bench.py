@@ -279,6 +279,17 @@ FP_COUNTS = {
 }
 
 
+# DRAM bytes per unit of the dominant kernels, from ncu captures with the state larger than
+# L2 (dram__bytes_read.sum + dram__bytes_write.sum; profiles/fp_counts_112cube.md), scaled by
+# the units of one 128^3 launch for the roofline's `traffic`.
+DRAM_TRAFFIC = {
+    ("fp64", "face_flux"): (248.2, "face"),    # mean of the x / y / z sweeps
+    ("mixed", "face_flux"): (296.5, "face"),
+    ("mixed", "chem_newton"): (440.6, "cell"),
+    ("fp64", "chem_rhs"): (357.3, "cell"),
+}
+
+
 def timed_form(torch, gbmv, fs, steps, warmup):
     for _ in range(warmup):
         fs.step()
@@ -353,6 +364,13 @@ def run_gbmv(args):
     avg_ms = dt_ms / max(nl, 1)
     key = "face_flux_mx" if (dom == "face_flux" and head == "mixed") else dom
     achieved = algo_bytes(key, args.n) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    traffic, traffic_note = None, None
+    if (head, dom) in DRAM_TRAFFIC:
+        per, unit = DRAM_TRAFFIC[(head, dom)]
+        units = (args.n + 1) * args.n * args.n if unit == "face" else ncell
+        traffic = round(per * units, 0)
+        traffic_note = (f"bytes per launch: {per} B/{unit} (ncu dram__bytes_read+write, 112^3 "
+                        f"capture, state > L2) x {units} {unit}s")
     pipe = None
     if (head, dom) in FP_COUNTS:
         pname, per_unit, unit = FP_COUNTS[(head, dom)]
@@ -374,7 +392,8 @@ def run_gbmv(args):
                    "l2": "inputs larger than L2 (state 252 MB)"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
                      "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
-                     "peak_kind": f"{peak_kind} hbm_gbs", "traffic": None,
+                     "peak_kind": f"{peak_kind} hbm_gbs", "traffic": traffic,
+                     "traffic_note": traffic_note,
                      "avg_launch_ms": round(avg_ms, 4),
                      "fp64_peak_tflops_measured": round(fp64_peak, 4),
                      "pipe": pipe},
