@@ -248,6 +248,17 @@ int gbmv_block_form_newton(long nblocks, double* J, double gamma, void* stream);
 int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* const* wdot,
                double energy_units, int precision, void* stream);
 
+/* ffast (src/multirate_chem_hydro_main.cpp:897-946), the fast right-hand side of the
+ * multirate driver: wdot[0..4] = 0, wdot[5] = time_units * f_chem(w[5]) (as gbmv_chem_rhs),
+ * then the MRI inner-stepper forcing on all six components,
+ *   wdot[k] += sum_{i < nforcing} tau^i forcing[i*6 + k],   tau = (t - tshift) / tscale,
+ * (MRIStepInnerStepper_GetForcingData + N_VLinearCombination).  forcing: host array of
+ * nforcing*6 device pointers laid out like w (NULL when nforcing == 0); nforcing <= 8.
+ * Asynchronous (no status to report). */
+int gbmv_ffast(gbmv_hydro h, gbmv_chem c, double t, const double* const* w, double* const* wdot,
+               double time_units, int nforcing, const double* const* forcing, double tshift,
+               double tscale, void* stream);
+
 /* Same, asynchronous and CUDA-graph capturable: the legal-state mask is OR-ed into
  * *d_status (device int) instead of being returned. */
 int gbmv_fexpl_async(gbmv_hydro h, gbmv_chem c, double t, double* const* w,

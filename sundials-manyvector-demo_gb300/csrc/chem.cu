@@ -5,6 +5,8 @@
 #include "chem.cuh"
 #include "chem_net.cuh"
 
+#include <algorithm>
+
 namespace gbmv {
 
 __global__ void __launch_bounds__(128) chem_rhs_kernel(ChemParams P, ChemState S, long n,
@@ -221,6 +223,50 @@ int energy_epilogue(const ChemState& S, double* chem, double* chemdot, double* e
   energy_epilogue_kernel<<<grid_for(n, 256), 256, 0, s>>>(S.scale, S.inv_scale, chem, chemdot,
                                                            etdot, n, nchem, exact);
   GBMV_LAUNCH_CHECK("energy_epilogue_kernel");
+  return GBMV_OK;
+}
+
+}  // namespace gbmv
+
+namespace gbmv {
+
+// MRI forcing of the fast right-hand side (ffast, src/multirate_chem_hydro_main.cpp:921-944):
+// for every ManyVector component k, wdot_k <- wdot_k + sum_i c_i forcing_i,k, summed in the
+// order of N_VLinearCombination with X[0] == z and c[0] == 1 (z += c_i X_i, i = 1, 2, ...).
+// blockIdx.y = component; components 0-4 have ncell entries, component 5 has 10 ncell.
+__global__ void mri_forcing_kernel(long ncell, int nf, ForcingSet F, DevFields6 wdot) {
+  const int k = blockIdx.y;
+  const long len = (k == 5) ? 10 * ncell : ncell;
+  double* __restrict__ z = wdot.f[k];
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < len;
+       j += (long)gridDim.x * blockDim.x) {
+    double acc = z[j];
+    for (int i = 0; i < nf; ++i) acc += F.c[i] * F.x[i][k][j];
+    z[j] = acc;
+  }
+}
+
+__global__ void zero_fluid_kernel(long ncell, DevFields6 wdot) {
+  const int k = blockIdx.y;
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < ncell;
+       j += (long)gridDim.x * blockDim.x)
+    wdot.f[k][j] = 0.0;
+}
+
+int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot, bool zero_fluid,
+                cudaStream_t s) {
+  const int threads = 256;
+  const long blocks_x = std::min<long>((10 * ncell + threads - 1) / threads, (long)kSM * 16);
+  ProfScope ps("glue", s);
+  if (zero_fluid) {
+    zero_fluid_kernel<<<dim3((unsigned)std::min<long>((ncell + threads - 1) / threads, (long)kSM * 16), 5),
+                        threads, 0, s>>>(ncell, wdot);
+    GBMV_LAUNCH_CHECK("zero_fluid_kernel");
+  }
+  if (nf > 0) {
+    mri_forcing_kernel<<<dim3((unsigned)blocks_x, 6), threads, 0, s>>>(ncell, nf, F, wdot);
+    GBMV_LAUNCH_CHECK("mri_forcing_kernel");
+  }
   return GBMV_OK;
 }
 

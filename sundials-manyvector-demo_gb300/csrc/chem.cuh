@@ -32,6 +32,18 @@ int energy_sync(const ChemState& S, double* const* w, long n, int nchem, double 
 int energy_epilogue(const ChemState& S, double* chem, double* chemdot, double* etdot, long n,
                     int nchem, int exact, cudaStream_t s);
 
+// MRI forcing of the fast RHS (ffast): wdot_k += sum_i c_i x_i,k over the six components
+constexpr int kMaxForcing = 8;
+struct DevFields6 {
+  double* f[6];
+};
+struct ForcingSet {
+  double c[kMaxForcing];                 // tau^i
+  const double* x[kMaxForcing][6];       // forcing vector i, component k
+};
+int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot, bool zero_fluid,
+                cudaStream_t s);
+
 // fused source + Jacobian + Newton matrix + LU solve (chem_newton.cu)
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,

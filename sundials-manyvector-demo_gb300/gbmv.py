@@ -87,6 +87,8 @@ SIGNATURES = [
     ("gbmv_chem_dirk_evolve_async", C.c_int, [_VP, C.c_double, C.c_double, _VP, C.c_double,
                                               C.POINTER(_DirkOpts), _VP, _VP, _VP]),
     ("gbmv_chem_dirk_block", C.c_int, [_VP, C.c_int]),
+    ("gbmv_ffast", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
+                             C.c_int, C.POINTER(_VP), C.c_double, C.c_double, _VP]),
     ("gbmv_postprocess_step", C.c_int, [_VP, _VP, C.POINTER(_VP), C.c_double, _VP]),
     ("gbmv_version", C.c_char_p, []),
     ("gbmv_last_error", C.c_char_p, []),
@@ -364,6 +366,21 @@ def chem_newton_async(chem: Chem, t, y, f, x, gamma, time_units, info, lu_precis
                                                 gamma, time_units, lu_precision, refine,
                                                 info.data_ptr(), _stream_ptr(stream)),
                   "gbmv_chem_newton_async")
+
+
+def ffast(hydro: Hydro, chem: Chem, t, w, wdot, time_units, forcing=(), tshift=0.0, tscale=1.0,
+          stream=None):
+    """ffast (src/multirate_chem_hydro_main.cpp:897): chemistry RHS times TimeUnits on the
+    chemistry component, zero fluid tendencies, plus the MRI forcing sum_i tau^i forcing[i]
+    (each forcing[i] a ManyVector like w)."""
+    nf = len(forcing)
+    arr = (_VP * max(1, 6 * nf))()
+    for i, fv in enumerate(forcing):
+        for k, comp in enumerate(fv):
+            arr[6 * i + k] = _dev_ptr(comp)
+    return _check(load().gbmv_ffast(hydro.h, chem.c, t, _vec(w), _vec(wdot), time_units, nf,
+                                    arr if nf else None, tshift, tscale, _stream_ptr(stream)),
+                  "gbmv_ffast")
 
 
 def PostprocessStep(hydro: Hydro, chem: Chem, w, energy_units, stream=None):

@@ -88,3 +88,40 @@ def test_stability_cfl(cuda):
     alpha = np.max(np.abs(mx / rho) + np.sqrt(wl["gamma"] * p / rho))  # |mx/rho| for all axes
     ref = 0.5 * min(1.0 / nx, 1.0 / ny, 1.0 / nz) / alpha
     assert abs(dt - ref) <= 1e-14 * ref
+
+
+@pytest.mark.parametrize("nforcing", [0, 2])
+def test_ffast_matches_oracle_composition(cuda, tables, nforcing):
+    """ffast = TimeUnits * f_chem on the chemistry component, zero fluid tendencies, plus
+    the MRI forcing sum_i tau^i r_i on all six components."""
+    torch = cuda
+    import gbmv
+    wl = W.chem_hydro(shape=(10, 8, 6))
+    TU = wl["units"]["TimeUnits"]
+    nz, ny, nx = wl["fields"][0].shape
+    n = nx * ny * nz
+    h = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"])
+    c = gbmv.Chem(n, tables)
+    c.set_scale(_dev(torch, wl["scale"].reshape(-1)))
+    w = [_dev(torch, f) for f in wl["fields"]]
+    wdot = [torch.full_like(f, np.nan) for f in w]
+    rng = np.random.default_rng(7)
+    forcing_h = [[rng.standard_normal(f.shape) for f in wl["fields"]] for _ in range(nforcing)]
+    forcing = [[_dev(torch, a) for a in fv] for fv in forcing_h]
+    t, tshift, tscale = 0.37, 0.1, 0.5
+    gbmv.ffast(h, c, t, w, wdot, TU, forcing, tshift, tscale)
+    torch.cuda.synchronize()
+    oc = O.Chem(tables, wl["scale"].reshape(-1))
+    ref = [np.zeros_like(f) for f in wl["fields"]]
+    ref[5] = (oc.rhs(wl["fields"][5].reshape(-1)) * TU).reshape(wl["fields"][5].shape)
+    tau = (t - tshift) / tscale
+    for i, fv in enumerate(forcing_h):
+        for k in range(6):
+            ref[k] = ref[k] + tau ** i * fv[k]
+    for k in range(6):
+        a, b = wdot[k].cpu().numpy(), ref[k]
+        if k == 5:
+            for s in range(10):
+                assert maxnorm_err(a[..., s], b[..., s]) <= 1e-12, (k, s)
+        else:
+            assert maxnorm_err(a, b) <= 1e-15, k
