@@ -214,6 +214,20 @@ int gbmv_chem_dirk_evolve_async(gbmv_chem c, double t0, double tout, double* y,
                                 double time_units, const gbmv_dirk_opts* opts, int* stats,
                                 int* d_nfail, void* stream);
 
+/* The rank-local MRI inner stepper's evolve (RankLocalStepper_Evolve,
+ * src/multirate_chem_hydro_main.cpp:1114-1160: ARKStepEvolve of ffast to tout) on the GPU:
+ * advances the fast problem w' = ffast(t, w) (see gbmv_ffast) from t0 to tout.  The
+ * chemistry component w[5] is integrated by the persistent DIRK of gbmv_chem_dirk_evolve with
+ * the forcing's chemistry component added to its right-hand side at every stage time; the
+ * fluid components, whose fast tendency is the forcing polynomial alone, receive its exact
+ * integral, w[k] += sum_i forcing[i*6+k] * tscale * (tau_out^(i+1) - tau_0^(i+1)) / (i+1).
+ * forcing/tshift/tscale as gbmv_ffast (MRIStepInnerStepper_GetForcingData).  Returns the
+ * number of failed cells (>= 0) or a negative code.  Synchronous. */
+int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, double* const* w,
+                         double time_units, int nforcing, const double* const* forcing,
+                         double tshift, double tscale, const gbmv_dirk_opts* opts, int* stats,
+                         void* stream);
+
 /* Block size the autotuner chose for a precision (0 = not tuned yet). */
 int gbmv_chem_dirk_block(gbmv_chem c, int precision);
 

@@ -639,8 +639,9 @@ static const double dk_gd = (2.0 - DK_SQRT2) / 2.0;
 static const double dk_w = DK_SQRT2 / 4.0;
 
 static void dirk_F(const orc_chem* c, const double* X, const double* sc, const double* isc,
-                   double md, double imd, double cie, double h2, double tunit, double* Ts,
-                   double* dTs, double* f) {
+                   double md, double imd, double cie, double h2, const orc_dirk_opts* O,
+                   long cell, double tf, double* Ts, double* dTs, double* f) {
+  const double tunit = O->tunit;
   double ya[10], k[NRATES], dk[NRATES], r[21];
   for (int s = 0; s < 10; ++s) ya[s] = X[s] * sc[s];
   temperature(c, ya, Ts, dTs);
@@ -650,6 +651,14 @@ static void dirk_F(const orc_chem* c, const double* X, const double* sc, const d
   double ge = ge_source(c, k, ya, *Ts, md, cie, h2) * isc[9];
   ge *= imd;
   f[9] = ge * tunit;
+  if (O->nforcing > 0) {
+    const double tau = (tf - O->tshift) / O->tscale;
+    double p = 1.0;
+    for (int q = 0; q < O->nforcing; ++q) {
+      for (int s = 0; s < 10; ++s) f[s] += p * O->fz[q][cell * 10 + s];
+      p *= tau;
+    }
+  }
 }
 
 static double dk_wrms(const double* v, const double* ew) {
@@ -680,7 +689,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
     int nst = 0, nst_lp = 0, nef_s = 0, ncf_s = 0;
     int nni = 0, netf = 0, ncf = 0, nsetup = 0, nfe = 0;
     int jcur = 0, force_setup = 1, last = 0, failed = 0;
-    dirk_F(c, Y, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, K1);
+    dirk_F(c, Y, sc, isc, md, imd, cie, h2, O, i, t, &Tsc, &dTsc, K1);
     ++nfe;
     Tsy = Tsc;
     dTsy = dTsc;
@@ -737,10 +746,11 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
       int conv = 1;
       for (int stage = 2; stage <= 3 && conv; ++stage) {
         const double gam = h * dk_gd, hw = h * dk_w;
+        const double tst = (stage == 2) ? t + (2.0 * dk_gd) * h : t + h;  /* c = (0, 2gd, 1) */
         int m = 0;
         conv = 0;
         for (;;) {
-          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, f);
+          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, f);
           ++nfe;
           double dl[10];
           for (int s = 0; s < 10; ++s)
@@ -761,7 +771,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
           delp = del;
         }
         if (conv && stage == 2) {
-          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, K2);
+          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, K2);
           ++nfe;
         }
       }
@@ -773,7 +783,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
         else force_setup = 1;
         continue;
       }
-      dirk_F(c, Z, sc, isc, md, imd, cie, h2, O->tunit, &Tsc, &dTsc, f);
+      dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, t + h, &Tsc, &dTsc, f);
       ++nfe;
       double err[10];
       for (int s = 0; s < 10; ++s) err[s] = h * ((e1 * K1[s] + e2 * K2[s]) + e3 * f[s]);

@@ -84,6 +84,11 @@ typedef struct {
   double t0, tout, tunit;
   double rtol, atol, nlscoef, h0, h0fac, safety, dgmax, growth, etamx1, hmax;
   int maxcor, max_steps, msbp, maxnef, maxncf;
+  /* MRI forcing added to the right-hand side: sum_i tau^i fz[i] (10 values per cell),
+   * tau = (t - tshift) / tscale (ffast, src/multirate_chem_hydro_main.cpp:921-944) */
+  int nforcing;
+  double tshift, tscale;
+  const double* fz[8];
 } orc_dirk_opts;
 
 /* Per-cell adaptive TR-BDF2 ESDIRK integration of dz/dt = tunit * f_chem(z) (scaled

@@ -48,7 +48,9 @@ class OrcDirkOpts(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("t0", "tout", "tunit", "rtol", "atol", "nlscoef", "h0",
                                           "h0fac", "safety", "dgmax", "growth", "etamx1",
                                           "hmax")] + \
-               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf")]
+               [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf",
+                                       "nforcing")] + \
+               [("tshift", C.c_double), ("tscale", C.c_double), ("fz", _P * 8)]
 
 
 # defaults of gbmv_dirk_opts_default (include/gbmv.h)
@@ -142,12 +144,18 @@ class Chem:
                            _ptr(self.h2), _ptr(self.Ts), _ptr(self.dTs_ge), _ptr(J))
         return J.reshape(self.n, 10, 10)  # [cell][col][row]
 
-    def dirk_evolve(self, y: np.ndarray, t0: float, tout: float, tunit: float, **opts):
-        """Per-cell adaptive TR-BDF2 integration from t0 to tout (orc_chem_dirk_evolve).
+    def dirk_evolve(self, y: np.ndarray, t0: float, tout: float, tunit: float, forcing=(),
+                    tshift=0.0, tscale=1.0, **opts):
+        """Per-cell adaptive TR-BDF2 integration from t0 to tout (orc_chem_dirk_evolve), with
+        the MRI forcing sum_i tau^i forcing[i] (chemistry components) added to the RHS.
         Returns (y(tout), stats[n, 8], number of failed cells); Ts / dTs_ge carried."""
         o = dict(DIRK_DEFAULTS, **opts)
         O = OrcDirkOpts()
         O.t0, O.tout, O.tunit = t0, tout, tunit
+        keep = [np.ascontiguousarray(f, dtype=np.float64).reshape(-1) for f in forcing]
+        O.nforcing, O.tshift, O.tscale = len(keep), tshift, tscale
+        for q, f in enumerate(keep):
+            O.fz[q] = _ptr(f)
         for k, v in o.items():
             setattr(O, k, v)
         O.h0fac = 0.5 * o["rtol"] ** (-2.0 / 3.0)

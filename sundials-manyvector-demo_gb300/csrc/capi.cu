@@ -468,6 +468,10 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
   O->maxncf = o->maxncf;
   O->refine = o->precision == GBMV_MIXED ? o->refine : 0;
   O->mixed_temp = o->precision == GBMV_MIXED;
+  O->nforcing = 0;
+  O->tshift = 0.0;
+  O->tscale = 1.0;
+  for (int q = 0; q < 8; ++q) O->fz[q] = nullptr;
   return GBMV_OK;
 }
 
@@ -683,7 +687,64 @@ int gbmv_ffast(gbmv_hydro h, gbmv_chem c, double t, const double* const* w, doub
   for (int k = 0; k < 6; ++k) D.f[k] = wdot[k];
   int rc = chem_rhs(c->P, c->S, c->n, w[5], wdot[5], time_units, s);  // wdot[5] fully written
   if (rc) return rc;
-  return mri_forcing(c->n, F, nforcing, D, true, s);
+  return mri_forcing(c->n, F, nforcing, D, true, 6, s);
+}
+
+int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, double* const* w,
+                         double time_units, int nforcing, const double* const* forcing,
+                         double tshift, double tscale, const gbmv_dirk_opts* opts, int* stats,
+                         void* stream) {
+  if (!h || !c || h->g.nchem != 10 || c->n != h->g.ncell || !fields_ok(w, 10)) {
+    set_error("mri_fast_evolve needs a 10-species hydro grid matching the chemistry cells");
+    return GBMV_EINVAL;
+  }
+  if (nforcing < 0 || nforcing > kMaxForcing || (nforcing > 0 && (!forcing || !(tscale != 0.0)))) {
+    set_error("bad forcing arguments (nforcing 0-%d, forcing pointers, tscale != 0)", kMaxForcing);
+    return GBMV_EINVAL;
+  }
+  DirkOpts O;
+  int rc = dirk_opts(opts, t0, tout, time_units, &O);
+  if (rc) return rc;
+  ForcingSet Ff{};
+  const double tau0 = nforcing > 0 ? (t0 - tshift) / tscale : 0.0;
+  const double tau1 = nforcing > 0 ? (tout - tshift) / tscale : 0.0;
+  double p0 = tau0, p1 = tau1;  // tau^(i+1)
+  for (int i = 0; i < nforcing; ++i) {
+    for (int k = 0; k < 6; ++k)
+      if (!forcing[i * 6 + k]) { set_error("null forcing vector %d component %d", i, k); return GBMV_EINVAL; }
+    // fluid components: exact integral of the forcing polynomial over [t0, tout]
+    Ff.c[i] = tscale * (p1 - p0) / (double)(i + 1);
+    for (int k = 0; k < 6; ++k) Ff.x[i][k] = forcing[i * 6 + k];
+    O.fz[i] = forcing[i * 6 + 5];  // chemistry component: inside the DIRK right-hand side
+    p0 *= tau0;
+    p1 *= tau1;
+  }
+  O.nforcing = nforcing;
+  O.tshift = tshift;
+  O.tscale = tscale;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nforcing > 0) {
+    DevFields6 D;
+    for (int k = 0; k < 6; ++k) D.f[k] = w[k];
+    rc = mri_forcing(c->n, Ff, nforcing, D, false, 5, s);  // components 0-4 only
+    if (rc) return rc;
+  }
+  const int mixed = opts->precision == GBMV_MIXED;
+  int block = opts->block ? opts->block : c->dirk_block[mixed];
+  if (!block) {
+    O.nforcing = 0;  // tune on the unforced problem (same work per evaluation within a few %)
+    rc = dirk_autotune(c, w[5], O, mixed, s);
+    if (rc) return rc;
+    O.nforcing = nforcing;
+    block = c->dirk_block[mixed];
+  }
+  GBMV_CUDA_TRY(cudaMemsetAsync(c->d_nfail, 0, sizeof(int), s));
+  rc = chem_dirk(c->P, c->S, c->n, w[5], O, mixed, block, c->d_next, stats, c->d_nfail, s);
+  if (rc) return rc;
+  int nf = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&nf, c->d_nfail, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  return nf;
 }
 
 int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double energy_units,

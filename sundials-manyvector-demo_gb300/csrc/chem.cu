@@ -254,7 +254,7 @@ __global__ void zero_fluid_kernel(long ncell, DevFields6 wdot) {
 }
 
 int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot, bool zero_fluid,
-                cudaStream_t s) {
+                int ncomp, cudaStream_t s) {
   const int threads = 256;
   const long blocks_x = std::min<long>((10 * ncell + threads - 1) / threads, (long)kSM * 16);
   ProfScope ps("glue", s);
@@ -264,7 +264,7 @@ int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot,
     GBMV_LAUNCH_CHECK("zero_fluid_kernel");
   }
   if (nf > 0) {
-    mri_forcing_kernel<<<dim3((unsigned)blocks_x, 6), threads, 0, s>>>(ncell, nf, F, wdot);
+    mri_forcing_kernel<<<dim3((unsigned)blocks_x, ncomp), threads, 0, s>>>(ncell, nf, F, wdot);
     GBMV_LAUNCH_CHECK("mri_forcing_kernel");
   }
   return GBMV_OK;

@@ -42,7 +42,7 @@ struct ForcingSet {
   const double* x[kMaxForcing][6];       // forcing vector i, component k
 };
 int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot, bool zero_fluid,
-                cudaStream_t s);
+                int ncomp, cudaStream_t s);
 
 // fused source + Jacobian + Newton matrix + LU solve (chem_newton.cu)
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
@@ -62,6 +62,11 @@ struct DirkOpts {
   int maxcor, max_steps, msbp, maxnef, maxncf;
   int refine;      // FP32 LU: refinement steps per Newton solve
   int mixed_temp;  // temperature iterations 1-8 in FP32
+  // MRI forcing added to F: sum_i tau^i fz[i] (chemistry components, 10 per cell),
+  // tau = (t - tshift) / tscale
+  int nforcing;
+  double tshift, tscale;
+  const double* fz[8];
 };
 constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
                                // matrix setups, Jacobians (= setups), F evaluations, failed

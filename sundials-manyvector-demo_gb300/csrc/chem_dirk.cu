@@ -52,11 +52,14 @@ constexpr double kE3 = kGd - kGd / 3.0;
 
 enum : int { kPhK1 = 0, kPhNewton = 1, kPhK2 = 2, kPhK3 = 3 };
 
-// F at a point given in the solver's scaled variables (strided shared-memory slice X).
+// F at a point given in the solver's scaled variables (strided shared-memory slice X) and
+// time tf: TimeUnits * f_chem plus the MRI forcing polynomial (ffast's order of summation).
 template <int BS>
 __device__ __forceinline__ void dirk_F(const ChemParams& P, const ChemState& S, long i,
-                                       const double* X, double tunit, bool mixed_temp,
-                                       double& Ts, double& dTs, double (&f)[10]) {
+                                       const double* X, const DirkOpts& O, double tf,
+                                       bool mixed_temp, double& Ts, double& dTs,
+                                       double (&f)[10]) {
+  const double tunit = O.tunit;
   const long j = i * 10;
   double ya[10];
 #pragma unroll
@@ -76,6 +79,16 @@ __device__ __forceinline__ void dirk_F(const ChemParams& P, const ChemState& S, 
   double ge = chem_ge_source(P, k, ya, Ts, Ax) * S.inv_scale[j + 9];
   ge *= Ax.imdens;
   f[9] = ge * tunit;
+  if (O.nforcing > 0) {
+    const double tau = (tf - O.tshift) / O.tscale;
+    double p = 1.0;
+    for (int q = 0; q < O.nforcing; ++q) {
+      const double* __restrict__ r = O.fz[q] + j;
+#pragma unroll
+      for (int s = 0; s < 10; ++s) f[s] += p * r[s];
+      p *= tau;
+    }
+  }
 }
 
 }  // namespace
@@ -182,7 +195,9 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 
     // ---- one evaluation of F per pass (at Y for the first stage, else at the iterate)
     double f[10];
-    dirk_F<BS>(P, S, i, phase == kPhK1 ? Y : Z, O.tunit, mixed_temp, Tsc, dTsc, f);
+    // stage abscissae of the ESDIRK: c = (0, 2 gd, 1)
+    const double tf = (phase == kPhK1) ? t : ((stage == 2) ? t + (2.0 * kGd) * h : t + h);
+    dirk_F<BS>(P, S, i, phase == kPhK1 ? Y : Z, O, tf, mixed_temp, Tsc, dTsc, f);
     ++c_nfe;
 
     bool setup = false, retire = false, failed = false;

@@ -87,6 +87,9 @@ SIGNATURES = [
     ("gbmv_chem_dirk_evolve_async", C.c_int, [_VP, C.c_double, C.c_double, _VP, C.c_double,
                                               C.POINTER(_DirkOpts), _VP, _VP, _VP]),
     ("gbmv_chem_dirk_block", C.c_int, [_VP, C.c_int]),
+    ("gbmv_mri_fast_evolve", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.POINTER(_VP),
+                                       C.c_double, C.c_int, C.POINTER(_VP), C.c_double,
+                                       C.c_double, C.POINTER(_DirkOpts), _VP, _VP]),
     ("gbmv_ffast", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
                              C.c_int, C.POINTER(_VP), C.c_double, C.c_double, _VP]),
     ("gbmv_postprocess_step", C.c_int, [_VP, _VP, C.POINTER(_VP), C.c_double, _VP]),
@@ -381,6 +384,25 @@ def ffast(hydro: Hydro, chem: Chem, t, w, wdot, time_units, forcing=(), tshift=0
     return _check(load().gbmv_ffast(hydro.h, chem.c, t, _vec(w), _vec(wdot), time_units, nf,
                                     arr if nf else None, tshift, tscale, _stream_ptr(stream)),
                   "gbmv_ffast")
+
+
+def mri_fast_evolve(hydro: Hydro, chem: Chem, t0, tout, w, time_units, forcing=(), tshift=0.0,
+                    tscale=1.0, stats=None, stream=None, **opts) -> int:
+    """RankLocalStepper_Evolve (src/multirate_chem_hydro_main.cpp:1114): advance the fast
+    problem w' = ffast(t, w) (chemistry by the persistent DIRK with the forcing's chemistry
+    component, fluid by the forcing's exact integral) from t0 to tout in place.  Returns the
+    number of failed cells."""
+    nf = len(forcing)
+    arr = (_VP * max(1, 6 * nf))()
+    for i, fv in enumerate(forcing):
+        for k, comp in enumerate(fv):
+            arr[6 * i + k] = _dev_ptr(comp)
+    o = dirk_opts(**opts)
+    return _check(load().gbmv_mri_fast_evolve(hydro.h, chem.c, t0, tout, _vec(w), time_units, nf,
+                                              arr if nf else None, tshift, tscale, C.byref(o),
+                                              stats.data_ptr() if stats is not None else None,
+                                              _stream_ptr(stream)),
+                  "gbmv_mri_fast_evolve", allow=range(0, chem.n + 1))
 
 
 def PostprocessStep(hydro: Hydro, chem: Chem, w, energy_units, stream=None):

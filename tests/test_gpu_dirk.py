@@ -154,3 +154,48 @@ def test_dirk_options_rejected(cuda, tables):
             c.dirk_evolve(0.0, 1e-3, z, TU, **bad)
     with pytest.raises(gbmv.GbmvError):
         c.dirk_evolve(1.0, 0.5, z, TU)   # tout must exceed t0
+
+
+def test_mri_fast_evolve_with_forcing(cuda, tables):
+    """RankLocalStepper_Evolve counterpart: chemistry by the DIRK with the forcing's chemistry
+    component in its right-hand side (against the oracle's forced integration), fluid
+    components by the forcing polynomial's exact integral."""
+    torch = cuda
+    import gbmv
+    wl = W.chem_hydro(shape=(8, 6, 5))
+    nz, ny, nx = wl["fields"][0].shape
+    n = nx * ny * nz
+    h = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"])
+    c = gbmv.Chem(n, tables)
+    c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    rng = np.random.default_rng(11)
+    fh = [[1e-2 * rng.standard_normal(f.shape) for f in wl["fields"]] for _ in range(2)]
+    forcing = [[torch.from_numpy(a).cuda() for a in fv] for fv in fh]
+    t0, tout, tshift, tscale = 0.2, 0.2 + 1e-4, 0.15, 1e-3
+    st = torch.zeros(8 * n, dtype=torch.int32, device="cuda")
+    nf = gbmv.mri_fast_evolve(h, c, t0, tout, w, TU, forcing, tshift, tscale, stats=st,
+                              precision=0, block=64, **OPTS)
+    torch.cuda.synchronize()
+    assert nf == 0
+    tau0, tau1 = (t0 - tshift) / tscale, (tout - tshift) / tscale
+    for k in range(5):
+        ref = wl["fields"][k] + sum(fh[i][k] * tscale * (tau1 ** (i + 1) - tau0 ** (i + 1)) / (i + 1)
+                                    for i in range(2))
+        assert np.max(np.abs(w[k].cpu().numpy() - ref)) <= 1e-14 * max(1.0, np.max(np.abs(ref)))
+    oc = O.Chem(tables, wl["scale"].reshape(-1))
+    zo, so, nfo = oc.dirk_evolve(wl["fields"][5].reshape(-1), t0, tout, TU,
+                                 forcing=[fv[5] for fv in fh], tshift=tshift, tscale=tscale,
+                                 **OPTS)
+    assert nfo == 0
+    zg = w[5].cpu().numpy().reshape(n, 10)
+    zo = zo.reshape(n, 10)
+    sg = st.cpu().numpy().reshape(n, 8)
+    same = np.all(sg[:, :7] == so[:, :7], axis=1)
+    assert same.mean() >= 0.75
+    err = _relerr(zg, zo, OPTS["atol"] / OPTS["rtol"]).max(axis=1)
+    assert np.median(err[same]) <= 1e-11 and np.max(err) <= 1e-3
+    # the forcing changed the chemistry: an unforced run lands elsewhere
+    oc2 = O.Chem(tables, wl["scale"].reshape(-1))
+    zu, _, _ = oc2.dirk_evolve(wl["fields"][5].reshape(-1), t0, tout, TU, **OPTS)
+    assert np.max(np.abs(zu.reshape(n, 10) - zo)) > 1e-8
