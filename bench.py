@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--dirk-n", type=int, default=64,
                    help="static-chemistry DIRK measurement on dirk_n^3 cells (0 = skip)")
+    p.add_argument("--weno-n", default="128,256",
+                   help="Rayleigh-Taylor WENO RHS throughput grids (comma list, '' = skip)")
     p.add_argument("--dirk-only", action="store_true",
                    help="run only the DIRK measurement (prints its object)")
     p.add_argument("--dirk-form", default="both", choices=["both", "fp64", "mixed"])
@@ -430,6 +432,12 @@ def run_gbmv(args):
                        "ms_per_step": round(ms_e2e, 4)}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(sample_n=(128, 128, 32))
+    if args.weno_n:
+        for r in res.values():
+            r["fs"] = None
+        fs = None
+        torch.cuda.empty_cache()
+        line["weno_rhs"] = run_weno(torch, gbmv, [int(x) for x in args.weno_n.split(",") if x])
     if args.dirk_n > 0:
         for k in ("fs",):
             for r in res.values():
@@ -439,6 +447,49 @@ def run_gbmv(args):
         line["chem_dirk"] = run_dirk(torch, gbmv, args.dirk_n, not args.no_cpu_baseline,
                                      args.dirk_form)
     print(json.dumps(line))
+
+
+# ----------------------------------------------------------------- WENO RHS throughput (RT)
+
+def run_weno(torch, gbmv, grids, steps=3, warmup=2):
+    """Rayleigh-Taylor WENO RHS (fEuler alone) at NVAR 15, both forms: RHS evaluations per
+    second, cell updates per second, algorithmic HBM GB/s (read w + write wdot = 240 B/cell)
+    and the FP64 form's FP64-pipe fraction from the counted flops per face."""
+    import workloads as W
+    fp64_peak = gbmv.fma_rate(True) / 1e12
+    hbm_peak, peak_kind = measured_peaks()
+    out = {"workload": "Rayleigh-Taylor: rho = 1.5 + 0.5 tanh((z-0.5)/0.02), hydrostatic p "
+                       "(g = -0.1, p(1) = 2.5), velocities U[-1e-2, 1e-2], 10 tracers U[0,1] rho; "
+                       "periodic x,y, reflecting z; constant force -0.1 on z-momentum",
+           "nvar": 15, "hbm_peak_gbs": hbm_peak, "fp64_peak_tflops": round(fp64_peak, 4),
+           "grids": {}}
+    for n in grids:
+        wl = W.rayleigh_taylor(n=n, nchem=10)
+        h = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"], wl["force"])
+        w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+        del wl
+        wdot = [torch.empty_like(f) for f in w]
+        ncell = n ** 3
+        faces = 3 * (n + 1) * n * n
+        g = {}
+        for name, prec in (("fp64", gbmv.FP64), ("mixed", gbmv.MIXED)):
+            def rhs():
+                if h.fEuler(0.0, w, wdot, prec) != 0:
+                    raise RuntimeError("fEuler failed")
+            ms = time_steps(torch, rhs, steps, warmup)
+            r = {"ms_per_rhs": round(ms, 3), "rhs_per_s": round(1e3 / ms, 2),
+                 "Mcell_updates_per_s": round(ncell / (ms * 1e-3) / 1e6, 2),
+                 "algorithmic_GBps": round(240.0 * ncell / (ms * 1e-3) / 1e9, 1),
+                 "hbm_frac": round(240.0 * ncell / (ms * 1e-3) / 1e9 / hbm_peak, 5)}
+            if name == "fp64":
+                fl = FP_COUNTS[("fp64", "face_flux")][1] * faces + 158.4 * ncell
+                r["fp64_pipe_frac"] = round(fl / (ms * 1e-3) / 1e12 / fp64_peak, 4)
+            g[name] = r
+        g["speedup_mixed_vs_fp64"] = round(g["fp64"]["ms_per_rhs"] / g["mixed"]["ms_per_rhs"], 3)
+        out["grids"][f"{n}^3"] = g
+        del h, w, wdot
+        torch.cuda.empty_cache()
+    return out
 
 
 # ----------------------------------------------------------------- static chemistry (DIRK)
