@@ -110,6 +110,22 @@ int gbmv_feuler_noalloc(const gbmv_grid* grid, const double* force_host, double 
 int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,
                    void* stream);
 
+/* Derivatives of fEuler in its FP64 form (no counterpart in the reference, which has no
+ * adjoint; for Newton-Krylov Jacobian actions, sensitivities and gradients through time steps):
+ *   gbmv_feuler_jvp: jv = (d fEuler / d w)(w) dw  (forward mode: the face flux on dual
+ *                    numbers, the exact linearisation of what gbmv_feuler computes);
+ *   gbmv_feuler_vjp: u = (d fEuler / d w)(w)^T v  (hand-written reverse mode of the face flux
+ *                    and the divergence, ghost rules inverted; deterministic, no atomics).
+ * All arguments are ManyVectors laid out like w.  The constant external force has no
+ * derivative.  At kinks (the Lax-Friedrichs max over the stencil, |u|) the branch the forward
+ * evaluation took is differentiated.  The first VJP call on a handle allocates
+ * 6 (5+nchem) x (faces of one direction) doubles: make it before any stream capture.
+ * Asynchronous; returns 0 or < 0. */
+int gbmv_feuler_jvp(gbmv_hydro h, double t, const double* const* w, const double* const* dw,
+                    double* const* jv, void* stream);
+int gbmv_feuler_vjp(gbmv_hydro h, double t, const double* const* w, const double* const* v,
+                    double* const* u, void* stream);
+
 /* -------------------------------------------------------------- chemistry (part b) */
 
 typedef struct gbmv_chem_s* gbmv_chem;
@@ -163,6 +179,16 @@ int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* 
 int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, double* x,
                            double gamma, double time_units, int lu_precision, int refine,
                            int* d_info, void* stream);
+
+/* Products with the chemistry Jacobian of gbmv_chem_jac (J = time_units * df/dy at the
+ * temperature state of the last gbmv_chem_rhs, entries rounded exactly as gbmv_chem_jac
+ * writes them) without forming it: gbmv_chem_jvp jv = J dy (the matrix-free Jacobian action
+ * of Newton-Krylov), gbmv_chem_vjp u = J^T v (the adjoint of the chemistry source).
+ * 10 * ncells doubles each.  Asynchronous. */
+int gbmv_chem_jvp(gbmv_chem c, double t, const double* y, const double* dy, double* jv,
+                  double time_units, void* stream);
+int gbmv_chem_vjp(gbmv_chem c, double t, const double* y, const double* v, double* u,
+                  double time_units, void* stream);
 
 /* Options of the persistent DIRK chemistry integrator (gbmv_chem_dirk_evolve). */
 typedef struct {

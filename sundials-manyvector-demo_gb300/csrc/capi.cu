@@ -73,6 +73,7 @@ struct gbmv_hydro_s {
   double* scratch = nullptr;
   size_t scratch_doubles = 0;
   float* prims = nullptr;  // float-float per-cell primitives of the mixed form (first use)
+  double* adj = nullptr;   // per-face stencil cotangents of the VJP (first use)
   int* d_status = nullptr;
 };
 
@@ -186,6 +187,7 @@ int gbmv_hydro_destroy(gbmv_hydro h) {
   if (!h) return GBMV_OK;
   cudaFree(h->scratch);
   cudaFree(h->prims);
+  cudaFree(h->adj);
   cudaFree(h->d_status);
   delete h;
   return GBMV_OK;
@@ -745,6 +747,74 @@ int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, doub
   GBMV_CUDA_TRY(cudaMemcpyAsync(&nf, c->d_nfail, sizeof(int), cudaMemcpyDeviceToHost, s));
   GBMV_CUDA_TRY(cudaStreamSynchronize(s));
   return nf;
+}
+
+static bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+int gbmv_feuler_jvp(gbmv_hydro h, double t, const double* const* w, const double* const* dw,
+                    double* const* jv, void* stream) {
+  (void)t;
+  if (!h || !fields_ok(w, h->g.nchem) || !fields_ok(dw, h->g.nchem) ||
+      !fields_ok(jv, h->g.nchem)) {
+    set_error("null handle or field pointer");
+    return GBMV_EINVAL;
+  }
+  Fields W, D, O;
+  for (int v = 0; v < 6; ++v) {
+    W.f[v] = const_cast<double*>(w[v]);
+    D.f[v] = const_cast<double*>(dw[v]);
+    O.f[v] = jv[v];
+  }
+  return feuler_jvp(h->g, W, D, O, h->scratch, (cudaStream_t)stream);
+}
+
+int gbmv_feuler_vjp(gbmv_hydro h, double t, const double* const* w, const double* const* v,
+                    double* const* u, void* stream) {
+  (void)t;
+  if (!h || !fields_ok(w, h->g.nchem) || !fields_ok(v, h->g.nchem) ||
+      !fields_ok(u, h->g.nchem)) {
+    set_error("null handle or field pointer");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->adj) {
+    if (capturing(s)) {
+      set_error("the first gbmv_feuler_vjp call on a handle allocates its buffer: make it "
+                "before any stream capture");
+      return GBMV_EINVAL;
+    }
+    const size_t nd = feuler_vjp_scratch_doubles(h->g);
+    if (cudaMalloc(&h->adj, nd * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      h->adj = nullptr;
+      set_error("device allocation of %zu adjoint doubles failed", nd);
+      return GBMV_ENOMEM;
+    }
+  }
+  Fields W, V, U;
+  for (int k = 0; k < 6; ++k) {
+    W.f[k] = const_cast<double*>(w[k]);
+    V.f[k] = const_cast<double*>(v[k]);
+    U.f[k] = u[k];
+  }
+  return feuler_vjp(h->g, W, V, U, h->adj, s);
+}
+
+int gbmv_chem_jvp(gbmv_chem c, double t, const double* y, const double* dy, double* jv,
+                  double time_units, void* stream) {
+  (void)t;
+  if (!c || !y || !dy || !jv) { set_error("null argument"); return GBMV_EINVAL; }
+  return chem_jvp(c->P, c->S, c->n, y, dy, jv, time_units, 0, (cudaStream_t)stream);
+}
+
+int gbmv_chem_vjp(gbmv_chem c, double t, const double* y, const double* v, double* u,
+                  double time_units, void* stream) {
+  (void)t;
+  if (!c || !y || !v || !u) { set_error("null argument"); return GBMV_EINVAL; }
+  return chem_jvp(c->P, c->S, c->n, y, v, u, time_units, 1, (cudaStream_t)stream);
 }
 
 int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double energy_units,

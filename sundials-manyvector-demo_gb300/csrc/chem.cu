@@ -62,6 +62,41 @@ __global__ void __launch_bounds__(128) chem_jac_kernel(ChemParams P, ChemState S
   }
 }
 
+// Jacobian-vector products with the chemistry Jacobian of chem_jac_kernel (same entries, same
+// rounding of each entry): TRANS = false: out = J dy; TRANS = true: out = J^T v.  The
+// derivatives of the chemistry source for Newton-Krylov (JVP) and adjoints (VJP), without
+// forming J in HBM.
+template <bool TRANS>
+__global__ void __launch_bounds__(128) chem_jvp_kernel(ChemParams P, ChemState S, long n,
+                                                       const double* __restrict__ y,
+                                                       const double* __restrict__ x,
+                                                       double* __restrict__ out, double tunit) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const long j = i * 10;
+    const double* __restrict__ sc = S.scale + j;
+    const double* __restrict__ isc = S.inv_scale + j;
+    double ya[10], xv[10], acc[10];
+#pragma unroll
+    for (int s = 0; s < 10; ++s) {
+      ya[s] = y[j + s] * sc[s];
+      xv[s] = x[j + s];
+      acc[s] = 0.0;
+    }
+    const double T = S.Ts[i];
+    double k[kNRates], dk[kNRates];
+    chem_rates<true>(P, T, k, dk);
+    const ChemAux A{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
+    chem_jacobian(P, k, dk, ya, T, S.dTs_ge[i], A, [&](int row, int col, double v) {
+      const double e = (v * (isc[row] * sc[col])) * tunit;
+      if (TRANS) acc[col] += e * xv[row];
+      else acc[row] += e * xv[col];
+    });
+#pragma unroll
+    for (int s = 0; s < 10; ++s) out[j + s] = acc[s];
+  }
+}
+
 // setting_up_extra_variables (src/raja_primordial_network.cpp:1969-2018)
 __global__ void chem_aux_kernel(ChemState S, long n) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
@@ -181,6 +216,17 @@ int chem_jac(const ChemParams& P, const ChemState& S, long n, const double* y, d
   ProfScope ps("chem_jac", s);
   chem_jac_kernel<<<grid_for(n, 128), 128, 0, s>>>(P, S, n, y, J, tunit);
   GBMV_LAUNCH_CHECK("chem_jac_kernel");
+  return GBMV_OK;
+}
+
+int chem_jvp(const ChemParams& P, const ChemState& S, long n, const double* y, const double* x,
+             double* out, double tunit, int transpose, cudaStream_t s) {
+  ProfScope ps(transpose ? "vjp" : "jvp", s);
+  if (transpose)
+    chem_jvp_kernel<true><<<grid_for(n, 128), 128, 0, s>>>(P, S, n, y, x, out, tunit);
+  else
+    chem_jvp_kernel<false><<<grid_for(n, 128), 128, 0, s>>>(P, S, n, y, x, out, tunit);
+  GBMV_LAUNCH_CHECK("chem_jvp_kernel");
   return GBMV_OK;
 }
 

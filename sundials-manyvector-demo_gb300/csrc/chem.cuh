@@ -24,6 +24,8 @@ int chem_rhs(const ChemParams& P, const ChemState& S, long n, const double* y, d
 int chem_jac(const ChemParams& P, const ChemState& S, long n, const double* y, double* J,
              double tunit, cudaStream_t s);
 int chem_aux(const ChemState& S, long n, cudaStream_t s);
+int chem_jvp(const ChemParams& P, const ChemState& S, long n, const double* y, const double* x,
+             double* out, double tunit, int transpose, cudaStream_t s);
 int chem_prepare(const ChemState& S, double* chem, long n, cudaStream_t s);
 int chem_set_scale(const ChemState& S, const double* scale, long n, cudaStream_t s);
 int chem_scaling(const ChemState& S, double* chem, long n, int mode, cudaStream_t s);

@@ -25,6 +25,13 @@ int feuler_mixed(const Grid& g, const Fields& w, const Fields& wdot, const Force
 
 int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s);
 
+// derivatives of the FP64 flux divergence (weno_ad.cu)
+size_t feuler_vjp_scratch_doubles(const Grid& g);
+int feuler_jvp(const Grid& g, const Fields& w, const Fields& dw, const Fields& out,
+               double* scratch, cudaStream_t s);
+int feuler_vjp(const Grid& g, const Fields& w, const Fields& v, const Fields& out, double* A,
+               cudaStream_t s);
+
 size_t feuler_f2_prims_floats(const Grid& g);
 int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
               double* scratch, float* prims, int* d_status, cudaStream_t s);

@@ -61,6 +61,12 @@ SIGNATURES = [
     ("gbmv_feuler_noalloc", C.c_int, [C.POINTER(_Grid), _P, C.c_double, C.POINTER(_VP),
                                       C.POINTER(_VP), _VP]),
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
+    ("gbmv_feuler_jvp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
+                                  C.POINTER(_VP), _VP]),
+    ("gbmv_feuler_vjp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
+                                  C.POINTER(_VP), _VP]),
+    ("gbmv_chem_jvp", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double, _VP]),
+    ("gbmv_chem_vjp", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double, _VP]),
     ("gbmv_chem_create", C.c_int, [C.c_long, _P, C.c_double, C.POINTER(_VP)]),
     ("gbmv_chem_destroy", C.c_int, [_VP]),
     ("gbmv_chem_prepare", C.c_int, [_VP, _VP, _VP]),
@@ -200,6 +206,16 @@ class Hydro:
                                                status.data_ptr(), _stream_ptr(stream)),
                       "gbmv_feuler_async")
 
+    def fEuler_jvp(self, t, w, dw, jv, stream=None) -> int:
+        """jv = (d fEuler / d w) dw (FP64 form, forward mode)."""
+        return _check(load().gbmv_feuler_jvp(self.h, t, _vec(w), _vec(dw), _vec(jv),
+                                             _stream_ptr(stream)), "gbmv_feuler_jvp")
+
+    def fEuler_vjp(self, t, w, v, u, stream=None) -> int:
+        """u = (d fEuler / d w)^T v (FP64 form, hand-written reverse mode)."""
+        return _check(load().gbmv_feuler_vjp(self.h, t, _vec(w), _vec(v), _vec(u),
+                                             _stream_ptr(stream)), "gbmv_feuler_vjp")
+
 
 class Chem:
     """Device-side cvklu_data: rate tables, scale arrays, temperature state."""
@@ -257,6 +273,16 @@ class Chem:
     def calculate_jacobian_cvklu(self, t, y, J, time_units=1.0, stream=None):
         return _check(load().gbmv_chem_jac(self.c, t, _dev_ptr(y), _dev_ptr(J), time_units,
                                            _stream_ptr(stream)), "gbmv_chem_jac")
+
+    def jvp(self, t, y, dy, out, time_units=1.0, stream=None) -> int:
+        """out = J dy with J = time_units * df/dy (entries of calculate_jacobian_cvklu)."""
+        return _check(load().gbmv_chem_jvp(self.c, t, _dev_ptr(y), _dev_ptr(dy), _dev_ptr(out),
+                                           time_units, _stream_ptr(stream)), "gbmv_chem_jvp")
+
+    def vjp(self, t, y, v, out, time_units=1.0, stream=None) -> int:
+        """out = J^T v (the adjoint of the chemistry source)."""
+        return _check(load().gbmv_chem_vjp(self.c, t, _dev_ptr(y), _dev_ptr(v), _dev_ptr(out),
+                                           time_units, _stream_ptr(stream)), "gbmv_chem_vjp")
 
     def dirk_evolve(self, t0, tout, y, time_units=1.0, stats=None, stream=None, **opts) -> int:
         """Evolve every cell's chemistry from t0 to tout in place (persistent batched DIRK +
