@@ -257,6 +257,13 @@ int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, doub
 /* Block size the autotuner chose for a precision (0 = not tuned yet). */
 int gbmv_chem_dirk_block(gbmv_chem c, int precision);
 
+/* Launch shape of gbmv_chem_newton(_async) on this handle: 0 (default) a deep grid-stride
+ * grid; n > 0 exactly n resident 64-thread blocks per SM, a persistent grid that leaves room
+ * on every SM for a kernel running beside it on another stream (for example the WENO sweep of
+ * the same stage: the chemistry and the flux divergence of a stage are independent and load
+ * different pipes, FP64 and FP32).  Returns 0 or GBMV_EINVAL. */
+int gbmv_chem_set_newton_occupancy(gbmv_chem c, int blocks_per_sm);
+
 /* Device pointers of the persistent per-cell state (for checkpoint/restart and tests):
  * which: 0 Ts, 1 dTs_ge, 2 mdensity, 3 inv_mdensity, 4 cie optical depth, 5 h2 optical depth,
  * 6 scale, 7 inv_scale. */
@@ -284,7 +291,10 @@ int gbmv_block_form_newton(long nblocks, double* J, double gamma, void* stream);
 /* fslow / fexpl (src/multirate_chem_hydro_main.cpp:996-1083, src/imex_chem_hydro_main.cpp:
  * 910-1000): apply the Dengo scaling to w[5], set et = ge/EnergyUnits + |m|^2/(2 rho) in w[4],
  * evaluate fEuler, move the total-energy tendency into the gas-energy species of wdot[5]
- * (etdot = 0), undo the scaling.  Synchronous like gbmv_feuler. */
+ * (etdot = 0), undo the scaling.  GBMV_FP64 reproduces the reference's in-place scale and
+ * unscale of w[5] (and its rounding); GBMV_MIXED leaves w[5] untouched (the scale is applied
+ * where the WENO reads the species), so w[5] may be read concurrently, e.g. by the chemistry
+ * of the same stage on another stream.  Synchronous like gbmv_feuler. */
 int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* const* wdot,
                double energy_units, int precision, void* stream);
 

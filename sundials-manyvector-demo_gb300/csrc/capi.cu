@@ -87,6 +87,7 @@ struct gbmv_chem_s {
   int* d_nfail = nullptr;              //   [0] info, [1] failed cells,
   unsigned long long* d_next = nullptr;  //   [16] DIRK work counter
   int dirk_block[2] = {0, 0};          // autotuned block size per precision (0 = not yet)
+  int newton_bps = 0;                  // fused Newton: resident blocks per SM (0 = default)
 };
 
 static int check_grid(const gbmv_grid* g) {
@@ -199,9 +200,21 @@ int gbmv_hydro_set_force(gbmv_hydro h, const double* force) {
   return GBMV_OK;
 }
 
+// fEuler dispatch; tscale (mixed form only): the chemistry component is in scaled units and
+// is multiplied by tscale where the WENO reads it.
+static int feuler_dispatch(gbmv_hydro h, const double* const* w, double* const* wdot,
+                           int precision, int flags, int* d_status, cudaStream_t s,
+                           const double* tscale);
+
 int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
                       int precision, int flags, int* d_status, void* stream) {
   (void)t;
+  return feuler_dispatch(h, w, wdot, precision, flags, d_status, (cudaStream_t)stream, nullptr);
+}
+
+static int feuler_dispatch(gbmv_hydro h, const double* const* w, double* const* wdot,
+                           int precision, int flags, int* d_status, cudaStream_t s,
+                           const double* tscale) {
   if (!h || !fields_ok(w, h->g.nchem) || !fields_ok(wdot, h->g.nchem) || !d_status) {
     set_error("null handle, field or status pointer");
     return GBMV_EINVAL;
@@ -218,7 +231,6 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
   if (!h->g.nchem) W.f[5] = nullptr;
   ForceTerm G = h->force;
   G.in_wdot = (flags & GBMV_FORCE_IN_WDOT) ? 1 : 0;
-  cudaStream_t s = (cudaStream_t)stream;
   if (precision == GBMV_FP64) return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
   if (!h->prims) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -235,7 +247,7 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
       return GBMV_ENOMEM;
     }
   }
-  return feuler_f2(h->g, W, Wd, G, h->scratch, h->prims, d_status, s);
+  return feuler_f2(h->g, W, Wd, G, h->scratch, h->prims, tscale, d_status, s);
 }
 
 int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
@@ -391,7 +403,7 @@ int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, do
     return GBMV_EINVAL;
   }
   return chem_newton(c->P, c->S, c->n, y, f, x, gamma, time_units, lu_precision == GBMV_MIXED,
-                     refine, d_info, (cudaStream_t)stream);
+                     refine, d_info, (cudaStream_t)stream, c->newton_bps);
 }
 
 int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* x,
@@ -406,7 +418,7 @@ int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* 
   cudaStream_t s = (cudaStream_t)stream;
   GBMV_CUDA_TRY(cudaMemsetAsync(c->d_info, 0, sizeof(int), s));
   int rc = chem_newton(c->P, c->S, c->n, y, f, x, gamma, time_units, lu_precision == GBMV_MIXED,
-                       refine, c->d_info, s);
+                       refine, c->d_info, s, c->newton_bps);
   if (rc) return rc;
   int h = 0;
   GBMV_CUDA_TRY(cudaMemcpyAsync(&h, c->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -582,6 +594,15 @@ int gbmv_chem_dirk_evolve_async(gbmv_chem c, double t0, double tout, double* y,
                      false);
 }
 
+int gbmv_chem_set_newton_occupancy(gbmv_chem c, int blocks_per_sm) {
+  if (!c || blocks_per_sm < 0 || blocks_per_sm > 32) {
+    set_error("blocks_per_sm must be 0 (default) to 32");
+    return GBMV_EINVAL;
+  }
+  c->newton_bps = blocks_per_sm;
+  return GBMV_OK;
+}
+
 int gbmv_chem_dirk_block(gbmv_chem c, int precision) {
   if (!c || (precision != GBMV_FP64 && precision != GBMV_MIXED)) return 0;
   return c->dirk_block[precision == GBMV_MIXED];
@@ -637,11 +658,17 @@ int gbmv_fexpl_async(gbmv_hydro h, gbmv_chem c, double t, double* const* w,
   }
   if (!fields_ok(w, 10) || !fields_ok(wdot, 10)) return GBMV_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, 0, s);
+  (void)t;
+  // FP64 form: the reference's in-place scale / unscale of the chemistry component (its
+  // rounding included); mixed form: w[5] is left untouched (the scale is applied where the
+  // WENO reads it), so a concurrent chemistry branch may read w[5] during the sweep
+  const bool fp64 = precision == GBMV_FP64;
+  int rc = energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, fp64 ? 0 : 2, s);
   if (rc) return rc;
-  rc = gbmv_feuler_async(h, t, (const double* const*)w, wdot, precision, 0, d_status, stream);
+  rc = feuler_dispatch(h, (const double* const*)w, wdot, precision, 0, d_status, s,
+                       fp64 ? nullptr : c->S.scale);
   if (rc) return rc;
-  return energy_epilogue(c->S, w[5], wdot[5], wdot[4], c->n, 10, precision == GBMV_FP64, s);
+  return energy_epilogue(c->S, w[5], wdot[5], wdot[4], c->n, 10, fp64 ? 1 : 2, s);
 }
 
 int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* const* wdot,
@@ -652,13 +679,17 @@ int gbmv_fexpl(gbmv_hydro h, gbmv_chem c, double t, double* const* w, double* co
   }
   if (!fields_ok(w, 10) || !fields_ok(wdot, 10)) return GBMV_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, 0, s);
+  GBMV_CUDA_TRY(cudaMemsetAsync(h->d_status, 0, sizeof(int), s));
+  int rc = gbmv_fexpl_async(h, c, t, w, wdot, energy_units, precision, h->d_status, stream);
   if (rc) return rc;
-  rc = gbmv_feuler(h, t, (const double* const*)w, wdot, precision, stream);
-  if (rc < 0 && rc != GBMV_ILLEGAL_STATE) return rc;
-  int rc2 = energy_epilogue(c->S, w[5], wdot[5], wdot[4], c->n, 10, precision == GBMV_FP64, s);
-  if (rc2) return rc2;
-  return rc;
+  int st = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st) {
+    set_error("illegal state (mask %d: 1 density, 2 energy, 4 pressure)", st);
+    return GBMV_ILLEGAL_STATE;
+  }
+  return GBMV_OK;
 }
 
 int gbmv_ffast(gbmv_hydro h, gbmv_chem c, double t, const double* const* w, double* const* wdot,

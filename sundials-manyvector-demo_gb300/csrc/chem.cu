@@ -164,11 +164,16 @@ __global__ void energy_sync_kernel(const double* __restrict__ scale, double* __r
        i += (long)gridDim.x * blockDim.x) {
     double* c = chem + (long)nchem * i;
     const double* s = scale + (long)nchem * i;
-    for (int v = 0; v < nchem; ++v) c[v] *= s[v];
-    const double ge = c[nchem - 1];
+    double ge;
+    if (restore == 2) {  // et only: the chemistry component stays in its scaled units
+      ge = c[nchem - 1] * s[nchem - 1];
+    } else {
+      for (int v = 0; v < nchem; ++v) c[v] *= s[v];
+      ge = c[nchem - 1];
+    }
     const double r = rho[i], a = mx[i], b = my[i], d = mz[i];
     et[i] = ge * eunit_scale + 0.5 / r * (a * a + b * b + d * d);
-    if (restore)
+    if (restore == 1)
       for (int v = 0; v < nchem; ++v) c[v] /= s[v];
   }
 }
@@ -176,7 +181,8 @@ __global__ void energy_sync_kernel(const double* __restrict__ scale, double* __r
 // fslow/fexpl epilogue: chemdot[ge] = etdot, etdot = 0, chem /= scale
 // (src/multirate_chem_hydro_main.cpp:1061-1077).
 // exact = 1 divides by scale as the reference's unapply does; exact = 0 multiplies by
-// inv_scale (one rounding apart, and no FP64 division: the mixed-precision form).
+// inv_scale (one rounding apart, and no FP64 division); exact = 2: nothing to undo (the
+// mixed form applies the scale inside the WENO primitives pass and never rescales w[5]).
 __global__ void energy_epilogue_kernel(const double* __restrict__ scale,
                                        const double* __restrict__ inv_scale,
                                        double* __restrict__ chem, double* __restrict__ chemdot,
@@ -186,13 +192,13 @@ __global__ void energy_epilogue_kernel(const double* __restrict__ scale,
     chemdot[(long)nchem * i + nchem - 1] = etdot[i];
     etdot[i] = 0.0;
     double* c = chem + (long)nchem * i;
-    if (exact) {
+    if (exact == 1) {
       const double* s = scale + (long)nchem * i;
       for (int v = 0; v < nchem; ++v) c[v] /= s[v];
-    } else {
+    } else if (exact == 0) {
       const double* s = inv_scale + (long)nchem * i;
       for (int v = 0; v < nchem; ++v) c[v] *= s[v];
-    }
+    }  // exact == 2: the chemistry component was never rescaled
   }
 }
 

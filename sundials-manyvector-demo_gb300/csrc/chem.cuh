@@ -49,7 +49,7 @@ int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot,
 // fused source + Jacobian + Newton matrix + LU solve (chem_newton.cu)
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
-                cudaStream_t s);
+                cudaStream_t s, int blocks_per_sm = 0);
 
 // persistent per-cell DIRK integration from t0 to tout (chem_dirk.cu)
 struct DirkOpts {

@@ -139,9 +139,11 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
 
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
-                cudaStream_t s) {
+                cudaStream_t s, int blocks_per_sm) {
   long b = (n + kNtThreads - 1) / kNtThreads;
-  const long cap = (long)kSM * 24;
+  // default: a deep grid-stride grid; blocks_per_sm > 0: exactly that many resident blocks per
+  // SM (a persistent grid leaving room for a kernel running beside it on another stream)
+  const long cap = (long)kSM * (blocks_per_sm > 0 ? blocks_per_sm : 24);
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   ProfScope ps("chem_newton", s);

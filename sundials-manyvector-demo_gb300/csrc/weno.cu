@@ -224,7 +224,8 @@ int feuler_mixed(const Grid& g, const Fields& w, const Fields& wdot, const Force
 
 constexpr int kQ2Base = 10;  // index of the first tracer in Q2
 
-__global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2* __restrict__ Q2) {
+__global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2* __restrict__ Q2,
+                                                       const double* __restrict__ tscale) {
   const long n = g.ncell;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
        c += (long)gridDim.x * blockDim.x) {
@@ -238,7 +239,9 @@ __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2*
       Q2[k * n + c] = make_float2(v.hi, v.lo);
     }
     for (int v = 0; v < g.nchem; ++v) {
-      const f2 x = f2_from_double(w.f[5][v + (long)g.nchem * c]);
+      // tscale: the chemistry component arrives in scaled units (x = chem * scale)
+      const long e = v + (long)g.nchem * c;
+      const f2 x = f2_from_double(tscale ? w.f[5][e] * tscale[e] : w.f[5][e]);
       Q2[(kQ2Base + v) * n + c] = make_float2(x.hi, x.lo);
     }
   }
@@ -349,7 +352,8 @@ __global__ void __launch_bounds__(128) face_flux_f2_kernel(Grid g, Fields w,
 
 template <int NCHEM>
 static int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
-                     double* scratch, float2* q2, int* d_status, cudaStream_t s) {
+                     double* scratch, float2* q2, const double* tscale, int* d_status,
+                     cudaStream_t s) {
   const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
   const long nf[3] = {(nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1)};
   double* F[3] = {scratch, scratch + (long)(5 + NCHEM) * nf[0],
@@ -361,7 +365,7 @@ static int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const F
   };
   {
     ProfScope ps("prims", s);
-    prims_f2_kernel<<<blocks(g.ncell, 256), 256, 0, s>>>(g, w, q2);
+    prims_f2_kernel<<<blocks(g.ncell, 256), 256, 0, s>>>(g, w, q2, tscale);
     GBMV_LAUNCH_CHECK("prims_f2_kernel");
   }
   {
@@ -389,14 +393,15 @@ static int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const F
 size_t feuler_f2_prims_floats(const Grid& g) { return (size_t)2 * (kQ2Base + g.nchem) * g.ncell; }
 
 int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
-              double* scratch, float* prims, int* d_status, cudaStream_t s) {
+              double* scratch, float* prims, const double* tscale, int* d_status,
+              cudaStream_t s) {
   float2* q2 = reinterpret_cast<float2*>(prims);
   switch (g.nchem) {
-    case 0: return launch_f2<0>(g, w, wdot, G, scratch, q2, d_status, s);
-    case 2: return launch_f2<2>(g, w, wdot, G, scratch, q2, d_status, s);
-    case 4: return launch_f2<4>(g, w, wdot, G, scratch, q2, d_status, s);
-    case 6: return launch_f2<6>(g, w, wdot, G, scratch, q2, d_status, s);
-    case 10: return launch_f2<10>(g, w, wdot, G, scratch, q2, d_status, s);
+    case 0: return launch_f2<0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 2: return launch_f2<2>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 4: return launch_f2<4>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 6: return launch_f2<6>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 10: return launch_f2<10>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
     default: set_error("nchem=%d not compiled (0,2,4,6,10)", g.nchem); return GBMV_EUNSUPPORTED;
   }
 }

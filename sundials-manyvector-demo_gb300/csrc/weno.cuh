@@ -33,7 +33,9 @@ int feuler_vjp(const Grid& g, const Fields& w, const Fields& v, const Fields& ou
                cudaStream_t s);
 
 size_t feuler_f2_prims_floats(const Grid& g);
+// tscale: null, or the per-entry scale of a chemistry component held in scaled units
 int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
-              double* scratch, float* prims, int* d_status, cudaStream_t s);
+              double* scratch, float* prims, const double* tscale, int* d_status,
+              cudaStream_t s);
 
 }  // namespace gbmv

@@ -93,6 +93,7 @@ SIGNATURES = [
     ("gbmv_chem_dirk_evolve_async", C.c_int, [_VP, C.c_double, C.c_double, _VP, C.c_double,
                                               C.POINTER(_DirkOpts), _VP, _VP, _VP]),
     ("gbmv_chem_dirk_block", C.c_int, [_VP, C.c_int]),
+    ("gbmv_chem_set_newton_occupancy", C.c_int, [_VP, C.c_int]),
     ("gbmv_mri_fast_evolve", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.POINTER(_VP),
                                        C.c_double, C.c_int, C.POINTER(_VP), C.c_double,
                                        C.c_double, C.POINTER(_DirkOpts), _VP, _VP]),
@@ -309,6 +310,10 @@ class Chem:
             self.c, t0, tout, _dev_ptr(y), time_units, C.byref(o),
             stats.data_ptr() if stats is not None else None, nfail.data_ptr(),
             _stream_ptr(stream)), "gbmv_chem_dirk_evolve_async")
+
+    def set_newton_occupancy(self, blocks_per_sm: int):
+        """Resident blocks per SM of the fused Newton kernel (0 = default deep grid)."""
+        _check(load().gbmv_chem_set_newton_occupancy(self.c, blocks_per_sm), "set_newton_occupancy")
 
     def dirk_block(self, precision=FP64) -> int:
         """Block size the autotuner picked for a precision (0 = not tuned yet)."""
