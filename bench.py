@@ -129,11 +129,12 @@ class FusedStep:
                   FP64-residual refinement, no Jacobian in HBM), the whole stage captured as
                   one CUDA graph and replayed."""
 
-    def __init__(self, torch, n, form, wl=None):
+    def __init__(self, torch, n, form, wl=None, concurrent=False, newton_bps=2):
         import gbmv
         import h5tables
         import workloads as W
         self.torch, self.gbmv, self.form = torch, gbmv, form
+        self.concurrent = concurrent
         self.precision = gbmv.MIXED if form == "mixed" else gbmv.FP64
         wl = wl if wl is not None else W.chem_hydro(n=n)
         self.wl = wl
@@ -156,6 +157,9 @@ class FusedStep:
         self.graph = None
         torch.cuda.synchronize()
         if form == "mixed":  # the whole stage as one CUDA graph (asynchronous entry points)
+            self.chem_stream = torch.cuda.Stream()
+            if concurrent:  # persistent Newton grid leaving room for the WENO sweep beside it
+                self.chem.set_newton_occupancy(newton_bps)
             self._stage_async()
             torch.cuda.synchronize()
             self.check_status()
@@ -167,13 +171,29 @@ class FusedStep:
             torch.cuda.synchronize()
 
     def _stage_async(self, t=0.0):
-        g = self.gbmv
+        g, torch = self.gbmv, self.torch
         EU, TU = self.units["EnergyUnits"], self.units["TimeUnits"]
         self.status.zero_()
+        if not self.concurrent:
+            g.fexpl_async(self.hydro, self.chem, t, self.w, self.wdot, EU, self.status[0:1],
+                          self.precision)
+            g.chem_newton_async(self.chem, t, self.w[5].view(-1), self.f, self.x, GAMMA_NEWTON,
+                                TU, self.status[1:2], lu_precision=g.MIXED, refine=4)
+            return
+        # two independent branches of the stage: the chemistry (FP64 pipe) beside the WENO
+        # sweep (FP32 pipes); the mixed fexpl never writes w[5], so both may read it
+        main = torch.cuda.current_stream()
+        fork = torch.cuda.Event()
+        fork.record(main)
+        self.chem_stream.wait_event(fork)
+        g.chem_newton_async(self.chem, t, self.w[5].view(-1), self.f, self.x, GAMMA_NEWTON, TU,
+                            self.status[1:2], lu_precision=g.MIXED, refine=4,
+                            stream=self.chem_stream)
         g.fexpl_async(self.hydro, self.chem, t, self.w, self.wdot, EU, self.status[0:1],
                       self.precision)
-        g.chem_newton_async(self.chem, t, self.w[5].view(-1), self.f, self.x, GAMMA_NEWTON, TU,
-                            self.status[1:2], lu_precision=g.MIXED, refine=4)
+        join = torch.cuda.Event()
+        join.record(self.chem_stream)
+        main.wait_event(join)
 
     def check_status(self):
         st = self.status.cpu().tolist()
@@ -317,10 +337,15 @@ def run_gbmv(args):
     gbmv.load()
     torch.cuda.set_device(0)
     wl = W.chem_hydro(n=args.n)
-    forms = ["fp64", "mixed"] if args.form == "best" else [args.form]
+    forms = ["fp64", "mixed", "mixed_concurrent"] if args.form == "best" else [args.form]
+
+    def make_fs(form):
+        return FusedStep(torch, args.n, "mixed" if form.startswith("mixed") else form, wl,
+                         concurrent=(form == "mixed_concurrent"))
+
     res = {}
     for form in forms:
-        fs = FusedStep(torch, args.n, form, wl)
+        fs = make_fs(form)
         ms, fam, launches, clk = timed_form(torch, gbmv, fs, args.steps, args.warmup)
         fam_steps = args.steps
         if fs.graph is not None:  # graph replays bypass the per-call timing events: time eagerly
@@ -342,10 +367,9 @@ def run_gbmv(args):
             res[form]["fs"] = None
             torch.cuda.empty_cache()
     ncell = args.n ** 3
-    errs = None
-    if "fp64" in res and "mixed" in res:
+    def form_errs(form):
         names = ["rho", "mx", "my", "mz", "et", "chem", "fimpl", "newton_x"]
-        ref, mx = res["fp64"]["out"], res["mixed"]["out"]
+        ref, mx = res["fp64"]["out"], res[form]["out"]
         errs = {}
         for nm, a, b in zip(names, mx, ref):
             if nm in ("chem", "fimpl", "newton_x"):
@@ -355,7 +379,12 @@ def run_gbmv(args):
             else:
                 e = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
             errs[nm] = e
-    head = "mixed" if ("mixed" in res and (errs is None or max(errs.values()) <= 1e-6)) else forms[0]
+        return errs
+
+    all_errs = {f: form_errs(f) for f in res if f.startswith("mixed")} if "fp64" in res else {}
+    ok = [f for f, e in all_errs.items() if max(e.values()) <= 1e-6]
+    head = min(ok, key=lambda f: res[f]["ms"]) if ok else forms[0]
+    errs = all_errs.get(head) if head != "fp64" else None
     R = res[head]
     ms, fam = R["ms"], R["fam"]
     value = ncell / (ms * 1e-3) / 1e6
@@ -364,18 +393,19 @@ def run_gbmv(args):
     fp64_peak = gbmv.fma_rate(True) / 1e12
     dt_ms, nl = fam[dom]
     avg_ms = dt_ms / max(nl, 1)
-    key = "face_flux_mx" if (dom == "face_flux" and head == "mixed") else dom
+    hform = "mixed" if head.startswith("mixed") else head
+    key = "face_flux_mx" if (dom == "face_flux" and hform == "mixed") else dom
     achieved = algo_bytes(key, args.n) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     traffic, traffic_note = None, None
-    if (head, dom) in DRAM_TRAFFIC:
-        per, unit = DRAM_TRAFFIC[(head, dom)]
+    if (hform, dom) in DRAM_TRAFFIC:
+        per, unit = DRAM_TRAFFIC[(hform, dom)]
         units = (args.n + 1) * args.n * args.n if unit == "face" else ncell
         traffic = round(per * units, 0)
         traffic_note = (f"bytes per launch: {per} B/{unit} (ncu dram__bytes_read+write, 112^3 "
                         f"capture, state > L2) x {units} {unit}s")
     pipe = None
-    if (head, dom) in FP_COUNTS:
-        pname, per_unit, unit = FP_COUNTS[(head, dom)]
+    if (hform, dom) in FP_COUNTS:
+        pname, per_unit, unit = FP_COUNTS[(hform, dom)]
         units = (args.n + 1) * args.n * args.n if unit == "face" else ncell
         peak_pipe = gbmv.fma_rate(pname == "fp64") / 1e12
         ach = per_unit * units / (avg_ms * 1e-3) / 1e12
@@ -410,10 +440,12 @@ def run_gbmv(args):
     }
     if errs is not None:
         line["mixed_vs_fp64_maxnorm_err"] = {k: float(f"{v:.3e}") for k, v in errs.items()}
-        line["speedup_vs_fp64_form"] = round(res["fp64"]["ms"] / res["mixed"]["ms"], 3)
+        line["speedup_vs_fp64_form"] = round(res["fp64"]["ms"] / res[head]["ms"], 3)
+        line["forms_maxnorm_err_vs_fp64"] = {f: float(f"{max(e.values()):.3e}")
+                                             for f, e in all_errs.items()}
 
     if not args.no_e2e:
-        fs = R["fs"] if R["fs"] is not None else FusedStep(torch, args.n, head, wl)
+        fs = R["fs"] if R["fs"] is not None else make_fs(head)
         pin_in = [torch.from_numpy(a).pin_memory() for a in fs.host]
         pin_out = [torch.empty(t.shape, dtype=torch.float64).pin_memory() for t in fs.wdot]
         pin_x = torch.empty(fs.x.shape, dtype=torch.float64).pin_memory()

@@ -55,3 +55,56 @@ def test_stage_graph_replay_matches_eager(cuda, tables):
     for a, b in zip(A[2] + A[3] + [A[4], A[5]], B[2] + B[3] + [B[4], B[5]]):
         assert torch.equal(a, b)
     assert torch.equal(A[1].state("Ts"), B[1].state("Ts"))
+
+
+def test_concurrent_branch_graph_matches_serial_eager(cuda, tables):
+    """The stage as two graph branches -- chemistry Newton on its own stream with a persistent
+    two-blocks-per-SM grid, WENO sweep on the capture stream -- gives the serial eager bits:
+    the mixed fexpl never writes w[5], so the branches share no written data."""
+    torch = cuda
+    import gbmv
+    wl = W.chem_hydro(shape=(24, 20, 16))
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    A = _make(torch, gbmv, wl, tables)
+    B = _make(torch, gbmv, wl, tables)
+    B[1].set_newton_occupancy(2)
+    status = torch.zeros(2, dtype=torch.int32, device="cuda")
+    chem_stream = torch.cuda.Stream()
+
+    def serial(h, c, w, wdot, f, x):
+        status.zero_()
+        gbmv.fexpl_async(h, c, 0.0, w, wdot, eu, status[0:1], gbmv.MIXED)
+        gbmv.chem_newton_async(c, 0.0, w[5].view(-1), f, x, 1e-4, tu, status[1:2],
+                               lu_precision=gbmv.MIXED, refine=4)
+
+    def branches(h, c, w, wdot, f, x):
+        status.zero_()
+        main = torch.cuda.current_stream()
+        fork = torch.cuda.Event()
+        fork.record(main)
+        chem_stream.wait_event(fork)
+        gbmv.chem_newton_async(c, 0.0, w[5].view(-1), f, x, 1e-4, tu, status[1:2],
+                               lu_precision=gbmv.MIXED, refine=4, stream=chem_stream)
+        gbmv.fexpl_async(h, c, 0.0, w, wdot, eu, status[0:1], gbmv.MIXED)
+        join = torch.cuda.Event()
+        join.record(chem_stream)
+        main.wait_event(join)
+
+    for _ in range(3):
+        serial(*A)
+    serial(*B)  # allocations outside the capture
+    torch.cuda.synchronize()
+    w5 = B[2][5].clone()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        branches(*B)
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert int(status.sum()) == 0
+    assert torch.equal(B[2][5], w5)  # the chemistry component was never rewritten
+    for a, b in zip(A[2] + A[3] + [A[4], A[5]], B[2] + B[3] + [B[4], B[5]]):
+        assert torch.equal(a, b)
+    assert torch.equal(A[1].state("Ts"), B[1].state("Ts"))
