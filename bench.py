@@ -56,6 +56,8 @@ def parse():
                    help="static-chemistry DIRK measurement on dirk_n^3 cells (0 = skip)")
     p.add_argument("--weno-n", default="128,256",
                    help="Rayleigh-Taylor WENO RHS throughput grids (comma list, '' = skip)")
+    p.add_argument("--ad-n", type=int, default=96,
+                   help="differentiation measurement on ad_n^3 x 9 fields (0 = skip)")
     p.add_argument("--dirk-only", action="store_true",
                    help="run only the DIRK measurement (prints its object)")
     p.add_argument("--dirk-form", default="both", choices=["both", "fp64", "mixed"])
@@ -470,6 +472,12 @@ def run_gbmv(args):
         fs = None
         torch.cuda.empty_cache()
         line["weno_rhs"] = run_weno(torch, gbmv, [int(x) for x in args.weno_n.split(",") if x])
+    if args.ad_n > 0:
+        for r in res.values():
+            r["fs"] = None
+        fs = None
+        torch.cuda.empty_cache()
+        line["differentiation"] = run_ad(torch, gbmv, args.ad_n)
     if args.dirk_n > 0:
         for k in ("fs",):
             for r in res.values():
@@ -522,6 +530,83 @@ def run_weno(torch, gbmv, grids, steps=3, warmup=2):
         del h, w, wdot
         torch.cuda.empty_cache()
     return out
+
+
+# ----------------------------------------------------------------- differentiation
+
+def run_ad(torch, gbmv, n, ndir=16, h=1e-7, nsteps=50, every=10):
+    """Smooth periodic flow (rho = 1 + 0.2 sin(2 pi (x+y+z)), p = 1, velocities U[-0.1, 0.1],
+    4 tracers) on n^3 x 9 fields: times of the FP64 RHS, its JVP and VJP; their agreement with
+    central differences (h = 1e-7) on `ndir` seeded directions; the gradient of the integral of
+    rho^2 after `nsteps` RK4 steps with checkpoints every `every` steps (autograd wrapper of
+    tests/ad_harness.py over the C ABI) against a central difference of the loss."""
+    import workloads as W
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import ad_harness as AD
+    wl = W.smooth_periodic(n=n, nchem=4)
+    hy = gbmv.Hydro((n, n, n), 4, wl["bc"], wl["gamma"])
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    del wl
+    out = [torch.empty_like(x) for x in w]
+    rng = np.random.default_rng(20261203 + 5)
+
+    def dirs():
+        return [torch.from_numpy(rng.standard_normal(tuple(x.shape))).cuda() *
+                float(x.abs().max()) for x in w]
+
+    def rhs(ws, o):
+        if hy.fEuler(0.0, ws, o, 0) != 0:
+            raise RuntimeError("fEuler failed")
+
+    d0 = dirs()
+    t_rhs = time_steps(torch, lambda: rhs(w, out), 3, 2)
+    t_jvp = time_steps(torch, lambda: hy.fEuler_jvp(0.0, w, d0, out), 3, 2)
+    t_vjp = time_steps(torch, lambda: hy.fEuler_vjp(0.0, w, d0, out), 3, 2)
+    dot = lambda a, b: sum(float((x * y).sum()) for x, y in zip(a, b))
+    jerr, verr = 0.0, 0.0
+    fp = [torch.empty_like(x) for x in w]
+    fm = [torch.empty_like(x) for x in w]
+    jv = [torch.empty_like(x) for x in w]
+    u = [torch.empty_like(x) for x in w]
+    for _ in range(ndir):
+        d = dirs()
+        hy.fEuler_jvp(0.0, w, d, jv)
+        rhs([a + h * b for a, b in zip(w, d)], fp)
+        rhs([a - h * b for a, b in zip(w, d)], fm)
+        for a, b, c in zip(jv, fp, fm):
+            fd = (b - c) / (2 * h)
+            jerr = max(jerr, float((a - fd).abs().max()) / max(float(fd.abs().max()), 1e-300))
+        v = dirs()
+        hy.fEuler_vjp(0.0, w, v, u)
+        lhs, r = dot(u, d), (dot(v, fp) - dot(v, fm)) / (2 * h)
+        verr = max(verr, abs(lhs - r) / max(abs(r), 1e-300))
+    dx = 1.0 / n
+    dt, vol = 0.2 * dx / 1.4, dx ** 3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    L, g = AD.loss_and_grad(hy, w, dt, nsteps, vol, checkpoint_every=every)
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    AD.loss_only(hy, w, dt, nsteps, vol)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    gerr = 0.0
+    for _ in range(2):
+        d = dirs()
+        ad = dot(g, d)
+        fd = (AD.loss_only(hy, [a + h * b for a, b in zip(w, d)], dt, nsteps, vol) -
+              AD.loss_only(hy, [a - h * b for a, b in zip(w, d)], dt, nsteps, vol)) / (2 * h)
+        gerr = max(gerr, abs(ad - fd) / abs(fd))
+    return {"workload": f"smooth periodic flow {n}^3 x 9 (rho = 1 + 0.2 sin(2 pi (x+y+z)), p = 1, "
+                        "velocities U[-0.1, 0.1], 4 tracers U[0,1] rho)",
+            "ms_rhs": round(t_rhs, 3), "ms_jvp": round(t_jvp, 3), "ms_vjp": round(t_vjp, 3),
+            "jvp_vs_central_diff_maxnorm_err": float(f"{jerr:.3e}"),
+            "vjp_vs_central_diff_rel_err": float(f"{verr:.3e}"), "directions": ndir, "h": h,
+            "gradient": {"loss": "integral of rho^2 at t_f", "rk4_steps": nsteps,
+                         "checkpoint_every": every, "s_forward_only": round(t_fwd, 3),
+                         "s_forward_and_gradient": round(t_grad, 3),
+                         "vs_central_diff_rel_err": float(f"{gerr:.3e}")}}
 
 
 # ----------------------------------------------------------------- static chemistry (DIRK)

@@ -120,6 +120,87 @@ struct DirkLayout {
   static constexpr size_t bytes = per_lane * BS;
 };
 
+// Newton-matrix setup of one cell: J at (Y, Ts(Y)) from rates with slopes, A = I - gam J,
+// for FP32 factors power-of-two equilibrated, factored with partial pivoting; returns the LU
+// info (0 or 1 + first zero pivot).
+template <typename LU, bool REF, int BS>
+__device__ __noinline__ int dirk_setup(const ChemParams& P, const ChemState& S, long i,
+                                       const DirkOpts& O, const double* Y, double* A, LU* L,
+                                       short* EQ, double gam, double Tsy, double dTsy,
+                                       int (&piv)[10]) {
+  const long j = i * 10;
+  double ya[10];
+#pragma unroll
+  for (int s = 0; s < 10; ++s) ya[s] = Y[s * BS] * S.scale[j + s];
+  double k[kNRates], dk[kNRates];
+  chem_rates<true>(P, Tsy, k, dk);
+  const ChemAux Ax{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
+  const double* __restrict__ sc = S.scale + j;
+  const double* __restrict__ isc = S.inv_scale + j;
+  const double mg = -gam * O.tunit;
+#pragma unroll
+  for (int e = 0; e < 100; ++e) L[e * BS] = LU(0);  // off-pattern entries
+  // A = I - gamma * tunit * (isc_r J_rc sc_c): every structural entry is put once
+  auto entry = [&](int row, int col, double v) {
+    return (row == col ? 1.0 : 0.0) + mg * ((v * isc[row]) * sc[col]);
+  };
+  if (sizeof(LU) == 8) {
+    chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+      L[(col * 10 + row) * BS] = (LU)entry(row, col, v);
+    });
+  } else {
+    // FP32 factor of R A C with power-of-two row scales R (row maxima to [0.5, 1)) and
+    // column scales C (then column maxima to [0.5, 1)), from the FP64 entries
+    double rmax[10], cmax[10];
+    int er[10], ec[10];
+#pragma unroll
+    for (int s = 0; s < 10; ++s) rmax[s] = cmax[s] = 0.0;
+    if (REF) {
+      chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+        const double a = entry(row, col, v);
+        A[(col * 10 + row) * BS] = a;
+        rmax[row] = fmax(rmax[row], fabs(a));
+      });
+    } else {
+      chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+        rmax[row] = fmax(rmax[row], fabs(entry(row, col, v)));
+      });
+    }
+#pragma unroll
+    for (int s = 0; s < 10; ++s) er[s] = eq_exponent(rmax[s]);
+    if (REF) {
+#pragma unroll
+      for (int e = 0; e < 64; ++e) {
+        const int row = kJacPattern[e][0], col = kJacPattern[e][1];
+        cmax[col] = fmax(cmax[col], fabs(A[(col * 10 + row) * BS] * pow2(er[row])));
+      }
+    } else {
+      chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+        cmax[col] = fmax(cmax[col], fabs(entry(row, col, v) * pow2(er[row])));
+      });
+    }
+#pragma unroll
+    for (int s = 0; s < 10; ++s) {
+      ec[s] = eq_exponent(cmax[s]);
+      EQ[s * BS] = (short)er[s];
+      EQ[(10 + s) * BS] = (short)ec[s];
+    }
+    if (REF) {
+#pragma unroll
+      for (int e = 0; e < 64; ++e) {
+        const int row = kJacPattern[e][0], col = kJacPattern[e][1];
+        L[(col * 10 + row) * BS] =
+            (LU)(A[(col * 10 + row) * BS] * pow2(er[row] + ec[col]));
+      }
+    } else {
+      chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+        L[(col * 10 + row) * BS] = (LU)(entry(row, col, v) * pow2(er[row] + ec[col]));
+      });
+    }
+  }
+  return lu10_strided<LU>(L, BS, piv);
+}
+
 template <typename LU, bool REF, int BS>
 __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S, long n,
                                                        double* __restrict__ y_io, DirkOpts O,
@@ -362,79 +443,10 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       }
       const double gam = h * kGd;
       if (force_setup || nst >= nst_lp + O.msbp || !(fabs(gam / gp - 1.0) <= O.dgmax)) {
-        // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored
-        const long j = i * 10;
-        double ya[10];
-#pragma unroll
-        for (int s = 0; s < 10; ++s) ya[s] = Y[s * BS] * S.scale[j + s];
-        double k[kNRates], dk[kNRates];
-        chem_rates<true>(P, Tsy, k, dk);
-        const ChemAux Ax{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
-        const double* __restrict__ sc = S.scale + j;
-        const double* __restrict__ isc = S.inv_scale + j;
-        const double mg = -gam * O.tunit;
-#pragma unroll
-        for (int e = 0; e < 100; ++e) L[e * BS] = LU(0);  // off-pattern entries
-        // A = I - gamma * tunit * (isc_r J_rc sc_c): every structural entry is put once
-        auto entry = [&](int row, int col, double v) {
-          return (row == col ? 1.0 : 0.0) + mg * ((v * isc[row]) * sc[col]);
-        };
-        if (sizeof(LU) == 8) {
-          chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-            L[(col * 10 + row) * BS] = (LU)entry(row, col, v);
-          });
-        } else {
-          // FP32 factor of R A C with power-of-two row scales R (row maxima to [0.5, 1)) and
-          // column scales C (then column maxima to [0.5, 1)), from the FP64 entries
-          double rmax[10], cmax[10];
-          int er[10], ec[10];
-#pragma unroll
-          for (int s = 0; s < 10; ++s) rmax[s] = cmax[s] = 0.0;
-          if (REF) {
-            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-              const double a = entry(row, col, v);
-              A[(col * 10 + row) * BS] = a;
-              rmax[row] = fmax(rmax[row], fabs(a));
-            });
-          } else {
-            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-              rmax[row] = fmax(rmax[row], fabs(entry(row, col, v)));
-            });
-          }
-#pragma unroll
-          for (int s = 0; s < 10; ++s) er[s] = eq_exponent(rmax[s]);
-          if (REF) {
-#pragma unroll
-            for (int e = 0; e < 64; ++e) {
-              const int row = kJacPattern[e][0], col = kJacPattern[e][1];
-              cmax[col] = fmax(cmax[col], fabs(A[(col * 10 + row) * BS] * pow2(er[row])));
-            }
-          } else {
-            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-              cmax[col] = fmax(cmax[col], fabs(entry(row, col, v) * pow2(er[row])));
-            });
-          }
-#pragma unroll
-          for (int s = 0; s < 10; ++s) {
-            ec[s] = eq_exponent(cmax[s]);
-            EQ[s * BS] = (short)er[s];
-            EQ[(10 + s) * BS] = (short)ec[s];
-          }
-          if (REF) {
-#pragma unroll
-            for (int e = 0; e < 64; ++e) {
-              const int row = kJacPattern[e][0], col = kJacPattern[e][1];
-              L[(col * 10 + row) * BS] =
-                  (LU)(A[(col * 10 + row) * BS] * pow2(er[row] + ec[col]));
-            }
-          } else {
-            chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-              L[(col * 10 + row) * BS] = (LU)(entry(row, col, v) * pow2(er[row] + ec[col]));
-            });
-          }
-        }
+        // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored (out of line:
+        // once per several passes, kept out of the hot loop's instruction footprint)
         int piv[10];
-        const int info = lu10_strided<LU>(L, BS, piv);
+        const int info = dirk_setup<LU, REF, BS>(P, S, i, O, Y, A, L, EQ, gam, Tsy, dTsy, piv);
 #pragma unroll
         for (int s = 0; s < 10; ++s) PV[s * BS] = (signed char)piv[s];
         gp = gam;
