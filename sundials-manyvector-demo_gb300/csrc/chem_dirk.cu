@@ -124,7 +124,7 @@ struct DirkLayout {
 // for FP32 factors power-of-two equilibrated, factored with partial pivoting; returns the LU
 // info (0 or 1 + first zero pivot).
 template <typename LU, bool REF, int BS>
-__device__ __noinline__ int dirk_setup(const ChemParams& P, const ChemState& S, long i,
+__device__ __forceinline__ int dirk_setup(const ChemParams& P, const ChemState& S, long i,
                                        const DirkOpts& O, const double* Y, double* A, LU* L,
                                        short* EQ, double gam, double Tsy, double dTsy,
                                        int (&piv)[10]) {
@@ -443,8 +443,8 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       }
       const double gam = h * kGd;
       if (force_setup || nst >= nst_lp + O.msbp || !(fabs(gam / gp - 1.0) <= O.dgmax)) {
-        // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored (out of line:
-        // once per several passes, kept out of the hot loop's instruction footprint)
+        // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored (inline: an
+        // out-of-line call measured 4 % slower in the mixed form)
         int piv[10];
         const int info = dirk_setup<LU, REF, BS>(P, S, i, O, Y, A, L, EQ, gam, Tsy, dTsy, piv);
 #pragma unroll
