@@ -126,6 +126,14 @@ int gbmv_feuler_jvp(gbmv_hydro h, double t, const double* const* w, const double
 int gbmv_feuler_vjp(gbmv_hydro h, double t, const double* const* w, const double* const* v,
                     double* const* u, void* stream);
 
+/* check_conservation (src/io.cpp:503-542): totals[0] = mass_factor * sum(rho),
+ * totals[1] = energy_factor * sum(et) over all cells, with the reference's factors
+ * mass_factor = dx dy dz LengthUnits^3 DensityUnits, energy_factor = dx dy dz LengthUnits^3
+ * EnergyUnits (pass 1, 1 for the raw sums).  FP64, compensated and deterministic (fixed
+ * reduction order, no atomics).  totals is host memory; synchronous. */
+int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
+                      double energy_factor, double* totals, void* stream);
+
 /* -------------------------------------------------------------- chemistry (part b) */
 
 typedef struct gbmv_chem_s* gbmv_chem;

@@ -74,6 +74,7 @@ struct gbmv_hydro_s {
   size_t scratch_doubles = 0;
   float* prims = nullptr;  // float-float per-cell primitives of the mixed form (first use)
   double* adj = nullptr;   // per-face stencil cotangents of the VJP (first use)
+  double* cons = nullptr;  // conservation-sum partials (first use)
   int* d_status = nullptr;
 };
 
@@ -189,6 +190,7 @@ int gbmv_hydro_destroy(gbmv_hydro h) {
   cudaFree(h->scratch);
   cudaFree(h->prims);
   cudaFree(h->adj);
+  cudaFree(h->cons);
   cudaFree(h->d_status);
   delete h;
   return GBMV_OK;
@@ -199,6 +201,8 @@ int gbmv_hydro_set_force(gbmv_hydro h, const double* force) {
   for (int v = 0; v < 16; ++v) h->force.c[v] = (force && v < 5 + h->g.nchem) ? force[v] : 0.0;
   return GBMV_OK;
 }
+
+static bool capturing(cudaStream_t s);
 
 // fEuler dispatch; tscale (mixed form only): the chemistry component is in scaled units and
 // is multiplied by tscale where the WENO reads it.
@@ -852,6 +856,38 @@ int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double en
                           void* stream) {
   if (!h || !c || h->g.nchem != 10 || !fields_ok(w, 10)) return GBMV_EINVAL;
   return energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, 1, (cudaStream_t)stream);
+}
+
+int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
+                      double energy_factor, double* totals, void* stream) {
+  if (!h || !fields_ok(w, 0) || !totals) {
+    set_error("null handle, field or output pointer");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->cons) {
+    if (capturing(s)) {
+      set_error("the first gbmv_conservation call on a handle allocates its buffer: make it "
+                "before any stream capture");
+      return GBMV_EINVAL;
+    }
+    if (cudaMalloc(&h->cons, conservation_scratch_doubles() * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      h->cons = nullptr;
+      return check_cuda(cudaErrorMemoryAllocation, "conservation scratch");
+    }
+  }
+  Fields W;
+  for (int v = 0; v < 6; ++v) W.f[v] = (v < 5) ? const_cast<double*>(w[v]) : nullptr;
+  int rc = conservation_sums(h->g, W, h->cons, s);
+  if (rc) return rc;
+  double t[2];
+  GBMV_CUDA_TRY(cudaMemcpyAsync(t, h->cons + conservation_scratch_doubles() - 2, sizeof t,
+                                cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  totals[0] = t[0] * mass_factor;
+  totals[1] = t[1] * energy_factor;
+  return GBMV_OK;
 }
 
 int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,

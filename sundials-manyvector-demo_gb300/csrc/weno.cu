@@ -434,6 +434,72 @@ __global__ void __launch_bounds__(256) wave_speed_max_kernel(Grid g, Fields w,
   if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
 
+// check_conservation (src/io.cpp:503-542): grid totals of rho and et.  Deterministic two-pass
+// reduction (fixed grid, per-block partial sums, then one block in a fixed order), FP64 with a
+// compensated (two-sum) accumulation per thread.
+constexpr int kConsBlocks = 1024;
+
+__device__ __forceinline__ void two_sum_acc(double& s, double& c, double x) {
+  const double t = s + x;
+  const double bp = t - s;
+  c += (s - (t - bp)) + (x - bp);
+  s = t;
+}
+
+__global__ void __launch_bounds__(256) conservation_partial_kernel(long n, const double* rho,
+                                                                   const double* et,
+                                                                   double* __restrict__ part) {
+  double s0 = 0.0, c0 = 0.0, s1 = 0.0, c1 = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    two_sum_acc(s0, c0, rho[i]);
+    two_sum_acc(s1, c1, et[i]);
+  }
+  double a = s0 + c0, b = s1 + c1;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, off);
+    b += __shfl_down_sync(0xffffffffu, b, off);
+  }
+  __shared__ double wa[8], wb[8];
+  if ((threadIdx.x & 31) == 0) {
+    wa[threadIdx.x >> 5] = a;
+    wb[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      ta += wa[k];
+      tb += wb[k];
+    }
+    part[blockIdx.x] = ta;
+    part[kConsBlocks + blockIdx.x] = tb;
+  }
+}
+
+__global__ void conservation_final_kernel(const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, c0 = 0.0, s1 = 0.0, c1 = 0.0;
+    for (int k = 0; k < kConsBlocks; ++k) {
+      two_sum_acc(s0, c0, part[k]);
+      two_sum_acc(s1, c1, part[kConsBlocks + k]);
+    }
+    out[0] = s0 + c0;
+    out[1] = s1 + c1;
+  }
+}
+
+int conservation_sums(const Grid& g, const Fields& w, double* d_scratch, cudaStream_t s) {
+  conservation_partial_kernel<<<kConsBlocks, 256, 0, s>>>(g.ncell, w.f[0], w.f[4], d_scratch);
+  GBMV_LAUNCH_CHECK("conservation_partial_kernel");
+  conservation_final_kernel<<<1, 32, 0, s>>>(d_scratch, d_scratch + 2 * kConsBlocks);
+  GBMV_LAUNCH_CHECK("conservation_final_kernel");
+  return GBMV_OK;
+}
+
+size_t conservation_scratch_doubles() { return 2 * kConsBlocks + 2; }
+
 int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s) {
   long b = (g.ncell + 255) / 256;
   if (b > (long)kSM * 8) b = (long)kSM * 8;

@@ -61,6 +61,7 @@ SIGNATURES = [
     ("gbmv_feuler_noalloc", C.c_int, [C.POINTER(_Grid), _P, C.c_double, C.POINTER(_VP),
                                       C.POINTER(_VP), _VP]),
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
+    ("gbmv_conservation", C.c_int, [_VP, C.POINTER(_VP), C.c_double, C.c_double, _P, _VP]),
     ("gbmv_feuler_jvp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
                                   C.POINTER(_VP), _VP]),
     ("gbmv_feuler_vjp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
@@ -206,6 +207,13 @@ class Hydro:
         return _check(load().gbmv_feuler_async(self.h, t, _vec(w), _vec(wdot), precision, flags,
                                                status.data_ptr(), _stream_ptr(stream)),
                       "gbmv_feuler_async")
+
+    def check_conservation(self, w, mass_factor=1.0, energy_factor=1.0, stream=None):
+        """(total mass, total energy) as check_conservation (src/io.cpp:503) sums them."""
+        out = (C.c_double * 2)()
+        _check(load().gbmv_conservation(self.h, _vec(w), mass_factor, energy_factor, out,
+                                        _stream_ptr(stream)), "gbmv_conservation")
+        return out[0], out[1]
 
     def fEuler_jvp(self, t, w, dw, jv, stream=None) -> int:
         """jv = (d fEuler / d w) dw (FP64 form, forward mode)."""
