@@ -1,0 +1,96 @@
+"""Multirate chemistry-hydrodynamics integration on the GPU (integrate.mri_erk22b_evolve: the
+slow WENO stage through gbmv_fexpl, the fast stages through gbmv_mri_fast_evolve) against the
+same scheme driven by the oracle (fexpl composition of the oracle's fEuler and scaling glue,
+the oracle's forced per-cell DIRK, the exact fluid forcing integral)."""
+import numpy as np
+import pytest
+
+import oracle_py as O
+import workloads as W
+from conftest import maxnorm_err
+
+pytestmark = pytest.mark.gpu
+FAST = dict(rtol=1e-8, atol=1e-12, maxcor=10, nlscoef=0.01)
+
+
+def _oracle_fexpl(wl_state, wl, eu):
+    f = [x.copy() for x in wl_state]
+    scale = wl["scale"]
+    phys = f[5] * scale
+    f[4] = phys[..., 9] * (1.0 / eu) + 0.5 / f[0] * (f[1] * f[1] + f[2] * f[2] + f[3] * f[3])
+    st, out = O.feuler(f[:5] + [phys], 10, wl["bc"], wl["gamma"], None)
+    assert st == 0
+    out[5][..., 9] = out[4]
+    out[4][:] = 0.0
+    f[5] = phys / scale
+    # slow chemistry forcing in the scaled fast variables (integrate.scaled_forcing)
+    out[5][..., :9] = out[5][..., :9] * (1.0 / scale[..., :9])
+    out[5][..., 9] = out[5][..., 9] * ((1.0 / scale[..., 9]) * eu)
+    return out, f
+
+
+def _oracle_mri(wl, tables, t0, h, nsteps, eu, tu):
+    y = [x.copy() for x in wl["fields"]]
+    oc = O.Chem(tables, wl["scale"].reshape(-1))
+    n = y[0].size
+
+    def fast(y, ta, tb, g):
+        for k in range(5):  # constant forcing: exact integral
+            y[k] = y[k] + (tb - ta) * g[k]
+        z, _, nf = oc.dirk_evolve(y[5].reshape(-1), ta, tb, tu, forcing=[g[5].reshape(-1)],
+                                  tshift=ta, tscale=1.0, **FAST)
+        assert nf == 0
+        y[5] = z.reshape(y[5].shape)
+        return y
+
+    for s in range(nsteps):
+        ta, tm, tb = t0 + s * h, t0 + (s + 0.5) * h, t0 + (s + 1) * h
+        g1, y = _oracle_fexpl(y, wl, eu)
+        y = fast(y, ta, tm, g1)
+        g2, y = _oracle_fexpl(y, wl, eu)
+        g2 = [2.0 * a - b for a, b in zip(g2, g1)]
+        y = fast(y, tm, tb, g2)
+    return y, n
+
+
+def _gpu_mri(torch, wl, tables, t0, h, nsteps, eu, tu, precision):
+    import gbmv
+    import integrate
+    nz, ny, nx = wl["fields"][0].shape
+    hy = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"])
+    c = gbmv.Chem(nx * ny * nz, tables)
+    c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    r = integrate.mri_erk22b_evolve(gbmv, hy, c, w, t0, t0 + nsteps * h, h, eu, tu,
+                                    precision=precision, block=64, **FAST)
+    torch.cuda.synchronize()
+    assert r.fast_failed_cells == 0 and r.slow_steps == nsteps
+    return [x.cpu().numpy() for x in w]
+
+
+def test_mri_fp64_matches_oracle_driven_scheme(cuda, tables):
+    wl = W.chem_hydro(shape=(8, 6, 5))
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    t0, h, ns = 0.0, 2e-6, 2
+    ref, n = _oracle_mri(wl, tables, t0, h, ns, eu, tu)
+    got = _gpu_mri(cuda, wl, tables, t0, h, ns, eu, tu, 0)
+    for k in range(5):
+        assert maxnorm_err(got[k], ref[k]) <= 1e-10, k
+    a, b = got[5].reshape(n, 10), ref[5].reshape(n, 10)
+    for s in range(10):
+        assert maxnorm_err(a[:, s], b[:, s]) <= 1e-6, s
+    # the run moved every field (slow and fast parts both active)
+    for k in range(6):
+        assert not np.array_equal(got[k], wl["fields"][k]) or k == 4
+
+
+def test_mri_mixed_matches_fp64(cuda, tables):
+    wl = W.chem_hydro(shape=(12, 10, 8))
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    a = _gpu_mri(cuda, wl, tables, 0.0, 2e-6, 3, eu, tu, 0)
+    b = _gpu_mri(cuda, wl, tables, 0.0, 2e-6, 3, eu, tu, 1)
+    for k in range(5):
+        assert maxnorm_err(b[k], a[k]) <= 1e-6, k
+    n = a[5].size // 10
+    for s in range(10):
+        assert maxnorm_err(b[5].reshape(n, 10)[:, s], a[5].reshape(n, 10)[:, s]) <= 1e-6, s
