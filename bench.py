@@ -58,6 +58,7 @@ def parse():
                    help="Rayleigh-Taylor WENO RHS throughput grids (comma list, '' = skip)")
     p.add_argument("--concurrent", action="store_true",
                    help="also time the mixed stage as two concurrent graph branches")
+    p.add_argument("--no-sod", action="store_true", help="skip the Sod whole-run measurement")
     p.add_argument("--mri-n", type=int, default=64,
                    help="multirate time-to-t_f measurement on mri_n^3 x 15 (0 = skip)")
     p.add_argument("--ad-n", type=int, default=96,
@@ -534,6 +535,8 @@ def run_gbmv(args):
         fs = None
         torch.cuda.empty_cache()
         line["weno_rhs"] = run_weno(torch, gbmv, [int(x) for x in args.weno_n.split(",") if x])
+    if not args.no_sod:
+        line["sod"] = run_sod(torch, gbmv, not args.no_cpu_baseline)
     if args.mri_n > 0:
         for r in res.values():
             r["fs"] = None
@@ -597,6 +600,61 @@ def run_weno(torch, gbmv, grids, steps=3, warmup=2):
         out["grids"][f"{n}^3"] = g
         del h, w, wdot
         torch.cuda.empty_cache()
+    return out
+
+
+# ----------------------------------------------------------------- Sod whole run
+
+def run_sod(torch, gbmv, with_cpu):
+    """Sod shock tube 128x3x3 (reflecting x, periodic y,z, gamma 1.4) to t_f = 0.2 with the
+    adaptive Dormand-Prince ERK (rtol 1e-6, atol 1e-11) over the GPU FP64 RHS: time to t_f,
+    steps, L1 error of density against the exact Riemann solution; the oracle-driven run on
+    one host core beside it."""
+    import integrate as I
+    import workloads as W
+    nx = 128
+    wl = W.sod(nx, 3, 3)
+    shape = wl["fields"][0].shape
+    n = int(np.prod(shape))
+    h = gbmv.Hydro((nx, 3, 3), 0, wl["bc"], wl["gamma"])
+    wdot = torch.empty((5, n), dtype=torch.float64, device="cuda")
+
+    def rhs_gpu(t, y):
+        w = [y[i].view(shape) for i in range(5)]
+        d = [wdot[i].view(shape) for i in range(5)]
+        if h.fEuler(t, w, d) != 0:
+            raise RuntimeError("illegal state")
+        return wdot.clone()
+
+    y0 = np.stack([f.reshape(-1) for f in wl["fields"]])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    yg, st = I.erk_evolve(rhs_gpu, 0.0, 0.2, torch.from_numpy(y0).cuda(), 1e-6, 1e-11)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    yg = yg.cpu().numpy()
+    x = (np.arange(nx) + 0.5) / nx
+    r, _, _ = I.sod_exact(x, 0.2)
+    rho = yg[0].reshape(shape)[1, 1]
+    out = {"workload": "Sod 128x3x3, reflecting x / periodic y,z, gamma 1.4, t_f 0.2, "
+                       "adaptive DP5(4) rtol 1e-6 atol 1e-11, FP64 RHS",
+           "s_to_tf": round(dt, 3), "steps": st.steps, "rhs_evals": st.nfe,
+           "l1_density_err_vs_exact": float(f"{np.mean(np.abs(rho - r)):.3e}")}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py as O
+
+        def rhs_cpu(t, y):
+            s_, o = O.feuler([y[i].reshape(shape) for i in range(5)], 0, wl["bc"], wl["gamma"],
+                             None)
+            return np.stack([a.reshape(-1) for a in o])
+
+        t0 = time.perf_counter()
+        yc, stc = I.erk_evolve(rhs_cpu, 0.0, 0.2, y0, 1e-6, 1e-11)
+        dtc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"s_to_tf": round(dtc, 3), "cores": 1, "kind": "port",
+                               "steps": stc.steps,
+                               "max_rel_diff_vs_gpu_run": float(f"{max(np.max(np.abs(yg[v] - yc[v])) / np.max(np.abs(yc[v])) for v in range(5)):.3e}")}
     return out
 
 
