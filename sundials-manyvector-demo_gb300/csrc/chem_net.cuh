@@ -120,6 +120,9 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
   const double ddensity = 2.0 * dH2_1 + 2.0 * dH2_2 + 1.00794 * dH_1 + 1.00794 * dH_2 +
                           1.00794 * dH_m0 + 4.002602 * dHe_1 + 4.002602 * dHe_2 + 4.002602 * dHe_3;
   const double dmh = ddensity * mhd;
+  // the FP64 tail multiplies by reciprocals where the FP64 form divides (one rounding apart;
+  // each FP64 division costs about as much as ten multiplies on this part)
+  const double kdmd = kbd / dmh;
   double Tc = Ts, Tnew = Ts, dge_dTd = 0.0;
 #pragma unroll 1
   for (int it = nfloat; it < 10; ++it) {
@@ -127,7 +130,7 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     double t1, t2;
     const double logT = log(Ts);
     const int b = chem_bin(P, logT, t1, t2);
-    const double Tdef = (logT - t1) / (t2 - t1);
+    const double Tdef = (logT - t1) * P.idbin;
     const double* lo = P.tab + (long)b * kNT;
     const double* hi = lo + kNT;
     const double g2 = lo[GAMMAH2_2] + Tdef * (hi[GAMMAH2_2] - lo[GAMMAH2_2]);
@@ -137,8 +140,8 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     const double i1 = 1.0 / (g1 - 1.0), i2 = 1.0 / (g2 - 1.0);
     const double nsum = dH2_1 * i1 + dH2_2 * i2 + dH_1 * gm1d + dH_2 * gm1d + dH_m0 * gm1d +
                         dHe_1 * gm1d + dHe_2 * gm1d + dHe_3 * gm1d + gm1d * dde;
-    dge_dTd = Tc * kbd * (-dH2_1 * i1 * i1 * dg1 - dH2_2 * i2 * i2 * dg2) / dmh + kbd * nsum / dmh;
-    const double dgev = Tc * kbd * nsum / dmh - dge0;
+    dge_dTd = kdmd * (Tc * (-dH2_1 * i1 * i1 * dg1 - dH2_2 * i2 * i2 * dg2) + nsum);
+    const double dgev = kdmd * Tc * nsum - dge0;
     Tnew = Tc - dgev / dge_dTd;
     Ts = Tnew;
   }
@@ -235,6 +238,42 @@ __device__ __forceinline__ double chem_ge_source(const ChemParams& P, const doub
          cie * k[COMPTON] * de * P.zp1_4 * (T - 2.73 * z - 2.73) + 0.5 / F * Hf;
 }
 
+// The four reciprocals of the cooling/heating terms (1/G, 1/D, 1/N, 1/F), shared by the gas-
+// energy source and its Jacobian row when both are evaluated together.
+struct GeRecip {
+  double iG, iD, iN, iF;
+};
+__device__ __forceinline__ GeRecip ge_recip(const double (&k)[kNRates], const double (&y)[10]) {
+  const double H2_1 = y[0], H_1 = y[2], H_2 = y[3], He_1 = y[5], de = y[8];
+  GeRecip r;
+  const double G = H2_1 * k[GAH2] + H_1 * k[GAHI] + H_2 * k[GAHP] + He_1 * k[GAHE] + de * k[GAEL];
+  r.iG = 1.0 / G;
+  r.iD = 1.0 / (k[H2LTE] * r.iG + 1.0);
+  r.iN = 1.0 / (H2_1 * k[NCRD2] + H_1 * k[NCRD1]);
+  r.iF = 1.0 / (k[NCRN] * r.iN + 1.0);
+  return r;
+}
+
+// chem_ge_source with the shared reciprocals (the fused kernels: one rounding apart from the
+// reference's divisions).
+__device__ __forceinline__ double chem_ge_source_r(const ChemParams& P, const double (&k)[kNRates],
+                                                   const double (&y)[10], double T,
+                                                   const ChemAux& A, const GeRecip& R) {
+  const double H2_1 = y[0], H_1 = y[2], H_2 = y[3], He_1 = y[5], He_2 = y[6], He_3 = y[7],
+               de = y[8];
+  const double z = P.z, cie = A.cie, h2oda = A.h2, mdens = A.mdens;
+  const double H13 = H_1 * H_1 * H_1;
+  const double Hf = -H2_1 * H_1 * k[H2MCOOL] + H13 * k[H2MHEAT];
+  const double de2 = de * de;
+  return -2.01588 * H2_1 * k[CIECO] * cie * mdens - H2_1 * cie * k[H2LTE] * h2oda * R.iD -
+         H_1 * k[CEHI] * cie * de - H_1 * k[CIHI] * cie * de - H_2 * cie * de * k[REHII] -
+         He_1 * k[CIHEI] * cie * de - He_2 * k[CEHEII] * cie * de - He_2 * k[CEHEI] * cie * de2 -
+         He_2 * k[CIHEII] * cie * de - He_2 * k[CIHEIS] * cie * de2 -
+         He_2 * cie * de * k[REHEII1] - He_2 * cie * de * k[REHEII2] -
+         He_3 * cie * de * k[REHEIII] - k[BREM] * cie * de * (H_2 + He_2 + 4.0 * He_3) -
+         cie * k[COMPTON] * de * P.zp1_4 * (T - 2.73 * z - 2.73) + 0.5 * R.iF * Hf;
+}
+
 // Analytic Jacobian in physical units, before the inv_scale*scale and time-unit factors;
 // rates k and slopes dk at the cell temperature.  Each of the 64 nonzeros is handed to
 // put(row, col, value) once, already multiplied by the factors the reference applies to that
@@ -242,7 +281,8 @@ __device__ __forceinline__ double chem_ge_source(const ChemParams& P, const doub
 template <class Put>
 __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double (&k)[kNRates],
                                               const double (&dk)[kNRates], const double (&y)[10],
-                                              double T, double Tge, const ChemAux& A, Put&& put) {
+                                              double T, double Tge, const ChemAux& A, Put&& put,
+                                              const GeRecip* shared = nullptr) {
   const double H2_1 = y[0], H2_2 = y[1], H_1 = y[2], H_2 = y[3], H_m0 = y[4], He_1 = y[5],
                He_2 = y[6], He_3 = y[7], de = y[8];
   const double z = P.z, h2oda = A.h2, md = A.mdens, imd = A.imdens;
@@ -309,14 +349,8 @@ __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double 
     for (int q = 0; q < 9; ++q) put(q, 9, s[q] * Tge);
   }
   // four reciprocals serve every ge-row entry (the reference divides ~20 times)
-  const double G = H2_1 * k[GAH2] + H_1 * k[GAHI] + H_2 * k[GAHP] + He_1 * k[GAHE] + de * k[GAEL];
-  const double iG = 1.0 / G;
-  const double D = k[H2LTE] * iG + 1.0;
-  const double iD = 1.0 / D;
-  const double N = H2_1 * k[NCRD2] + H_1 * k[NCRD1];
-  const double iN = 1.0 / N;
-  const double F = k[NCRN] * iN + 1.0;
-  const double iF = 1.0 / F;
+  const GeRecip R = shared ? *shared : ge_recip(k, y);
+  const double iG = R.iG, iD = R.iD, iN = R.iN, iF = R.iF;
   const double H13 = H1sq * H_1;
   const double Hf = -H2_1 * H_1 * k[H2MCOOL] + H13 * k[H2MHEAT];
   const double lte2 = k[H2LTE] * k[H2LTE];

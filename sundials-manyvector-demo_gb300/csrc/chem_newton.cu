@@ -51,13 +51,14 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
     {  // source and Newton matrix from one rate evaluation (rates and T slopes)
       double k[kNRates], dk[kNRates];
       chem_rates<true>(P, Ts, k, dk);
+      const GeRecip Rg = ge_recip(k, ya);  // shared by the source and the Jacobian's ge row
       {
         double r[21], sp[9];
         chem_fluxes(k, ya, r);
         chem_species(r, sp);
 #pragma unroll
         for (int s = 0; s < 9; ++s) f[s] = (sp[s] * isc[s]) * tunit;
-        double ge = chem_ge_source(P, k, ya, Ts, Ax) * isc[9];
+        double ge = chem_ge_source_r(P, k, ya, Ts, Ax, Rg) * isc[9];
         ge *= Ax.imdens;
         f[9] = ge * tunit;
       }
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
         const double a = (v * rf[row]) * sc[col] + (row == col ? 1.0 : 0.0);
         A[(col * 10 + row) * kNtThreads] = a;
         L[(col * 10 + row) * kNtThreads] = (LU)a;
-      });
+      }, &Rg);
     }
 #pragma unroll
     for (int s = 0; s < 10; ++s) f[s] = fout[j + s];
