@@ -223,7 +223,7 @@ static int feuler_dispatch(gbmv_hydro h, const double* const* w, double* const* 
     set_error("null handle, field or status pointer");
     return GBMV_EINVAL;
   }
-  if (precision != GBMV_FP64 && precision != GBMV_MIXED) {
+  if (precision != GBMV_FP64 && precision != GBMV_MIXED && precision != GBMV_MIXED_FAST) {
     set_error("unknown precision %d", precision);
     return GBMV_EINVAL;
   }
@@ -251,7 +251,8 @@ static int feuler_dispatch(gbmv_hydro h, const double* const* w, double* const* 
       return GBMV_ENOMEM;
     }
   }
-  return feuler_f2(h->g, W, Wd, G, h->scratch, h->prims, tscale, d_status, s);
+  return feuler_f2(h->g, W, Wd, G, h->scratch, h->prims, tscale, d_status, s,
+                   precision == GBMV_MIXED_FAST);
 }
 
 int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,

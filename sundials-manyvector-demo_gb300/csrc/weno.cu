@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2*
   }
 }
 
-template <int NCHEM, int DIR>
+template <int NCHEM, int DIR, int WV>
 __global__ void __launch_bounds__(128) face_flux_f2_kernel(Grid g, Fields w,
                                                            const float2* __restrict__ Q2,
                                                            double* __restrict__ F, long nfaces) {
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(128) face_flux_f2_kernel(Grid g, Fields w,
     double out[5];
     if (ok) {
       f2 o[5];
-      fluid_face_flux<f2, true>(W, g.gamma, S, o, &pre);
+      fluid_face_flux<f2, true, WV>(W, g.gamma, S, o, &pre);
 #pragma unroll
       for (int v = 0; v < 5; ++v) out[v] = o[v].to_double();
     } else {  // FP64, exactly the FP64 form's arithmetic
@@ -345,12 +345,12 @@ __global__ void __launch_bounds__(128) face_flux_f2_kernel(Grid g, Fields w,
         const float2 t = __ldg(Q2 + (kQ2Base + c) * n + cell[l]);
         cv[l] = nall[l] ? f2(-t.x, -t.y) : f2(t.x, t.y);
       }
-      F[(5 + c) * nfaces + f] = tracer_face_flux<f2>(S, cv).to_double();
+      F[(5 + c) * nfaces + f] = tracer_face_flux<f2, WV>(S, cv).to_double();
     }
   }
 }
 
-template <int NCHEM>
+template <int NCHEM, int WV>
 static int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
                      double* scratch, float2* q2, const double* tscale, int* d_status,
                      cudaStream_t s) {
@@ -370,17 +370,17 @@ static int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const F
   }
   {
     ProfScope ps("face_flux", s);
-    face_flux_f2_kernel<NCHEM, 0><<<blocks(nf[0], 128), 128, 0, s>>>(g, w, q2, F[0], nf[0]);
+    face_flux_f2_kernel<NCHEM, 0, WV><<<blocks(nf[0], 128), 128, 0, s>>>(g, w, q2, F[0], nf[0]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<x>");
   }
   {
     ProfScope ps("face_flux", s);
-    face_flux_f2_kernel<NCHEM, 1><<<blocks(nf[1], 128), 128, 0, s>>>(g, w, q2, F[1], nf[1]);
+    face_flux_f2_kernel<NCHEM, 1, WV><<<blocks(nf[1], 128), 128, 0, s>>>(g, w, q2, F[1], nf[1]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<y>");
   }
   {
     ProfScope ps("face_flux", s);
-    face_flux_f2_kernel<NCHEM, 2><<<blocks(nf[2], 128), 128, 0, s>>>(g, w, q2, F[2], nf[2]);
+    face_flux_f2_kernel<NCHEM, 2, WV><<<blocks(nf[2], 128), 128, 0, s>>>(g, w, q2, F[2], nf[2]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<z>");
   }
   ProfScope ps("divergence", s);
@@ -392,16 +392,31 @@ static int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const F
 
 size_t feuler_f2_prims_floats(const Grid& g) { return (size_t)2 * (kQ2Base + g.nchem) * g.ncell; }
 
+template <int WV>
+static int feuler_f2_wv(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
+                        double* scratch, float2* q2, const double* tscale, int* d_status,
+                        cudaStream_t s) {
+  switch (g.nchem) {
+    case 0: return launch_f2<0, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 2: return launch_f2<2, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 4: return launch_f2<4, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 6: return launch_f2<6, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 10: return launch_f2<10, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    default: set_error("nchem=%d not compiled (0,2,4,6,10)", g.nchem); return GBMV_EUNSUPPORTED;
+  }
+}
+
 int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
               double* scratch, float* prims, const double* tscale, int* d_status,
-              cudaStream_t s) {
+              cudaStream_t s, int fast_weights) {
   float2* q2 = reinterpret_cast<float2*>(prims);
+  if (fast_weights) return feuler_f2_wv<1>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
   switch (g.nchem) {
-    case 0: return launch_f2<0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
-    case 2: return launch_f2<2>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
-    case 4: return launch_f2<4>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
-    case 6: return launch_f2<6>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
-    case 10: return launch_f2<10>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 0: return launch_f2<0, 0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 2: return launch_f2<2, 0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 4: return launch_f2<4, 0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 6: return launch_f2<6, 0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 10: return launch_f2<10, 0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
     default: set_error("nchem=%d not compiled (0,2,4,6,10)", g.nchem); return GBMV_EUNSUPPORTED;
   }
 }

@@ -39,6 +39,6 @@ size_t feuler_f2_prims_floats(const Grid& g);
 // tscale: null, or the per-entry scale of a chemistry component held in scaled units
 int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
               double* scratch, float* prims, const double* tscale, int* d_status,
-              cudaStream_t s);
+              cudaStream_t s, int fast_weights = 0);
 
 }  // namespace gbmv

@@ -167,6 +167,60 @@ __device__ __forceinline__ f2 weno_safe(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
   return weno_side_f2_fallback<Plus>(f0, f1, f2_, f3, f4);
 }
 
+// Reconstruction in correction form (the GBMV_MIXED_FAST weights): with the central point f2_
+// in float-float, r = f2_ + sum_k w_k (q_k - f2_).  The corrections q_k - f2_ and the
+// smoothness indicators are built from the neighbour differences D01..D34 (exact float-float
+// subtractions, then rounded to float), and the weights and the weighted correction are FP32:
+// a relative weight error e changes r by e |q_k - f2_| -- an O(dx) difference in smooth flow,
+// the jump across a discontinuity -- never by e |r|, because the base value is not weighted
+// (the three weights need not sum to exactly one).
+template <bool Plus>
+__device__ __noinline__ f2 weno_side_f2d(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
+  const float D01 = (f0 - f1).to_float(), D12 = (f1 - f2_).to_float(),
+              D23 = (f2_ - f3).to_float(), D34 = (f3 - f4).to_float();
+  const float dA = D23 - D34, dB = D12 - D23, dC = D01 - D12;  // second differences
+  const float eA = dA + 2.f * D23, eB = D12 + D23, eC = dC - 2.f * D12;
+  const float b13 = 13.f / 12.f, sixth = 1.f / 6.f;
+  const float aA = 1e-6f + (b13 * (dA * dA) + 0.25f * (eA * eA));
+  const float aB = 1e-6f + (b13 * (dB * dB) + 0.25f * (eB * eB));
+  const float aC = 1e-6f + (b13 * (dC * dC) + 0.25f * (eC * eC));
+  float cA, cB, cC, wA, wB, wC;  // candidate minus central point, linear weights
+  if (Plus) {
+    cA = (D34 - 4.f * D23) * sixth;
+    cB = -(D12 + 2.f * D23) * sixth;
+    cC = (2.f * D01 - 5.f * D12) * sixth;
+    wA = 0.3f; wB = 0.6f; wC = 0.1f;
+  } else {
+    cA = (5.f * D23 - 2.f * D34) * sixth;
+    cB = (2.f * D12 + D23) * sixth;
+    cC = (4.f * D12 - D01) * sixth;
+    wA = 0.1f; wB = 0.6f; wC = 0.3f;
+  }
+  const float m = fminf(fminf(aA, aB), aC);
+  const float rA = m / aA, rB = m / aB, rC = m / aC;
+  const float tA = wA * (rA * rA), tB = wB * (rB * rB), tC = wC * (rC * rC);
+  const float corr = (tA * cA + tB * cB + tC * cC) / (tA + tB + tC);
+  return f2_ + f2(corr, 0.f);
+}
+template <bool Plus>
+__device__ __forceinline__ f2 weno_safe_d(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
+  const float m = fmaxf(fmaxf(fmaxf(fabsf(f0.hi), fabsf(f1.hi)), fmaxf(fabsf(f2_.hi), fabsf(f3.hi))),
+                        fabsf(f4.hi));
+  if (m < 1e18f) return weno_side_f2d<Plus>(f0, f1, f2_, f3, f4);
+  return weno_side_f2_fallback<Plus>(f0, f1, f2_, f3, f4);
+}
+template <bool Plus>
+__device__ __forceinline__ double weno_safe_d(double f0, double f1, double f2_, double f3,
+                                              double f4) {
+  return weno_safe<Plus>(f0, f1, f2_, f3, f4);
+}
+// WV = 0: weights in the arithmetic type T; WV = 1: the correction form above
+template <bool Plus, int WV, typename T>
+__device__ __forceinline__ T weno_pick(T f0, T f1, T f2_, T f3, T f4) {
+  if constexpr (WV == 1) return weno_safe_d<Plus>(f0, f1, f2_, f3, f4);
+  else return weno_safe<Plus>(f0, f1, f2_, f3, f4);
+}
+
 // Face-local data shared by the fluid and tracer parts.
 template <typename T>
 struct FaceState {
@@ -181,7 +235,7 @@ struct PointPrims {
   T p[6], u[6], c[6];
 };
 
-template <typename T, bool Pre = false>
+template <typename T, bool Pre = false, int WV = 0>
 __device__ __forceinline__ void fluid_face_flux(const T (&W)[6][5], double gamma_d,
                                                 FaceState<T>& S, T (&out)[5],
                                                 const PointPrims<T>* pre = nullptr) {
@@ -263,9 +317,9 @@ __device__ __forceinline__ void fluid_face_flux(const T (&W)[6][5], double gamma
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
       if (side == 0)
-        ff[i] = weno_safe<true>(pr[0][i], pr[1][i], pr[2][i], pr[3][i], pr[4][i]);
+        ff[i] = weno_pick<true, WV>(pr[0][i], pr[1][i], pr[2][i], pr[3][i], pr[4][i]);
       else
-        ff[i] = ff[i] + weno_safe<false>(pr[0][i], pr[1][i], pr[2][i], pr[3][i], pr[4][i]);
+        ff[i] = ff[i] + weno_pick<false, WV>(pr[0][i], pr[1][i], pr[2][i], pr[3][i], pr[4][i]);
     }
   }
   // right eigenvector columns (src/utilities.cpp:318-340)
@@ -277,12 +331,12 @@ __device__ __forceinline__ void fluid_face_flux(const T (&W)[6][5], double gamma
 }
 
 // Tracer part for one advected field from its 6 stencil values.
-template <typename T>
+template <typename T, int WV = 0>
 __device__ __forceinline__ T tracer_face_flux(const FaceState<T>& S, const T (&cv)[6]) {
-  T r = weno_safe<true>(cv[0] * S.hp[0], cv[1] * S.hp[1], cv[2] * S.hp[2], cv[3] * S.hp[3],
-                        cv[4] * S.hp[4]);
-  r = r + weno_safe<false>(cv[1] * S.hm[1], cv[2] * S.hm[2], cv[3] * S.hm[3], cv[4] * S.hm[4],
-                           cv[5] * S.hm[5]);
+  T r = weno_pick<true, WV>(cv[0] * S.hp[0], cv[1] * S.hp[1], cv[2] * S.hp[2], cv[3] * S.hp[3],
+                            cv[4] * S.hp[4]);
+  r = r + weno_pick<false, WV>(cv[1] * S.hm[1], cv[2] * S.hm[2], cv[3] * S.hm[3],
+                               cv[4] * S.hm[4], cv[5] * S.hm[5]);
   return r;
 }
 

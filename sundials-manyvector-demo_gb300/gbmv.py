@@ -25,7 +25,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libgbmv.so")
 
 BC_PERIODIC, BC_NEUMANN, BC_DIRICHLET, BC_REFLECTING = 0, 1, 2, 3
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_FAST = 0, 1, 2
 FORCE_IN_WDOT = 1
 
 

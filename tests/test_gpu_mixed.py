@@ -25,7 +25,7 @@ def _run(torch, wl, precision):
     return st, [x.cpu().numpy() for x in wdot]
 
 
-@pytest.mark.parametrize("precision", [1])
+@pytest.mark.parametrize("precision", [1, 2])
 @pytest.mark.parametrize("case", ["rt", "chemhydro", "smooth", "sod"])
 def test_mixed_weno_within_1e6_of_oracle(cuda, precision, case):
     if case == "rt":
