@@ -40,11 +40,12 @@ extern "C" {
 #define GBMV_MIXED 1  /* face fluxes in float-float arithmetic on the FP32 pipes (~48-bit
                          significand, native-FP64 fallback outside the float range), divergence
                          and conservation sums in FP64 (<=1e-6 vs the FP64 oracle) */
-#define GBMV_MIXED_FAST 2 /* as GBMV_MIXED, but each WENO reconstruction is the float-float
-                         central value plus an FP32-weighted correction built from float-float
-                         neighbour differences (smoothness indicators and weights in FP32 on
-                         differences, so their rounding scales with the local variation, not
-                         with the value); flux divergence only (<=1e-6 vs the FP64 oracle) */
+#define GBMV_MIXED_FAST 2 /* as GBMV_MIXED, but each species (tracer) reconstruction is the
+                         float-float central value plus an FP32-weighted correction built from
+                         float-float neighbour differences (smoothness indicators and weights
+                         in FP32 on differences, so their rounding scales with the local
+                         variation, not with the value); the characteristic fluid fields keep
+                         float-float weights (<=1e-6 vs the FP64 oracle) */
 
 /* Grid + problem description: the fields of EulerData the RHS needs
  * (src/euler3D.hpp:183-253).  nchem must be one of 0, 2, 4, 6, 10 (NVAR 5, 7, 9, 11, 15,

@@ -303,7 +303,9 @@ __global__ void __launch_bounds__(128) face_flux_f2_kernel(Grid g, Fields w,
     double out[5];
     if (ok) {
       f2 o[5];
-      fluid_face_flux<f2, true, WV>(W, g.gamma, S, o, &pre);
+      // characteristic fields keep float-float weights in every mixed form: the reference's
+      // eigenbasis (conditioning ~1/c^2) amplifies weight rounding in the back-projection
+      fluid_face_flux<f2, true, 0>(W, g.gamma, S, o, &pre);
 #pragma unroll
       for (int v = 0; v < 5; ++v) out[v] = o[v].to_double();
     } else {  // FP64, exactly the FP64 form's arithmetic

@@ -167,13 +167,16 @@ __device__ __forceinline__ f2 weno_safe(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
   return weno_side_f2_fallback<Plus>(f0, f1, f2_, f3, f4);
 }
 
-// Reconstruction in correction form (the GBMV_MIXED_FAST weights): with the central point f2_
+// Reconstruction in correction form (GBMV_MIXED_FAST, species fields): with the central point f2_
 // in float-float, r = f2_ + sum_k w_k (q_k - f2_).  The corrections q_k - f2_ and the
 // smoothness indicators are built from the neighbour differences D01..D34 (exact float-float
 // subtractions, then rounded to float), and the weights and the weighted correction are FP32:
 // a relative weight error e changes r by e |q_k - f2_| -- an O(dx) difference in smooth flow,
 // the jump across a discontinuity -- never by e |r|, because the base value is not weighted
-// (the three weights need not sum to exactly one).
+// (the three weights need not sum to exactly one).  Used for the componentwise species
+// reconstructions only: the characteristic values of the fluid part are back-projected through
+// an eigenbasis with condition ~1/c^2, which would amplify the weight rounding (measured:
+// 2e-5 on the chem-hydro state).
 template <bool Plus>
 __device__ __noinline__ f2 weno_side_f2d(f2 f0, f2 f1, f2 f2_, f2 f3, f2 f4) {
   const float D01 = (f0 - f1).to_float(), D12 = (f1 - f2_).to_float(),
