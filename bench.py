@@ -357,7 +357,9 @@ FP_COUNTS = {
     ("fp64", "chem_jac"): ("fp64", 1003.0, "cell"),
     ("fp64", "block_lu_factor"): ("fp64", 759.0, "cell"),
     ("mixed", "face_flux"): ("fp32", 25990.0, "face"),
-    ("mixed", "chem_newton"): ("fp64", 2151.1, "cell"),
+    ("mixed", "chem_newton"): ("fp64", 1807.0, "cell"),
+    ("mixed_fast", "face_flux"): ("fp32", 16335.0, "face"),
+    ("mixed_fast", "chem_newton"): ("fp64", 1807.0, "cell"),
 }
 
 
@@ -367,7 +369,9 @@ FP_COUNTS = {
 DRAM_TRAFFIC = {
     ("fp64", "face_flux"): (248.2, "face"),    # mean of the x / y / z sweeps
     ("mixed", "face_flux"): (296.5, "face"),
-    ("mixed", "chem_newton"): (440.6, "cell"),
+    ("mixed", "chem_newton"): (487.5, "cell"),
+    ("mixed_fast", "face_flux"): (295.2, "face"),
+    ("mixed_fast", "chem_newton"): (487.5, "cell"),
     ("fp64", "chem_rhs"): (357.3, "cell"),
 }
 
@@ -455,8 +459,8 @@ def run_gbmv(args):
     fp64_peak = gbmv.fma_rate(True) / 1e12
     dt_ms, nl = fam[dom]
     avg_ms = dt_ms / max(nl, 1)
-    hform = "mixed" if head.startswith("mixed") else head
-    key = "face_flux_mx" if (dom == "face_flux" and hform == "mixed") else dom
+    hform = "mixed" if head == "mixed_concurrent" else head
+    key = "face_flux_mx" if (dom == "face_flux" and hform != "fp64") else dom
     achieved = algo_bytes(key, args.n) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     traffic, traffic_note = None, None
     if (hform, dom) in DRAM_TRAFFIC:
