@@ -117,3 +117,18 @@ def test_fused_newton_against_oracle(cuda, tables):
     for s in range(10):
         assert maxnorm_err(fo[:, s], fr.reshape(n, 10)[:, s]) <= 1e-9
         assert maxnorm_err(xo[:, s], xr.reshape(n, 10)[:, s]) <= 1e-8
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("bc", [(2, 2, 0, 0, 1, 3), (1, 3, 2, 1, 0, 0), (3, 1, 1, 3, 2, 2)])
+def test_mixed_every_boundary_type(cuda, precision, bc):
+    """Mixed forms on every boundary type, homogeneous Dirichlet included: there the reference's
+    ghost density is negative and its fluxes are NaN; the mixed forms take their FP64 path on
+    those faces and must put NaN exactly where the oracle does, and agree to 1e-6 elsewhere."""
+    wl = W.rayleigh_taylor(shape=(10, 9, 8), nchem=4, seed=W.SEED_BASE + 320)
+    wl["bc"] = bc
+    st0, ref = O.feuler(wl["fields"], wl["nchem"], wl["bc"], wl["gamma"], wl["force"])
+    st1, out = _run(cuda, wl, precision)
+    assert st0 == st1 == 0
+    errs = [maxnorm_err(a, b) for a, b in zip(out, ref)]  # NaN positions must coincide
+    assert max(errs) <= TOL_MIXED, errs
