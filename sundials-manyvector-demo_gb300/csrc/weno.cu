@@ -247,8 +247,10 @@ __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2*
   }
 }
 
+// WV = 1 (fewer instructions per face) runs faster at 3 resident blocks per SM even with the
+// register cap's spills (measured 6.11 -> 5.63 ms per 128^3 RHS); WV = 0 is faster at 2.
 template <int NCHEM, int DIR, int WV>
-__global__ void __launch_bounds__(128) face_flux_f2_kernel(Grid g, Fields w,
+__global__ void __launch_bounds__(128, WV == 1 ? 3 : 1) face_flux_f2_kernel(Grid g, Fields w,
                                                            const float2* __restrict__ Q2,
                                                            double* __restrict__ F, long nfaces) {
   const long nx = g.n[0], ny = g.n[1], n = g.ncell;
