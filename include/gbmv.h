@@ -132,6 +132,14 @@ int gbmv_feuler_jvp(gbmv_hydro h, double t, const double* const* w, const double
 int gbmv_feuler_vjp(gbmv_hydro h, double t, const double* const* w, const double* const* v,
                     double* const* u, void* stream);
 
+/* pack1D_x / pack1D_y / pack1D_z and their _bdry variants (EulerData, src/euler3D.hpp:
+ * 1197-1378), for all faces at once: the six-point stencils the face fluxes of direction dir
+ * (0 x, 1 y, 2 z) read, after the periodic wrap and the boundary ghost rules.  out (device):
+ * 6 * (5+nchem) * nfaces doubles, out[(l * (5+nchem) + v) * nfaces + f], f the face index
+ * i + (nx+1) (j + ny k) for x faces (y, z likewise), stencil point l = 0..5 at cell index
+ * (face - 3 + l) along dir, v in ManyVector field order.  Asynchronous. */
+int gbmv_pack1d(gbmv_hydro h, const double* const* w, int dir, double* out, void* stream);
+
 /* check_conservation (src/io.cpp:503-542): totals[0] = mass_factor * sum(rho),
  * totals[1] = energy_factor * sum(et) over all cells, with the reference's factors
  * mass_factor = dx dy dz LengthUnits^3 DensityUnits, energy_factor = dx dy dz LengthUnits^3

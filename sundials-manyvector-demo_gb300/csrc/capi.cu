@@ -859,6 +859,16 @@ int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double en
   return energy_sync(c->S, w, c->n, 10, 1.0 / energy_units, 1, (cudaStream_t)stream);
 }
 
+int gbmv_pack1d(gbmv_hydro h, const double* const* w, int dir, double* out, void* stream) {
+  if (!h || !fields_ok(w, h->g.nchem) || !out || dir < 0 || dir > 2) {
+    set_error("bad pack1d arguments (dir 0, 1 or 2)");
+    return GBMV_EINVAL;
+  }
+  Fields W;
+  for (int v = 0; v < 6; ++v) W.f[v] = (v < 5 || h->g.nchem) ? const_cast<double*>(w[v]) : nullptr;
+  return pack1d(h->g, W, dir, out, (cudaStream_t)stream);
+}
+
 int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
                       double energy_factor, double* totals, void* stream) {
   if (!h || !fields_ok(w, 0) || !totals) {

@@ -453,6 +453,47 @@ __global__ void __launch_bounds__(256) wave_speed_max_kernel(Grid g, Fields w,
   if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
 
+// pack1D_x/y/z and their _bdry variants (src/euler3D.hpp:1197-1378): for every face normal to
+// DIR (all (n+1) per row, as the flux loops), the six-point stencil w1d[l][v] the face flux
+// reads, ghost rules applied, fields in the ManyVector order (rho, mx, my, mz, et, species),
+// written to out[(l * NVAR + v) * nfaces + f].
+template <int DIR>
+__global__ void __launch_bounds__(128) pack1d_kernel(Grid g, Fields w, double* __restrict__ out,
+                                                     long nfaces) {
+  const long nx = g.n[0], ny = g.n[1];
+  const int nv = 5 + g.nchem;
+  for (long f = blockIdx.x * (long)blockDim.x + threadIdx.x; f < nfaces;
+       f += (long)gridDim.x * blockDim.x) {
+    long i, j, k;
+    face_coords<DIR>(f, g, i, j, k);
+    const long base[3] = {i, j, k};
+    for (int l = 0; l < 6; ++l) {
+      bool nall, nnorm;
+      long q[3] = {i, j, k};
+      q[DIR] = ghost_src(base[DIR] - 3 + l, g.n[DIR], g.bc[2 * DIR], g.bc[2 * DIR + 1], &nall,
+                         &nnorm);
+      const long c = q[0] + nx * (q[1] + ny * q[2]);
+      for (int v = 0; v < nv; ++v) {
+        double x = (v < 5) ? w.f[v][c] : w.f[5][(v - 5) + (long)g.nchem * c];
+        if (nall || (nnorm && v == 1 + DIR)) x = -x;
+        out[((long)l * nv + v) * nfaces + f] = x;
+      }
+    }
+  }
+}
+
+int pack1d(const Grid& g, const Fields& w, int dir, double* out, cudaStream_t s) {
+  const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  const long nf[3] = {(nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1)};
+  long b = (nf[dir] + 127) / 128;
+  if (b > (long)kSM * 16) b = (long)kSM * 16;
+  if (dir == 0) pack1d_kernel<0><<<(int)b, 128, 0, s>>>(g, w, out, nf[0]);
+  else if (dir == 1) pack1d_kernel<1><<<(int)b, 128, 0, s>>>(g, w, out, nf[1]);
+  else pack1d_kernel<2><<<(int)b, 128, 0, s>>>(g, w, out, nf[2]);
+  GBMV_LAUNCH_CHECK("pack1d_kernel");
+  return GBMV_OK;
+}
+
 // check_conservation (src/io.cpp:503-542): grid totals of rho and et.  Deterministic two-pass
 // reduction (fixed grid, per-block partial sums, then one block in a fixed order), FP64 with a
 // compensated (two-sum) accumulation per thread.

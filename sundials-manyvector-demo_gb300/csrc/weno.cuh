@@ -24,6 +24,7 @@ int feuler_mixed(const Grid& g, const Fields& w, const Fields& wdot, const Force
                  double* scratch, int* d_status, cudaStream_t s);
 
 int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s);
+int pack1d(const Grid& g, const Fields& w, int dir, double* out, cudaStream_t s);
 // totals of rho and et into d_scratch[2 * 1024 + 0..1] (scratch: conservation_scratch_doubles)
 size_t conservation_scratch_doubles();
 int conservation_sums(const Grid& g, const Fields& w, double* d_scratch, cudaStream_t s);

@@ -61,6 +61,7 @@ SIGNATURES = [
     ("gbmv_feuler_noalloc", C.c_int, [C.POINTER(_Grid), _P, C.c_double, C.POINTER(_VP),
                                       C.POINTER(_VP), _VP]),
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
+    ("gbmv_pack1d", C.c_int, [_VP, C.POINTER(_VP), C.c_int, _VP, _VP]),
     ("gbmv_conservation", C.c_int, [_VP, C.POINTER(_VP), C.c_double, C.c_double, _P, _VP]),
     ("gbmv_feuler_jvp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
                                   C.POINTER(_VP), _VP]),
@@ -207,6 +208,12 @@ class Hydro:
         return _check(load().gbmv_feuler_async(self.h, t, _vec(w), _vec(wdot), precision, flags,
                                                status.data_ptr(), _stream_ptr(stream)),
                       "gbmv_feuler_async")
+
+    def pack1D(self, w, direction, out, stream=None):
+        """Stencils of every face normal to `direction` (pack1D_x/y/z(_bdry),
+        src/euler3D.hpp:1197): out is a CUDA float64 tensor of 6 * NVAR * nfaces."""
+        return _check(load().gbmv_pack1d(self.h, _vec(w), direction, _dev_ptr(out),
+                                         _stream_ptr(stream)), "gbmv_pack1d")
 
     def check_conservation(self, w, mass_factor=1.0, energy_factor=1.0, stream=None):
         """(total mass, total energy) as check_conservation (src/io.cpp:503) sums them."""
