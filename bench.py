@@ -527,15 +527,19 @@ def run_gbmv(args):
                 h.copy_(d, non_blocking=True)
             pin_x.copy_(fs.x, non_blocking=True)
 
-        e2e_steps = max(4, args.steps)
-        ms_serial = time_steps(torch, e2e_step, e2e_steps, 1)
-        ms_pipe = e2e_pipelined(torch, [fs, make_fs(head)], pin_in, e2e_steps)
+        e2e_steps = max(10, args.steps)
+        ms_serial = statistics.median(time_steps(torch, e2e_step, e2e_steps, 1)
+                                      for _ in range(3))
+        sets = [fs, make_fs(head)]
+        ms_pipe = statistics.median(e2e_pipelined(torch, sets, pin_in, e2e_steps)
+                                    for _ in range(3))
         ms_e2e = min(ms_serial, ms_pipe)
         line["e2e"] = {"value": round(ncell / (ms_e2e * 1e-3) / 1e6, 3), "unit": "Mcells/s",
                        "h2d_bytes_per_step": fs.bytes_in(), "d2h_bytes_per_step": fs.bytes_out(),
                        "ms_per_step": round(ms_e2e, 4),
                        "ms_per_step_serial_copies": round(ms_serial, 4),
                        "ms_per_step_pipelined": round(ms_pipe, 4),
+                       "repeats": "median of 3 runs of max(10, steps) steps each",
                        "note": ("every step copies its inputs from pinned host memory and its "
                                 "tendencies and Newton update back inside the timed region; "
                                 "pipelined = two device state sets, copies of one step overlap "
