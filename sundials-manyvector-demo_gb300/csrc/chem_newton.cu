@@ -16,19 +16,25 @@
 
 namespace gbmv {
 
-constexpr int kNtThreads = 64;
+// Threads per block.  Shared memory per cell: the FP32-LU form keeps the 64 structural
+// nonzeros of the FP64 Newton matrix (for the refinement residuals) and the 100-entry FP32
+// factor, 912 bytes; the FP64-LU form only its 100-entry FP64 factor.  With 32-thread blocks
+// seven blocks (seven warps) fit an SM, against six with 64-thread blocks.
+constexpr int kNtThreads = 32;
 
-template <typename LU>
-__global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, ChemState S, long n,
-                                                                 const double* __restrict__ y,
-                                                                 double* __restrict__ fout,
-                                                                 double* __restrict__ xout,
-                                                                 double gamma, double tunit,
-                                                                 int refine,
-                                                                 int* __restrict__ info_out) {
+template <typename LU, int BS>
+__global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState S, long n,
+                                                         const double* __restrict__ y,
+                                                         double* __restrict__ fout,
+                                                         double* __restrict__ xout,
+                                                         double gamma, double tunit,
+                                                         int refine,
+                                                         int* __restrict__ info_out) {
   extern __shared__ unsigned char smem_raw[];
-  double* A = reinterpret_cast<double*>(smem_raw) + threadIdx.x;  // A[e * kNtThreads]
-  LU* L = reinterpret_cast<LU*>(reinterpret_cast<double*>(smem_raw) + 100 * kNtThreads) +
+  constexpr bool kMixed = sizeof(LU) == 4;
+  // FP32-LU form: As[e * BS] = FP64 matrix entry e of kJacPattern; L[(col*10+row) * BS] factor
+  double* As = reinterpret_cast<double*>(smem_raw) + threadIdx.x;
+  LU* L = reinterpret_cast<LU*>(reinterpret_cast<double*>(smem_raw) + (kMixed ? 64 * BS : 0)) +
           threadIdx.x;
   int bad = 0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
@@ -69,14 +75,15 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
 #pragma unroll
       for (int r = 0; r < 10; ++r) rf[r] = (-gamma * tunit) * isc[r];
 #pragma unroll
-      for (int e = 0; e < 100; ++e) {
-        A[e * kNtThreads] = (e % 11 == 0) ? 1.0 : 0.0;
-        L[e * kNtThreads] = (e % 11 == 0) ? LU(1) : LU(0);
-      }
+      for (int e = 0; e < 100; ++e) L[e * BS] = LU(0);  // structural zeros
+      // every structural entry (the diagonal included) is put exactly once
       chem_jacobian(P, k, dk, ya, Ts, dTs, Ax, [&](int row, int col, double v) {
         const double a = (v * rf[row]) * sc[col] + (row == col ? 1.0 : 0.0);
-        A[(col * 10 + row) * kNtThreads] = a;
-        L[(col * 10 + row) * kNtThreads] = (LU)a;
+        if (kMixed) {
+          const int e = kJacIndex[row][col];
+          if (e >= 0) As[e * BS] = a;
+        }
+        L[(col * 10 + row) * BS] = (LU)a;
       }, &Rg);
     }
 #pragma unroll
@@ -84,13 +91,13 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
 
     int piv[10];
     double x[10];
-    int info = lu10_strided<LU>(L, kNtThreads, piv);
+    int info = lu10_strided<LU>(L, BS, piv);
     bool fp64_fallback = (sizeof(LU) == 4) && info != 0;
     if (!fp64_fallback) {
       LU xs[10];
 #pragma unroll
       for (int s = 0; s < 10; ++s) xs[s] = (LU)f[s];
-      lus10_strided<LU, LU>(L, kNtThreads, piv, xs);
+      lus10_strided<LU, LU>(L, BS, piv, xs);
 #pragma unroll
       for (int s = 0; s < 10; ++s) x[s] = (double)xs[s];
       if (sizeof(LU) == 4) {
@@ -102,14 +109,12 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
 #pragma unroll
           for (int row = 0; row < 10; ++row) rr[row] = f[row];
 #pragma unroll
-          for (int e = 0; e < 64; ++e) {  // the 64 structural nonzeros (diagonal included)
-            const int row = kJacPattern[e][0], col = kJacPattern[e][1];
-            rr[row] -= A[(col * 10 + row) * kNtThreads] * x[col];
-          }
+          for (int e = 0; e < 64; ++e)  // the 64 structural nonzeros (diagonal included)
+            rr[kJacPattern[e][0]] -= As[e * BS] * x[kJacPattern[e][1]];
           LU ds[10];
 #pragma unroll
           for (int s = 0; s < 10; ++s) ds[s] = (LU)rr[s];
-          lus10_strided<LU, LU>(L, kNtThreads, piv, ds);
+          lus10_strided<LU, LU>(L, BS, piv, ds);
           float dmax = 0.f, xmax = 0.f;
 #pragma unroll
           for (int s = 0; s < 10; ++s) {
@@ -125,11 +130,15 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
         fp64_fallback = !finite;
       }
     }
-    if (fp64_fallback) {  // FP32 factor singular or out of range: factor the FP64 matrix
-      info = lu10_strided<double>(A, kNtThreads, piv);
+    if (fp64_fallback) {  // FP32 factor singular or out of range: factor the FP64 matrix,
+                          // rebuilt densely in (per-thread local) memory -- a rare path
+      double Ad[100];
+      for (int e = 0; e < 100; ++e) Ad[e] = 0.0;
+      for (int e = 0; e < 64; ++e) Ad[kJacPattern[e][1] * 10 + kJacPattern[e][0]] = As[e * BS];
+      info = lu10_strided<double>(Ad, 1, piv);
 #pragma unroll
       for (int s = 0; s < 10; ++s) x[s] = f[s];
-      lus10_strided<double, double>(A, kNtThreads, piv, x);
+      lus10_strided<double, double>(Ad, 1, piv, x);
     }
     if (info && (sizeof(LU) == 8 || fp64_fallback)) bad = 1;
 #pragma unroll
@@ -138,32 +147,34 @@ __global__ void __launch_bounds__(kNtThreads) chem_newton_kernel(ChemParams P, C
   if (bad) atomicMax(info_out, 1);
 }
 
+template <typename LU>
+static int launch_newton(const ChemParams& P, const ChemState& S, long n, const double* y,
+                         double* f, double* x, double gamma, double tunit, int refine,
+                         int* d_info, cudaStream_t s, long blocks) {
+  constexpr int BS = kNtThreads;
+  const size_t shm = (size_t)BS * (sizeof(LU) == 4 ? 64 * sizeof(double) + 100 * sizeof(float)
+                                                   : 100 * sizeof(double));
+  // a function attribute, not a stream operation: also legal during graph capture
+  GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_newton_kernel<LU, BS>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+  chem_newton_kernel<LU, BS><<<(int)blocks, BS, shm, s>>>(P, S, n, y, f, x, gamma, tunit,
+                                                          refine, d_info);
+  GBMV_LAUNCH_CHECK("chem_newton_kernel");
+  return GBMV_OK;
+}
+
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
                 cudaStream_t s, int blocks_per_sm) {
   long b = (n + kNtThreads - 1) / kNtThreads;
   // default: a deep grid-stride grid; blocks_per_sm > 0: exactly that many resident blocks per
   // SM (a persistent grid leaving room for a kernel running beside it on another stream)
-  const long cap = (long)kSM * (blocks_per_sm > 0 ? blocks_per_sm : 24);
+  const long cap = (long)kSM * (blocks_per_sm > 0 ? blocks_per_sm : 48);
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   ProfScope ps("chem_newton", s);
-  if (lu_fp32) {
-    const size_t shm = (size_t)kNtThreads * 100 * (sizeof(double) + sizeof(float));
-    // a function attribute, not a stream operation: also legal during graph capture
-    GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_newton_kernel<float>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-    chem_newton_kernel<float><<<(int)b, kNtThreads, shm, s>>>(P, S, n, y, f, x, gamma, tunit,
-                                                              refine, d_info);
-  } else {
-    const size_t shm = (size_t)kNtThreads * 100 * 2 * sizeof(double);
-    GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_newton_kernel<double>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-    chem_newton_kernel<double><<<(int)b, kNtThreads, shm, s>>>(P, S, n, y, f, x, gamma, tunit,
-                                                               refine, d_info);
-  }
-  GBMV_LAUNCH_CHECK("chem_newton_kernel");
-  return GBMV_OK;
+  if (lu_fp32) return launch_newton<float>(P, S, n, y, f, x, gamma, tunit, refine, d_info, s, b);
+  return launch_newton<double>(P, S, n, y, f, x, gamma, tunit, refine, d_info, s, b);
 }
 
 }  // namespace gbmv
