@@ -28,7 +28,7 @@ def _oracle_fexpl(wl, energy_units):
     return st, out, f
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_fexpl_matches_oracle_composition(cuda, tables, precision):
     torch = cuda
     import gbmv
