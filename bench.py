@@ -874,7 +874,9 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
         c.set_scale(scale)
         z = torch.ones(10 * n, dtype=torch.float64, device="cuda")
         st = torch.zeros(8 * n, dtype=torch.int32, device="cuda")
-        c.dirk_evolve(0.0, DIRK_TOUT * 0.01, z, 1e11, precision=prec, **DIRK_OPTS)  # + autotune
+        # warm-up call over the full interval: the block-size autotuner times its candidates
+        # on this call's work, which must be representative of the timed one
+        c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, precision=prec, **DIRK_OPTS)
         z.fill_(1.0)
         c.state("Ts").fill_(1000.0)
         torch.cuda.synchronize()

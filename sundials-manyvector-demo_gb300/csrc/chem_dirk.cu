@@ -174,14 +174,16 @@ __device__ __forceinline__ int dirk_setup(const ChemParams& P, const ChemState& 
         const int row = kJacPattern[e][0], col = kJacPattern[e][1];
         cmax[col] = fmax(cmax[col], fabs(A[(col * 10 + row) * BS] * pow2(er[row])));
       }
+#pragma unroll
+      for (int s = 0; s < 10; ++s) ec[s] = eq_exponent(cmax[s]);
     } else {
-      chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-        cmax[col] = fmax(cmax[col], fabs(entry(row, col, v) * pow2(er[row])));
-      });
+      // without an FP64 copy every pass re-evaluates the Jacobian: rows only (scaled partial
+      // pivoting), two passes instead of three
+#pragma unroll
+      for (int s = 0; s < 10; ++s) ec[s] = 0;
     }
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
-      ec[s] = eq_exponent(cmax[s]);
       EQ[s * BS] = (short)er[s];
       EQ[(10 + s) * BS] = (short)ec[s];
     }
