@@ -59,7 +59,7 @@ def parse():
     p.add_argument("--concurrent", action="store_true",
                    help="also time the mixed stage as two concurrent graph branches")
     p.add_argument("--no-sod", action="store_true", help="skip the Sod whole-run measurement")
-    p.add_argument("--mri-n", type=int, default=64,
+    p.add_argument("--mri-n", type=int, default=128,
                    help="multirate time-to-t_f measurement on mri_n^3 x 15 (0 = skip)")
     p.add_argument("--ad-n", type=int, default=96,
                    help="differentiation measurement on ad_n^3 x 9 fields (0 = skip)")
