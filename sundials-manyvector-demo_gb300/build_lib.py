@@ -28,7 +28,9 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    # largest first: the slowest units start at once and the short ones fill in around them
+    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu")]
+    return sorted(srcs, key=lambda p: (-os.path.getsize(p), p))
 
 
 def _deps():
@@ -60,7 +62,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
             if f.endswith(".o"):
                 os.remove(os.path.join(OUT, f))
     srcs = sources()
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1, len(srcs)))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         tmp = LIB + f".tmp{os.getpid()}"

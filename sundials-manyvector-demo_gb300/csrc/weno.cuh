@@ -20,8 +20,9 @@ size_t feuler_fp64_scratch_doubles(const Grid& g);
 int feuler_fp64(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
                 double* scratch, int* d_status, cudaStream_t s);
 
-int feuler_mixed(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
-                 double* scratch, int* d_status, cudaStream_t s);
+// pass 2 of every form: wdot = G - div F from the three per-direction face-flux arrays
+int divergence(const Grid& g, const Fields& w, const Fields& wdot, double* const (&F)[3],
+               const ForceTerm& G, int* d_status, cudaStream_t s);
 
 int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s);
 int pack1d(const Grid& g, const Fields& w, int dir, double* out, cudaStream_t s);
@@ -29,13 +30,14 @@ int pack1d(const Grid& g, const Fields& w, int dir, double* out, cudaStream_t s)
 size_t conservation_scratch_doubles();
 int conservation_sums(const Grid& g, const Fields& w, double* d_scratch, cudaStream_t s);
 
-// derivatives of the FP64 flux divergence (weno_ad.cu)
+// derivatives of the FP64 flux divergence (weno_jvp.cu, weno_vjp.cu)
 size_t feuler_vjp_scratch_doubles(const Grid& g);
 int feuler_jvp(const Grid& g, const Fields& w, const Fields& dw, const Fields& out,
                double* scratch, cudaStream_t s);
 int feuler_vjp(const Grid& g, const Fields& w, const Fields& v, const Fields& out, double* A,
                cudaStream_t s);
 
+// float-float form (weno_f2.cu)
 size_t feuler_f2_prims_floats(const Grid& g);
 // tscale: null, or the per-entry scale of a chemistry component held in scaled units
 int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,

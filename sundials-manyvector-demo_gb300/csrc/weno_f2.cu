@@ -1,0 +1,47 @@
+// Float-float WENO flux divergence: the per-cell primitive pass and the WV = 0 sweep
+// (float-float weights everywhere), with the entry point that picks the weight variant.
+#include "weno_f2.cuh"
+
+namespace gbmv {
+
+__global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2* __restrict__ Q2,
+                                                       const double* __restrict__ tscale) {
+  const long n = g.ncell;
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+       c += (long)gridDim.x * blockDim.x) {
+    const double rho = w.f[0][c], mx = w.f[1][c], my = w.f[2][c], mz = w.f[3][c], et = w.f[4][c];
+    const double p = eos64(g.gamma, rho, mx, my, mz, et);
+    double q[kQ2Base] = {rho, mx, my, mz, et, p, mx / rho, my / rho, mz / rho,
+                         sqrt0(g.gamma * p / rho)};
+#pragma unroll
+    for (int k = 0; k < kQ2Base; ++k) {
+      const f2 v = f2_from_double(q[k]);
+      Q2[k * n + c] = make_float2(v.hi, v.lo);
+    }
+    for (int v = 0; v < g.nchem; ++v) {
+      // tscale: the chemistry component arrives in scaled units (x = chem * scale)
+      const long e = v + (long)g.nchem * c;
+      const f2 x = f2_from_double(tscale ? w.f[5][e] * tscale[e] : w.f[5][e]);
+      Q2[(kQ2Base + v) * n + c] = make_float2(x.hi, x.lo);
+    }
+  }
+}
+
+int prims_f2(const Grid& g, const Fields& w, float2* q2, const double* tscale, cudaStream_t s) {
+  ProfScope ps("prims", s);
+  prims_f2_kernel<<<sweep_blocks(g.ncell, 256), 256, 0, s>>>(g, w, q2, tscale);
+  GBMV_LAUNCH_CHECK("prims_f2_kernel");
+  return GBMV_OK;
+}
+
+size_t feuler_f2_prims_floats(const Grid& g) { return (size_t)2 * (kQ2Base + g.nchem) * g.ncell; }
+
+int feuler_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
+              double* scratch, float* prims, const double* tscale, int* d_status,
+              cudaStream_t s, int fast_weights) {
+  float2* q2 = reinterpret_cast<float2*>(prims);
+  if (fast_weights) return feuler_f2_fast(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+  return feuler_f2_wv<0>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+}
+
+}  // namespace gbmv

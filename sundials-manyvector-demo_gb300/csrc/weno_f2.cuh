@@ -1,0 +1,184 @@
+// Float-float (mixed) form of the WENO flux divergence (src/utilities.cpp:17-253):
+//
+//   prims_f2_kernel: once per cell, in FP64 exactly as the reference evaluates them per
+//     stencil point -- pressure (eos), the three velocities m/rho and the sound speed
+//     sqrt(gamma p / rho) -- then every field and primitive split into float pairs (hi, lo):
+//     Q2[q][cell], q = rho, mx, my, mz, et, p, ux, uy, uz, c, tracers...;
+//   face_flux_f2_kernel<NCHEM, DIR>: the face flux in float-float arithmetic from Q2 (no FP64
+//     instruction on the common path); faces whose states leave the float range, or touch a
+//     non-positive density (homogeneous Dirichlet ghosts), are computed in FP64 from w;
+//   divergence: the FP64 pass of the FP64 form (weno.cu).
+//
+// The face-flux kernel is a template over the tracer count, the sweep direction and the weight
+// variant WV (0: float-float weights everywhere; 1: FP32 weights and smoothness indicators for
+// the tracer reconstructions, which are in correction form); weno_f2.cu instantiates WV = 0 and
+// weno_f2_fast.cu WV = 1, so the two compile in parallel.
+#pragma once
+
+#include "common.cuh"
+#include "weno_face.cuh"
+#include "weno_sweep.cuh"
+
+namespace gbmv {
+
+constexpr int kQ2Base = 10;  // index of the first tracer in Q2
+
+// Q2 from w (weno_f2.cu)
+int prims_f2(const Grid& g, const Fields& w, float2* q2, const double* tscale, cudaStream_t s);
+// the WV = 1 sweep (weno_f2_fast.cu)
+int feuler_f2_fast(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
+                   double* scratch, float2* q2, const double* tscale, int* d_status,
+                   cudaStream_t s);
+
+// WV = 1 (fewer instructions per face) runs faster at 3 resident blocks per SM even with the
+// register cap's spills (measured 6.11 -> 5.63 ms per 128^3 RHS); WV = 0 is faster at 2.
+template <int NCHEM, int DIR, int WV>
+__global__ void __launch_bounds__(128, WV == 1 ? 3 : 1) face_flux_f2_kernel(Grid g, Fields w,
+                                                           const float2* __restrict__ Q2,
+                                                           double* __restrict__ F, long nfaces) {
+  const long nx = g.n[0], ny = g.n[1], n = g.ncell;
+  for (long f = blockIdx.x * (long)blockDim.x + threadIdx.x; f < nfaces;
+       f += (long)gridDim.x * blockDim.x) {
+    long i, j, k;
+    face_coords<DIR>(f, g, i, j, k);
+    const long base[3] = {i, j, k};
+    long cell[6];
+    bool nall[6], nnorm[6];
+#pragma unroll
+    for (int l = 0; l < 6; ++l) {
+      long p = base[DIR] - 3 + l;
+      p = ghost_src(p, g.n[DIR], g.bc[2 * DIR], g.bc[2 * DIR + 1], &nall[l], &nnorm[l]);
+      long q[3] = {i, j, k};
+      q[DIR] = p;
+      cell[l] = q[0] + nx * (q[1] + ny * q[2]);
+    }
+    f2 W[6][5];
+    PointPrims<f2> pre;
+    bool ok = true;
+#pragma unroll
+    for (int l = 0; l < 6; ++l) {
+      // slots: rho, m_normal, m_t1, m_t2, et, p, u_normal, c
+      const int src[8] = {0, 1 + DIR, DIR == 1 ? 1 : 2, DIR == 2 ? 1 : 3, 4, 5, 6 + DIR, 9};
+      f2 q[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const float2 t = __ldg(Q2 + src[m] * n + cell[l]);
+        q[m] = f2(t.x, t.y);
+      }
+      // homogeneous Dirichlet negates every conserved field (so p too; u and c unchanged);
+      // reflecting negates the normal momentum (so the normal velocity)
+      if (nall[l]) {
+#pragma unroll
+        for (int m = 0; m < 6; ++m) q[m] = -q[m];
+      }
+      if (nnorm[l]) {
+        q[1] = -q[1];
+        q[6] = -q[6];
+      }
+#pragma unroll
+      for (int m = 0; m < 5; ++m) W[l][m] = q[m];
+      pre.p[l] = q[5];
+      pre.u[l] = q[6];
+      pre.c[l] = q[7];
+      ok = ok && (q[0].hi > 0.f);
+#pragma unroll
+      for (int m = 0; m < 6; ++m) ok = ok && (fabsf(q[m].hi) < 1e15f);
+    }
+    FaceState<f2> S;
+    double out[5];
+    if (ok) {
+      f2 o[5];
+      // characteristic fields keep float-float weights in every mixed form: the reference's
+      // eigenbasis (conditioning ~1/c^2) amplifies weight rounding in the back-projection
+      fluid_face_flux<f2, true, 0>(W, g.gamma, S, o, &pre);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) out[v] = o[v].to_double();
+    } else {  // FP64, exactly the FP64 form's arithmetic
+      double Wd[6][5];
+#pragma unroll
+      for (int l = 0; l < 6; ++l) {
+        double q[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) q[v] = __ldg(w.f[v] + cell[l]);
+        if (nall[l]) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) q[v] = -q[v];
+        }
+        if (nnorm[l]) q[1 + DIR] = -q[1 + DIR];
+        Wd[l][0] = q[0];
+        Wd[l][1] = q[1 + DIR];
+        Wd[l][2] = (DIR == 1) ? q[1] : q[2];
+        Wd[l][3] = (DIR == 2) ? q[1] : q[3];
+        Wd[l][4] = q[4];
+      }
+      FaceState<double> S64;
+      fluid_face_flux<double>(Wd, g.gamma, S64, out);
+#pragma unroll
+      for (int l = 0; l < 6; ++l) {
+        S.hp[l] = f2_from_double(S64.hp[l]);
+        S.hm[l] = f2_from_double(S64.hm[l]);
+      }
+    }
+    const double o1 = out[1], oD = out[1 + DIR];
+    out[1] = oD;
+    out[1 + DIR] = o1;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v * nfaces + f] = out[v];
+#pragma unroll 1
+    for (int c = 0; c < NCHEM; ++c) {
+      f2 cv[6];
+#pragma unroll
+      for (int l = 0; l < 6; ++l) {
+        const float2 t = __ldg(Q2 + (kQ2Base + c) * n + cell[l]);
+        cv[l] = nall[l] ? f2(-t.x, -t.y) : f2(t.x, t.y);
+      }
+      F[(5 + c) * nfaces + f] = tracer_face_flux<f2, WV>(S, cv).to_double();
+    }
+  }
+}
+
+template <int NCHEM, int WV>
+int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
+              double* scratch, float2* q2, const double* tscale, int* d_status, cudaStream_t s) {
+  long nf[3];
+  face_counts(g, nf);
+  double* F[3] = {scratch, scratch + (long)(5 + NCHEM) * nf[0],
+                  scratch + (long)(5 + NCHEM) * (nf[0] + nf[1])};
+  int rc = prims_f2(g, w, q2, tscale, s);
+  if (rc != GBMV_OK) return rc;
+  {
+    ProfScope ps("face_flux", s);
+    face_flux_f2_kernel<NCHEM, 0, WV><<<sweep_blocks(nf[0], 128), 128, 0, s>>>(g, w, q2, F[0],
+                                                                                nf[0]);
+    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<x>");
+  }
+  {
+    ProfScope ps("face_flux", s);
+    face_flux_f2_kernel<NCHEM, 1, WV><<<sweep_blocks(nf[1], 128), 128, 0, s>>>(g, w, q2, F[1],
+                                                                                nf[1]);
+    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<y>");
+  }
+  {
+    ProfScope ps("face_flux", s);
+    face_flux_f2_kernel<NCHEM, 2, WV><<<sweep_blocks(nf[2], 128), 128, 0, s>>>(g, w, q2, F[2],
+                                                                                nf[2]);
+    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<z>");
+  }
+  return divergence(g, w, wdot, F, G, d_status, s);
+}
+
+template <int WV>
+int feuler_f2_wv(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
+                 double* scratch, float2* q2, const double* tscale, int* d_status,
+                 cudaStream_t s) {
+  switch (g.nchem) {
+    case 0: return launch_f2<0, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 2: return launch_f2<2, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 4: return launch_f2<4, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 6: return launch_f2<6, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    case 10: return launch_f2<10, WV>(g, w, wdot, G, scratch, q2, tscale, d_status, s);
+    default: set_error("nchem=%d not compiled (0,2,4,6,10)", g.nchem); return GBMV_EUNSUPPORTED;
+  }
+}
+
+}  // namespace gbmv

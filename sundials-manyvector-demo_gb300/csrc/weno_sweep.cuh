@@ -1,0 +1,78 @@
+// Face indexing and stencil gather shared by every face-sweep kernel (the FP64 and float-float
+// face fluxes, pack1D, the JVP and VJP sweeps).
+//
+// A sweep normal to DIR visits every face of the (n_DIR + 1) per row, the lower faces of all
+// cells plus the upper boundary faces, as the reference's interior and boundary flux loops do
+// together (src/utilities.cpp:17-253).  Face f has coordinates (i, j, k) in the face grid of
+// extents n + e_DIR; its stencil points sit at positions i_DIR - 3 .. i_DIR + 2 along DIR and
+// take their values through the ghost rule of common.cuh (ghost_src).
+#pragma once
+
+#include "common.cuh"
+#include "weno.cuh"
+
+namespace gbmv {
+
+template <int DIR>
+__device__ __forceinline__ void face_coords(long f, const Grid& g, long& i, long& j, long& k) {
+  const long ex = g.n[0] + (DIR == 0), ey = g.n[1] + (DIR == 1);
+  i = f % ex;
+  const long r = f / ex;
+  j = r % ey;
+  k = r / ey;
+}
+
+// cells and ghost signs of the six stencil points of face f
+template <int DIR>
+__device__ __forceinline__ void stencil(const Grid& g, long f, long (&cell)[6], bool (&nall)[6],
+                                        bool (&nnorm)[6], long (&ijk)[3]) {
+  long i, j, k;
+  face_coords<DIR>(f, g, i, j, k);
+  ijk[0] = i;
+  ijk[1] = j;
+  ijk[2] = k;
+#pragma unroll
+  for (int l = 0; l < 6; ++l) {
+    long q[3] = {i, j, k};
+    q[DIR] = ghost_src(q[DIR] - 3 + l, g.n[DIR], g.bc[2 * DIR], g.bc[2 * DIR + 1], &nall[l],
+                       &nnorm[l]);
+    cell[l] = q[0] + g.n[0] * (q[1] + g.n[1] * q[2]);
+  }
+}
+
+// the five fluid values of a stencil point in face order (normal momentum in slot 1, the
+// direction swap of src/utilities.cpp:283-285), ghost signs applied
+template <int DIR>
+__device__ __forceinline__ void load_point(const Fields& w, long c, bool nall, bool nnorm,
+                                           double (&W)[5]) {
+  double q[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) q[v] = __ldg(w.f[v] + c);
+  if (nall) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) q[v] = -q[v];
+  }
+  if (nnorm) q[1 + DIR] = -q[1 + DIR];
+  W[0] = q[0];
+  W[1] = q[1 + DIR];
+  W[2] = (DIR == 1) ? q[1] : q[2];
+  W[3] = (DIR == 2) ? q[1] : q[3];
+  W[4] = q[4];
+}
+
+// grid-stride launch size: ceil(n / t) blocks, at least 1, at most 16 per SM
+inline int sweep_blocks(long n, int t) {
+  long b = (n + t - 1) / t;
+  const long cap = (long)kSM * 16;
+  return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
+}
+
+// faces normal to x, y, z
+inline void face_counts(const Grid& g, long (&nf)[3]) {
+  const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  nf[0] = (nx + 1) * ny * nz;
+  nf[1] = nx * (ny + 1) * nz;
+  nf[2] = nx * ny * (nz + 1);
+}
+
+}  // namespace gbmv

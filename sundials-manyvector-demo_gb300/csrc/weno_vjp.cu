@@ -1,8 +1,4 @@
 // Derivatives of the WENO flux divergence (the FP64 form of fEuler, src/utilities.cpp:17-253):
-//
-//   JVP  jv = (d fEuler / d w) dw : forward mode -- the face flux evaluated on dual numbers
-//        (value, tangent), the same templated code as the FP64 form, so the tangent is the
-//        exact linearisation of what the FP64 kernel computes; then the (linear) divergence.
 //   VJP  u = (d fEuler / d w)^T v : reverse mode, hand-written.  Per face: the face cotangent
 //        from the divergence, cF = (v_{i} - v_{i-1}) / dx along the face normal, then the
 //        adjoint of the characteristic face flux (Roe average, eigenvectors, Lax-Friedrichs
@@ -15,173 +11,9 @@
 #include "common.cuh"
 #include "weno.cuh"
 #include "weno_face.cuh"
+#include "weno_sweep.cuh"
 
 namespace gbmv {
-
-// ------------------------------------------------------------------ dual numbers (JVP)
-
-struct Dual {
-  double v, d;
-  Dual() = default;
-  __host__ __device__ constexpr Dual(double x) : v(x), d(0.0) {}
-  __host__ __device__ constexpr Dual(double x, double y) : v(x), d(y) {}
-};
-__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
-__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
-__device__ __forceinline__ Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
-__device__ __forceinline__ Dual operator*(Dual a, Dual b) {
-  return Dual(a.v * b.v, a.v * b.d + a.d * b.v);
-}
-__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
-  const double q = a.v / b.v;
-  return Dual(q, (a.d - q * b.d) / b.v);
-}
-__device__ __forceinline__ bool operator<(Dual a, Dual b) { return a.v < b.v; }
-__device__ __forceinline__ bool operator<=(Dual a, Dual b) { return a.v <= b.v; }
-__device__ __forceinline__ Dual num_from(double x, Dual*) { return Dual(x); }
-__device__ __forceinline__ double num_to_double(Dual x) { return x.v; }
-__device__ __forceinline__ Dual num_sqrt(Dual x) {
-  const double s = sqrt(x.v);
-  return Dual(s, x.d / (2.0 * s));
-}
-__device__ __forceinline__ Dual num_fabs(Dual x) { return x.v < 0.0 ? -x : x; }
-__device__ __forceinline__ Dual num_fma(Dual a, Dual b, Dual c) {
-  return Dual(fma(a.v, b.v, c.v), a.v * b.d + a.d * b.v + c.d);
-}
-// the FP64 weight combination (product form, one division) on duals
-__device__ __forceinline__ Dual weno_combine(Dual bA, Dual bB, Dual bC, Dual qA, Dual qB, Dual qC,
-                                             Dual dA, Dual dB, Dual dC) {
-  const Dual eps(1e-6);
-  Dual aA = eps + bA, aB = eps + bB, aC = eps + bC;
-  aA = aA * aA;
-  aB = aB * aB;
-  aC = aC * aC;
-  const Dual tA = dA * (aB * aC), tB = dB * (aA * aC), tC = dC * (aA * aB);
-  return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
-}
-template <bool Plus>
-__device__ __forceinline__ Dual weno_safe(Dual f0, Dual f1, Dual f2_, Dual f3, Dual f4) {
-  return weno_side<Plus>(f0, f1, f2_, f3, f4);
-}
-
-// ------------------------------------------------------------------ shared stencil gather
-
-template <int DIR>
-__device__ __forceinline__ void ad_face_coords(long f, const Grid& g, long& i, long& j, long& k) {
-  const long ex = g.n[0] + (DIR == 0), ey = g.n[1] + (DIR == 1);
-  i = f % ex;
-  const long r = f / ex;
-  j = r % ey;
-  k = r / ey;
-}
-
-// cells and ghost signs of the six stencil points of face f (as face_flux_kernel)
-template <int DIR>
-__device__ __forceinline__ void stencil(const Grid& g, long f, long (&cell)[6], bool (&nall)[6],
-                                        bool (&nnorm)[6], long (&ijk)[3]) {
-  long i, j, k;
-  ad_face_coords<DIR>(f, g, i, j, k);
-  ijk[0] = i;
-  ijk[1] = j;
-  ijk[2] = k;
-#pragma unroll
-  for (int l = 0; l < 6; ++l) {
-    long q[3] = {i, j, k};
-    q[DIR] = ghost_src(q[DIR] - 3 + l, g.n[DIR], g.bc[2 * DIR], g.bc[2 * DIR + 1], &nall[l],
-                       &nnorm[l]);
-    cell[l] = q[0] + g.n[0] * (q[1] + g.n[1] * q[2]);
-  }
-}
-
-// the five fluid values of a stencil point in face order (normal momentum in slot 1), signed
-template <int DIR>
-__device__ __forceinline__ void load_point(const Fields& w, long c, bool nall, bool nnorm,
-                                           double (&W)[5]) {
-  double q[5];
-#pragma unroll
-  for (int v = 0; v < 5; ++v) q[v] = __ldg(w.f[v] + c);
-  if (nall) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) q[v] = -q[v];
-  }
-  if (nnorm) q[1 + DIR] = -q[1 + DIR];
-  W[0] = q[0];
-  W[1] = q[1 + DIR];
-  W[2] = (DIR == 1) ? q[1] : q[2];
-  W[3] = (DIR == 2) ? q[1] : q[3];
-  W[4] = q[4];
-}
-
-// ------------------------------------------------------------------ JVP
-
-template <int NCHEM, int DIR>
-__global__ void __launch_bounds__(128) face_flux_jvp_kernel(Grid g, Fields w, Fields dw,
-                                                            double* __restrict__ dF, long nfaces) {
-  Dual* tag = nullptr;
-  for (long f = blockIdx.x * (long)blockDim.x + threadIdx.x; f < nfaces;
-       f += (long)gridDim.x * blockDim.x) {
-    long cell[6], ijk[3];
-    bool nall[6], nnorm[6];
-    stencil<DIR>(g, f, cell, nall, nnorm, ijk);
-    Dual W[6][5];
-#pragma unroll
-    for (int l = 0; l < 6; ++l) {
-      double a[5], b[5];
-      load_point<DIR>(w, cell[l], nall[l], nnorm[l], a);
-      load_point<DIR>(dw, cell[l], nall[l], nnorm[l], b);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) W[l][v] = Dual(a[v], b[v]);
-    }
-    FaceState<Dual> S;
-    Dual out[5];
-    fluid_face_flux<Dual>(W, g.gamma, S, out);
-    double o[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) o[v] = out[v].d;
-    const double o1 = o[1];
-    o[1] = o[1 + DIR];
-    o[1 + DIR] = o1;
-#pragma unroll
-    for (int v = 0; v < 5; ++v) dF[v * nfaces + f] = o[v];
-#pragma unroll 1
-    for (int c = 0; c < NCHEM; ++c) {
-      Dual cv[6];
-#pragma unroll
-      for (int l = 0; l < 6; ++l) {
-        const double x = __ldg(w.f[5] + c + (long)NCHEM * cell[l]);
-        const double dx = __ldg(dw.f[5] + c + (long)NCHEM * cell[l]);
-        cv[l] = nall[l] ? Dual(-x, -dx) : Dual(x, dx);
-      }
-      dF[(5 + c) * nfaces + f] = tracer_face_flux<Dual>(S, cv).d;
-    }
-    (void)tag;
-  }
-}
-
-// jv = -sum_d (dF_{d,+} - dF_{d,-}) / d_d
-template <int NCHEM>
-__global__ void __launch_bounds__(256) divergence_lin_kernel(Grid g, Fields out,
-                                                             const double* __restrict__ Fx,
-                                                             const double* __restrict__ Fy,
-                                                             const double* __restrict__ Fz) {
-  const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  const long nfx = (nx + 1) * ny * nz, nfy = nx * (ny + 1) * nz, nfz = nx * ny * (nz + 1);
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < g.ncell;
-       c += (long)gridDim.x * blockDim.x) {
-    const long i = c % nx, r = c / nx, j = r % ny, k = r / ny;
-    const long fx = i + (nx + 1) * (j + ny * k);
-    const long fy = i + nx * (j + (ny + 1) * k);
-    const long fz = c;
-#pragma unroll
-    for (int v = 0; v < 5 + NCHEM; ++v) {
-      const double div = (Fx[v * nfx + fx + 1] - Fx[v * nfx + fx]) * g.inv_d[0] +
-                         (Fy[v * nfy + fy + nx] - Fy[v * nfy + fy]) * g.inv_d[1] +
-                         (Fz[v * nfz + fz + nx * ny] - Fz[v * nfz + fz]) * g.inv_d[2];
-      double* dst = (v < 5) ? (out.f[v] + c) : (out.f[5] + (v - 5) + (long)NCHEM * c);
-      *dst = -div;
-    }
-  }
-}
 
 // ------------------------------------------------------------------ VJP
 
@@ -654,50 +486,25 @@ __global__ void __launch_bounds__(256) vjp_gather_kernel(Grid g, const double* _
   }
 }
 
-// ------------------------------------------------------------------ launchers
-
-static int blocks_for(long n, int t) {
-  long b = (n + t - 1) / t;
-  const long cap = (long)kSM * 16;
-  return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
-}
-
-template <int NCHEM>
-static int jvp_t(const Grid& g, const Fields& w, const Fields& dw, const Fields& out,
-                 double* scratch, cudaStream_t s) {
-  const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  const long nf[3] = {(nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1)};
-  double* F[3] = {scratch, scratch + (long)(5 + NCHEM) * nf[0],
-                  scratch + (long)(5 + NCHEM) * (nf[0] + nf[1])};
-  ProfScope ps("jvp", s);
-  face_flux_jvp_kernel<NCHEM, 0><<<blocks_for(nf[0], 128), 128, 0, s>>>(g, w, dw, F[0], nf[0]);
-  GBMV_LAUNCH_CHECK("face_flux_jvp_kernel<x>");
-  face_flux_jvp_kernel<NCHEM, 1><<<blocks_for(nf[1], 128), 128, 0, s>>>(g, w, dw, F[1], nf[1]);
-  GBMV_LAUNCH_CHECK("face_flux_jvp_kernel<y>");
-  face_flux_jvp_kernel<NCHEM, 2><<<blocks_for(nf[2], 128), 128, 0, s>>>(g, w, dw, F[2], nf[2]);
-  GBMV_LAUNCH_CHECK("face_flux_jvp_kernel<z>");
-  divergence_lin_kernel<NCHEM><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g, out, F[0], F[1], F[2]);
-  GBMV_LAUNCH_CHECK("divergence_lin_kernel");
-  return GBMV_OK;
-}
+// ------------------------------------------------------------------ launcher
 
 template <int NCHEM>
 static int vjp_t(const Grid& g, const Fields& w, const Fields& v, const Fields& out, double* A,
                  cudaStream_t s) {
-  const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  const long nf[3] = {(nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1)};
+  long nf[3];
+  face_counts(g, nf);
   ProfScope ps("vjp", s);
-  face_flux_vjp_kernel<NCHEM, 0><<<blocks_for(nf[0], 128), 128, 0, s>>>(g, w, v, A, nf[0]);
+  face_flux_vjp_kernel<NCHEM, 0><<<sweep_blocks(nf[0], 128), 128, 0, s>>>(g, w, v, A, nf[0]);
   GBMV_LAUNCH_CHECK("face_flux_vjp_kernel<x>");
-  vjp_gather_kernel<NCHEM, 0><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g, A, out, nf[0], 1);
+  vjp_gather_kernel<NCHEM, 0><<<sweep_blocks(g.ncell, 256), 256, 0, s>>>(g, A, out, nf[0], 1);
   GBMV_LAUNCH_CHECK("vjp_gather_kernel<x>");
-  face_flux_vjp_kernel<NCHEM, 1><<<blocks_for(nf[1], 128), 128, 0, s>>>(g, w, v, A, nf[1]);
+  face_flux_vjp_kernel<NCHEM, 1><<<sweep_blocks(nf[1], 128), 128, 0, s>>>(g, w, v, A, nf[1]);
   GBMV_LAUNCH_CHECK("face_flux_vjp_kernel<y>");
-  vjp_gather_kernel<NCHEM, 1><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g, A, out, nf[1], 0);
+  vjp_gather_kernel<NCHEM, 1><<<sweep_blocks(g.ncell, 256), 256, 0, s>>>(g, A, out, nf[1], 0);
   GBMV_LAUNCH_CHECK("vjp_gather_kernel<y>");
-  face_flux_vjp_kernel<NCHEM, 2><<<blocks_for(nf[2], 128), 128, 0, s>>>(g, w, v, A, nf[2]);
+  face_flux_vjp_kernel<NCHEM, 2><<<sweep_blocks(nf[2], 128), 128, 0, s>>>(g, w, v, A, nf[2]);
   GBMV_LAUNCH_CHECK("face_flux_vjp_kernel<z>");
-  vjp_gather_kernel<NCHEM, 2><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g, A, out, nf[2], 0);
+  vjp_gather_kernel<NCHEM, 2><<<sweep_blocks(g.ncell, 256), 256, 0, s>>>(g, A, out, nf[2], 0);
   GBMV_LAUNCH_CHECK("vjp_gather_kernel<z>");
   return GBMV_OK;
 }
@@ -708,18 +515,6 @@ size_t feuler_vjp_scratch_doubles(const Grid& g) {
   if (nx * (ny + 1) * nz > m) m = nx * (ny + 1) * nz;
   if (nx * ny * (nz + 1) > m) m = nx * ny * (nz + 1);
   return (size_t)6 * (5 + g.nchem) * (size_t)m;
-}
-
-int feuler_jvp(const Grid& g, const Fields& w, const Fields& dw, const Fields& out,
-               double* scratch, cudaStream_t s) {
-  switch (g.nchem) {
-    case 0: return jvp_t<0>(g, w, dw, out, scratch, s);
-    case 2: return jvp_t<2>(g, w, dw, out, scratch, s);
-    case 4: return jvp_t<4>(g, w, dw, out, scratch, s);
-    case 6: return jvp_t<6>(g, w, dw, out, scratch, s);
-    case 10: return jvp_t<10>(g, w, dw, out, scratch, s);
-    default: return GBMV_EUNSUPPORTED;
-  }
 }
 
 int feuler_vjp(const Grid& g, const Fields& w, const Fields& v, const Fields& out, double* A,
