@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--no-sod", action="store_true", help="skip the Sod whole-run measurement")
     p.add_argument("--mri-n", type=int, default=128,
                    help="multirate time-to-t_f measurement on mri_n^3 x 15 (0 = skip)")
+    p.add_argument("--imex-n", type=int, default=64,
+                   help="ARK-IMEX time-to-t_f measurement on imex_n^3 x 15 (0 = skip)")
+    p.add_argument("--imex-tf", type=float, default=4e-6)
     p.add_argument("--ad-n", type=int, default=96,
                    help="differentiation measurement on ad_n^3 x 9 fields (0 = skip)")
     p.add_argument("--dirk-only", action="store_true",
@@ -560,6 +563,12 @@ def run_gbmv(args):
         fs = None
         torch.cuda.empty_cache()
         line["multirate"] = run_mri(torch, gbmv, args.mri_n)
+    if args.imex_n > 0:
+        for r in res.values():
+            r["fs"] = None
+        fs = None
+        torch.cuda.empty_cache()
+        line["imex"] = run_imex(torch, gbmv, args.imex_n, args.imex_tf, not args.no_cpu_baseline)
     if args.ad_n > 0:
         for r in res.values():
             r["fs"] = None
@@ -729,6 +738,74 @@ def run_mri(torch, gbmv, n):
     out["mixed_vs_fp64_maxnorm_err"] = errs
     out["speedup_mixed_vs_fp64"] = round(out["forms"]["fp64"]["s_to_tf"] /
                                          out["forms"]["mixed"]["s_to_tf"], 3)
+    return out
+
+
+IMEX_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bias=2.0,
+                 growth=2.0)
+
+
+def run_imex(torch, gbmv, n, tf, with_cpu):
+    """ARK-IMEX chemistry-hydrodynamics to t_f on the chem_hydro state (integrate.ark_imex_evolve
+    over integrate.ChemHydroImex: ARK3(2)4L[2]SA, WENO explicit, chemistry implicit with the
+    FP64 Jacobian and block LU, device WRMS norms; the reference IMEX inputs' step control),
+    with the FP64 and the GBMV_MIXED_FAST explicit RHS: time-to-t_f, step and solver
+    statistics, their max-normalised difference; the oracle-driven run of the same driver on
+    an 8x6x5 sample on one host core beside it."""
+    import h5tables
+    import integrate
+    import workloads as W
+    wl = W.chem_hydro(n=n)
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    tables = h5tables.load_table_block(TABLES)
+    out = {"workload": (f"chem_hydro {n}^3 x 15 to t_f = {tf} x 1e11 s, ARK3(2)4L[2]SA IMEX "
+                        "(WENO explicit, chemistry implicit), rtol 1e-6 atol 1e-10, maxcor 10, "
+                        "nlscoef 0.01, I controller safety 0.99 bias 2 growth 2"), "forms": {}}
+    finals = {}
+    for name, prec in (("fp64", gbmv.FP64), ("mixed_fast", gbmv.MIXED_FAST)):
+        hy = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"])
+        c = gbmv.Chem(n ** 3, tables)
+        c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
+        w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+        prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, IMEX_OPTS["rtol"], IMEX_OPTS["atol"],
+                                       prec)
+        wc = [x.clone() for x in w]  # warm-up on a copy (allocations)
+        integrate.ark_imex_evolve(prob, 0.0, tf * 1e-3, wc, max_steps=50, **IMEX_OPTS)
+        c.state("Ts").fill_(1000.0)
+        del wc
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = integrate.ark_imex_evolve(prob, 0.0, tf, w, **IMEX_OPTS)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        finals[name] = [x.cpu().numpy() for x in w]
+        out["forms"][name] = {"s_to_tf": round(dt, 3), "steps": st.steps,
+                              "attempts": st.attempts, "error_test_fails": st.netf,
+                              "newton_fails": st.ncf, "newton_iters": st.nni,
+                              "setups": st.nsetups, "fe_evals": st.nfe, "fi_evals": st.nfi,
+                              "Mcell_steps_per_s": round(n ** 3 * st.steps / dt / 1e6, 4)}
+        del hy, c, w, prob
+        torch.cuda.empty_cache()
+    errs = {}
+    for nm, a, b in zip(["rho", "mx", "my", "mz", "et", "chem"], finals["mixed_fast"],
+                        finals["fp64"]):
+        errs[nm] = float(f"{float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)):.3e}")
+    out["mixed_fast_vs_fp64_maxnorm_err"] = errs
+    out["speedup_mixed_fast_vs_fp64"] = round(out["forms"]["fp64"]["s_to_tf"] /
+                                              out["forms"]["mixed_fast"]["s_to_tf"], 3)
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py as O
+        sw = W.chem_hydro(shape=(8, 6, 5))
+        y = [f.copy() for f in sw["fields"]]
+        prob = O.ImexChemHydro(sw, tables, sw["units"]["EnergyUnits"],
+                               sw["units"]["TimeUnits"], IMEX_OPTS["rtol"], IMEX_OPTS["atol"])
+        t0 = time.perf_counter()
+        st = integrate.ark_imex_evolve(prob, 0.0, tf, y, **IMEX_OPTS)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"Mcell_steps_per_s": round(240 * st.steps / dt / 1e6, 6),
+                               "s_to_tf": round(dt, 3), "steps": st.steps, "cores": 1,
+                               "kind": "port", "sample": "8x6x5 cells of the same workload"}
     return out
 
 

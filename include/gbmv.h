@@ -148,6 +148,15 @@ int gbmv_pack1d(gbmv_hydro h, const double* const* w, int dir, double* out, void
 int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
                       double energy_factor, double* totals, void* stream);
 
+/* N_VWrmsNorm of a ManyVector with ARKODE's error weights (the norm ARKStep's error test and
+ * its Newton convergence test take after ARKStepSVtolerances, src/imex_chem_hydro_main.cpp:463,
+ * and the MRIStep / ERKStep equivalents): *norm = sqrt(sum (v_i ewt_i)^2 / N), ewt_i =
+ * 1 / (rtol |y_i| + atol), over the five fluid fields and the chemistry field of the handle's
+ * grid (N = (5 + nchem) ncells).  FP64, compensated and deterministic.  norm is host memory;
+ * synchronous.  Returns 0, or GBMV_EINVAL for null pointers or rtol, atol < 0 (or both 0). */
+int gbmv_wrms_norm(gbmv_hydro h, const double* const* v, const double* const* y, double rtol,
+                   double atol, double* norm, void* stream);
+
 /* -------------------------------------------------------------- chemistry (part b) */
 
 typedef struct gbmv_chem_s* gbmv_chem;

@@ -7,6 +7,7 @@ baseline legs, never by the product path.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -175,6 +176,68 @@ def block_newton_solve(J: np.ndarray, gamma: float, b: np.ndarray):
     bad = lib().orc_block_newton_solve(C.c_long(b.size // 10), _ptr(J), C.c_double(gamma),
                                        _ptr(b), _ptr(x))
     return int(bad), x
+
+
+class ImexChemHydro:
+    """The IMEX callbacks of src/imex_chem_hydro_main.cpp over the oracle, in the problem
+    protocol of the package's ARK-IMEX driver (fe, fi, setup, solve, norm, postprocess):
+    fexpl (:910-1000: et from the physical gas energy, fEuler on the physical chemistry, the et
+    tendency moved to the gas-energy slot, the in-place scale / unscale round trip of the
+    chemistry component), its chemistry tendency converted to the scaled variables (species
+    / scale, gas energy x EnergyUnits / scale); fimpl (:811-848, TimeUnits x the source);
+    Jimpl (:850-908, TimeUnits x J) with I - gamma J solved per block by orc_block_newton_solve
+    (the BDMPIMV solver, :1075-1194); PostprocessStep (:1002-1051); WRMS norms with weights
+    1 / (rtol |y| + atol).  `wl` holds bc, gamma and the per-entry scale."""
+
+    def __init__(self, wl, tables, eu, tu, rtol, atol):
+        self.wl, self.eu, self.tu = wl, eu, tu
+        self.rtol, self.atol = rtol, atol
+        self.scale = wl["scale"]
+        self.oc = Chem(tables, self.scale.reshape(-1))
+        self.inv = 1.0 / self.scale
+        self.J, self.g = None, None
+
+    def _sync(self, y):
+        phys = y[5] * self.scale
+        y[4][...] = phys[..., 9] * (1.0 / self.eu) + 0.5 / y[0] * (
+            y[1] * y[1] + y[2] * y[2] + y[3] * y[3])
+        return phys
+
+    def fe(self, t, y):
+        phys = self._sync(y)
+        st, out = feuler(y[:5] + [phys], 10, self.wl["bc"], self.wl["gamma"], None)
+        if st != 0:
+            raise RuntimeError("fexpl: illegal state")
+        out[5][..., 9] = out[4]
+        out[4][:] = 0.0
+        y[5][...] = phys / self.scale
+        out[5][..., :9] = out[5][..., :9] * self.inv[..., :9]
+        out[5][..., 9] = out[5][..., 9] * (self.inv[..., 9] * self.eu)
+        return out
+
+    def fi(self, t, y):
+        f = self.oc.rhs(y[5].reshape(-1)) * self.tu
+        return [None] * 5 + [f.reshape(y[5].shape)]
+
+    def setup(self, t, y, gamma):
+        self.J = self.oc.jac(y[5].reshape(-1)) * self.tu
+        self.g = gamma
+        return 0
+
+    def solve(self, b):
+        bad, x = block_newton_solve(self.J, self.g, b[5].reshape(-1))
+        if bad:
+            raise RuntimeError("singular Newton block")
+        return list(b[:5]) + [x.reshape(b[5].shape)]
+
+    def norm(self, v, y):
+        s = sum(float(((a * (1.0 / (self.rtol * np.abs(w) + self.atol))) ** 2).sum())
+                for a, w in zip(v, y))
+        return math.sqrt(s / sum(w.size for w in y))
+
+    def postprocess(self, t, y):
+        phys = self._sync(y)
+        y[5][...] = phys / self.scale
 
 
 # ---------------------------------------------------------------- reference build (here only)

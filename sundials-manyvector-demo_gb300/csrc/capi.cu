@@ -869,6 +869,23 @@ int gbmv_pack1d(gbmv_hydro h, const double* const* w, int dir, double* out, void
   return pack1d(h->g, W, dir, out, (cudaStream_t)stream);
 }
 
+// the reduction scratch of a hydro handle (conservation totals, WRMS norms), allocated on
+// first use
+static int reduction_scratch(gbmv_hydro h, cudaStream_t s, const char* who) {
+  if (h->cons) return GBMV_OK;
+  if (capturing(s)) {
+    set_error("the first %s call on a handle allocates its buffer: make it before any stream "
+              "capture", who);
+    return GBMV_EINVAL;
+  }
+  if (cudaMalloc(&h->cons, conservation_scratch_doubles() * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    h->cons = nullptr;
+    return check_cuda(cudaErrorMemoryAllocation, "reduction scratch");
+  }
+  return GBMV_OK;
+}
+
 int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
                       double energy_factor, double* totals, void* stream) {
   if (!h || !fields_ok(w, 0) || !totals) {
@@ -876,18 +893,7 @@ int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
     return GBMV_EINVAL;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  if (!h->cons) {
-    if (capturing(s)) {
-      set_error("the first gbmv_conservation call on a handle allocates its buffer: make it "
-                "before any stream capture");
-      return GBMV_EINVAL;
-    }
-    if (cudaMalloc(&h->cons, conservation_scratch_doubles() * sizeof(double)) != cudaSuccess) {
-      cudaGetLastError();
-      h->cons = nullptr;
-      return check_cuda(cudaErrorMemoryAllocation, "conservation scratch");
-    }
-  }
+  if (int rc = reduction_scratch(h, s, "gbmv_conservation")) return rc;
   Fields W;
   for (int v = 0; v < 6; ++v) W.f[v] = (v < 5) ? const_cast<double*>(w[v]) : nullptr;
   int rc = conservation_sums(h->g, W, h->cons, s);
@@ -898,6 +904,31 @@ int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
   GBMV_CUDA_TRY(cudaStreamSynchronize(s));
   totals[0] = t[0] * mass_factor;
   totals[1] = t[1] * energy_factor;
+  return GBMV_OK;
+}
+
+int gbmv_wrms_norm(gbmv_hydro h, const double* const* v, const double* const* y, double rtol,
+                   double atol, double* norm, void* stream) {
+  if (!h || !fields_ok(v, h->g.nchem) || !fields_ok(y, h->g.nchem) || !norm) {
+    set_error("null handle, field or output pointer");
+    return GBMV_EINVAL;
+  }
+  if (!(rtol >= 0.0) || !(atol >= 0.0) || !(rtol > 0.0 || atol > 0.0)) {
+    set_error("rtol, atol must be >= 0 and not both 0");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (int rc = reduction_scratch(h, s, "gbmv_wrms_norm")) return rc;
+  Fields V, Y;
+  for (int k = 0; k < 6; ++k) {
+    V.f[k] = const_cast<double*>(v[k]);
+    Y.f[k] = const_cast<double*>(y[k]);
+  }
+  int rc = wrms_norm(h->g, V, Y, rtol, atol, h->cons, s);
+  if (rc) return rc;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(norm, h->cons + conservation_scratch_doubles() - 2,
+                                sizeof(double), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
   return GBMV_OK;
 }
 

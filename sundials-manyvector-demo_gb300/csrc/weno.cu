@@ -287,6 +287,60 @@ int conservation_sums(const Grid& g, const Fields& w, double* d_scratch, cudaStr
 
 size_t conservation_scratch_doubles() { return 2 * kConsBlocks + 2; }
 
+// N_VWrmsNorm of the six-component ManyVector (the norm ARKODE's error test and Newton
+// convergence test take, src/imex_chem_hydro_main.cpp:463): ewt = 1 / (rtol |y| + atol) per
+// entry, sum of (v ewt)^2 over the five fluid fields (ncell each) and the chemistry field
+// (nchem ncell), divided by the total length, square root.  Same fixed-grid compensated
+// two-pass reduction as the conservation totals; partials in scratch[0..kConsBlocks), result
+// in scratch[2 kConsBlocks].
+__global__ void __launch_bounds__(256) wrms_partial_kernel(long ncell, int nchem, Fields v,
+                                                           Fields y, double rtol, double atol,
+                                                           double* __restrict__ part) {
+  double s0 = 0.0, c0 = 0.0;
+  for (int k = 0; k < 6; ++k) {
+    const long n = (k < 5) ? ncell : (long)nchem * ncell;
+    const double* __restrict__ vk = v.f[k];
+    const double* __restrict__ yk = y.f[k];
+    if (n == 0) continue;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+      const double ew = 1.0 / (rtol * fabs(yk[i]) + atol);
+      const double q = vk[i] * ew;
+      two_sum_acc(s0, c0, q * q);
+    }
+  }
+  double a = s0 + c0;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
+  __shared__ double wa[8];
+  if ((threadIdx.x & 31) == 0) wa[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) ta += wa[k];
+    part[blockIdx.x] = ta;
+  }
+}
+
+__global__ void wrms_final_kernel(const double* __restrict__ part, double ntotal,
+                                  double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, c0 = 0.0;
+    for (int k = 0; k < kConsBlocks; ++k) two_sum_acc(s0, c0, part[k]);
+    out[0] = sqrt((s0 + c0) / ntotal);
+  }
+}
+
+int wrms_norm(const Grid& g, const Fields& v, const Fields& y, double rtol, double atol,
+              double* d_scratch, cudaStream_t s) {
+  wrms_partial_kernel<<<kConsBlocks, 256, 0, s>>>(g.ncell, g.nchem, v, y, rtol, atol, d_scratch);
+  GBMV_LAUNCH_CHECK("wrms_partial_kernel");
+  const double ntotal = (double)(5 + g.nchem) * (double)g.ncell;
+  wrms_final_kernel<<<1, 32, 0, s>>>(d_scratch, ntotal, d_scratch + 2 * kConsBlocks);
+  GBMV_LAUNCH_CHECK("wrms_final_kernel");
+  return GBMV_OK;
+}
+
 int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s) {
   long b = (g.ncell + 255) / 256;
   if (b > (long)kSM * 8) b = (long)kSM * 8;

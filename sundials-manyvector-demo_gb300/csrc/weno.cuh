@@ -29,6 +29,10 @@ int pack1d(const Grid& g, const Fields& w, int dir, double* out, cudaStream_t s)
 // totals of rho and et into d_scratch[2 * 1024 + 0..1] (scratch: conservation_scratch_doubles)
 size_t conservation_scratch_doubles();
 int conservation_sums(const Grid& g, const Fields& w, double* d_scratch, cudaStream_t s);
+// ManyVector WRMS norm of v with weights 1 / (rtol |y| + atol) into
+// d_scratch[conservation_scratch_doubles() - 2] (scratch: conservation_scratch_doubles)
+int wrms_norm(const Grid& g, const Fields& v, const Fields& y, double rtol, double atol,
+              double* d_scratch, cudaStream_t s);
 
 // derivatives of the FP64 flux divergence (weno_jvp.cu, weno_vjp.cu)
 size_t feuler_vjp_scratch_doubles(const Grid& g);

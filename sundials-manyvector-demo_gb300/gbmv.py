@@ -63,6 +63,8 @@ SIGNATURES = [
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
     ("gbmv_pack1d", C.c_int, [_VP, C.POINTER(_VP), C.c_int, _VP, _VP]),
     ("gbmv_conservation", C.c_int, [_VP, C.POINTER(_VP), C.c_double, C.c_double, _P, _VP]),
+    ("gbmv_wrms_norm", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.c_double, C.c_double,
+                                 _P, _VP]),
     ("gbmv_feuler_jvp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
                                   C.POINTER(_VP), _VP]),
     ("gbmv_feuler_vjp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
@@ -221,6 +223,13 @@ class Hydro:
         _check(load().gbmv_conservation(self.h, _vec(w), mass_factor, energy_factor, out,
                                         _stream_ptr(stream)), "gbmv_conservation")
         return out[0], out[1]
+
+    def wrms_norm(self, v, y, rtol, atol, stream=None) -> float:
+        """ARKODE's WRMS norm of the ManyVector v with weights 1 / (rtol |y| + atol)."""
+        out = (C.c_double * 1)()
+        _check(load().gbmv_wrms_norm(self.h, _vec(v), _vec(y), rtol, atol, out,
+                                     _stream_ptr(stream)), "gbmv_wrms_norm")
+        return out[0]
 
     def fEuler_jvp(self, t, w, dw, jv, stream=None) -> int:
         """jv = (d fEuler / d w) dw (FP64 form, forward mode)."""

@@ -213,3 +213,281 @@ def mri_erk22b_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units,
         res.slow_steps += 1
         t = t_end
     return res
+
+
+# ---------------------------------------------------------------------------- ARK-IMEX
+#
+# ARK3(2)4L[2]SA, the additive Runge-Kutta pair of C. A. Kennedy and M. H. Carpenter,
+# Appl. Numer. Math. 44 (2003) 139-181: explicit ERK and stiffly accurate ESDIRK sharing the
+# abscissae c and the weights b, third order with a second-order embedding, diagonal gamma
+# = 1767732205903 / 4055673282236.  Rows of AI include the diagonal entry.
+_AG = 1767732205903 / 4055673282236
+ARK324 = {
+    "name": "ARK3(2)4L[2]SA",
+    "q": 3,  # method order
+    "p": 2,  # embedding order
+    "c": [0.0, 1767732205903 / 2027836641118, 3 / 5, 1.0],
+    "ae": [[],
+           [1767732205903 / 2027836641118],
+           [5535828885825 / 10492691773637, 788022342437 / 10882634858940],
+           [6485989280629 / 16251701735622, -4246266847089 / 9704473918619,
+            10755448449292 / 10357097424841]],
+    "ai": [[0.0],
+           [_AG, _AG],
+           [2746238789719 / 10658868560708, -640167445237 / 6845629431997, _AG],
+           [1471266399579 / 7840856788654, -4482444167858 / 7529755066697,
+            11266239266428 / 11593286722821, _AG]],
+    "b": [1471266399579 / 7840856788654, -4482444167858 / 7529755066697,
+          11266239266428 / 11593286722821, _AG],
+    "bhat": [2756255671327 / 12835298489170, -10771552573575 / 22201958757719,
+             9247589265047 / 10645013368117, 2193209047091 / 5459859503100],
+}
+
+
+class ImexResult:
+    def __init__(self):
+        self.steps = 0       # accepted steps
+        self.attempts = 0    # step attempts
+        self.netf = 0        # error-test failures
+        self.ncf = 0         # nonlinear (Newton) convergence failures
+        self.nni = 0         # Newton iterations
+        self.nsetups = 0     # Newton-matrix setups (Jacobian + factorisation)
+        self.nfe = 0         # explicit RHS evaluations
+        self.nfi = 0         # implicit RHS evaluations
+        self.h_last = 0.0
+
+
+def _combo(base, terms):
+    """base + sum coef * vec over ManyVector component lists (None components are zero);
+    base None: the sum alone."""
+    out = []
+    for k in range(len(terms[0][1]) if base is None else len(base)):
+        acc = None if base is None else base[k]
+        for coef, vec in terms:
+            v = vec[k]
+            if v is not None and coef != 0.0:
+                acc = coef * v if acc is None else acc + coef * v
+        out.append(acc)
+    return out
+
+
+def _clone(x):
+    return x.clone() if hasattr(x, "clone") else x.copy()
+
+
+def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.inf,
+                    fixed_h=0.0, safety=0.96, bias=1.5, growth=20.0, etamx1=1e4, etamxf=0.3,
+                    small_nef=2, etacf=0.25, maxnef=7, maxncf=10, maxcor=3, nlscoef=0.1,
+                    crdown=0.3, rdiv=2.3, dgmax=0.2, msbp=20, max_steps=5000, table=ARK324):
+    """Adaptive additive Runge-Kutta (IMEX) integration of y' = fe(t, y) + fi(t, y) from t0 to
+    tf, the ARKStep configuration of src/imex_chem_hydro_main.cpp:337-475 (fexpl explicit,
+    fimpl implicit, the block-diagonal direct solver on the chemistry subvector, a
+    PostprocessStep after every step).  `y` is a list of ManyVector components (numpy arrays
+    or torch tensors) advanced in place; `prob` supplies
+
+      fe(t, y) -> list               explicit RHS (may rewrite dependent fields of y, as the
+                                     reference's fexpl rewrites et)
+      fi(t, y) -> list               implicit RHS, None for components it does not touch
+      setup(t, y, gamma) -> int      form and factor M = I - gamma dfi/dy at y (0 ok, > 0 a
+                                     recoverable failure such as a singular block)
+      solve(b) -> list               M^{-1} b (identity on the components fi does not touch)
+      norm(v, y) -> float            WRMS norm of v with weights 1 / (rtol |y| + atol)
+      postprocess(t, y)              optional, after every accepted step
+
+    Each implicit stage z = a + gamma fi(t_i, z) is solved by modified Newton from the trivial
+    predictor z = y_n with ARKODE's rules: matrix set up again when gamma moved by more than
+    dgmax since the last setup, after msbp steps, or after a convergence failure with a matrix
+    from an earlier step; correction scaled by 2 / (1 + gamma / gamma_p) against a lagged
+    matrix; rate estimate crate = max(crdown crate, del / del_p); converged when
+    min(1, crate) del / nlscoef <= 1; divergence when del > rdiv del_p; at most maxcor
+    iterations; a failure with a current matrix cuts the step by etacf.  Error control: WRMS
+    norm dsm of the embedded difference with weights from y_n, accepted when dsm <= 1; I
+    controller eta = safety (bias dsm)^(-1/p) (p the embedding order, ARKODE's convention),
+    bounded by etamx1 on the first step and growth after, kept at 1 inside [1, 1.5) (the
+    matrix-reuse window) and after a failure, at least 0.1, at most etamxf after small_nef
+    error failures in one step; h <= hmax.  fixed_h > 0 takes fixed steps without error
+    control.  Defaults are ARKODE's; the reference's IMEX inputs use safety 0.99, bias 2,
+    growth 2, maxcor 10, nlscoef 0.01.  Returns an ImexResult; raises RuntimeError when a step
+    cannot be completed."""
+    st = ImexResult()
+    ae, ai, c = table["ae"], table["ai"], table["c"]
+    b, bh = table["b"], table["bhat"]
+    e = [x - xh for x, xh in zip(b, bh)]
+    ns = len(c)
+    kexp = -1.0 / table["p"]
+    post = getattr(prob, "postprocess", None)
+    t = t0
+    gp, nst_lp, crate = 0.0, 0, 1.0
+    force_setup, jcur = True, False
+    F0 = None  # (Fe, Fi) at (t, y), kept across retries of a step
+    h = fixed_h if fixed_h > 0.0 else h0
+    first = True
+    nef_s = ncf_s = 0
+    while t < tf:
+        if st.attempts >= max_steps:
+            raise RuntimeError("ark_imex_evolve: max_steps attempts reached")
+        if F0 is None:
+            F0 = (prob.fe(t, y), prob.fi(t, y))
+            st.nfe += 1
+            st.nfi += 1
+        if h <= 0.0:  # initial step from the size of the full RHS at t0
+            fn = prob.norm(_combo(F0[0], [(1.0, F0[1])]), y)
+            h = 0.5 / fn if fn > 0.0 else tf - t
+        h = min(h, hmax)
+        last = tf - t <= h * (1.0 + 1e-8)  # stretch a step by a rounding sliver onto tf
+        if last:
+            h = tf - t
+        st.attempts += 1
+        Fe, Fi = [F0[0]], [F0[1]]
+        conv_fail = False
+        for i in range(1, ns):
+            ti = t + c[i] * h
+            gam = h * ai[i][i]
+            a = _combo(y, [(h * ae[i][j], Fe[j]) for j in range(i)] +
+                       [(h * ai[i][j], Fi[j]) for j in range(i)])
+            z = [_clone(x) for x in y]  # trivial predictor
+            m, delp = 0, 0.0
+            while True:
+                fiz = prob.fi(ti, z)
+                st.nfi += 1
+                if force_setup or st.steps >= nst_lp + msbp or not abs(gam / gp - 1.0) <= dgmax:
+                    rc = prob.setup(ti, z, gam)
+                    st.nsetups += 1
+                    gp, nst_lp, crate = gam, st.steps, 1.0
+                    jcur, force_setup = True, False
+                    if rc != 0:
+                        conv_fail = True
+                        break
+                r = _combo(a, [(-1.0, z), (gam, fiz)])
+                d = prob.solve(r)
+                if gam != gp:
+                    sc = 2.0 / (1.0 + gam / gp)
+                    d = [x * sc for x in d]
+                z = _combo(z, [(1.0, d)])
+                dn = prob.norm(d, y)
+                m += 1
+                st.nni += 1
+                if m > 1:
+                    crate = max(crdown * crate, dn / delp)
+                if min(crate, 1.0) * dn / nlscoef <= 1.0:
+                    break
+                if (m > 1 and dn > rdiv * delp) or m >= maxcor or not math.isfinite(dn):
+                    conv_fail = True
+                    break
+                delp = dn
+            if conv_fail:
+                break
+            Fe.append(prob.fe(ti, z))
+            Fi.append(prob.fi(ti, z))
+            st.nfe += 1
+            st.nfi += 1
+        if conv_fail:
+            st.ncf += 1
+            ncf_s += 1
+            if ncf_s >= maxncf:
+                raise RuntimeError("ark_imex_evolve: too many Newton failures in one step")
+            if fixed_h > 0.0:
+                raise RuntimeError("ark_imex_evolve: Newton failure at a fixed step")
+            if jcur:
+                h *= etacf
+            else:
+                force_setup = True
+            continue
+        F = [_combo(fe_, [(1.0, fi_)]) for fe_, fi_ in zip(Fe, Fi)]
+        ynew = _combo(y, [(h * b[j], F[j]) for j in range(ns)])
+        if fixed_h > 0.0:
+            dsm = 0.0
+        else:
+            err = _combo(None, [(h * e[j], F[j]) for j in range(ns)])
+            dsm = prob.norm(err, y)
+            if not math.isfinite(dsm):
+                dsm = 1e10
+        if dsm <= 1.0:
+            t = tf if last else t + h
+            for k in range(len(y)):
+                if hasattr(y[k], "copy_"):
+                    y[k].copy_(ynew[k])
+                else:
+                    y[k][...] = ynew[k]
+            st.steps += 1
+            st.h_last = h
+            if post is not None:
+                post(t, y)
+            F0 = None
+            jcur = False
+            if fixed_h > 0.0:
+                h = fixed_h
+            else:
+                eta = safety * max(bias * dsm, 1e-10) ** kexp
+                eta = min(eta, etamx1 if first else growth)
+                if nef_s > 0 or ncf_s > 0:
+                    eta = min(eta, 1.0)
+                if 1.0 <= eta < 1.5:
+                    eta = 1.0
+                eta = max(eta, 0.1)
+                h = min(h * eta, hmax)
+            first = False
+            nef_s = ncf_s = 0
+        else:
+            st.netf += 1
+            nef_s += 1
+            if nef_s >= maxnef:
+                raise RuntimeError("ark_imex_evolve: too many error-test failures in one step")
+            eta = max(0.1, min(1.0, safety * max(bias * dsm, 1e-10) ** kexp))
+            if nef_s >= small_nef:
+                eta = min(eta, etamxf)
+            h *= eta
+    return st
+
+
+class ChemHydroImex:
+    """The reference's IMEX splitting (src/imex_chem_hydro_main.cpp) over the drop-in entry
+    points, all on the device: fe = fexpl (WENO flux divergence of every field and the
+    gas-energy coupling, :910-1000; its chemistry tendency converted to the scaled variables
+    by `scaled_forcing`, as the multirate driver does), fi = fimpl (TimeUnits x the chemistry
+    source on component 5, zero on the fluid, :811-848), the Newton matrix I - gamma Jimpl
+    (:850-908) from gbmv_chem_jac + gbmv_block_form_newton, factored and solved by the
+    block-diagonal LU (SUNLinSol_BDMPIMV, :1075-1194), PostprocessStep after every step
+    (:1002-1051), WRMS norms by gbmv_wrms_norm.  `precision` selects the fexpl form."""
+
+    def __init__(self, gbmv, hydro, chem, energy_units, time_units, rtol, atol, precision=0):
+        import torch
+        self.g, self.hydro, self.chem = gbmv, hydro, chem
+        self.eu, self.tu = energy_units, time_units
+        self.rtol, self.atol = rtol, atol
+        self.precision = precision
+        n = chem.n
+        self.J = torch.empty(100 * n, dtype=torch.float64, device="cuda")
+        self.ls = gbmv.BlockLinearSolver(n)
+        self.inv_scale = chem.state("inv_scale").view(-1, 10)
+
+    def fe(self, t, y):
+        import torch
+        out = [torch.empty_like(x) for x in y]
+        if self.g.fexpl(self.hydro, self.chem, t, y, out, self.eu, self.precision) != 0:
+            raise RuntimeError("fexpl: illegal state")
+        scaled_forcing(out[5].view(-1, 10), self.inv_scale, self.eu)
+        return out
+
+    def fi(self, t, y):
+        import torch
+        f = torch.empty_like(y[5])
+        self.chem.calculate_rhs_cvklu(t, y[5].view(-1), f.view(-1), self.tu)
+        return [None] * 5 + [f]
+
+    def setup(self, t, y, gamma):
+        self.chem.calculate_jacobian_cvklu(t, y[5].view(-1), self.J, self.tu)
+        self.g.form_newton_matrix(self.J, gamma)
+        return self.ls.setup(self.J)
+
+    def solve(self, b):
+        import torch
+        x = torch.empty_like(b[5])
+        self.ls.solve(self.J, x.view(-1), b[5].view(-1))
+        return list(b[:5]) + [x]
+
+    def norm(self, v, y):
+        return self.hydro.wrms_norm(v, y, self.rtol, self.atol)
+
+    def postprocess(self, t, y):
+        self.g.PostprocessStep(self.hydro, self.chem, y, self.eu)

@@ -1,0 +1,93 @@
+"""ARK-IMEX chemistry-hydrodynamics integration on the GPU (integrate.ark_imex_evolve over
+integrate.ChemHydroImex: fexpl, fimpl, Jimpl + block LU, PostprocessStep, device WRMS norms)
+against the same driver over the oracle (the oracle's fEuler with the reference's fexpl glue,
+chemistry source and Jacobian, dense per-block Newton solves, numpy norms); and the device
+WRMS norm against numpy."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+import workloads as W
+from conftest import maxnorm_err
+
+pytestmark = pytest.mark.gpu
+OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bias=2.0, growth=2.0)
+
+
+def _gpu_problem(torch, wl, tables, eu, tu, precision=0):
+    import gbmv
+    import integrate
+    nz, ny, nx = wl["fields"][0].shape
+    hy = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"])
+    c = gbmv.Chem(nx * ny * nz, tables)
+    c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, OPTS["rtol"], OPTS["atol"], precision)
+    return hy, prob, w
+
+
+def test_wrms_norm_matches_numpy(cuda):
+    torch = cuda
+    import gbmv
+    rng = np.random.default_rng(7)
+    shape = (6, 5, 7)
+    hy = gbmv.Hydro(shape[::-1], 10, (0,) * 6, 1.4)
+    v = [rng.standard_normal(shape) for _ in range(5)] + [rng.standard_normal(shape + (10,))]
+    y = [rng.standard_normal(shape) * 10.0 ** rng.integers(-8, 8, size=shape) for _ in range(5)]
+    y.append(rng.standard_normal(shape + (10,)))
+    for rtol, atol in ((1e-6, 1e-10), (1e-3, 0.0), (0.0, 1.0)):
+        ref = math.sqrt(sum(float(((a * (1.0 / (rtol * np.abs(b) + atol))) ** 2).sum())
+                            for a, b in zip(v, y)) / (15 * np.prod(shape)))
+        got = hy.wrms_norm([torch.from_numpy(a).cuda() for a in v],
+                           [torch.from_numpy(b).cuda() for b in y], rtol, atol)
+        assert abs(got - ref) <= 1e-14 * ref, (rtol, atol)
+    zero = [torch.zeros_like(torch.from_numpy(a)).cuda() for a in v]
+    assert hy.wrms_norm(zero, [torch.from_numpy(b).cuda() for b in y], 1e-6, 1e-10) == 0.0
+    with pytest.raises(Exception):
+        hy.wrms_norm(zero, zero, 0.0, 0.0)
+
+
+def test_imex_fp64_matches_oracle_driven_run(cuda, tables):
+    torch = cuda
+    import integrate
+    wl = W.chem_hydro(shape=(8, 6, 5))
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    tf = 4e-6
+    y_ref = [f.copy() for f in wl["fields"]]
+    oracle_prob = O.ImexChemHydro(wl, tables, eu, tu, OPTS["rtol"], OPTS["atol"])
+    st_ref = integrate.ark_imex_evolve(oracle_prob, 0.0, tf, y_ref, **OPTS)
+    _, prob, w = _gpu_problem(torch, wl, tables, eu, tu)
+    st = integrate.ark_imex_evolve(prob, 0.0, tf, w, **OPTS)
+    torch.cuda.synchronize()
+    got = [x.cpu().numpy() for x in w]
+    # the same step sequence, then the same states to well inside the tolerance
+    assert (st.steps, st.netf, st.ncf) == (st_ref.steps, st_ref.netf, st_ref.ncf)
+    assert st.steps >= 3 and st.nsetups >= 1
+    for k in range(5):
+        assert maxnorm_err(got[k], y_ref[k]) <= 1e-10, k
+    n = got[5].size // 10
+    a, b = got[5].reshape(n, 10), y_ref[5].reshape(n, 10)
+    for s in range(10):
+        assert maxnorm_err(a[:, s], b[:, s]) <= 1e-8, s
+    for k in range(6):  # the run moved the state
+        assert not np.array_equal(got[k], wl["fields"][k])
+
+
+def test_imex_mixed_fexpl_matches_fp64(cuda, tables):
+    """The float-float WENO in the explicit part changes the run by far less than the
+    integration tolerance."""
+    torch = cuda
+    import integrate
+    wl = W.chem_hydro(shape=(12, 10, 8))
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    runs = []
+    for precision in (0, 2):
+        _, prob, w = _gpu_problem(torch, wl, tables, eu, tu, precision)
+        st = integrate.ark_imex_evolve(prob, 0.0, 4e-6, w, **OPTS)
+        runs.append(([x.cpu().numpy() for x in w], st))
+    (a, sa), (b, sb) = runs
+    assert abs(sa.steps - sb.steps) <= max(2, sa.steps // 20)
+    for k in range(6):
+        assert maxnorm_err(b[k], a[k]) <= 1e-6, k

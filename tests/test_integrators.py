@@ -1,0 +1,162 @@
+"""Host integrator layer (integrate.py) on the CPU: the Butcher tables' order conditions, the
+ARK-IMEX driver's convergence order and error control on a manufactured split problem, its
+recovery from a failed Newton-matrix setup, and the Dormand-Prince driver's error control.
+numpy backends stand in for the device problem; the drivers are array-library agnostic."""
+import math
+
+import numpy as np
+import pytest
+
+import integrate as I
+
+
+def _tables():
+    t = I.ARK324
+    n = len(t["c"])
+    AE = np.zeros((n, n))
+    AI = np.zeros((n, n))
+    for i in range(n):
+        AE[i, :len(t["ae"][i])] = t["ae"][i]
+        AI[i, :len(t["ai"][i])] = t["ai"][i]
+    return AE, AI, np.array(t["b"]), np.array(t["bhat"]), np.array(t["c"])
+
+
+def test_ark324_order_conditions():
+    AE, AI, b, bh, c = _tables()
+    tol = 1e-14
+    for A in (AE, AI):
+        assert np.allclose(A.sum(axis=1), c, atol=tol, rtol=0)  # row sums = abscissae
+        assert abs(b.sum() - 1) < tol
+        assert abs(b @ c - 1 / 2) < tol
+        assert abs(b @ c ** 2 - 1 / 3) < tol
+        assert abs(b @ (A @ c) - 1 / 6) < tol
+    # the embedding is second order and not third
+    assert abs(bh.sum() - 1) < tol and abs(bh @ c - 1 / 2) < tol
+    assert abs(bh @ c ** 2 - 1 / 3) > 1e-3 or abs(bh @ (AE @ c) - 1 / 6) > 1e-3
+    # explicit part strictly lower triangular; implicit part ESDIRK, stiffly accurate
+    assert np.all(np.triu(AE) == 0)
+    assert AI[0, 0] == 0 and np.allclose(np.diag(AI)[1:], I.ARK324["ai"][1][1])
+    assert np.array_equal(AI[-1], b)
+    # L-stability of the implicit part: R(z) = det(I - zA + z 1 b^T) / det(I - zA) decays
+    # like 1/z as z -> -inf
+    e = np.ones(len(c))
+    for z in (-1e4, -1e6):
+        R = (np.linalg.det(np.eye(len(c)) - z * AI + z * np.outer(e, b)) /
+             np.linalg.det(np.eye(len(c)) - z * AI))
+        assert abs(R) < 5.0 / abs(z)
+
+
+def test_dormand_prince_order_conditions():
+    A = np.zeros((7, 7))
+    for i, row in enumerate(I._A):
+        A[i, :len(row)] = row
+    c, b, bs = np.array(I._C), np.array(I._B), np.array(I._BSTAR)
+    assert np.allclose(A.sum(axis=1), c, atol=1e-15)
+    for k in range(5):  # quadrature conditions up to order 5
+        assert abs(b @ c ** k - 1 / (k + 1)) < 1e-14
+    for k in range(4):
+        assert abs(bs @ c ** k - 1 / (k + 1)) < 1e-14
+    assert abs(b @ (A @ c) - 1 / 6) < 1e-14 and abs(b @ (A @ c ** 2) - 1 / 12) < 1e-14
+
+
+class SplitProblem:
+    """x' = y (explicit only), y' = -x (explicit) + lam (y - cos t) (implicit): exact
+    x = sin t, y = cos t for x(0) = 0, y(0) = 1; the implicit part touches component 1 only."""
+
+    def __init__(self, lam, rtol=1e-6, atol=1e-10, fail_setups=0):
+        self.lam, self.rtol, self.atol = lam, rtol, atol
+        self.fail_setups = fail_setups
+        self.g = None
+        self.post = 0
+
+    def fe(self, t, y):
+        return [y[1].copy(), -y[0]]
+
+    def fi(self, t, y):
+        return [None, self.lam * (y[1] - math.cos(t))]
+
+    def setup(self, t, y, gamma):
+        if self.fail_setups > 0:  # a singular block, recoverable
+            self.fail_setups -= 1
+            return 1
+        self.g = gamma
+        return 0
+
+    def solve(self, b):
+        return [b[0], b[1] / (1.0 - self.g * self.lam)]
+
+    def norm(self, v, y):
+        s = sum(float(((a / (self.rtol * np.abs(w) + self.atol)) ** 2).sum()) for a, w in zip(v, y))
+        return math.sqrt(s / 2.0)
+
+    def postprocess(self, t, y):
+        self.post += 1
+
+
+def _run(prob, T, **kw):
+    y = [np.zeros(1), np.ones(1)]
+    st = I.ark_imex_evolve(prob, 0.0, T, y, rtol=prob.rtol, atol=prob.atol, **kw)
+    return y, st
+
+
+@pytest.mark.parametrize("lam,order", [(-2.0, 2.85), (-1e4, 1.9)])
+def test_imex_fixed_step_order(lam, order):
+    """Third order on the nonstiff problem; in the stiff limit the classical reduction to the
+    stage order (2) of the ESDIRK."""
+    T = 2.0
+    errs = []
+    for h in (0.1, 0.05, 0.025, 0.0125):
+        y, st = _run(SplitProblem(lam), T, fixed_h=h, maxcor=10, nlscoef=1e-3)
+        errs.append(max(abs(y[0][0] - math.sin(T)), abs(y[1][0] - math.cos(T))))
+        assert st.steps == round(T / h) and st.netf == 0
+    orders = [math.log2(errs[i] / errs[i + 1]) for i in range(3)]
+    assert min(orders[1:]) > order, (errs, orders)
+
+
+def test_imex_adaptive_error_tracks_tolerance():
+    T = 3.0
+    errs, steps = [], []
+    for rtol in (1e-4, 1e-6, 1e-8):
+        p = SplitProblem(-1e4, rtol=rtol, atol=rtol * 1e-3)
+        y, st = _run(p, T)
+        errs.append(max(abs(y[0][0] - math.sin(T)), abs(y[1][0] - math.cos(T))))
+        steps.append(st.steps)
+        assert p.post == st.steps  # PostprocessStep after every accepted step
+        assert st.nni >= 3 * st.steps and st.nsetups >= 1 and st.nfe == st.nfi - st.nni
+    assert errs[0] > errs[1] > errs[2] and errs[2] < 1e-6
+    assert steps[0] < steps[1] < steps[2]
+    # the stiff implicit part does not limit the step: far fewer steps than |lam| T
+    assert steps[1] < 1e4 * T / 50
+
+
+def test_imex_recovers_from_failed_setup():
+    _, base = _run(SplitProblem(-50.0), 1.0)
+    p = SplitProblem(-50.0, fail_setups=2)
+    y, st = _run(p, 1.0)
+    assert st.ncf == base.ncf + 2 and st.nsetups >= base.nsetups + 2 and st.steps > 0
+    assert abs(y[0][0] - math.sin(1.0)) < 1e-4 and abs(y[1][0] - math.cos(1.0)) < 1e-4
+
+
+def test_imex_gives_up_on_persistent_failure():
+    p = SplitProblem(-50.0, fail_setups=10 ** 6)
+    with pytest.raises(RuntimeError, match="Newton failures"):
+        _run(p, 1.0)
+
+
+def test_erk_error_control():
+    def rhs(t, y):
+        return np.array([y[1], -y[0]])
+    for rtol in (1e-6, 1e-9):
+        y, st = I.erk_evolve(rhs, 0.0, 5.0, np.array([0.0, 1.0]), rtol, rtol * 1e-3)
+        err = max(abs(y[0] - math.sin(5.0)), abs(y[1] - math.cos(5.0)))
+        assert err < 100 * rtol and st.steps > 5
+
+
+def test_scaled_forcing_units():
+    torch = pytest.importorskip("torch")
+    g = torch.arange(1.0, 21.0, dtype=torch.float64).view(2, 10)
+    inv = torch.full((2, 10), 0.5, dtype=torch.float64)
+    ref = g.clone()
+    I.scaled_forcing(g, inv, 4.0)
+    assert torch.equal(g[:, :9], ref[:, :9] * 0.5)
+    assert torch.equal(g[:, 9], ref[:, 9] * 2.0)
