@@ -166,6 +166,46 @@ class _File:
         addr = layout[0] + self.base
         return np.frombuffer(self.d, dtype="<f8", count=n, offset=addr).copy().reshape(dims)
 
+    def read_array(self, ohdr):
+        """A contiguous dataset of little-endian float64, or of signed 32/64-bit integers, of
+        any rank (a rank-0 version-1 dataspace is a scalar)."""
+        d = self.d
+        dtype = None
+        for mtype, body, _size in self.messages(ohdr):
+            if mtype == 0x0003:
+                dclass, bits0 = d[body] & 0x0F, d[body + 1]
+                esize = struct.unpack_from("<I", d, body + 4)[0]
+                if bits0 & 1:
+                    raise ValueError("big-endian datasets not supported")
+                if dclass == 1 and esize == 8:
+                    dtype = "<f8"
+                elif dclass == 0 and esize in (4, 8) and (bits0 & 0x08):
+                    dtype = "<i4" if esize == 4 else "<i8"
+                else:
+                    raise ValueError(f"datatype class {dclass} size {esize} not supported")
+        if dtype is None:
+            raise ValueError("dataset header lacks a datatype")
+        if dtype == "<f8":
+            return self.read_f64(ohdr)
+        dims = layout = None
+        for mtype, body, _size in self.messages(ohdr):
+            if mtype == 0x0001:
+                ver, ndim = d[body], d[body + 1]
+                dims = struct.unpack_from(f"<{ndim}Q", d, body + (8 if ver == 1 else 4))
+            elif mtype == 0x0008 and d[body] == 3 and d[body + 1] == 1:
+                layout = struct.unpack_from("<Q", d, body + 2)[0]
+        if dims is None or layout is None:
+            raise ValueError("integer dataset lacks a dataspace or a contiguous layout")
+        n = int(np.prod(dims))
+        return np.frombuffer(d, dtype=dtype, count=n, offset=layout + self.base).copy().reshape(dims)
+
+
+def read_datasets(path: str) -> dict[str, np.ndarray]:
+    """Every root-group dataset of a file in the supported subset (float64 or integer)."""
+    with open(path, "rb") as f:
+        hf = _File(f.read())
+    return {name: hf.read_array(oh) for name, oh in hf.group_entries()}
+
 
 def read_tables(path: str) -> dict[str, np.ndarray]:
     """Read every dataset of the root group into a dict name -> float64 array."""

@@ -134,7 +134,8 @@ def sod_exact(x, t, gamma=1.4, left=(1.0, 0.0, 1.0), right=(0.125, 0.0, 0.1), x0
         elif s < stail:  # inside the left rarefaction fan
             uf = 2 / (gamma + 1) * (cl + (gamma - 1) / 2 * ul + s)
             cf = 2 / (gamma + 1) * (cl + (gamma - 1) / 2 * (ul - s))
-            rho[n], u[n], pp[n] = rl * (cf / cl) ** (2 / (gamma - 1)), uf, pl * (cf / cl) ** (2 * gamma / (gamma - 1))
+            rho[n], u[n], pp[n] = (rl * (cf / cl) ** (2 / (gamma - 1)), uf,
+                                   pl * (cf / cl) ** (2 * gamma / (gamma - 1)))
         elif s < us:
             rho[n], u[n], pp[n] = rsl, us, p
         elif s < sshock:
