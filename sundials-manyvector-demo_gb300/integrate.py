@@ -276,6 +276,43 @@ def _clone(x):
     return x.clone() if hasattr(x, "clone") else x.copy()
 
 
+def _initial_step(prob, t0, tf, y, f0, atol):
+    """First step size when none is given, by the rule ARKODE (arkHin) and CVODE (CVHin) use:
+    bounds hlb = 100 u max(|t0|, |tf|) and hub = min(0.1 |tf - t0|, 1 / max_i |f_i| /
+    (0.1 |y_i| + atol)); starting from sqrt(hlb hub), up to four estimates
+    h = sqrt(2 / ||y''||) with y'' ~ (f(t0 + h, y0 + h f0) - f0) / h, accepted when two agree
+    within a factor 2; then half of it, clipped to [hlb, hub].  The trial evaluations use a
+    copy of y."""
+    tdist = abs(tf - t0)
+    hlb = 100.0 * 2.220446049250313e-16 * max(abs(t0), abs(tf))
+    inv = 0.0
+    for yk, fk in zip(y, f0):
+        if (fk.numel() if hasattr(fk, "numel") else fk.size) > 0:
+            inv = max(inv, float((abs(fk) / (0.1 * abs(yk) + atol)).max()))
+    hub = 0.1 * tdist
+    if hub * inv > 1.0:
+        hub = 1.0 / inv
+    hg = math.sqrt(hlb * hub)
+    if hub < hlb:
+        return hg
+    hnew = hg
+    for count in range(1, 5):
+        ytry = _combo(y, [(hg, f0)])
+        ftry = _combo(prob.fe(t0 + hg, ytry), [(1.0, prob.fi(t0 + hg, ytry))])
+        ydd = prob.norm(_combo(None, [(1.0 / hg, ftry), (-1.0 / hg, f0)]), y)
+        hnew = math.sqrt(2.0 / ydd) if ydd * hub * hub > 2.0 else math.sqrt(hg * hub)
+        if count == 4:
+            break
+        hrat = hnew / hg
+        if 0.5 < hrat < 2.0:
+            break
+        if count >= 2 and hrat > 2.0:
+            hnew = hg
+            break
+        hg = hnew
+    return min(max(0.5 * hnew, hlb), hub)
+
+
 def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.inf,
                     fixed_h=0.0, safety=0.96, bias=1.5, growth=20.0, etamx1=1e4, etamxf=0.3,
                     small_nef=2, etacf=0.25, maxnef=7, maxncf=10, maxcor=3, nlscoef=0.1,
@@ -331,9 +368,8 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
             F0 = (prob.fe(t, y), prob.fi(t, y))
             st.nfe += 1
             st.nfi += 1
-        if h <= 0.0:  # initial step from the size of the full RHS at t0
-            fn = prob.norm(_combo(F0[0], [(1.0, F0[1])]), y)
-            h = 0.5 / fn if fn > 0.0 else tf - t
+        if h <= 0.0:
+            h = _initial_step(prob, t, tf, y, _combo(F0[0], [(1.0, F0[1])]), atol)
         h = min(h, hmax)
         last = tf - t <= h * (1.0 + 1e-8)  # stretch a step by a rounding sliver onto tf
         if last:
