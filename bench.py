@@ -770,7 +770,7 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
         prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, IMEX_OPTS["rtol"], IMEX_OPTS["atol"],
                                        prec)
         wc = [x.clone() for x in w]  # warm-up on a copy (allocations)
-        integrate.ark_imex_evolve(prob, 0.0, tf * 1e-14, wc, **IMEX_OPTS)  # a few steps
+        integrate.ark_imex_evolve(prob, 0.0, tf * 1e-17, wc, **IMEX_OPTS)  # a few steps
         c.state("Ts").fill_(1000.0)
         del wc
         torch.cuda.synchronize()
