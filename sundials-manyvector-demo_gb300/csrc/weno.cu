@@ -63,7 +63,8 @@ __global__ void __launch_bounds__(256) divergence_kernel(Grid g, Fields w, Field
   int bad = 0;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < g.ncell;
        c += (long)gridDim.x * blockDim.x) {
-    const long i = c % nx, r = c / nx, j = r % ny, k = r / ny;
+    long i, j, k;
+    split3(c, nx, ny, i, j, k);
     const long fx = i + (nx + 1) * (j + ny * k);
     const long fy = i + nx * (j + (ny + 1) * k);
     const long fz = c;

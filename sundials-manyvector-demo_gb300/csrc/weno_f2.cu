@@ -10,9 +10,12 @@ __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2*
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
        c += (long)gridDim.x * blockDim.x) {
     const double rho = w.f[0][c], mx = w.f[1][c], my = w.f[2][c], mz = w.f[3][c], et = w.f[4][c];
-    const double p = eos64(g.gamma, rho, mx, my, mz, et);
-    double q[kQ2Base] = {rho, mx, my, mz, et, p, mx / rho, my / rho, mz / rho,
-                         sqrt0(g.gamma * p / rho)};
+    // one FP64 division per cell: the primitives are multiplied by 1/rho (each within an ulp
+    // of the reference's quotients, far inside the float-float representation error)
+    const double ir = 1.0 / rho;
+    const double p = (g.gamma - 1.0) * (et - (mx * mx + my * my + mz * mz) * 0.5 * ir);
+    double q[kQ2Base] = {rho, mx, my, mz, et, p, mx * ir, my * ir, mz * ir,
+                         sqrt0(g.gamma * p * ir)};
 #pragma unroll
     for (int k = 0; k < kQ2Base; ++k) {
       const f2 v = f2_from_double(q[k]);

@@ -13,13 +13,26 @@
 
 namespace gbmv {
 
+// (i, j, k) of the linear index c = i + ex (j + ey k): 32-bit unsigned division while c fits
+// (a 64-bit division is a long emulated sequence, comparable to the rest of a cheap pass)
+__device__ __forceinline__ void split3(long c, long ex, long ey, long& i, long& j, long& k) {
+  if ((unsigned long)c <= 0xffffffffUL) {
+    const unsigned u = (unsigned)c, ux = (unsigned)ex, uy = (unsigned)ey;
+    const unsigned r = u / ux, q = r / uy;
+    i = (long)(u - r * ux);
+    j = (long)(r - q * uy);
+    k = (long)q;
+  } else {
+    const long r = c / ex, q = r / ey;
+    i = c - r * ex;
+    j = r - q * ey;
+    k = q;
+  }
+}
+
 template <int DIR>
 __device__ __forceinline__ void face_coords(long f, const Grid& g, long& i, long& j, long& k) {
-  const long ex = g.n[0] + (DIR == 0), ey = g.n[1] + (DIR == 1);
-  i = f % ex;
-  const long r = f / ex;
-  j = r % ey;
-  k = r / ey;
+  split3(f, g.n[0] + (DIR == 0), g.n[1] + (DIR == 1), i, j, k);
 }
 
 // cells and ghost signs of the six stencil points of face f

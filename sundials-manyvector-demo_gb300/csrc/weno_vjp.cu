@@ -447,7 +447,8 @@ __global__ void __launch_bounds__(256) vjp_gather_kernel(Grid g, const double* _
   const int blo = g.bc[2 * DIR], bhi = g.bc[2 * DIR + 1];
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < g.ncell;
        c += (long)gridDim.x * blockDim.x) {
-    const long i0 = c % nx, r = c / nx, j0 = r % ny, k0 = r / ny;
+    long i0, j0, k0;
+    split3(c, nx, ny, i0, j0, k0);
     const long pos[3] = {i0, j0, k0};
     const long id = pos[DIR];
     long cand[4];
