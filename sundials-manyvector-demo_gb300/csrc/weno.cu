@@ -110,6 +110,75 @@ int divergence(const Grid& g, const Fields& w, const Fields& wdot, double* const
   return GBMV_OK;
 }
 
+// Pass 2 of the float-float form: the same divergence over fluxes kept as float pairs.  On
+// GB300 the FP64 pipe runs at 1/64 of the FP32 rate, so the divergence's FP64 differences made
+// it FP64-bound (81 % of the pipe) at three times its HBM time; here the differences and the
+// 1/d scaling are float-float (FP32 pipes) and only G - div and the legal-state check are FP64.
+template <int NCHEM>
+__global__ void __launch_bounds__(256) divergence_f2_kernel(Grid g, Fields w, Fields wdot,
+                                                            const float2* __restrict__ Fx,
+                                                            const float2* __restrict__ Fy,
+                                                            const float2* __restrict__ Fz,
+                                                            ForceTerm G, int* __restrict__ status) {
+  const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  const long nfx = (nx + 1) * ny * nz, nfy = nx * (ny + 1) * nz, nfz = nx * ny * (nz + 1);
+  const f2 idx = f2_from_double(g.inv_d[0]), idy = f2_from_double(g.inv_d[1]),
+           idz = f2_from_double(g.inv_d[2]);
+  int bad = 0;
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < g.ncell;
+       c += (long)gridDim.x * blockDim.x) {
+    long i, j, k;
+    split3(c, nx, ny, i, j, k);
+    const long fx = i + (nx + 1) * (j + ny * k);
+    const long fy = i + nx * (j + (ny + 1) * k);
+    const long fz = c;
+    {
+      const double rho = w.f[0][c], mx = w.f[1][c], my = w.f[2][c], mz = w.f[3][c],
+                   et = w.f[4][c];
+      int s = 0;
+      if (!(rho > 0.0)) s |= 1;
+      if (!(et > 0.0)) s |= 2;
+      if (!(eos64(g.gamma, rho, mx, my, mz, et) > 0.0)) s |= 4;
+      bad |= s;
+    }
+#pragma unroll
+    for (int v = 0; v < 5 + NCHEM; ++v) {
+      const float2 a0 = Fx[v * nfx + fx], a1 = Fx[v * nfx + fx + 1];
+      const float2 b0 = Fy[v * nfy + fy], b1 = Fy[v * nfy + fy + nx];
+      const float2 c0 = Fz[v * nfz + fz], c1 = Fz[v * nfz + fz + nx * ny];
+      const f2 div = (f2(a1.x, a1.y) - f2(a0.x, a0.y)) * idx +
+                     (f2(b1.x, b1.y) - f2(b0.x, b0.y)) * idy +
+                     (f2(c1.x, c1.y) - f2(c0.x, c0.y)) * idz;
+      double* dst = (v < 5) ? (wdot.f[v] + c) : (wdot.f[5] + (v - 5) + (long)NCHEM * c);
+      const double base = G.in_wdot ? *dst : G.c[v];
+      *dst = base - div.to_double();
+    }
+  }
+  bad = __reduce_or_sync(0xffffffffu, bad);
+  if (bad && (threadIdx.x & 31) == 0) atomicOr(status, bad);
+}
+
+int divergence_f2(const Grid& g, const Fields& w, const Fields& wdot, float2* const (&F)[3],
+                  const ForceTerm& G, int* d_status, cudaStream_t s) {
+  ProfScope ps("divergence", s);
+  const int b = sweep_blocks(g.ncell, 256);
+  switch (g.nchem) {
+#define GBMV_DIV_F2(NC)                                                                     \
+  case NC:                                                                                 \
+    divergence_f2_kernel<NC><<<b, 256, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); \
+    break;
+    GBMV_DIV_F2(0)
+    GBMV_DIV_F2(2)
+    GBMV_DIV_F2(4)
+    GBMV_DIV_F2(6)
+    GBMV_DIV_F2(10)
+#undef GBMV_DIV_F2
+    default: set_error("nchem=%d not compiled (0,2,4,6,10)", g.nchem); return GBMV_EUNSUPPORTED;
+  }
+  GBMV_LAUNCH_CHECK("divergence_f2_kernel");
+  return GBMV_OK;
+}
+
 template <int NCHEM>
 static int launch_fp64(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
                        double* scratch, int* d_status, cudaStream_t s) {

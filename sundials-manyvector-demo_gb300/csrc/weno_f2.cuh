@@ -7,7 +7,8 @@
 //   face_flux_f2_kernel<NCHEM, DIR>: the face flux in float-float arithmetic from Q2 (no FP64
 //     instruction on the common path); faces whose states leave the float range, or touch a
 //     non-positive density (homogeneous Dirichlet ghosts), are computed in FP64 from w;
-//   divergence: the FP64 pass of the FP64 form (weno.cu).
+//   divergence_f2: the FP64 form's divergence pass over fluxes kept as float pairs, the
+//     differences in float-float, the final G - div in FP64 (weno.cu).
 //
 // The face-flux kernel is a template over the tracer count, the sweep direction and the weight
 // variant WV (0: float-float weights everywhere; 1: FP32 weights and smoothness indicators for
@@ -35,7 +36,7 @@ int feuler_f2_fast(const Grid& g, const Fields& w, const Fields& wdot, const For
 template <int NCHEM, int DIR, int WV>
 __global__ void __launch_bounds__(128, WV == 1 ? 3 : 1) face_flux_f2_kernel(Grid g, Fields w,
                                                            const float2* __restrict__ Q2,
-                                                           double* __restrict__ F, long nfaces) {
+                                                           float2* __restrict__ F, long nfaces) {
   const long nx = g.n[0], ny = g.n[1], n = g.ncell;
   for (long f = blockIdx.x * (long)blockDim.x + threadIdx.x; f < nfaces;
        f += (long)gridDim.x * blockDim.x) {
@@ -85,14 +86,11 @@ __global__ void __launch_bounds__(128, WV == 1 ? 3 : 1) face_flux_f2_kernel(Grid
       for (int m = 0; m < 6; ++m) ok = ok && (fabsf(q[m].hi) < 1e15f);
     }
     FaceState<f2> S;
-    double out[5];
+    f2 o[5];
     if (ok) {
-      f2 o[5];
       // characteristic fields keep float-float weights in every mixed form: the reference's
       // eigenbasis (conditioning ~1/c^2) amplifies weight rounding in the back-projection
       fluid_face_flux<f2, true, 0>(W, g.gamma, S, o, &pre);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) out[v] = o[v].to_double();
     } else {  // FP64, exactly the FP64 form's arithmetic
       double Wd[6][5];
 #pragma unroll
@@ -112,18 +110,22 @@ __global__ void __launch_bounds__(128, WV == 1 ? 3 : 1) face_flux_f2_kernel(Grid
         Wd[l][4] = q[4];
       }
       FaceState<double> S64;
+      double out[5];
       fluid_face_flux<double>(Wd, g.gamma, S64, out);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) o[v] = f2_from_double(out[v]);
 #pragma unroll
       for (int l = 0; l < 6; ++l) {
         S.hp[l] = f2_from_double(S64.hp[l]);
         S.hm[l] = f2_from_double(S64.hm[l]);
       }
     }
-    const double o1 = out[1], oD = out[1 + DIR];
-    out[1] = oD;
-    out[1 + DIR] = o1;
+    // fluxes stay float pairs: the divergence pass differences them in float-float
+    const f2 o1 = o[1], oD = o[1 + DIR];
+    o[1] = oD;
+    o[1 + DIR] = o1;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) F[v * nfaces + f] = out[v];
+    for (int v = 0; v < 5; ++v) F[v * nfaces + f] = make_float2(o[v].hi, o[v].lo);
 #pragma unroll 1
     for (int c = 0; c < NCHEM; ++c) {
       f2 cv[6];
@@ -132,7 +134,8 @@ __global__ void __launch_bounds__(128, WV == 1 ? 3 : 1) face_flux_f2_kernel(Grid
         const float2 t = __ldg(Q2 + (kQ2Base + c) * n + cell[l]);
         cv[l] = nall[l] ? f2(-t.x, -t.y) : f2(t.x, t.y);
       }
-      F[(5 + c) * nfaces + f] = tracer_face_flux<f2, WV>(S, cv).to_double();
+      const f2 r = tracer_face_flux<f2, WV>(S, cv);
+      F[(5 + c) * nfaces + f] = make_float2(r.hi, r.lo);
     }
   }
 }
@@ -142,8 +145,8 @@ int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTer
               double* scratch, float2* q2, const double* tscale, int* d_status, cudaStream_t s) {
   long nf[3];
   face_counts(g, nf);
-  double* F[3] = {scratch, scratch + (long)(5 + NCHEM) * nf[0],
-                  scratch + (long)(5 + NCHEM) * (nf[0] + nf[1])};
+  float2* const F2 = reinterpret_cast<float2*>(scratch);  // 8 bytes per flux, as a double
+  float2* F[3] = {F2, F2 + (long)(5 + NCHEM) * nf[0], F2 + (long)(5 + NCHEM) * (nf[0] + nf[1])};
   int rc = prims_f2(g, w, q2, tscale, s);
   if (rc != GBMV_OK) return rc;
   {
@@ -164,7 +167,7 @@ int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTer
                                                                                 nf[2]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<z>");
   }
-  return divergence(g, w, wdot, F, G, d_status, s);
+  return divergence_f2(g, w, wdot, F, G, d_status, s);
 }
 
 template <int WV>
