@@ -369,6 +369,14 @@ int gbmv_profile_get(const char* family, double* total_ms, long* launches);
  * FP64 (fp64=1) or FP32 (fp64=0), in flop/s (2 per FMA) -- the FP64 roofline denominator. */
 int gbmv_diag_fma_rate(int fp64, double* flops_per_s);
 
+/* Self-check of the integer-instruction double <-> float conversions the mixed kernels use in
+ * place of conversion instructions (which run at the FP64 rate): for each of the n device
+ * doubles, the conversions and float-pair splits must match the hardware round-to-nearest
+ * results bit for bit; *mismatches (host) counts the differences.  Synchronous.  (No
+ * counterpart in the reference.) */
+int gbmv_diag_convert_check(const double* d_in, long n, unsigned long long* mismatches,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -192,11 +192,11 @@ __device__ __forceinline__ int dirk_setup(const ChemParams& P, const ChemState& 
       for (int e = 0; e < 64; ++e) {
         const int row = kJacPattern[e][0], col = kJacPattern[e][1];
         L[(col * 10 + row) * BS] =
-            (LU)(A[(col * 10 + row) * BS] * pow2(er[row] + ec[col]));
+            to_lu<LU>(A[(col * 10 + row) * BS] * pow2(er[row] + ec[col]));
       }
     } else {
       chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-        L[(col * 10 + row) * BS] = (LU)(entry(row, col, v) * pow2(er[row] + ec[col]));
+        L[(col * 10 + row) * BS] = to_lu<LU>(entry(row, col, v) * pow2(er[row] + ec[col]));
       });
     }
   }
@@ -326,10 +326,10 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         // equilibrated FP32 solve: (R A C) u = R g, dl = C u
         LU u[10];
 #pragma unroll
-        for (int s = 0; s < 10; ++s) u[s] = (LU)(g[s] * pow2(EQ[s * BS]));
+        for (int s = 0; s < 10; ++s) u[s] = to_lu<LU>(g[s] * pow2(EQ[s * BS]));
         lus10_strided<LU, LU>(L, BS, piv, u);
 #pragma unroll
-        for (int s = 0; s < 10; ++s) dl[s] = (double)u[s] * pow2(EQ[(10 + s) * BS]);
+        for (int s = 0; s < 10; ++s) dl[s] = from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
         if (REF) {
           for (int it = 0; it < O.refine; ++it) {  // r = g - A dl in FP64, solve, update
             double r[10];
@@ -341,10 +341,10 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
               r[row] -= A[(col * 10 + row) * BS] * dl[col];
             }
 #pragma unroll
-            for (int s = 0; s < 10; ++s) u[s] = (LU)(r[s] * pow2(EQ[s * BS]));
+            for (int s = 0; s < 10; ++s) u[s] = to_lu<LU>(r[s] * pow2(EQ[s * BS]));
             lus10_strided<LU, LU>(L, BS, piv, u);
 #pragma unroll
-            for (int s = 0; s < 10; ++s) dl[s] += (double)u[s] * pow2(EQ[(10 + s) * BS]);
+            for (int s = 0; s < 10; ++s) dl[s] += from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
           }
         }
       }
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         Z[s * BS] += dl[s];
-        const double v = dl[s] * (double)EW[s * BS];
+        const double v = dl[s] * f64_of_f32(EW[s * BS]);
         s2 += v * v;
       }
       const double del = sqrt(s2 / 10.0);
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         const double e = h * ((kE1 * K1[s * BS] + kE2 * K2[s * BS]) + kE3 * f[s]);
-        const double v = e * (double)EW[s * BS];
+        const double v = e * f64_of_f32(EW[s * BS]);
         s2 += v * v;
       }
       const double dsm = sqrt(s2 / 10.0);
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         const double ys = Y[s * BS];
-        EW[s * BS] = (float)(1.0 / (O.rtol * fabs(ys) + O.atol));
+        EW[s * BS] = f32_of_f64(1.0 / (O.rtol * fabs(ys) + O.atol));
         Z[s * BS] = ys;  // trivial predictor
       }
       const double gam = h * kGd;

@@ -3,7 +3,21 @@
 // LU with partial pivoting on a per-thread strided slice of shared memory.
 #pragma once
 
+#include "df64.cuh"
+
 namespace gbmv {
+
+// Casts to and from the factor's precision: for an FP32 factor the integer-instruction
+// conversions of df64.cuh (bit-identical to the casts, without the FP64-rate conversion
+// instructions), the identity for an FP64 factor.
+template <typename LU>
+__device__ __forceinline__ LU to_lu(double x);
+template <>
+__device__ __forceinline__ float to_lu<float>(double x) { return f32_of_f64(x); }
+template <>
+__device__ __forceinline__ double to_lu<double>(double x) { return x; }
+__device__ __forceinline__ double from_lu(float x) { return f64_of_f32(x); }
+__device__ __forceinline__ double from_lu(double x) { return x; }
 
 // Structural nonzeros (row, col) of the network Jacobian (the CSR pattern of
 // src/raja_primordial_network.cpp:1869-1948); every diagonal entry is among them.

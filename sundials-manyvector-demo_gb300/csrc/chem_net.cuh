@@ -9,6 +9,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "df64.cuh"
 
 namespace gbmv {
 
@@ -27,7 +28,12 @@ enum : int {
 
 struct ChemParams {
   const double* tab;  // device, bin-major: tab[bin * kNT + row]
+  // the four H2 adiabatic-index tables for the FP32 temperature iterations, per bin:
+  // (float) value and (float)(next - value) of gammaH2_2, dgammaH2_2_dT, gammaH2_1,
+  // dgammaH2_1_dT -- the roundings the FP32 iterations apply, done once at setup
+  const float* gtab;  // device, gtab[bin * 8 + 2 * table + {0 value, 1 slope}]
   double dbin, idbin, lb, tlo, thi, z, zp1_4;
+  float dbinf, idbinf, lbf;  // (float) of dbin, idbin, lb
   int nbins;
 };
 
@@ -84,14 +90,17 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
 __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, const double (&y)[10],
                                                        double& Ts, double& dTs_ge, int nfloat) {
   const float kb = 1.3806504e-16f, mh = 1.67e-24f, gm1 = 1.5f;
-  const float H2_1 = (float)y[0], H2_2 = (float)y[1], H_1 = (float)y[2], H_2 = (float)y[3],
-              H_m0 = (float)y[4], He_1 = (float)y[5], He_2 = (float)y[6], He_3 = (float)y[7],
-              de = (float)y[8], ge = (float)y[9];
+  // double -> float by integer instructions (f32_of_f64: the hardware's rounding, without the
+  // FP64-rate conversion instructions)
+  const float H2_1 = f32_of_f64(y[0]), H2_2 = f32_of_f64(y[1]), H_1 = f32_of_f64(y[2]),
+              H_2 = f32_of_f64(y[3]), H_m0 = f32_of_f64(y[4]), He_1 = f32_of_f64(y[5]),
+              He_2 = f32_of_f64(y[6]), He_3 = f32_of_f64(y[7]), de = f32_of_f64(y[8]),
+              ge = f32_of_f64(y[9]);
   const float density = 2.f * H2_1 + 2.f * H2_2 + 1.00794f * H_1 + 1.00794f * H_2 +
                         1.00794f * H_m0 + 4.002602f * He_1 + 4.002602f * He_2 + 4.002602f * He_3;
   const float kdm = kb / (density * mh);
-  const float lb = (float)P.lb, idbin = (float)P.idbin, dbin = (float)P.dbin;
-  float T = (float)Ts;
+  const float lb = P.lbf, idbin = P.idbinf, dbin = P.dbinf;
+  float T = f32_of_f64(Ts);
 #pragma unroll 1
   for (int it = 0; it < nfloat; ++it) {
     const float logT = logf(T);
@@ -99,12 +108,12 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     b = b <= 0 ? 0 : (b >= P.nbins ? P.nbins - 1 : b);
     const float t1 = lb + b * dbin;
     const float Tdef = (logT - t1) / dbin;
-    const double* lo = P.tab + (long)b * kNT;
-    const double* hi = lo + kNT;
-    const float g2 = (float)lo[GAMMAH2_2] + Tdef * (float)(hi[GAMMAH2_2] - lo[GAMMAH2_2]);
-    const float dg2 = (float)lo[DGAMMAH2_2] + Tdef * (float)(hi[DGAMMAH2_2] - lo[DGAMMAH2_2]);
-    const float g1 = (float)lo[GAMMAH2_1] + Tdef * (float)(hi[GAMMAH2_1] - lo[GAMMAH2_1]);
-    const float dg1 = (float)lo[DGAMMAH2_1] + Tdef * (float)(hi[DGAMMAH2_1] - lo[DGAMMAH2_1]);
+    const float4 ga = __ldg(reinterpret_cast<const float4*>(P.gtab + (long)b * 8));
+    const float4 gb = __ldg(reinterpret_cast<const float4*>(P.gtab + (long)b * 8 + 4));
+    const float g2 = ga.x + Tdef * ga.y;
+    const float dg2 = ga.z + Tdef * ga.w;
+    const float g1 = gb.x + Tdef * gb.y;
+    const float dg1 = gb.z + Tdef * gb.w;
     const float i1 = 1.f / (g1 - 1.f), i2 = 1.f / (g2 - 1.f);
     const float nsum = H2_1 * i1 + H2_2 * i2 +
                        gm1 * (H_1 + H_2 + H_m0 + He_1 + He_2 + He_3 + de);
@@ -112,7 +121,7 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     const float dge = kdm * T * nsum - ge;
     T = T - dge / dge_dT;
   }
-  Ts = (double)T;
+  Ts = f64_of_f32(T);
   // remaining iterations (and dT/dge) in FP64: exactly chem_temperature's loop body
   const double kbd = 1.3806504e-16, mhd = 1.67e-24, gm1d = 1.0 / (5.e0 / 3.e0 - 1);
   const double dH2_1 = y[0], dH2_2 = y[1], dH_1 = y[2], dH_2 = y[3], dH_m0 = y[4], dHe_1 = y[5],

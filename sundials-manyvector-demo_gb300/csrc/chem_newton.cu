@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
           const int e = kJacIndex[row][col];
           if (e >= 0) As[e * BS] = a;
         }
-        L[(col * 10 + row) * BS] = (LU)a;
+        L[(col * 10 + row) * BS] = to_lu<LU>(a);
       }, &Rg);
     }
 #pragma unroll
@@ -96,10 +96,10 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
     if (!fp64_fallback) {
       LU xs[10];
 #pragma unroll
-      for (int s = 0; s < 10; ++s) xs[s] = (LU)f[s];
+      for (int s = 0; s < 10; ++s) xs[s] = to_lu<LU>(f[s]);
       lus10_strided<LU, LU>(L, BS, piv, xs);
 #pragma unroll
-      for (int s = 0; s < 10; ++s) x[s] = (double)xs[s];
+      for (int s = 0; s < 10; ++s) x[s] = from_lu(xs[s]);
       if (sizeof(LU) == 4) {
         // iterative refinement against FP64 residuals; a cell stops as soon as its correction
         // is below 1e-13 of the solution (well-conditioned cells need one step, the
@@ -113,14 +113,14 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
             rr[kJacPattern[e][0]] -= As[e * BS] * x[kJacPattern[e][1]];
           LU ds[10];
 #pragma unroll
-          for (int s = 0; s < 10; ++s) ds[s] = (LU)rr[s];
+          for (int s = 0; s < 10; ++s) ds[s] = to_lu<LU>(rr[s]);
           lus10_strided<LU, LU>(L, BS, piv, ds);
           float dmax = 0.f, xmax = 0.f;
 #pragma unroll
           for (int s = 0; s < 10; ++s) {
-            x[s] += (double)ds[s];
+            x[s] += from_lu(ds[s]);
             dmax = fmaxf(dmax, fabsf((float)ds[s]));
-            xmax = fmaxf(xmax, fabsf((float)x[s]));
+            xmax = fmaxf(xmax, fabsf(f32_of_f64(x[s])));
           }
           if (dmax <= 1e-13f * xmax) break;
         }

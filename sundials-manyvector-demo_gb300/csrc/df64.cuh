@@ -80,6 +80,48 @@ __device__ __forceinline__ f2 f2_from_double(double d) {
   return f2(h, __double2float_rn(d - (double)h));
 }
 
+// Conversions between double and float from the bit patterns, with integer instructions.
+// Conversion instructions with a 64-bit operand run at the FP64 rate, 1/64 of the FP32 rate on
+// GB300, so in passes that mostly convert (the float-float primitives, the FP32 factors of the
+// Newton matrices) they set the time.  Each helper returns exactly what the round-to-nearest
+// hardware conversion returns: the integer path covers every normal float result, anything
+// else (zero, subnormal, overflow, inf, NaN) takes the hardware conversion.
+
+// double -> float, round to nearest even: drop 29 mantissa bits on the pattern (a carry into
+// the exponent is the correct rounding), re-bias the exponent (1023 - 127 = 896)
+__device__ __forceinline__ float f32_of_f64(double d) {
+  const unsigned long long p = (unsigned long long)__double_as_longlong(d);
+  const unsigned e = (unsigned)(p >> 52) & 0x7FFu;
+  if (e - 897u > 1149u - 897u) return __double2float_rn(d);  // result not surely a normal float
+  const unsigned long long r = p + 0x0FFFFFFFull + ((p >> 29) & 1ull);
+  const unsigned hi = (unsigned)(r >> 32);
+  const unsigned s = hi & 0x80000000u;
+  const unsigned er = (hi >> 20) & 0x7FFu;
+  const unsigned m = (unsigned)(r >> 29) & 0x7FFFFFu;
+  return __uint_as_float(s | ((er - 896u) << 23) | m);
+}
+
+// float -> double, exact
+__device__ __forceinline__ double f64_of_f32(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  if (e - 1u > 253u) return (double)f;  // zero, subnormal, inf, NaN
+  const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+  const unsigned lo = u << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// f2_from_double without conversion instructions (bit-identical to it)
+__device__ __forceinline__ f2 f2_split(double d) {
+  const float h = f32_of_f64(d);
+  return f2(h, f32_of_f64(d - f64_of_f32(h)));
+}
+
+// f2::to_double without conversion instructions (bit-identical to it)
+__device__ __forceinline__ double f2_to_double(f2 x) {
+  return f64_of_f32(x.hi) + f64_of_f32(x.lo);
+}
+
 __device__ __forceinline__ bool operator<(f2 a, f2 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool operator>(f2 a, f2 b) { return b < a; }
 __device__ __forceinline__ bool operator<=(f2 a, f2 b) { return !(b < a); }

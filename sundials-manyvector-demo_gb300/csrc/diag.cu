@@ -2,6 +2,7 @@
 // the FP64 (and FP32) fused multiply-add rate of the SIMT pipes.  Each thread runs 8
 // independent FMA chains for a fixed number of iterations; flops = 2 * FMAs.
 #include "common.cuh"
+#include "df64.cuh"
 
 namespace gbmv {
 
@@ -55,9 +56,59 @@ static int probe(double* flops_per_s, int blocks_per_sm) {
   return GBMV_OK;
 }
 
+// Self-check of the integer-instruction conversions of df64.cuh against the hardware
+// round-to-nearest conversions: for every input double, f32_of_f64, f64_of_f32 (of the
+// hardware float), f2_split and f2_to_double (of the hardware pair) must give the same bits.
+__global__ void __launch_bounds__(256) convert_check_kernel(const double* __restrict__ in,
+                                                            long n,
+                                                            unsigned long long* __restrict__ bad) {
+  unsigned long long mine = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const double d = in[i];
+    const float hw = __double2float_rn(d);
+    mine += __float_as_uint(f32_of_f64(d)) != __float_as_uint(hw);
+    mine += __double_as_longlong(f64_of_f32(hw)) != __double_as_longlong((double)hw);
+    const f2 a = f2_split(d), b = f2_from_double(d);
+    mine += __float_as_uint(a.hi) != __float_as_uint(b.hi);
+    mine += __float_as_uint(a.lo) != __float_as_uint(b.lo);
+    mine += __double_as_longlong(f2_to_double(b)) != __double_as_longlong(b.to_double());
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, off);
+  if ((threadIdx.x & 31) == 0 && mine) atomicAdd(bad, mine);
+}
+
 }  // namespace gbmv
 
 extern "C" int gbmv_diag_fma_rate(int fp64, double* flops_per_s) {
   if (!flops_per_s) return GBMV_EINVAL;
   return fp64 ? gbmv::probe<double>(flops_per_s, 8) : gbmv::probe<float>(flops_per_s, 8);
+}
+
+extern "C" int gbmv_diag_convert_check(const double* d_in, long n, unsigned long long* mismatches,
+                                       void* stream) {
+  using namespace gbmv;
+  if (!d_in || n < 0 || !mismatches) return GBMV_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  auto ok = [](cudaError_t e, const char* where) {
+    return e == cudaSuccess ? GBMV_OK : check_cuda(e, where);
+  };
+  unsigned long long* d_bad = nullptr;
+  GBMV_CUDA_TRY(cudaMalloc(&d_bad, sizeof(unsigned long long)));
+  int rc = ok(cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), s), "convert check memset");
+  if (rc == GBMV_OK) {
+    long b = (n + 255) / 256;
+    if (b > (long)kSM * 8) b = (long)kSM * 8;
+    if (b < 1) b = 1;
+    convert_check_kernel<<<(int)b, 256, 0, s>>>(d_in, n, d_bad);
+    count_launch();
+    rc = ok(cudaGetLastError(), "convert_check_kernel");
+  }
+  if (rc == GBMV_OK)
+    rc = ok(cudaMemcpyAsync(mismatches, d_bad, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, s), "convert check copy");
+  if (rc == GBMV_OK) rc = ok(cudaStreamSynchronize(s), "convert check sync");
+  cudaFree(d_bad);
+  return rc;
 }

@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(256) divergence_f2_kernel(Grid g, Fields w, Fi
                      (f2(c1.x, c1.y) - f2(c0.x, c0.y)) * idz;
       double* dst = (v < 5) ? (wdot.f[v] + c) : (wdot.f[5] + (v - 5) + (long)NCHEM * c);
       const double base = G.in_wdot ? *dst : G.c[v];
-      *dst = base - div.to_double();
+      *dst = base - f2_to_double(div);
     }
   }
   bad = __reduce_or_sync(0xffffffffu, bad);

@@ -18,13 +18,13 @@ __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2*
                          sqrt0(g.gamma * p * ir)};
 #pragma unroll
     for (int k = 0; k < kQ2Base; ++k) {
-      const f2 v = f2_from_double(q[k]);
+      const f2 v = f2_split(q[k]);
       Q2[k * n + c] = make_float2(v.hi, v.lo);
     }
     for (int v = 0; v < g.nchem; ++v) {
       // tscale: the chemistry component arrives in scaled units (x = chem * scale)
       const long e = v + (long)g.nchem * c;
-      const f2 x = f2_from_double(tscale ? w.f[5][e] * tscale[e] : w.f[5][e]);
+      const f2 x = f2_split(tscale ? w.f[5][e] * tscale[e] : w.f[5][e]);
       Q2[(kQ2Base + v) * n + c] = make_float2(x.hi, x.lo);
     }
   }

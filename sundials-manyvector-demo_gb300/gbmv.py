@@ -108,6 +108,7 @@ SIGNATURES = [
     ("gbmv_last_error", C.c_char_p, []),
     ("gbmv_launch_count", C.c_long, []),
     ("gbmv_diag_fma_rate", C.c_int, [C.c_int, _P]),
+    ("gbmv_diag_convert_check", C.c_int, [_VP, C.c_long, C.POINTER(C.c_ulonglong), _VP]),
     ("gbmv_profile_enable", C.c_int, [C.c_int]),
     ("gbmv_profile_reset", C.c_int, []),
     ("gbmv_profile_get", C.c_int, [C.c_char_p, _P, C.POINTER(C.c_long)]),
@@ -463,6 +464,15 @@ def mri_fast_evolve(hydro: Hydro, chem: Chem, t0, tout, w, time_units, forcing=(
 def PostprocessStep(hydro: Hydro, chem: Chem, w, energy_units, stream=None):
     return _check(load().gbmv_postprocess_step(hydro.h, chem.c, _vec(w), energy_units,
                                                _stream_ptr(stream)), "gbmv_postprocess_step")
+
+
+def convert_check(d) -> int:
+    """Mismatches of the integer-instruction conversions against the hardware ones over the
+    doubles of the CUDA tensor d (0 when they agree bit for bit)."""
+    out = C.c_ulonglong(0)
+    _check(load().gbmv_diag_convert_check(_dev_ptr(d), d.numel(), C.byref(out), None),
+           "gbmv_diag_convert_check")
+    return int(out.value)
 
 
 def fma_rate(fp64: bool = True) -> float:
