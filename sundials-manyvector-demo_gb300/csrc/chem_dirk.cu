@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         Z[s * BS] += dl[s];
-        const double v = dl[s] * f64_of_f32(EW[s * BS]);
+        const double v = dl[s] * (double)EW[s * BS];
         s2 += v * v;
       }
       const double del = sqrt(s2 / 10.0);
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         const double e = h * ((kE1 * K1[s * BS] + kE2 * K2[s * BS]) + kE3 * f[s]);
-        const double v = e * f64_of_f32(EW[s * BS]);
+        const double v = e * (double)EW[s * BS];
         s2 += v * v;
       }
       const double dsm = sqrt(s2 / 10.0);
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
         const double ys = Y[s * BS];
-        EW[s * BS] = f32_of_f64(1.0 / (O.rtol * fabs(ys) + O.atol));
+        EW[s * BS] = (float)(1.0 / (O.rtol * fabs(ys) + O.atol));
         Z[s * BS] = ys;  // trivial predictor
       }
       const double gam = h * kGd;

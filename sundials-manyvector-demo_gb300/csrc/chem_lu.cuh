@@ -7,16 +7,13 @@
 
 namespace gbmv {
 
-// Casts to and from the factor's precision: for an FP32 factor the integer-instruction
-// conversions of df64.cuh (bit-identical to the casts, without the FP64-rate conversion
-// instructions), the identity for an FP64 factor.
+// Casts to and from the factor's precision.  These stay conversion instructions: the Newton
+// and DIRK kernels run few warps per SM and are latency-bound, and the integer-instruction
+// conversions of df64.cuh (which win in the throughput-bound float-float passes) lengthen
+// their dependency chains (measured 1 % slower fused Newton, 8 % slower mixed DIRK).
 template <typename LU>
-__device__ __forceinline__ LU to_lu(double x);
-template <>
-__device__ __forceinline__ float to_lu<float>(double x) { return f32_of_f64(x); }
-template <>
-__device__ __forceinline__ double to_lu<double>(double x) { return x; }
-__device__ __forceinline__ double from_lu(float x) { return f64_of_f32(x); }
+__device__ __forceinline__ LU to_lu(double x) { return (LU)x; }
+__device__ __forceinline__ double from_lu(float x) { return (double)x; }
 __device__ __forceinline__ double from_lu(double x) { return x; }
 
 // Structural nonzeros (row, col) of the network Jacobian (the CSR pattern of

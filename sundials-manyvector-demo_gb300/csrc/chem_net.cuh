@@ -84,23 +84,21 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
 }
 
 // The same ten-iteration Newton solve with the first `nfloat` iterations in FP32 (table
-// lookups on the FP64 tables, rounded) and the rest in FP64.  From the converged basin the
+// lookups on float copies of the four adiabatic-index tables, value and slope per bin, rounded
+// once at setup exactly as the iterations would round the FP64 entries) and the rest in FP64.  From the converged basin the
 // FP64 iterations restore full accuracy (Newton's quadratic convergence), so the result
 // matches chem_temperature's to rounding whenever the reference's ten iterations converge.
 __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, const double (&y)[10],
                                                        double& Ts, double& dTs_ge, int nfloat) {
   const float kb = 1.3806504e-16f, mh = 1.67e-24f, gm1 = 1.5f;
-  // double -> float by integer instructions (f32_of_f64: the hardware's rounding, without the
-  // FP64-rate conversion instructions)
-  const float H2_1 = f32_of_f64(y[0]), H2_2 = f32_of_f64(y[1]), H_1 = f32_of_f64(y[2]),
-              H_2 = f32_of_f64(y[3]), H_m0 = f32_of_f64(y[4]), He_1 = f32_of_f64(y[5]),
-              He_2 = f32_of_f64(y[6]), He_3 = f32_of_f64(y[7]), de = f32_of_f64(y[8]),
-              ge = f32_of_f64(y[9]);
+  const float H2_1 = (float)y[0], H2_2 = (float)y[1], H_1 = (float)y[2], H_2 = (float)y[3],
+              H_m0 = (float)y[4], He_1 = (float)y[5], He_2 = (float)y[6], He_3 = (float)y[7],
+              de = (float)y[8], ge = (float)y[9];
   const float density = 2.f * H2_1 + 2.f * H2_2 + 1.00794f * H_1 + 1.00794f * H_2 +
                         1.00794f * H_m0 + 4.002602f * He_1 + 4.002602f * He_2 + 4.002602f * He_3;
   const float kdm = kb / (density * mh);
   const float lb = P.lbf, idbin = P.idbinf, dbin = P.dbinf;
-  float T = f32_of_f64(Ts);
+  float T = (float)Ts;
 #pragma unroll 1
   for (int it = 0; it < nfloat; ++it) {
     const float logT = logf(T);
@@ -121,7 +119,7 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     const float dge = kdm * T * nsum - ge;
     T = T - dge / dge_dT;
   }
-  Ts = f64_of_f32(T);
+  Ts = (double)T;
   // remaining iterations (and dT/dge) in FP64: exactly chem_temperature's loop body
   const double kbd = 1.3806504e-16, mhd = 1.67e-24, gm1d = 1.0 / (5.e0 / 3.e0 - 1);
   const double dH2_1 = y[0], dH2_2 = y[1], dH_1 = y[2], dH_2 = y[3], dH_m0 = y[4], dHe_1 = y[5],

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
           for (int s = 0; s < 10; ++s) {
             x[s] += from_lu(ds[s]);
             dmax = fmaxf(dmax, fabsf((float)ds[s]));
-            xmax = fmaxf(xmax, fabsf(f32_of_f64(x[s])));
+            xmax = fmaxf(xmax, fabsf((float)x[s]));
           }
           if (dmax <= 1e-13f * xmax) break;
         }
