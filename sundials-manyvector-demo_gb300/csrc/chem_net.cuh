@@ -158,15 +158,18 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
   dTs_ge = 1.0 / dge_dTd;
 }
 
-// Rates at temperature Ts (and their T-derivatives when WithSlopes).
-template <bool WithSlopes>
+// Rates at temperature Ts (and their T-derivatives when WithSlopes).  Reciprocal: the
+// interpolation weight and the slope factor multiply by 1 / dbin instead of dividing by the
+// bin width t2 - t1 (one division per cell instead of three, within an ulp or two of the
+// quotients; the mixed forms' choice -- the FP64 forms divide, as the reference does).
+template <bool WithSlopes, bool Reciprocal = false>
 __device__ __forceinline__ void chem_rates(const ChemParams& P, double Ts, double (&k)[kNRates],
                                            double (&dk)[kNRates]) {
   double t1, t2;
   const double logT = log(Ts);
   const int b = chem_bin(P, logT, t1, t2);
-  const double Tdef = (logT - t1) / (t2 - t1);
-  const double Tfactor = (1.0 / Ts) / (t2 - t1);
+  const double Tdef = Reciprocal ? (logT - t1) * P.idbin : (logT - t1) / (t2 - t1);
+  const double Tfactor = Reciprocal ? P.idbin / Ts : (1.0 / Ts) / (t2 - t1);
   const double* lo = P.tab + (long)b * kNT;
   const double* hi = lo + kNT;
 #pragma unroll

@@ -46,8 +46,10 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
 #pragma unroll
     for (int s = 0; s < 10; ++s) ya[s] = y[j + s] * sc[s];
     double Ts = S.Ts[i], dTs = 0.0;
+    // mixed form: 9 FP32 iterations and one FP64 one (quadratic convergence takes the FP32
+    // iterate, good to ~1e-7, to ~1e-14 in one FP64 step)
     if (sizeof(LU) == 4)
-      chem_temperature_mixed(P, ya, Ts, dTs, 8);  // mixed form: 8 FP32 + 2 FP64 iterations
+      chem_temperature_mixed(P, ya, Ts, dTs, 9);
     else
       chem_temperature(P, ya, Ts, dTs);
     S.Ts[i] = Ts;
@@ -56,7 +58,7 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
     double f[10];
     {  // source and Newton matrix from one rate evaluation (rates and T slopes)
       double k[kNRates], dk[kNRates];
-      chem_rates<true>(P, Ts, k, dk);
+      chem_rates<true, kMixed>(P, Ts, k, dk);
       const GeRecip Rg = ge_recip(k, ya);  // shared by the source and the Jacobian's ge row
       {
         double r[21], sp[9];
