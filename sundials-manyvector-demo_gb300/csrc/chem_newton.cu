@@ -46,10 +46,10 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
 #pragma unroll
     for (int s = 0; s < 10; ++s) ya[s] = y[j + s] * sc[s];
     double Ts = S.Ts[i], dTs = 0.0;
-    // mixed form: 9 FP32 iterations and one FP64 one (quadratic convergence takes the FP32
-    // iterate, good to ~1e-7, to ~1e-14 in one FP64 step)
+    // mixed form: 8 FP32 iterations, then FP64 ones; the second FP64 iteration only for cells
+    // whose first FP64 correction was above 1e-7 T
     if (sizeof(LU) == 4)
-      chem_temperature_mixed(P, ya, Ts, dTs, 9);
+      chem_temperature_mixed(P, ya, Ts, dTs, 8, true);
     else
       chem_temperature(P, ya, Ts, dTs);
     S.Ts[i] = Ts;
