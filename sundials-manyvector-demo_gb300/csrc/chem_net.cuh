@@ -88,12 +88,8 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
 // once at setup exactly as the iterations would round the FP64 entries) and the rest in FP64.  From the converged basin the
 // FP64 iterations restore full accuracy (Newton's quadratic convergence), so the result
 // matches chem_temperature's to rounding whenever the reference's ten iterations converge.
-//   skip_converged: stop the FP64 iterations after the first whose correction is below
-//   1e-7 T (from there Newton's quadratic convergence leaves ~1e-14); cells whose FP32 phase
-//   ended farther off still take every iteration.
 __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, const double (&y)[10],
-                                                       double& Ts, double& dTs_ge, int nfloat,
-                                                       bool skip_converged = false) {
+                                                       double& Ts, double& dTs_ge, int nfloat) {
   const float kb = 1.3806504e-16f, mh = 1.67e-24f, gm1 = 1.5f;
   const float H2_1 = (float)y[0], H2_2 = (float)y[1], H_1 = (float)y[2], H_2 = (float)y[3],
               H_m0 = (float)y[4], He_1 = (float)y[5], He_2 = (float)y[6], He_3 = (float)y[7],
@@ -155,7 +151,6 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     const double dgev = kdmd * Tc * nsum - dge0;
     Tnew = Tc - dgev / dge_dTd;
     Ts = Tnew;
-    if (skip_converged && fabs(Tnew - Tc) <= 1e-7 * fabs(Tnew)) break;
   }
   Ts = Tnew;
   if (Ts < P.tlo) Ts = P.tlo;
