@@ -749,11 +749,12 @@ IMEX_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bi
 
 def run_imex(torch, gbmv, n, tf, with_cpu):
     """ARK-IMEX chemistry-hydrodynamics to t_f on the chem_hydro state (integrate.ark_imex_evolve
-    over integrate.ChemHydroImex: ARK3(2)4L[2]SA, WENO explicit, chemistry implicit with the
-    FP64 Jacobian and block LU, device WRMS norms; the reference IMEX inputs' step control),
-    with the FP64 and the GBMV_MIXED_FAST explicit RHS: time-to-t_f, step and solver
-    statistics, their max-normalised difference; the oracle-driven run of the same driver on
-    an 8x6x5 sample on one host core beside it."""
+    over integrate.ChemHydroImex: ARK3(2)4L[2]SA, WENO explicit, chemistry implicit, device
+    WRMS norms; the reference IMEX inputs' step control): the FP64 and the GBMV_MIXED_FAST
+    explicit RHS with ARKODE's modified Newton over the FP64 Jacobian and block LU, and
+    GBMV_MIXED_FAST with full Newton corrections from the fused per-cell kernel: time-to-t_f,
+    step and solver statistics, max-normalised differences from the FP64 run; the
+    oracle-driven run of the same driver on an 8x6x5 sample on one host core beside it."""
     import h5tables
     import integrate
     import workloads as W
@@ -764,13 +765,17 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
                         "(WENO explicit, chemistry implicit), rtol 1e-6 atol 1e-10, maxcor 10, "
                         "nlscoef 0.01, I controller safety 0.99 bias 2 growth 2"), "forms": {}}
     finals = {}
-    for name, prec in (("fp64", gbmv.FP64), ("mixed_fast", gbmv.MIXED_FAST)):
+    # fp64 / mixed_fast: ARKODE's modified Newton over fimpl, Jimpl and the block LU;
+    # mixed_fast_fused: full Newton stage corrections from the fused per-cell kernel
+    for name, prec, fused in (("fp64", gbmv.FP64, False), ("mixed_fast", gbmv.MIXED_FAST, False),
+                              ("mixed_fast_fused", gbmv.MIXED_FAST, True)):
         hy = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"])
         c = gbmv.Chem(n ** 3, tables)
         c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
         w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
         prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, IMEX_OPTS["rtol"], IMEX_OPTS["atol"],
-                                       prec)
+                                       prec, fused_newton=fused, lu_precision=gbmv.MIXED,
+                                       refine=1)
         wc = [x.clone() for x in w]  # warm-up on a copy (allocations)
         integrate.ark_imex_evolve(prob, 0.0, tf * 1e-17, wc, **IMEX_OPTS)  # a few steps
         c.state("Ts").fill_(1000.0)
@@ -788,13 +793,14 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
                               "Mcell_steps_per_s": round(n ** 3 * st.steps / dt / 1e6, 4)}
         del hy, c, w, prob
         torch.cuda.empty_cache()
-    errs = {}
-    for nm, a, b in zip(["rho", "mx", "my", "mz", "et", "chem"], finals["mixed_fast"],
-                        finals["fp64"]):
-        errs[nm] = float(f"{float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)):.3e}")
-    out["mixed_fast_vs_fp64_maxnorm_err"] = errs
-    out["speedup_mixed_fast_vs_fp64"] = round(out["forms"]["fp64"]["s_to_tf"] /
-                                              out["forms"]["mixed_fast"]["s_to_tf"], 3)
+    for form in ("mixed_fast", "mixed_fast_fused"):
+        errs = {}
+        for nm, a, b in zip(["rho", "mx", "my", "mz", "et", "chem"], finals[form],
+                            finals["fp64"]):
+            errs[nm] = float(f"{float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)):.3e}")
+        out[f"{form}_vs_fp64_maxnorm_err"] = errs
+        out[f"speedup_{form}_vs_fp64"] = round(out["forms"]["fp64"]["s_to_tf"] /
+                                               out["forms"][form]["s_to_tf"], 3)
     if with_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle_py as O

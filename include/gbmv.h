@@ -205,6 +205,16 @@ int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* 
                      double gamma, double time_units, int lu_precision, int refine,
                      void* stream);
 
+/* Implicit-stage form of gbmv_chem_newton: f = TimeUnits * f(y) and
+ *   x = (I - gamma * J(y))^{-1} (b + gamma * f)
+ * -- one full Newton correction of the stage equation z = a + gamma f(z) at the iterate y = z
+ * with b = a - z, the Newton matrix formed afresh at y (the ARKStep implicit stage of
+ * src/imex_chem_hydro_main.cpp with fimpl, Jimpl and the block solver fused per cell).  Same
+ * precisions and return values as gbmv_chem_newton; b, f, x: 10 * ncells doubles. */
+int gbmv_chem_newton_stage(gbmv_chem c, double t, const double* y, const double* b, double* f,
+                           double* x, double gamma, double time_units, int lu_precision,
+                           int refine, void* stream);
+
 /* Same, asynchronous and CUDA-graph capturable: a singular block raises *d_info (device int,
  * atomicMax to 1) instead of being returned. */
 int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, double* x,

@@ -454,6 +454,27 @@ int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* 
   return GBMV_OK;
 }
 
+int gbmv_chem_newton_stage(gbmv_chem c, double t, const double* y, const double* b, double* f,
+                           double* x, double gamma, double time_units, int lu_precision,
+                           int refine, void* stream) {
+  (void)t;
+  if (!c || !y || !b || !f || !x || refine < 0 || refine > 8 ||
+      (lu_precision != GBMV_FP64 && lu_precision != GBMV_MIXED)) {
+    set_error("bad chem_newton_stage arguments");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  GBMV_CUDA_TRY(cudaMemsetAsync(c->d_info, 0, sizeof(int), s));
+  int rc = chem_newton(c->P, c->S, c->n, y, f, x, gamma, time_units, lu_precision == GBMV_MIXED,
+                       refine, c->d_info, s, c->newton_bps, b);
+  if (rc) return rc;
+  int h = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&h, c->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h) { set_error("singular Newton block"); return 1; }
+  return GBMV_OK;
+}
+
 /* ------------------------------------------------------------------ DIRK integrator */
 
 void gbmv_dirk_opts_default(gbmv_dirk_opts* o) {

@@ -47,9 +47,10 @@ int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot,
                 int ncomp, cudaStream_t s);
 
 // fused source + Jacobian + Newton matrix + LU solve (chem_newton.cu)
+// b: null, or the implicit-stage right-hand side base: x = (I - gamma J)^{-1} (b + gamma f)
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
-                cudaStream_t s, int blocks_per_sm = 0);
+                cudaStream_t s, int blocks_per_sm = 0, const double* b = nullptr);
 
 // persistent per-cell DIRK integration from t0 to tout (chem_dirk.cu)
 struct DirkOpts {

@@ -29,7 +29,8 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
                                                          double* __restrict__ xout,
                                                          double gamma, double tunit,
                                                          int refine,
-                                                         int* __restrict__ info_out) {
+                                                         int* __restrict__ info_out,
+                                                         const double* __restrict__ bst) {
   extern __shared__ unsigned char smem_raw[];
   constexpr bool kMixed = sizeof(LU) == 4;
   // FP32-LU form: As[e * BS] = FP64 matrix entry e of kJacPattern; L[(col*10+row) * BS] factor
@@ -91,6 +92,10 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
     }
 #pragma unroll
     for (int s = 0; s < 10; ++s) f[s] = fout[j + s];
+    if (bst) {  // implicit-stage form: right-hand side b + gamma f(y)
+#pragma unroll
+      for (int s = 0; s < 10; ++s) f[s] = fma(gamma, f[s], bst[j + s]);
+    }
 
     int piv[10];
     double x[10];
@@ -157,7 +162,7 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
 template <typename LU>
 static int launch_newton(const ChemParams& P, const ChemState& S, long n, const double* y,
                          double* f, double* x, double gamma, double tunit, int refine,
-                         int* d_info, cudaStream_t s, long blocks) {
+                         int* d_info, cudaStream_t s, long blocks, const double* b) {
   constexpr int BS = kNtThreads;
   const size_t shm = (size_t)BS * (sizeof(LU) == 4 ? 64 * sizeof(double) + 100 * sizeof(float)
                                                    : 100 * sizeof(double));
@@ -165,23 +170,24 @@ static int launch_newton(const ChemParams& P, const ChemState& S, long n, const 
   GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_newton_kernel<LU, BS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   chem_newton_kernel<LU, BS><<<(int)blocks, BS, shm, s>>>(P, S, n, y, f, x, gamma, tunit,
-                                                          refine, d_info);
+                                                          refine, d_info, b);
   GBMV_LAUNCH_CHECK("chem_newton_kernel");
   return GBMV_OK;
 }
 
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
-                cudaStream_t s, int blocks_per_sm) {
-  long b = (n + kNtThreads - 1) / kNtThreads;
+                cudaStream_t s, int blocks_per_sm, const double* b) {
+  long blk = (n + kNtThreads - 1) / kNtThreads;
   // default: a deep grid-stride grid; blocks_per_sm > 0: exactly that many resident blocks per
   // SM (a persistent grid leaving room for a kernel running beside it on another stream)
   const long cap = (long)kSM * (blocks_per_sm > 0 ? blocks_per_sm : 48);
-  if (b > cap) b = cap;
-  if (b < 1) b = 1;
+  if (blk > cap) blk = cap;
+  if (blk < 1) blk = 1;
   ProfScope ps("chem_newton", s);
-  if (lu_fp32) return launch_newton<float>(P, S, n, y, f, x, gamma, tunit, refine, d_info, s, b);
-  return launch_newton<double>(P, S, n, y, f, x, gamma, tunit, refine, d_info, s, b);
+  if (lu_fp32)
+    return launch_newton<float>(P, S, n, y, f, x, gamma, tunit, refine, d_info, s, blk, b);
+  return launch_newton<double>(P, S, n, y, f, x, gamma, tunit, refine, d_info, s, blk, b);
 }
 
 }  // namespace gbmv

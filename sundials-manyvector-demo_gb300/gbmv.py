@@ -89,6 +89,8 @@ SIGNATURES = [
                              C.c_int, _VP]),
     ("gbmv_fexpl_async", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
                                    C.c_double, C.c_int, _VP, _VP]),
+    ("gbmv_chem_newton_stage", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, _VP, C.c_double,
+                                         C.c_double, C.c_int, C.c_int, _VP]),
     ("gbmv_chem_newton_async", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double, C.c_double,
                                          C.c_int, C.c_int, _VP, _VP]),
     ("gbmv_dirk_opts_default", None, [C.POINTER(_DirkOpts)]),
@@ -295,6 +297,15 @@ class Chem:
                                               gamma, time_units, lu_precision, refine,
                                               _stream_ptr(stream)),
                       "gbmv_chem_newton", allow=(0, 1))
+
+    def newton_stage(self, t, y, b, f, x, gamma, time_units=1.0, lu_precision=FP64, refine=2,
+                     stream=None) -> int:
+        """Fused implicit-stage correction: f = TimeUnits*f(y) and
+        x = (I - gamma*J(y))^{-1} (b + gamma*f); 0, or 1 if a block is singular."""
+        return _check(load().gbmv_chem_newton_stage(self.c, t, _dev_ptr(y), _dev_ptr(b),
+                                                    _dev_ptr(f), _dev_ptr(x), gamma, time_units,
+                                                    lu_precision, refine, _stream_ptr(stream)),
+                      "gbmv_chem_newton_stage", allow=(0, 1))
 
     def calculate_jacobian_cvklu(self, t, y, J, time_units=1.0, stream=None):
         return _check(load().gbmv_chem_jac(self.c, t, _dev_ptr(y), _dev_ptr(J), time_units,

@@ -331,6 +331,9 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
       solve(b) -> list               M^{-1} b (identity on the components fi does not touch)
       norm(v, y) -> float            WRMS norm of v with weights 1 / (rtol |y| + atol)
       postprocess(t, y)              optional, after every accepted step
+      correction(t, z, a, gamma)     optional: one full Newton correction of the stage equation
+                                     at z with the Newton matrix formed afresh (used instead of
+                                     fi / setup / solve when prob.fused_newton is true)
 
     Each implicit stage z = a + gamma fi(t_i, z) is solved by modified Newton from the trivial
     predictor z = y_n with ARKODE's rules: matrix set up again when gamma moved by more than
@@ -338,7 +341,10 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
     from an earlier step; correction scaled by 2 / (1 + gamma / gamma_p) against a lagged
     matrix; rate estimate crate = max(crdown crate, del / del_p); converged when
     min(1, crate) del / nlscoef <= 1; divergence when del > rdiv del_p; at most maxcor
-    iterations; a failure with a current matrix cuts the step by etacf.  Error control: WRMS
+    iterations; a failure with a current matrix cuts the step by etacf.  With
+    prob.fused_newton the stage iterations are full Newton steps from prob.correction (the
+    matrix current at every iterate, so no setups, lagging or gamma-ratio scaling) under the
+    same convergence test.  Error control: WRMS
     norm dsm of the embedded difference with weights from y_n, accepted when dsm <= 1; I
     controller eta = safety (bias dsm)^(-1/p) (p the embedding order, ARKODE's convention),
     bounded by etamx1 on the first step and growth after, kept at 1 inside [1, 1.5) (the
@@ -354,6 +360,7 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
     ns = len(c)
     kexp = -1.0 / table["p"]
     post = getattr(prob, "postprocess", None)
+    fused = bool(getattr(prob, "fused_newton", False))
     t = t0
     gp, nst_lp, crate = 0.0, 0, 1.0
     force_setup, jcur = True, False
@@ -384,22 +391,33 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
                        [(h * ai[i][j], Fi[j]) for j in range(i)])
             z = [_clone(x) for x in y]  # trivial predictor
             m, delp = 0, 0.0
+            if fused:
+                jcur = True  # the rate estimate carries across stages, as between setups
             while True:
-                fiz = prob.fi(ti, z)
-                st.nfi += 1
-                if force_setup or st.steps >= nst_lp + msbp or not abs(gam / gp - 1.0) <= dgmax:
-                    rc = prob.setup(ti, z, gam)
+                if fused:
+                    d = prob.correction(ti, z, a, gam)
+                    st.nfi += 1
                     st.nsetups += 1
-                    gp, nst_lp, crate = gam, st.steps, 1.0
-                    jcur, force_setup = True, False
-                    if rc != 0:
+                    if d is None:  # a singular block
                         conv_fail = True
                         break
-                r = _combo(a, [(-1.0, z), (gam, fiz)])
-                d = prob.solve(r)
-                if gam != gp:
-                    sc = 2.0 / (1.0 + gam / gp)
-                    d = [x * sc for x in d]
+                else:
+                    fiz = prob.fi(ti, z)
+                    st.nfi += 1
+                    if (force_setup or st.steps >= nst_lp + msbp or
+                            not abs(gam / gp - 1.0) <= dgmax):
+                        rc = prob.setup(ti, z, gam)
+                        st.nsetups += 1
+                        gp, nst_lp, crate = gam, st.steps, 1.0
+                        jcur, force_setup = True, False
+                        if rc != 0:
+                            conv_fail = True
+                            break
+                    r = _combo(a, [(-1.0, z), (gam, fiz)])
+                    d = prob.solve(r)
+                    if gam != gp:
+                        sc = 2.0 / (1.0 + gam / gp)
+                        d = [x * sc for x in d]
                 z = _combo(z, [(1.0, d)])
                 dn = prob.norm(d, y)
                 m += 1
@@ -485,11 +503,19 @@ class ChemHydroImex:
     source on component 5, zero on the fluid, :811-848), the Newton matrix I - gamma Jimpl
     (:850-908) from gbmv_chem_jac + gbmv_block_form_newton, factored and solved by the
     block-diagonal LU (SUNLinSol_BDMPIMV, :1075-1194), PostprocessStep after every step
-    (:1002-1051), WRMS norms by gbmv_wrms_norm.  `precision` selects the fexpl form."""
+    (:1002-1051), WRMS norms by gbmv_wrms_norm.  `precision` selects the fexpl form;
+    `fused_newton` replaces fi / setup / solve in the stage iterations by the fused per-cell
+    kernel's full Newton corrections."""
 
-    def __init__(self, gbmv, hydro, chem, energy_units, time_units, rtol, atol, precision=0):
+    def __init__(self, gbmv, hydro, chem, energy_units, time_units, rtol, atol, precision=0,
+                 fused_newton=False, lu_precision=1, refine=1):
         import torch
         self.g, self.hydro, self.chem = gbmv, hydro, chem
+        # fused_newton: stage corrections from gbmv_chem_newton_stage (source, Jacobian and
+        # factor per cell and per iterate, FP32 LU with `refine` FP64-residual refinements when
+        # lu_precision is GBMV_MIXED), no Jacobian in HBM
+        self.fused_newton = fused_newton
+        self.lu_precision, self.refine = lu_precision, refine
         self.eu, self.tu = energy_units, time_units
         self.rtol, self.atol = rtol, atol
         self.precision = precision
@@ -522,6 +548,15 @@ class ChemHydroImex:
         x = torch.empty_like(b[5])
         self.ls.solve(self.J, x.view(-1), b[5].view(-1))
         return list(b[:5]) + [x]
+
+    def correction(self, t, z, a, gamma):
+        import torch
+        b = a[5] - z[5]
+        f, x = torch.empty_like(z[5]), torch.empty_like(z[5])
+        if self.chem.newton_stage(t, z[5].view(-1), b.view(-1), f.view(-1), x.view(-1), gamma,
+                                  self.tu, self.lu_precision, self.refine) != 0:
+            return None
+        return [ai - zi for ai, zi in zip(a[:5], z[:5])] + [x]
 
     def norm(self, v, y):
         return self.hydro.wrms_norm(v, y, self.rtol, self.atol)

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bias=2.0, growth=2.0)
 
 
-def _gpu_problem(torch, wl, tables, eu, tu, precision=0):
+def _gpu_problem(torch, wl, tables, eu, tu, precision=0, **kw):
     import gbmv
     import integrate
     nz, ny, nx = wl["fields"][0].shape
@@ -24,7 +24,8 @@ def _gpu_problem(torch, wl, tables, eu, tu, precision=0):
     c = gbmv.Chem(nx * ny * nz, tables)
     c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
     w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
-    prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, OPTS["rtol"], OPTS["atol"], precision)
+    prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, OPTS["rtol"], OPTS["atol"], precision,
+                                   **kw)
     return hy, prob, w
 
 
@@ -89,5 +90,24 @@ def test_imex_mixed_fexpl_matches_fp64(cuda, tables):
         runs.append(([x.cpu().numpy() for x in w], st))
     (a, sa), (b, sb) = runs
     assert abs(sa.steps - sb.steps) <= max(2, sa.steps // 20)
+    for k in range(6):
+        assert maxnorm_err(b[k], a[k]) <= 1e-6, k
+
+
+def test_imex_fused_newton_matches_modified(cuda, tables):
+    """Stage solves by the fused per-cell kernel (full Newton, FP32 LU + one FP64-residual
+    refinement) against ARKODE's modified Newton over the separate entries: the same solution
+    to well inside the integration tolerance, in no more Newton iterations."""
+    torch = cuda
+    import integrate
+    wl = W.chem_hydro(shape=(12, 10, 8))
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    runs = []
+    for fused in (False, True):
+        _, prob, w = _gpu_problem(torch, wl, tables, eu, tu, 0, fused_newton=fused)
+        st = integrate.ark_imex_evolve(prob, 0.0, 4e-6, w, **OPTS)
+        runs.append(([x.cpu().numpy() for x in w], st))
+    (a, sa), (b, sb) = runs
+    assert sb.ncf == 0 and sb.nni <= sa.nni
     for k in range(6):
         assert maxnorm_err(b[k], a[k]) <= 1e-6, k

@@ -129,6 +129,28 @@ def test_imex_adaptive_error_tracks_tolerance():
     assert steps[1] < 1e4 * T / 50
 
 
+class FusedSplitProblem(SplitProblem):
+    """The same problem with full Newton corrections (the fused-kernel protocol)."""
+    fused_newton = True
+
+    def correction(self, t, z, a, gamma):
+        r = [a[0] - z[0], (a[1] - z[1]) + gamma * self.lam * (z[1] - math.cos(t))]
+        return [r[0], r[1] / (1.0 - gamma * self.lam)]
+
+
+def test_imex_fused_newton_matches_modified():
+    T = 2.0
+    p1 = SplitProblem(-1e3, rtol=1e-8, atol=1e-11)
+    p2 = FusedSplitProblem(-1e3, rtol=1e-8, atol=1e-11)
+    y1, s1 = _run(p1, T)
+    y2, s2 = _run(p2, T)
+    for y in (y1, y2):
+        assert abs(y[0][0] - math.sin(T)) < 1e-6 and abs(y[1][0] - math.cos(T)) < 1e-6
+    assert abs(y1[1][0] - y2[1][0]) < 1e-7
+    # a linear implicit part: the full Newton step is exact, so each stage converges at once
+    assert s2.ncf == 0 and s2.nni <= s1.nni
+
+
 def test_imex_recovers_from_failed_setup():
     _, base = _run(SplitProblem(-50.0), 1.0)
     p = SplitProblem(-50.0, fail_setups=2)
