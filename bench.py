@@ -766,7 +766,8 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
                         "nlscoef 0.01, I controller safety 0.99 bias 2 growth 2"), "forms": {}}
     finals = {}
     # fp64 / mixed_fast: ARKODE's modified Newton over fimpl, Jimpl and the block LU;
-    # mixed_fast_fused: full Newton stage corrections from the fused per-cell kernel
+    # mixed_fast_fused: full Newton stage corrections from the fused per-cell kernel (FP64
+    # factor)
     for name, prec, fused in (("fp64", gbmv.FP64, False), ("mixed_fast", gbmv.MIXED_FAST, False),
                               ("mixed_fast_fused", gbmv.MIXED_FAST, True)):
         hy = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"])
@@ -774,8 +775,7 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
         c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
         w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
         prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, IMEX_OPTS["rtol"], IMEX_OPTS["atol"],
-                                       prec, fused_newton=fused, lu_precision=gbmv.MIXED,
-                                       refine=1)
+                                       prec, fused_newton=fused)
         wc = [x.clone() for x in w]  # warm-up on a copy (allocations)
         integrate.ark_imex_evolve(prob, 0.0, tf * 1e-17, wc, **IMEX_OPTS)  # a few steps
         c.state("Ts").fill_(1000.0)

@@ -95,9 +95,9 @@ def test_imex_mixed_fexpl_matches_fp64(cuda, tables):
 
 
 def test_imex_fused_newton_matches_modified(cuda, tables):
-    """Stage solves by the fused per-cell kernel (full Newton, FP32 LU + one FP64-residual
-    refinement) against ARKODE's modified Newton over the separate entries: the same solution
-    to well inside the integration tolerance, in no more Newton iterations."""
+    """Stage solves by the fused per-cell kernel (full Newton with the FP64 factor) against
+    ARKODE's modified Newton over the separate entries: the same solution to well inside the
+    integration tolerance, in fewer Newton iterations."""
     torch = cuda
     import integrate
     wl = W.chem_hydro(shape=(12, 10, 8))
