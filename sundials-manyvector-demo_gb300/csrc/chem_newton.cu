@@ -115,7 +115,10 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
       if (sizeof(LU) == 4) {
         // iterative refinement against FP64 residuals; a cell stops as soon as its correction
         // is below 1e-13 of the solution (well-conditioned cells need one step, the
-        // ill-conditioned ones use up to `refine`)
+        // ill-conditioned ones use up to `refine`); a cell whose last correction is still above
+        // 1e-6 of its solution (the FP32 factor too poor a preconditioner for its block)
+        // takes the FP64 factor below
+        float dlast = 0.f, xlast = 1.f;
         for (int it = 0; it < refine; ++it) {
           double rr[10];
 #pragma unroll
@@ -134,12 +137,14 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
             dmax = fmaxf(dmax, fabsf((float)ds[s]));
             xmax = fmaxf(xmax, fabsf((float)x[s]));
           }
+          dlast = dmax;
+          xlast = xmax;
           if (dmax <= 1e-13f * xmax) break;
         }
         bool finite = true;
 #pragma unroll
         for (int s = 0; s < 10; ++s) finite = finite && isfinite(x[s]);
-        fp64_fallback = !finite;
+        fp64_fallback = !finite || !(dlast <= 1e-6f * xlast);
       }
     }
     if (fp64_fallback) {  // FP32 factor singular or out of range: factor the FP64 matrix,
