@@ -26,8 +26,6 @@ namespace gbmv {
 // ---- conversions used by the type-generic code
 __device__ __forceinline__ double num_from(double d, double*) { return d; }
 __device__ __forceinline__ f2 num_from(double d, f2*) { return f2_from_double(d); }
-__device__ __forceinline__ double num_to_double(double x) { return x; }
-__device__ __forceinline__ double num_to_double(f2 x) { return x.to_double(); }
 
 __device__ __forceinline__ double num_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ f2 num_sqrt(f2 x) { return f2_sqrt(x); }
@@ -75,17 +73,6 @@ __device__ __forceinline__ double weno_combine(double bA, double bB, double bC, 
   aB = aB * aB;
   aC = aC * aC;
   const double tA = dA * (aB * aC), tB = dB * (aA * aC), tC = dC * (aA * aB);
-  return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
-}
-__device__ __forceinline__ f2 weno_combine(f2 bA, f2 bB, f2 bC, f2 qA, f2 qB, f2 qC, f2 dA, f2 dB,
-                                           f2 dC) {
-  // normalised by the smallest a_k: ratios in (0, 1], nothing overflows the float range
-  const f2 eps(1e-6);
-  const f2 aA = eps + bA, aB = eps + bB, aC = eps + bC;
-  f2 m = aA < aB ? aA : aB;
-  m = m < aC ? m : aC;
-  const f2 rA = m / aA, rB = m / aB, rC = m / aC;
-  const f2 tA = dA * (rA * rA), tB = dB * (rB * rB), tC = dC * (rC * rC);
   return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
 }
 

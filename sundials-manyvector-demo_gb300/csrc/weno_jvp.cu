@@ -33,7 +33,6 @@ __device__ __forceinline__ Dual operator/(Dual a, Dual b) {
 __device__ __forceinline__ bool operator<(Dual a, Dual b) { return a.v < b.v; }
 __device__ __forceinline__ bool operator<=(Dual a, Dual b) { return a.v <= b.v; }
 __device__ __forceinline__ Dual num_from(double x, Dual*) { return Dual(x); }
-__device__ __forceinline__ double num_to_double(Dual x) { return x.v; }
 __device__ __forceinline__ Dual num_sqrt(Dual x) {
   const double s = sqrt(x.v);
   return Dual(s, x.d / (2.0 * s));
