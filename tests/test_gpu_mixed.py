@@ -100,6 +100,36 @@ def test_fused_newton_matches_separate_path(cuda, tables, lu):
         assert np.max(np.abs(t1 - t2) / t1) <= 1e-12
 
 
+@pytest.mark.parametrize("lu", [0, 1])
+def test_newton_stage_matches_separate_path(cuda, tables, lu):
+    """gbmv_chem_newton_stage == rhs + jac + (I - gamma J) + factor + solve of b + gamma f."""
+    torch = cuda
+    import gbmv
+    n, gamma, tu = 4096, 3e-4, 1.0e11
+    c1, y, state = _chem_setup(torch, tables, n, 402)
+    c2, _, _ = _chem_setup(torch, tables, n, 402)
+    rng = np.random.default_rng(402)
+    ys = torch.from_numpy(state).cuda()
+    b = torch.from_numpy(rng.uniform(-1e-3, 1e-3, size=10 * n) * state).cuda()
+    f1, x1 = torch.empty_like(ys), torch.empty_like(ys)
+    J = torch.empty(100 * n, dtype=torch.float64, device="cuda")
+    c1.calculate_rhs_cvklu(0.0, ys, f1, tu)
+    c1.calculate_jacobian_cvklu(0.0, ys, J, tu)
+    gbmv.form_newton_matrix(J, gamma)
+    ls = gbmv.BlockLinearSolver(n)
+    assert ls.setup(J) == 0
+    ls.solve(J, x1, b + gamma * f1)
+    f2, x2 = torch.empty_like(ys), torch.empty_like(ys)
+    assert c2.newton_stage(0.0, ys, b, f2, x2, gamma, tu, lu_precision=lu, refine=4) == 0
+    torch.cuda.synchronize()
+    a_, b_ = f1.cpu().numpy().reshape(n, 10), f2.cpu().numpy().reshape(n, 10)
+    xa, xb = x1.cpu().numpy().reshape(n, 10), x2.cpu().numpy().reshape(n, 10)
+    ftol, xtol = (1e-12, 1e-10) if lu == 0 else (1e-9, 1e-8)
+    for s in range(10):
+        assert maxnorm_err(b_[:, s], a_[:, s]) <= ftol, s
+        assert maxnorm_err(xb[:, s], xa[:, s]) <= xtol, (s, maxnorm_err(xb[:, s], xa[:, s]))
+
+
 def test_fused_newton_against_oracle(cuda, tables):
     torch = cuda
     n, gamma, tu = 512, 3e-5, 1.0e11
