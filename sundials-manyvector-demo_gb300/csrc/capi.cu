@@ -433,34 +433,15 @@ int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, do
                      refine, d_info, (cudaStream_t)stream, c->newton_bps);
 }
 
-int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* x,
-                     double gamma, double time_units, int lu_precision, int refine,
-                     void* stream) {
-  (void)t;
+}  // extern "C"
+
+// synchronous fused Newton (b null: gbmv_chem_newton; b set: its implicit-stage form)
+static int newton_sync(gbmv_chem c, const double* y, const double* b, double* f, double* x,
+                       double gamma, double time_units, int lu_precision, int refine,
+                       void* stream) {
   if (!c || !y || !f || !x || refine < 0 || refine > 8 ||
       (lu_precision != GBMV_FP64 && lu_precision != GBMV_MIXED)) {
     set_error("bad chem_newton arguments");
-    return GBMV_EINVAL;
-  }
-  cudaStream_t s = (cudaStream_t)stream;
-  GBMV_CUDA_TRY(cudaMemsetAsync(c->d_info, 0, sizeof(int), s));
-  int rc = chem_newton(c->P, c->S, c->n, y, f, x, gamma, time_units, lu_precision == GBMV_MIXED,
-                       refine, c->d_info, s, c->newton_bps);
-  if (rc) return rc;
-  int h = 0;
-  GBMV_CUDA_TRY(cudaMemcpyAsync(&h, c->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
-  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
-  if (h) { set_error("singular Newton block"); return 1; }
-  return GBMV_OK;
-}
-
-int gbmv_chem_newton_stage(gbmv_chem c, double t, const double* y, const double* b, double* f,
-                           double* x, double gamma, double time_units, int lu_precision,
-                           int refine, void* stream) {
-  (void)t;
-  if (!c || !y || !b || !f || !x || refine < 0 || refine > 8 ||
-      (lu_precision != GBMV_FP64 && lu_precision != GBMV_MIXED)) {
-    set_error("bad chem_newton_stage arguments");
     return GBMV_EINVAL;
   }
   cudaStream_t s = (cudaStream_t)stream;
@@ -473,6 +454,26 @@ int gbmv_chem_newton_stage(gbmv_chem c, double t, const double* y, const double*
   GBMV_CUDA_TRY(cudaStreamSynchronize(s));
   if (h) { set_error("singular Newton block"); return 1; }
   return GBMV_OK;
+}
+
+extern "C" {
+
+int gbmv_chem_newton(gbmv_chem c, double t, const double* y, double* f, double* x,
+                     double gamma, double time_units, int lu_precision, int refine,
+                     void* stream) {
+  (void)t;
+  return newton_sync(c, y, nullptr, f, x, gamma, time_units, lu_precision, refine, stream);
+}
+
+int gbmv_chem_newton_stage(gbmv_chem c, double t, const double* y, const double* b, double* f,
+                           double* x, double gamma, double time_units, int lu_precision,
+                           int refine, void* stream) {
+  (void)t;
+  if (!b) {
+    set_error("chem_newton_stage needs the stage base b");
+    return GBMV_EINVAL;
+  }
+  return newton_sync(c, y, b, f, x, gamma, time_units, lu_precision, refine, stream);
 }
 
 /* ------------------------------------------------------------------ DIRK integrator */
