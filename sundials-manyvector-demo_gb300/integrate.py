@@ -255,7 +255,8 @@ class ImexResult:
         self.nsetups = 0     # Newton-matrix setups (Jacobian + factorisation)
         self.nfe = 0         # explicit RHS evaluations
         self.nfi = 0         # implicit RHS evaluations
-        self.h_last = 0.0
+        self.h_last = 0.0    # last accepted step
+        self.h_next = 0.0    # the step the controller would attempt next (the restart h0)
 
 
 def _combo(base, terms):
@@ -492,6 +493,7 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
             if nef_s >= small_nef:
                 eta = min(eta, etamxf)
             h *= eta
+    st.h_next = h
     return st
 
 
