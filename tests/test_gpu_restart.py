@@ -44,7 +44,8 @@ def test_restart_continues_the_run(cuda, tables, tmp_path):
     assert st1.steps > 3 and st1.h_next > 0.0
     path = h5io.write_solution(str(tmp_path), 1, t1, w, DOMAIN, field_units)
     params = {k: (0 if kind == "i" else 0.0) for k, kind in h5io.PARAMETERS}
-    params.update(nx=8, ny=10, nz=12, nout=2, tf=t2, rtol=OPTS["rtol"], atol=OPTS["atol"],
+    nz, ny, nx = wl["fields"][0].shape
+    params.update(nx=nx, ny=ny, nz=nz, nout=2, tf=t2, rtol=OPTS["rtol"], atol=OPTS["atol"],
                   MassUnits=u["MassUnits"], LengthUnits=u["LengthUnits"],
                   TimeUnits=u["TimeUnits"], gamma=wl["gamma"], xr=1.0, yr=1.0, zr=1.0)
     h5io.write_parameters(str(tmp_path), params, tcur=t1, hcur=st1.h_next, iout=1)
@@ -53,8 +54,8 @@ def test_restart_continues_the_run(cuda, tables, tmp_path):
     # the restarted run: state and step size from the files, fresh handles
     p = h5io.read_parameters(str(tmp_path / "restart_parameters.txt"))
     assert p["restart"] == 1 and p["t0"] == t1 and p["nout"] == 1
-    t, fields = h5io.read_restart(str(tmp_path), p["restart"], 10, DOMAIN, (12, 10, 8),
-                                  field_units)
+    t, fields = h5io.read_restart(str(tmp_path), p["restart"], 10, DOMAIN,
+                                  wl["fields"][0].shape, field_units)
     assert t == t1 and path.endswith("output-0000001.hdf5")
     prob2, w2 = _problem(torch, wl, tables, fields)
     integrate.ark_imex_evolve(prob2, t, t2, w2, h0=p["h0"], **OPTS)
