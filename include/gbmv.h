@@ -157,6 +157,14 @@ int gbmv_conservation(gbmv_hydro h, const double* const* w, double mass_factor,
 int gbmv_wrms_norm(gbmv_hydro h, const double* const* v, const double* const* y, double rtol,
                    double atol, double* norm, void* stream);
 
+/* print_stats (src/io.cpp:552-640): rms[v] = sqrt(sum over cells of (w_v * units_v)^2 / ncells)
+ * for the 5 + nchem fields, units_v = density_units for rho, momentum_units for mx, my, mz,
+ * energy_units for et (all 1 for the dimensionless output, the reference's units = 0), the
+ * chemistry fields as stored.  FP64, compensated and deterministic.  rms is host memory (5 +
+ * nchem doubles); synchronous. */
+int gbmv_print_stats(gbmv_hydro h, const double* const* w, double density_units,
+                     double momentum_units, double energy_units, double* rms, void* stream);
+
 /* -------------------------------------------------------------- chemistry (part b) */
 
 typedef struct gbmv_chem_s* gbmv_chem;

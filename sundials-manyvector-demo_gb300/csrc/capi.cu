@@ -1,5 +1,6 @@
 // The C ABI (include/gbmv.h): handles mirroring EulerData / cvklu_data, argument checking,
 // dispatch to the kernels, ARKODE-convention return codes.
+#include <nvtx3/nvToolsExt.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -41,6 +42,7 @@ static bool g_prof_on = false;
 static std::vector<ProfRec> g_prof;
 
 ProfScope::ProfScope(const char* family, cudaStream_t s) : slot(-1), stream(s) {
+  nvtxRangePushA(family);
   if (!g_prof_on) return;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
@@ -58,9 +60,11 @@ ProfScope::ProfScope(const char* family, cudaStream_t s) : slot(-1), stream(s) {
   g_prof.push_back(r);
 }
 ProfScope::~ProfScope() {
-  if (slot < 0) return;
-  std::lock_guard<std::mutex> lk(g_prof_mu);
-  cudaEventRecord(g_prof[slot].e1, stream);
+  if (slot >= 0) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    cudaEventRecord(g_prof[slot].e1, stream);
+  }
+  nvtxRangePop();
 }
 
 }  // namespace gbmv
@@ -922,7 +926,7 @@ static int reduction_scratch(gbmv_hydro h, cudaStream_t s, const char* who) {
               "capture", who);
     return GBMV_EINVAL;
   }
-  if (cudaMalloc(&h->cons, conservation_scratch_doubles() * sizeof(double)) != cudaSuccess) {
+  if (cudaMalloc(&h->cons, reduction_scratch_doubles() * sizeof(double)) != cudaSuccess) {
     cudaGetLastError();
     h->cons = nullptr;
     return check_cuda(cudaErrorMemoryAllocation, "reduction scratch");
@@ -972,6 +976,25 @@ int gbmv_wrms_norm(gbmv_hydro h, const double* const* v, const double* const* y,
   if (rc) return rc;
   GBMV_CUDA_TRY(cudaMemcpyAsync(norm, h->cons + conservation_scratch_doubles() - 2,
                                 sizeof(double), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBMV_OK;
+}
+
+int gbmv_print_stats(gbmv_hydro h, const double* const* w, double density_units,
+                     double momentum_units, double energy_units, double* rms, void* stream) {
+  if (!h || !fields_ok(w, h->g.nchem) || !rms) {
+    set_error("null handle, field or output pointer");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (int rc = reduction_scratch(h, s, "gbmv_print_stats")) return rc;
+  Fields W;
+  for (int k = 0; k < 6; ++k) W.f[k] = (k < 5 || h->g.nchem) ? const_cast<double*>(w[k]) : nullptr;
+  int rc = field_rms(h->g, W, density_units, momentum_units, energy_units, h->cons, s);
+  if (rc) return rc;
+  const int nv = 5 + h->g.nchem;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(rms, h->cons + reduction_scratch_doubles() - 16,
+                                sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
   GBMV_CUDA_TRY(cudaStreamSynchronize(s));
   return GBMV_OK;
 }

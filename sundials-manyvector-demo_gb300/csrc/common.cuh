@@ -28,6 +28,8 @@ int check_cuda(cudaError_t e, const char* where);
 
 // Optional per-kernel-family timing with CUDA events on the launching stream
 // (gbmv_profile_enable); a no-op when disabled.
+// Per-family profiling scope around the kernel launches of one entry point: an NVTX range
+// (visible to ncu / nsys filters) always, CUDA events while gbmv_profile_enable is on.
 struct ProfScope {
   ProfScope(const char* family, cudaStream_t s);
   ~ProfScope();

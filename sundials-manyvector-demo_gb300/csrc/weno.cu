@@ -411,6 +411,86 @@ int wrms_norm(const Grid& g, const Fields& v, const Fields& y, double rtol, doub
   return GBMV_OK;
 }
 
+// print_stats (src/io.cpp:552-640): per field the root mean square over the grid,
+// sqrt(sum_cells (x * units)^2 / ncells), fluid fields in code units times the density,
+// momentum and energy units (1 for dimensionless output), the chemistry fields as stored.
+// Same fixed-grid compensated two-pass reduction as the conservation totals; partials in
+// scratch[v * kConsBlocks + block], results in scratch[16 * kConsBlocks + v].
+constexpr int kRmsMaxFields = 16;
+
+template <int NCHEM>
+__global__ void __launch_bounds__(256) field_rms_partial_kernel(long n, Fields w, double du,
+                                                                double mu, double eu,
+                                                                double* __restrict__ part) {
+  constexpr int NV = 5 + NCHEM;
+  double s[NV], c[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) s[v] = c[v] = 0.0;
+  const double u[5] = {du, mu, mu, mu, eu};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double x = w.f[v][i] * u[v];
+      two_sum_acc(s[v], c[v], x * x);
+    }
+#pragma unroll
+    for (int v = 0; v < NCHEM; ++v) {
+      const double x = w.f[5][v + (long)NCHEM * i];
+      two_sum_acc(s[5 + v], c[5 + v], x * x);
+    }
+  }
+  __shared__ double wsum[8][NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    double a = s[v] + c[v];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5][v] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += wsum[k][threadIdx.x];
+    part[threadIdx.x * kConsBlocks + blockIdx.x] = t;
+  }
+}
+
+__global__ void field_rms_final_kernel(const double* __restrict__ part, int nv, double ncell,
+                                       double* __restrict__ out) {
+  const int v = threadIdx.x;
+  if (v < nv) {
+    double s0 = 0.0, c0 = 0.0;
+    for (int k = 0; k < kConsBlocks; ++k) two_sum_acc(s0, c0, part[v * kConsBlocks + k]);
+    out[v] = sqrt((s0 + c0) / ncell);
+  }
+}
+
+size_t reduction_scratch_doubles() { return (size_t)kRmsMaxFields * kConsBlocks + kRmsMaxFields; }
+
+int field_rms(const Grid& g, const Fields& w, double du, double mu, double eu, double* d_scratch,
+              cudaStream_t s) {
+  switch (g.nchem) {
+#define GBMV_RMS(NC)                                                                   \
+  case NC:                                                                            \
+    field_rms_partial_kernel<NC><<<kConsBlocks, 256, 0, s>>>(g.ncell, w, du, mu, eu,   \
+                                                            d_scratch);               \
+    break;
+    GBMV_RMS(0)
+    GBMV_RMS(2)
+    GBMV_RMS(4)
+    GBMV_RMS(6)
+    GBMV_RMS(10)
+#undef GBMV_RMS
+    default: set_error("nchem=%d not compiled (0,2,4,6,10)", g.nchem); return GBMV_EUNSUPPORTED;
+  }
+  GBMV_LAUNCH_CHECK("field_rms_partial_kernel");
+  field_rms_final_kernel<<<1, 32, 0, s>>>(d_scratch, 5 + g.nchem, (double)g.ncell,
+                                         d_scratch + (size_t)kRmsMaxFields * kConsBlocks);
+  GBMV_LAUNCH_CHECK("field_rms_final_kernel");
+  return GBMV_OK;
+}
+
 int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s) {
   long b = (g.ncell + 255) / 256;
   if (b > (long)kSM * 8) b = (long)kSM * 8;

@@ -36,6 +36,11 @@ int conservation_sums(const Grid& g, const Fields& w, double* d_scratch, cudaStr
 // d_scratch[conservation_scratch_doubles() - 2] (scratch: conservation_scratch_doubles)
 int wrms_norm(const Grid& g, const Fields& v, const Fields& y, double rtol, double atol,
               double* d_scratch, cudaStream_t s);
+// per-field RMS (print_stats) into d_scratch[16 * 1024 + v]; every reduction of a handle shares
+// one scratch of reduction_scratch_doubles() (>= conservation_scratch_doubles())
+size_t reduction_scratch_doubles();
+int field_rms(const Grid& g, const Fields& w, double du, double mu, double eu, double* d_scratch,
+              cudaStream_t s);
 
 // derivatives of the FP64 flux divergence (weno_jvp.cu, weno_vjp.cu)
 size_t feuler_vjp_scratch_doubles(const Grid& g);

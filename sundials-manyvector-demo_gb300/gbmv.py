@@ -65,6 +65,8 @@ SIGNATURES = [
     ("gbmv_conservation", C.c_int, [_VP, C.POINTER(_VP), C.c_double, C.c_double, _P, _VP]),
     ("gbmv_wrms_norm", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.c_double, C.c_double,
                                  _P, _VP]),
+    ("gbmv_print_stats", C.c_int, [_VP, C.POINTER(_VP), C.c_double, C.c_double, C.c_double,
+                                   _P, _VP]),
     ("gbmv_feuler_jvp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
                                   C.POINTER(_VP), _VP]),
     ("gbmv_feuler_vjp", C.c_int, [_VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
@@ -233,6 +235,15 @@ class Hydro:
         _check(load().gbmv_wrms_norm(self.h, _vec(v), _vec(y), rtol, atol, out,
                                      _stream_ptr(stream)), "gbmv_wrms_norm")
         return out[0]
+
+    def print_stats(self, w, units=(1.0, 1.0, 1.0), stream=None):
+        """Per-field RMS over the grid as print_stats (src/io.cpp:552) computes it; units =
+        (DensityUnits, MomentumUnits, EnergyUnits) for CGS output."""
+        nv = 5 + self.nchem
+        out = (C.c_double * nv)()
+        _check(load().gbmv_print_stats(self.h, _vec(w), units[0], units[1], units[2], out,
+                                       _stream_ptr(stream)), "gbmv_print_stats")
+        return list(out)
 
     def fEuler_jvp(self, t, w, dw, jv, stream=None) -> int:
         """jv = (d fEuler / d w) dw (FP64 form, forward mode)."""

@@ -151,3 +151,29 @@ def test_check_conservation_sums(cuda):
     w1 = [a + 1e-3 * b for a, b in zip(wp, wd)]
     m1, e1 = hp.check_conservation(w1)
     assert abs(m1 - m0) <= 1e-13 * abs(m0) and abs(e1 - e0) <= 1e-13 * abs(e0)
+
+
+@pytest.mark.parametrize("nchem", [0, 10])
+def test_print_stats_rms(cuda, nchem):
+    """print_stats (src/io.cpp:552-640): per-field RMS over the grid, fluid fields through the
+    CGS units when asked, chemistry as stored; against exactly rounded sums to 1e-14,
+    bitwise repeatable."""
+    torch = cuda
+    import math
+    import gbmv
+    wl = W.rayleigh_taylor(shape=(20, 18, 14), nchem=nchem)
+    nz, ny, nx = wl["fields"][0].shape
+    h = gbmv.Hydro((nx, ny, nz), nchem, wl["bc"], wl["gamma"])
+    w = [_dev(torch, f) for f in wl["fields"]]
+    n = nx * ny * nz
+    for units in ((1.0, 1.0, 1.0), (1.0210809016257265e-21, 0.031507493381465045, 9.7e17)):
+        rms = h.print_stats(w, units)
+        assert len(rms) == 5 + nchem
+        u = (units[0], units[1], units[1], units[1], units[2])
+        for v in range(5):
+            ref = math.sqrt(math.fsum(((wl["fields"][v] * u[v]) ** 2).ravel()) / n)
+            assert abs(rms[v] - ref) <= 1e-14 * ref, v
+        for v in range(nchem):
+            ref = math.sqrt(math.fsum((wl["fields"][5][..., v] ** 2).ravel()) / n)
+            assert abs(rms[5 + v] - ref) <= 1e-14 * ref, v
+        assert h.print_stats(w, units) == rms
