@@ -160,17 +160,66 @@ class MRIResult:
         self.fast_failed_cells = 0
 
 
-def mri_erk22b_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units,
-                      precision=0, slow_rhs=None, **fast_opts):
+# Explicit MRI-GARK coupling tables (A. Sandu, SIAM J. Sci. Comput. 41 (2019) A2260-A2292): slow
+# abscissae c and coefficient matrices G[k][i-1][j] -- the inner problem of stage i (from
+# T_{i-1} = t + c_{i-1} h to T_i) is v' = ffast(v) + r_i(tau), r_i(tau) = (1/dc_i) sum_k tau^k
+# sum_j G[k][i-1][j] fs(Y_j), tau = (t - T_{i-1}) / (dc_i h) in [0, 1], dc_i = c_i - c_{i-1};
+# the last stage is y_{n+1}.
+MRI_ERK22B = {"name": "MRI-GARK-ERK22b", "order": 2, "c": [0.0, 0.5, 1.0],
+              "G": [[[0.5], [-0.5, 1.0]]]}
+# the Knoth-Wolke third-order multirate infinitesimal step (MIS) method, whose slow table is
+# c = (0, 1/3, 3/4), a21 = 1/3, a31 = -3/16, a32 = 15/16, b = (1/6, 3/10, 8/15)
+# (O. Knoth, R. Wolke, Appl. Numer. Math. 28 (1998) 327-341), in MRI-GARK form:
+# G[0][i-1][j] = a_{i,j} - a_{i-1,j} with a_{s+1,j} = b_j
+MRI_KW3 = {"name": "MIS-KW3", "order": 3, "c": [0.0, 1.0 / 3.0, 0.75, 1.0],
+           "G": [[[1.0 / 3.0], [-25.0 / 48.0, 15.0 / 16.0],
+                  [17.0 / 48.0, -51.0 / 80.0, 8.0 / 15.0]]]}
+MRI_ERK33A = {"name": "MRI-GARK-ERK33a", "order": 3, "c": [0.0, 1.0 / 3.0, 2.0 / 3.0, 1.0],
+              "G": [[[1.0 / 3.0], [-1.0 / 3.0, 2.0 / 3.0], [0.0, -2.0 / 3.0, 1.0]],
+                    [[0.0], [0.0, 0.0], [0.5, 0.0, -0.5]]]}
+
+
+def mri_gark_evolve(slow_rhs, fast_evolve, t0, tf, y, h, table=MRI_ERK22B):
+    """Explicit MRI-GARK integration with a fixed slow step h (MRIStep's slow stepping):
+    slow_rhs(t, y) -> list of slow tendencies; fast_evolve(ta, tb, y, forcing, tshift, tscale)
+    advances y in place over [ta, tb] under ffast + sum_k ((t - tshift)/tscale)^k forcing[k].
+    Array-library agnostic.  Returns an MRIResult."""
+    res = MRIResult()
+    c, G = table["c"], table["G"]
+    ns = len(c)
+    nsteps = int(round((tf - t0) / h))
+    if nsteps < 1 or abs(nsteps * h - (tf - t0)) > 1e-12 * max(abs(tf), 1.0):
+        raise ValueError("tf - t0 must be a whole number of slow steps")
+    for n in range(nsteps):
+        t = t0 + n * h
+        F = [slow_rhs(t, y)]
+        res.slow_rhs += 1
+        for i in range(1, ns):
+            dc = c[i] - c[i - 1]
+            ta, tb = t + c[i - 1] * h, t + c[i] * h
+            forcing = []
+            for Gk in G:
+                row = Gk[i - 1]
+                terms = [(row[j] / dc, F[j]) for j in range(len(row)) if row[j] != 0.0]
+                forcing.append(_combo(None, terms) if terms else [x * 0.0 for x in F[0]])
+            while len(forcing) > 1 and all(v == 0.0 for v in G[len(forcing) - 1][i - 1]):
+                forcing.pop()  # drop vanishing top powers for this stage
+            res.fast_failed_cells += fast_evolve(ta, tb, y, forcing, ta, dc * h) or 0
+            if i < ns - 1:
+                F.append(slow_rhs(tb, y))
+                res.slow_rhs += 1
+        res.slow_steps += 1
+    return res
+
+
+def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=MRI_ERK22B,
+               precision=0, slow_rhs=None, **fast_opts):
     """Multirate chemistry-hydrodynamics integration (the MRIStep driver of
-    src/multirate_chem_hydro_main.cpp) with a fixed slow step h: second-order explicit
-    MRI-GARK coupling of the slow explicit midpoint rule (stage abscissae 0, 1/2, 1; inner
-    forcings g1 = fs(Y1) on [t, t+h/2] and g2 = 2 fs(Y2) - fs(Y1) on [t+h/2, t+h], constant
-    in time), the slow RHS fs = fexpl (WENO hydro + glue, `precision`), each fast problem
-    w' = ffast(t, w) + g integrated by gbmv_mri_fast_evolve (persistent batched DIRK for the
-    chemistry, exact forcing integral for the fluid).  With ffast = 0 it is the explicit
-    midpoint rule, with fs = 0 the fast integrator alone.  `w` (six torch CUDA tensors) is
-    advanced in place; returns an MRIResult.
+    src/multirate_chem_hydro_main.cpp) with a fixed slow step h and an explicit MRI-GARK
+    coupling `table`: the slow RHS fs = fexpl (WENO hydro + glue, `precision`), each fast
+    problem w' = ffast(t, w) + r(t) with the stage's forcing polynomial integrated by
+    gbmv_mri_fast_evolve (persistent batched DIRK for the chemistry, exact forcing integral
+    for the fluid).  `w` (six torch CUDA tensors) is advanced in place; returns an MRIResult.
 
     Units of the slow chemistry forcing: fexpl returns the chemistry tendency of the physical
     densities, with the total-energy tendency (code units) in the gas-energy slot, as the
@@ -180,40 +229,30 @@ def mri_erk22b_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units,
     tendencies divided by scale, the gas-energy slot EnergyUnits * etdot / scale -- so that the
     coupling is dimensionally consistent (`scaled_forcing`)."""
     import torch
-    res = MRIResult()
     fs0 = slow_rhs or (lambda t, y, out: gbmv.fexpl(hydro, chem, t, y, out, energy_units,
                                                     precision))
     inv_scale = chem.state("inv_scale").view(-1, 10)
 
-    def fs(t, y, out):
-        rc = fs0(t, y, out)
-        if rc == 0:
-            scaled_forcing(out[5].view(-1, 10), inv_scale, energy_units)
-        return rc
-    g1 = [torch.empty_like(x) for x in w]
-    g2 = [torch.empty_like(x) for x in w]
-    nsteps = int(round((tf - t0) / h))
-    if nsteps < 1 or abs(nsteps * h - (tf - t0)) > 1e-12 * max(abs(tf), 1.0):
-        raise ValueError("tf - t0 must be a whole number of slow steps")
-    t = t0
-    for n in range(nsteps):
-        t_mid, t_end = t0 + (n + 0.5) * h, t0 + (n + 1) * h
-        if fs(t, w, g1) != 0:
+    def fs(t, y):
+        out = [torch.empty_like(x) for x in y]
+        if fs0(t, y, out) != 0:
             raise RuntimeError("slow RHS failed (illegal state)")
-        nf = gbmv.mri_fast_evolve(hydro, chem, t, t_mid, w, time_units, [g1], t, 1.0,
-                                  precision=precision, **fast_opts)
-        res.fast_failed_cells += nf
-        if fs(t_mid, w, g2) != 0:
-            raise RuntimeError("slow RHS failed (illegal state)")
-        for a, b in zip(g2, g1):
-            a.mul_(2.0).sub_(b)
-        nf = gbmv.mri_fast_evolve(hydro, chem, t_mid, t_end, w, time_units, [g2], t_mid, 1.0,
-                                  precision=precision, **fast_opts)
-        res.fast_failed_cells += nf
-        res.slow_rhs += 2
-        res.slow_steps += 1
-        t = t_end
-    return res
+        scaled_forcing(out[5].view(-1, 10), inv_scale, energy_units)
+        return out
+
+    def fast(ta, tb, y, forcing, tshift, tscale):
+        return gbmv.mri_fast_evolve(hydro, chem, ta, tb, y, time_units, forcing, tshift, tscale,
+                                    precision=precision, **fast_opts)
+
+    return mri_gark_evolve(fs, fast, t0, tf, w, h, table)
+
+
+def mri_erk22b_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units,
+                      precision=0, slow_rhs=None, **fast_opts):
+    """mri_evolve with the second-order MRI-GARK-ERK22b coupling (explicit midpoint: forcings
+    g1 = fs(Y1) on [t, t+h/2] and g2 = 2 fs(Y2) - fs(Y1) on [t+h/2, t+h])."""
+    return mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, MRI_ERK22B,
+                      precision, slow_rhs, **fast_opts)
 
 
 # ---------------------------------------------------------------------------- ARK-IMEX

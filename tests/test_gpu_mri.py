@@ -1,6 +1,7 @@
-"""Multirate chemistry-hydrodynamics integration on the GPU (integrate.mri_erk22b_evolve: the
-slow WENO stage through gbmv_fexpl, the fast stages through gbmv_mri_fast_evolve) against the
-same scheme driven by the oracle (fexpl composition of the oracle's fEuler and scaling glue,
+"""Multirate chemistry-hydrodynamics integration on the GPU (integrate.mri_evolve with the
+MRI-GARK-ERK22b, MIS-KW3 and MRI-GARK-ERK33a couplings: the slow WENO stages through
+gbmv_fexpl, the fast stages through gbmv_mri_fast_evolve) against the same scheme driven by
+the oracle (fexpl composition of the oracle's fEuler and scaling glue,
 the oracle's forced per-cell DIRK, the exact fluid forcing integral)."""
 import numpy as np
 import pytest
@@ -29,31 +30,38 @@ def _oracle_fexpl(wl_state, wl, eu):
     return out, f
 
 
-def _oracle_mri(wl, tables, t0, h, nsteps, eu, tu):
+def _oracle_mri(wl, tables, t0, h, nsteps, eu, tu, table):
+    """The explicit MRI-GARK step written out over the oracle: stage i's forcing polynomial
+    r(tau) = sum_k tau^k sum_j G[k][i-1][j] / dc F_j, tau = (t - ta) / (dc h)."""
     y = [x.copy() for x in wl["fields"]]
     oc = O.Chem(tables, wl["scale"].reshape(-1))
     n = y[0].size
+    c, G = table["c"], table["G"]
 
     def fast(y, ta, tb, g):
-        for k in range(5):  # constant forcing: exact integral
-            y[k] = y[k] + (tb - ta) * g[k]
-        z, _, nf = oc.dirk_evolve(y[5].reshape(-1), ta, tb, tu, forcing=[g[5].reshape(-1)],
-                                  tshift=ta, tscale=1.0, **FAST)
+        for k in range(5):  # polynomial forcing: exact integral over tau in [0, 1]
+            y[k] = y[k] + sum((tb - ta) / (q + 1) * gq[k] for q, gq in enumerate(g))
+        z, _, nf = oc.dirk_evolve(y[5].reshape(-1), ta, tb, tu,
+                                  forcing=[gq[5].reshape(-1) for gq in g],
+                                  tshift=ta, tscale=tb - ta, **FAST)
         assert nf == 0
         y[5] = z.reshape(y[5].shape)
         return y
 
     for s in range(nsteps):
-        ta, tm, tb = t0 + s * h, t0 + (s + 0.5) * h, t0 + (s + 1) * h
-        g1, y = _oracle_fexpl(y, wl, eu)
-        y = fast(y, ta, tm, g1)
-        g2, y = _oracle_fexpl(y, wl, eu)
-        g2 = [2.0 * a - b for a, b in zip(g2, g1)]
-        y = fast(y, tm, tb, g2)
+        t = t0 + s * h
+        Fs = []
+        for i in range(1, len(c)):
+            f, y = _oracle_fexpl(y, wl, eu)
+            Fs.append(f)
+            dc = c[i] - c[i - 1]
+            g = [[sum(Gk[i - 1][j] / dc * Fs[j][k] for j in range(i)) for k in range(6)]
+                 for Gk in G]
+            y = fast(y, t + c[i - 1] * h, t + c[i] * h, g)
     return y, n
 
 
-def _gpu_mri(torch, wl, tables, t0, h, nsteps, eu, tu, precision):
+def _gpu_mri(torch, wl, tables, t0, h, nsteps, eu, tu, precision, table=None):
     import gbmv
     import integrate
     nz, ny, nx = wl["fields"][0].shape
@@ -61,19 +69,31 @@ def _gpu_mri(torch, wl, tables, t0, h, nsteps, eu, tu, precision):
     c = gbmv.Chem(nx * ny * nz, tables)
     c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
     w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
-    r = integrate.mri_erk22b_evolve(gbmv, hy, c, w, t0, t0 + nsteps * h, h, eu, tu,
-                                    precision=precision, block=64, **FAST)
+    if table is None:
+        r = integrate.mri_erk22b_evolve(gbmv, hy, c, w, t0, t0 + nsteps * h, h, eu, tu,
+                                        precision=precision, block=64, **FAST)
+    else:
+        r = integrate.mri_evolve(gbmv, hy, c, w, t0, t0 + nsteps * h, h, eu, tu, table,
+                                 precision=precision, block=64, **FAST)
     torch.cuda.synchronize()
     assert r.fast_failed_cells == 0 and r.slow_steps == nsteps
     return [x.cpu().numpy() for x in w]
 
 
-def test_mri_fp64_matches_oracle_driven_scheme(cuda, tables):
+def _tables():
+    import integrate
+    return [None, integrate.MRI_KW3, integrate.MRI_ERK33A]
+
+
+@pytest.mark.parametrize("which", [0, 1, 2], ids=["erk22b", "kw3", "erk33a"])
+def test_mri_fp64_matches_oracle_driven_scheme(cuda, tables, which):
+    import integrate
+    table = _tables()[which]
     wl = W.chem_hydro(shape=(8, 6, 5))
     eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
     t0, h, ns = 0.0, 2e-6, 2
-    ref, n = _oracle_mri(wl, tables, t0, h, ns, eu, tu)
-    got = _gpu_mri(cuda, wl, tables, t0, h, ns, eu, tu, 0)
+    ref, n = _oracle_mri(wl, tables, t0, h, ns, eu, tu, table or integrate.MRI_ERK22B)
+    got = _gpu_mri(cuda, wl, tables, t0, h, ns, eu, tu, 0, table)
     for k in range(5):
         assert maxnorm_err(got[k], ref[k]) <= 1e-10, k
     a, b = got[5].reshape(n, 10), ref[5].reshape(n, 10)

@@ -182,3 +182,52 @@ def test_scaled_forcing_units():
     I.scaled_forcing(g, inv, 4.0)
     assert torch.equal(g[:, :9], ref[:, :9] * 0.5)
     assert torch.equal(g[:, 9], ref[:, 9] * 2.0)
+
+
+def _mri_linear(table, h, T=1.0):
+    """y' = Lf y + Ls y (non-commuting 2x2 parts), exact y = expm((Lf + Ls) t) y0; the fast
+    problems v' = Lf v + r(tau) solved by fine RK4 substeps (far below the method error)."""
+    import scipy.linalg as sl
+    Lf = np.array([[-20.0, 5.0], [3.0, -12.0]])
+    Ls = np.array([[-0.5, 1.0], [-1.0, -0.3]])
+    y0 = np.array([1.0, 0.5])
+
+    def slow(t, y):
+        return [Ls @ y[0]]
+
+    def fast(ta, tb, y, forcing, tshift, tscale):
+        nsub = 200
+        dt = (tb - ta) / nsub
+
+        def f(t, v):
+            tau = (t - tshift) / tscale
+            r = sum((tau ** k) * fk[0] for k, fk in enumerate(forcing))
+            return Lf @ v + r
+        v, t = y[0].copy(), ta
+        for _ in range(nsub):
+            k1 = f(t, v)
+            k2 = f(t + dt / 2, v + dt / 2 * k1)
+            k3 = f(t + dt / 2, v + dt / 2 * k2)
+            k4 = f(t + dt, v + dt * k3)
+            v = v + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+            t += dt
+        y[0][...] = v
+        return 0
+    y = [y0.copy()]
+    I.mri_gark_evolve(slow, fast, 0.0, T, y, h, table)
+    return np.max(np.abs(y[0] - sl.expm((Lf + Ls) * T) @ y0))
+
+
+@pytest.mark.parametrize("table", [I.MRI_ERK22B, I.MRI_KW3, I.MRI_ERK33A],
+                         ids=lambda t: t["name"])
+def test_mri_gark_tables_order(table):
+    """Each coupling table reaches its order on a linear multirate problem, and its rows are
+    consistent (the constant-term rows sum to the stage length, higher powers to zero)."""
+    c, G = table["c"], table["G"]
+    for i in range(1, len(c)):
+        assert abs(sum(G[0][i - 1]) - (c[i] - c[i - 1])) < 1e-15
+        for Gk in G[1:]:
+            assert abs(sum(Gk[i - 1])) < 1e-15
+    errs = [_mri_linear(table, h) for h in (0.1, 0.05, 0.025)]
+    orders = [math.log2(errs[k] / errs[k + 1]) for k in range(2)]
+    assert min(orders) > table["order"] - 0.25, (errs, orders)
