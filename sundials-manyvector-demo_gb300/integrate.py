@@ -212,11 +212,13 @@ def mri_gark_evolve(slow_rhs, fast_evolve, t0, tf, y, h, table=MRI_ERK22B):
     return res
 
 
-def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=MRI_ERK22B,
+def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=MRI_KW3,
                precision=0, slow_rhs=None, **fast_opts):
     """Multirate chemistry-hydrodynamics integration (the MRIStep driver of
     src/multirate_chem_hydro_main.cpp) with a fixed slow step h and an explicit MRI-GARK
-    coupling `table`: the slow RHS fs = fexpl (WENO hydro + glue, `precision`), each fast
+    coupling `table`, by default MIS-KW3, MRIStep's default third-order explicit coupling that
+    the reference runs when its input leaves `mtable` negative
+    (src/multirate_chem_hydro_main.cpp:18, :545-551; inputs/input_generic.txt:49): the slow RHS fs = fexpl (WENO hydro + glue, `precision`), each fast
     problem w' = ffast(t, w) + r(t) with the stage's forcing polynomial integrated by
     gbmv_mri_fast_evolve (persistent batched DIRK for the chemistry, exact forcing integral
     for the fluid).  `w` (six torch CUDA tensors) is advanced in place; returns an MRIResult.
