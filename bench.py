@@ -11,10 +11,11 @@ per-step host->device copies of the state from pinned memory and device->host co
 outputs (tendency vector and Newton update) through the public Python API.
 
   python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl gbmv|reference]
-                  [--form best|fp64|mixed]
---form best (default) times the plain FP64 form and the mixed-precision batched form, checks
-the mixed form's outputs against the FP64 form's (max-normalised per field), and reports the
-mixed form as the headline when that error is <= 1e-6.
+                  [--form best|fp64|mixed|mixed_fast|mixed_fast_concurrent]
+--form best (default) times the plain FP64 form and the mixed-precision forms (the last with
+the chemistry Newton on a second stream beside the WENO sweep inside the step's graph), checks
+each mixed form's outputs against the FP64 form's (max-normalised per field), and reports the
+fastest form whose error is <= 1e-6 as the headline.
 """
 from __future__ import annotations
 
@@ -48,7 +49,8 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gbmv", choices=["gbmv", "reference"])
-    p.add_argument("--form", default="best", choices=["best", "fp64", "mixed", "mixed_fast"])
+    p.add_argument("--form", default="best",
+                   choices=["best", "fp64", "mixed", "mixed_fast", "mixed_fast_concurrent"])
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -139,7 +141,7 @@ class FusedStep:
                   FP64-residual refinement, no Jacobian in HBM), the whole stage captured as
                   one CUDA graph and replayed."""
 
-    def __init__(self, torch, n, form, wl=None, concurrent=False, newton_bps=2):
+    def __init__(self, torch, n, form, wl=None, concurrent=False, newton_bps=4):
         import gbmv
         import h5tables
         import workloads as W
@@ -179,6 +181,9 @@ class FusedStep:
             with torch.cuda.graph(self.graph, stream=side):
                 self._stage_async()
             torch.cuda.synchronize()
+            # the captured launches keep their grid; eager calls (the per-kernel timings) use
+            # the default deep grid again
+            self.chem.set_newton_occupancy(0)
 
     def _stage_async(self, t=0.0):
         g, torch = self.gbmv, self.torch
@@ -404,13 +409,14 @@ def run_gbmv(args):
     gbmv.load()
     torch.cuda.set_device(0)
     wl = W.chem_hydro(n=args.n)
-    forms = ["fp64", "mixed", "mixed_fast"] if args.form == "best" else [args.form]
+    forms = (["fp64", "mixed", "mixed_fast", "mixed_fast_concurrent"] if args.form == "best"
+             else [args.form])
     if args.concurrent and "mixed" in forms:
         forms.append("mixed_concurrent")
 
     def make_fs(form):
-        base = "mixed" if form == "mixed_concurrent" else form
-        return FusedStep(torch, args.n, base, wl, concurrent=(form == "mixed_concurrent"))
+        base = form.replace("_concurrent", "")
+        return FusedStep(torch, args.n, base, wl, concurrent=form.endswith("_concurrent"))
 
     res = {}
     for form in forms:
@@ -462,7 +468,7 @@ def run_gbmv(args):
     fp64_peak = gbmv.fma_rate(True) / 1e12
     dt_ms, nl = fam[dom]
     avg_ms = dt_ms / max(nl, 1)
-    hform = "mixed" if head == "mixed_concurrent" else head
+    hform = head.replace("_concurrent", "")
     key = "face_flux_mx" if (dom == "face_flux" and hform != "fp64") else dom
     achieved = algo_bytes(key, args.n) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     traffic, traffic_note = None, None
@@ -489,7 +495,7 @@ def run_gbmv(args):
         "dtype": {"fp64": "f64",
                   "mixed_fast": ("f64 state; float-float WENO with f32 weights on differences, "
                                  "f32 LU + f64 refinement")}.get(
-            head, "f64 state; f32 + float-float WENO, f32 LU + f64 refinement"),
+            hform, "f64 state; f32 + float-float WENO, f32 LU + f64 refinement"),
         "data": "synthetic (seeded numpy PCG64; rate tables from the reference's primordial_tables.h5)",
         "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "nvar": 15, "cells": ncell,
                    "form": head, "newton_gamma": GAMMA_NEWTON,
@@ -510,6 +516,12 @@ def run_gbmv(args):
         "forms": {f: {"ms_per_step": round(r["ms"], 4),
                       "value": round(ncell / (r["ms"] * 1e-3) / 1e6, 3)} for f, r in res.items()},
     }
+    if head.endswith("_concurrent"):
+        line["config"]["schedule"] = (
+            "one CUDA graph per step with two branches: the chemistry Newton on a second stream "
+            "(persistent grid, 4 one-warp blocks per SM) beside the WENO sweep; outputs "
+            "bit-identical to the serial graph; kernel_ms_per_step and roofline time each "
+            "kernel alone (eager, serial), so their sum exceeds ms_per_step by the overlap")
     if errs is not None:
         line["mixed_vs_fp64_maxnorm_err"] = {k: float(f"{v:.3e}") for k, v in errs.items()}
         line["speedup_vs_fp64_form"] = round(res["fp64"]["ms"] / res[head]["ms"], 3)

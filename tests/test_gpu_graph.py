@@ -57,23 +57,25 @@ def test_stage_graph_replay_matches_eager(cuda, tables):
     assert torch.equal(A[1].state("Ts"), B[1].state("Ts"))
 
 
-def test_concurrent_branch_graph_matches_serial_eager(cuda, tables):
+@pytest.mark.parametrize("form,bps", [("MIXED", 2), ("MIXED_FAST", 4)])
+def test_concurrent_branch_graph_matches_serial_eager(cuda, tables, form, bps):
     """The stage as two graph branches -- chemistry Newton on its own stream with a persistent
-    two-blocks-per-SM grid, WENO sweep on the capture stream -- gives the serial eager bits:
-    the mixed fexpl never writes w[5], so the branches share no written data."""
+    grid of `bps` blocks per SM, WENO sweep on the capture stream -- gives the serial eager
+    bits: the mixed fexpl never writes w[5], so the branches share no written data."""
     torch = cuda
     import gbmv
+    prec = getattr(gbmv, form)
     wl = W.chem_hydro(shape=(24, 20, 16))
     eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
     A = _make(torch, gbmv, wl, tables)
     B = _make(torch, gbmv, wl, tables)
-    B[1].set_newton_occupancy(2)
+    B[1].set_newton_occupancy(bps)
     status = torch.zeros(2, dtype=torch.int32, device="cuda")
     chem_stream = torch.cuda.Stream()
 
     def serial(h, c, w, wdot, f, x):
         status.zero_()
-        gbmv.fexpl_async(h, c, 0.0, w, wdot, eu, status[0:1], gbmv.MIXED)
+        gbmv.fexpl_async(h, c, 0.0, w, wdot, eu, status[0:1], prec)
         gbmv.chem_newton_async(c, 0.0, w[5].view(-1), f, x, 1e-4, tu, status[1:2],
                                lu_precision=gbmv.MIXED, refine=4)
 
@@ -85,7 +87,7 @@ def test_concurrent_branch_graph_matches_serial_eager(cuda, tables):
         chem_stream.wait_event(fork)
         gbmv.chem_newton_async(c, 0.0, w[5].view(-1), f, x, 1e-4, tu, status[1:2],
                                lu_precision=gbmv.MIXED, refine=4, stream=chem_stream)
-        gbmv.fexpl_async(h, c, 0.0, w, wdot, eu, status[0:1], gbmv.MIXED)
+        gbmv.fexpl_async(h, c, 0.0, w, wdot, eu, status[0:1], prec)
         join = torch.cuda.Event()
         join.record(chem_stream)
         main.wait_event(join)
