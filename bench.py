@@ -361,13 +361,13 @@ def algo_bytes(fam, n):
 # roofline; the denominator is the FMA rate measured by gbmv_diag_fma_rate.
 FP_COUNTS = {
     ("fp64", "face_flux"): ("fp64", 3841.3, "face"),
-    ("fp64", "chem_rhs"): ("fp64", 2527.0, "cell"),
-    ("fp64", "chem_jac"): ("fp64", 1003.0, "cell"),
+    ("fp64", "chem_rhs"): ("fp64", 2440.9, "cell"),
+    ("fp64", "chem_jac"): ("fp64", 957.0, "cell"),
     ("fp64", "block_lu_factor"): ("fp64", 759.0, "cell"),
     ("mixed", "face_flux"): ("fp32", 25990.0, "face"),
-    ("mixed", "chem_newton"): ("fp64", 1745.0, "cell"),
+    ("mixed", "chem_newton"): ("fp64", 1687.1, "cell"),
     ("mixed_fast", "face_flux"): ("fp32", 16190.0, "face"),
-    ("mixed_fast", "chem_newton"): ("fp64", 1745.0, "cell"),
+    ("mixed_fast", "chem_newton"): ("fp64", 1687.1, "cell"),
 }
 
 

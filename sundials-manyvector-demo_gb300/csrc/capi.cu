@@ -289,13 +289,17 @@ int gbmv_chem_create(long ncells, const double* tables_host, double current_z, g
   if (!h) { delete c; return GBMV_ENOMEM; }
   for (int b = 0; b < kTSize; ++b)
     for (int r = 0; r < kNT; ++r) h[b * kNT + r] = tables_host[(long)r * kTSize + b];
-  // float copies of the four H2 adiabatic-index tables for the FP32 temperature iterations,
-  // after the double table: per bin (value, next - value) of gammaH2_2, dgammaH2_2_dT,
-  // gammaH2_1, dgammaH2_1_dT, each rounded to float once
+  // after the double table: the per-bin differences next - value in FP64 (dtab), then float
+  // copies of the four H2 adiabatic-index tables for the FP32 temperature iterations: per bin
+  // (value, next - value) of gammaH2_2, dgammaH2_2_dT, gammaH2_1, dgammaH2_1_dT, each rounded
+  // to float once
   const size_t tab_doubles = (size_t)kNT * kTSize;
   const size_t gtab_floats = (size_t)8 * kTSize;
   float* gh = (float*)calloc(gtab_floats, sizeof(float));
-  if (!gh) { free(h); delete c; return GBMV_ENOMEM; }
+  double* dh = (double*)calloc(tab_doubles, sizeof(double));
+  if (!gh || !dh) { free(h); free(gh); free(dh); delete c; return GBMV_ENOMEM; }
+  for (int b = 0; b + 1 < kTSize; ++b)
+    for (int r = 0; r < kNT; ++r) dh[b * kNT + r] = h[(b + 1) * kNT + r] - h[b * kNT + r];
   const int grow[4] = {GAMMAH2_2, DGAMMAH2_2, GAMMAH2_1, DGAMMAH2_1};
   for (int b = 0; b + 1 < kTSize; ++b)
     for (int q = 0; q < 4; ++q) {
@@ -304,13 +308,14 @@ int gbmv_chem_create(long ncells, const double* tables_host, double current_z, g
       gh[b * 8 + 2 * q + 1] = (float)(hi - lo);
     }
   const size_t per_cell = 10 + 10 + 6;
-  if (cudaMalloc(&c->tab, sizeof(double) * tab_doubles + sizeof(float) * gtab_floats) !=
+  if (cudaMalloc(&c->tab, sizeof(double) * 2 * tab_doubles + sizeof(float) * gtab_floats) !=
           cudaSuccess ||
       cudaMalloc(&c->cell, sizeof(double) * per_cell * ncells) != cudaSuccess ||
       cudaMalloc(&c->d_info, 64) != cudaSuccess) {
     cudaGetLastError();
     free(h);
     free(gh);
+    free(dh);
     cudaFree(c->tab);
     cudaFree(c->cell);
     delete c;
@@ -320,19 +325,22 @@ int gbmv_chem_create(long ncells, const double* tables_host, double current_z, g
   c->d_nfail = c->d_info + 1;
   c->d_next = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(c->d_info) + 16);
   cudaMemcpy(c->tab, h, sizeof(double) * tab_doubles, cudaMemcpyHostToDevice);
-  cudaMemcpy(c->tab + tab_doubles, gh, sizeof(float) * gtab_floats, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->tab + tab_doubles, dh, sizeof(double) * tab_doubles, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->tab + 2 * tab_doubles, gh, sizeof(float) * gtab_floats, cudaMemcpyHostToDevice);
   free(h);
   free(gh);
+  free(dh);
   // constants of cvklu_setup_data (src/raja_primordial_network.cpp:190-194)
   ChemParams& P = c->P;
   P.tab = c->tab;
+  P.dtab = c->tab + tab_doubles;
   P.tlo = 1.0;
   P.thi = 100000.0;
   P.nbins = kTSize - 1;
   P.lb = log(P.tlo);
   P.dbin = (log(P.thi) - log(P.tlo)) / P.nbins;
   P.idbin = (double)(1.0L / (long double)P.dbin);
-  P.gtab = reinterpret_cast<const float*>(c->tab + tab_doubles);  // 16-byte aligned
+  P.gtab = reinterpret_cast<const float*>(c->tab + 2 * tab_doubles);  // 16-byte aligned
   P.dbinf = (float)P.dbin;
   P.idbinf = (float)P.idbin;
   P.lbf = (float)P.lb;

@@ -28,6 +28,9 @@ enum : int {
 
 struct ChemParams {
   const double* tab;  // device, bin-major: tab[bin * kNT + row]
+  // dtab[bin * kNT + row] = tab[(bin + 1) * kNT + row] - tab[bin * kNT + row]: the FP64
+  // difference every interpolation in the bin takes, formed once at setup (same rounding)
+  const double* dtab;
   // the four H2 adiabatic-index tables for the FP32 temperature iterations, per bin:
   // (float) value and (float)(next - value) of gammaH2_2, dgammaH2_2_dT, gammaH2_1,
   // dgammaH2_1_dT -- the roundings the FP32 iterations apply, done once at setup
@@ -64,11 +67,11 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
     const int b = chem_bin(P, logT, t1, t2);
     const double Tdef = (logT - t1) / (t2 - t1);
     const double* lo = P.tab + (long)b * kNT;
-    const double* hi = lo + kNT;
-    const double g2 = lo[GAMMAH2_2] + Tdef * (hi[GAMMAH2_2] - lo[GAMMAH2_2]);
-    const double dg2 = lo[DGAMMAH2_2] + Tdef * (hi[DGAMMAH2_2] - lo[DGAMMAH2_2]);
-    const double g1 = lo[GAMMAH2_1] + Tdef * (hi[GAMMAH2_1] - lo[GAMMAH2_1]);
-    const double dg1 = lo[DGAMMAH2_1] + Tdef * (hi[DGAMMAH2_1] - lo[DGAMMAH2_1]);
+    const double* dl = P.dtab + (long)b * kNT;
+    const double g2 = lo[GAMMAH2_2] + Tdef * dl[GAMMAH2_2];
+    const double dg2 = lo[DGAMMAH2_2] + Tdef * dl[DGAMMAH2_2];
+    const double g1 = lo[GAMMAH2_1] + Tdef * dl[GAMMAH2_1];
+    const double dg1 = lo[DGAMMAH2_1] + Tdef * dl[DGAMMAH2_1];
     const double i1 = 1.0 / (g1 - 1.0), i2 = 1.0 / (g2 - 1.0);
     const double nsum = H2_1 * i1 + H2_2 * i2 + H_1 * gm1 + H_2 * gm1 + H_m0 * gm1 + He_1 * gm1 +
                         He_2 * gm1 + He_3 * gm1 + gm1 * de;
@@ -139,11 +142,11 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     const int b = chem_bin(P, logT, t1, t2);
     const double Tdef = (logT - t1) * P.idbin;
     const double* lo = P.tab + (long)b * kNT;
-    const double* hi = lo + kNT;
-    const double g2 = lo[GAMMAH2_2] + Tdef * (hi[GAMMAH2_2] - lo[GAMMAH2_2]);
-    const double dg2 = lo[DGAMMAH2_2] + Tdef * (hi[DGAMMAH2_2] - lo[DGAMMAH2_2]);
-    const double g1 = lo[GAMMAH2_1] + Tdef * (hi[GAMMAH2_1] - lo[GAMMAH2_1]);
-    const double dg1 = lo[DGAMMAH2_1] + Tdef * (hi[DGAMMAH2_1] - lo[DGAMMAH2_1]);
+    const double* dl = P.dtab + (long)b * kNT;
+    const double g2 = lo[GAMMAH2_2] + Tdef * dl[GAMMAH2_2];
+    const double dg2 = lo[DGAMMAH2_2] + Tdef * dl[DGAMMAH2_2];
+    const double g1 = lo[GAMMAH2_1] + Tdef * dl[GAMMAH2_1];
+    const double dg1 = lo[DGAMMAH2_1] + Tdef * dl[DGAMMAH2_1];
     const double i1 = 1.0 / (g1 - 1.0), i2 = 1.0 / (g2 - 1.0);
     const double nsum = dH2_1 * i1 + dH2_2 * i2 + dH_1 * gm1d + dH_2 * gm1d + dH_m0 * gm1d +
                         dHe_1 * gm1d + dHe_2 * gm1d + dHe_3 * gm1d + gm1d * dde;
@@ -171,10 +174,10 @@ __device__ __forceinline__ void chem_rates(const ChemParams& P, double Ts, doubl
   const double Tdef = Reciprocal ? (logT - t1) * P.idbin : (logT - t1) / (t2 - t1);
   const double Tfactor = Reciprocal ? P.idbin / Ts : (1.0 / Ts) / (t2 - t1);
   const double* lo = P.tab + (long)b * kNT;
-  const double* hi = lo + kNT;
+  const double* dl = P.dtab + (long)b * kNT;
 #pragma unroll
   for (int r = 0; r < kNRates; ++r) {
-    const double a = __ldg(lo + r), d = __ldg(hi + r) - a;
+    const double a = __ldg(lo + r), d = __ldg(dl + r);
     k[r] = a + Tdef * d;
     if (WithSlopes) dk[r] = d * Tfactor;
   }
