@@ -40,11 +40,15 @@ class ERKResult:
         self.steps = 0
         self.fails = 0
         self.nfe = 0
+        self.h_next = 0.0  # the step the controller proposes after the last one
 
 
 def erk_evolve(rhs, t0, tf, y0, rtol=1e-6, atol=1e-11, h0=0.0, safety=0.9, etamax=5.0,
-               etamin=0.2, hmax=math.inf, max_steps=100000):
-    """Integrate dy/dt = rhs(t, y) from t0 to tf; returns (y(tf), stats)."""
+               etamin=0.2, hmax=math.inf, max_steps=100000, fixed_h=0.0, stability=None):
+    """Integrate dy/dt = rhs(t, y) from t0 to tf; returns (y(tf), stats).  fixed_h > 0: steps
+    of fixed_h (the last one shortened to reach tf) without error control, as ARKStep's fixed
+    step mode.  stability(t, y): an explicitly stable step bound applied to every adaptive
+    step (ARKStepSetStabilityFn, as the reference's CFL function `stability` is used)."""
     st = ERKResult()
     y = y0.clone() if hasattr(y0, "clone") else y0.copy()
     t = t0
@@ -54,11 +58,18 @@ def erk_evolve(rhs, t0, tf, y0, rtol=1e-6, atol=1e-11, h0=0.0, safety=0.9, etama
         d0 = _wrms(y, y, rtol, atol)
         d1 = _wrms(k1, y, rtol, atol)
         h0 = 0.01 * d0 / d1 if d0 > 1e-5 and d1 > 1e-5 else 1e-6
-    h = min(h0, tf - t0, hmax)
+    h = fixed_h if fixed_h > 0.0 else min(h0, tf - t0, hmax)
     while t < tf:
         if st.steps + st.fails > max_steps:
             raise RuntimeError("erk_evolve: too many steps")
+        if stability is not None and fixed_h <= 0.0:
+            h = min(h, stability(t, y))
+        hp = h  # proposal before the cut to tf
         h = min(h, tf - t)
+        cut = h < hp
+        if fixed_h > 0.0 and h <= 1e-14 * max(abs(tf), 1.0):  # roundoff sliver of a fixed grid
+            t = tf
+            break
         ks = [k1]
         for s in range(1, 7):
             ys = y
@@ -75,18 +86,24 @@ def erk_evolve(rhs, t0, tf, y0, rtol=1e-6, atol=1e-11, h0=0.0, safety=0.9, etama
         for e, k in zip(_E, ks):
             if e != 0.0:
                 err = (h * e) * k if err is None else err + (h * e) * k
-        en = _wrms(err, ynew, rtol, atol)
+        en = 0.0 if fixed_h > 0.0 else _wrms(err, ynew, rtol, atol)
         if not math.isfinite(en):
             en = 1e10
         if en <= 1.0:
-            t += h
+            t = tf if h == tf - t else t + h
             y = ynew
             k1 = ks[6]  # FSAL
             st.steps += 1
         else:
             st.fails += 1
+        if fixed_h > 0.0:
+            h = fixed_h
+            st.h_next = fixed_h
+            continue
         fac = etamax if en == 0.0 else min(etamax, max(etamin, safety * en ** (-1.0 / 5.0)))
         h = min(h * fac, hmax)
+        # a step cut short to land on tf does not shrink the proposal for the next interval
+        st.h_next = max(h, hp) if (cut and en <= 1.0) else h
     return y, st
 
 
