@@ -35,7 +35,6 @@ alter the run; a zero option means "the integrator's default", as in the referen
 from __future__ import annotations
 
 import math
-import os
 import re
 import sys
 
