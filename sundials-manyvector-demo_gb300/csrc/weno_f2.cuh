@@ -33,10 +33,15 @@ int feuler_f2_fast(const Grid& g, const Fields& w, const Fields& wdot, const For
 
 // WV = 1 (fewer instructions per face) runs faster at 3 resident blocks per SM even with the
 // register cap's spills (measured 6.11 -> 5.63 ms per 128^3 RHS); WV = 0 is faster at 2.
+// GBMV_F2_FAST_MINB: the WV = 1 residency target, a build-time tuning knob (register
+// allocation only: results are the same bit for bit at any value).
+#ifndef GBMV_F2_FAST_MINB
+#define GBMV_F2_FAST_MINB 3
+#endif
 template <int NCHEM, int DIR, int WV>
-__global__ void __launch_bounds__(128, WV == 1 ? 3 : 1) face_flux_f2_kernel(Grid g, Fields w,
-                                                           const float2* __restrict__ Q2,
-                                                           float2* __restrict__ F, long nfaces) {
+__global__ void __launch_bounds__(128, WV == 1 ? GBMV_F2_FAST_MINB : 1)
+    face_flux_f2_kernel(Grid g, Fields w, const float2* __restrict__ Q2,
+                        float2* __restrict__ F, long nfaces) {
   const long nx = g.n[0], ny = g.n[1], n = g.ncell;
   for (long f = blockIdx.x * (long)blockDim.x + threadIdx.x; f < nfaces;
        f += (long)gridDim.x * blockDim.x) {
