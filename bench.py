@@ -53,6 +53,8 @@ def parse():
                    choices=["best", "fp64", "mixed", "mixed_fast", "mixed_fast_concurrent"])
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--newton-refine", type=int, default=None,
+                   help="FP64-residual refinement cap of the fused Newton (default 2)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--dirk-n", type=int, default=64,
                    help="static-chemistry DIRK measurement on dirk_n^3 cells (0 = skip)")
@@ -409,6 +411,9 @@ def run_gbmv(args):
     gbmv.load()
     torch.cuda.set_device(0)
     wl = W.chem_hydro(n=args.n)
+    global NEWTON_REFINE
+    if args.newton_refine is not None:
+        NEWTON_REFINE = args.newton_refine
     forms = (["fp64", "mixed", "mixed_fast", "mixed_fast_concurrent"] if args.form == "best"
              else [args.form])
     if args.concurrent and "mixed" in forms:
@@ -498,7 +503,7 @@ def run_gbmv(args):
             hform, "f64 state; f32 + float-float WENO, f32 LU + f64 refinement"),
         "data": "synthetic (seeded numpy PCG64; rate tables from the reference's primordial_tables.h5)",
         "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "nvar": 15, "cells": ncell,
-                   "form": head, "newton_gamma": GAMMA_NEWTON,
+                   "form": head, "newton_gamma": GAMMA_NEWTON, "newton_refine": NEWTON_REFINE,
                    "l2": "inputs larger than L2 (state 252 MB)"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
                      "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
