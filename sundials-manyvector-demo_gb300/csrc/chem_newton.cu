@@ -110,15 +110,20 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
 #pragma unroll
       for (int s = 0; s < 10; ++s) xs[s] = to_lu<LU>(f[s]);
       lus10_strided<LU, LU>(L, BS, piv, xs);
+      float xmax = 0.f;  // solution size for the stopping tests, from the FP32 solve: the
+                         // refinements move it by ~1e-7 relative, far below either threshold
 #pragma unroll
-      for (int s = 0; s < 10; ++s) x[s] = from_lu(xs[s]);
+      for (int s = 0; s < 10; ++s) {
+        x[s] = from_lu(xs[s]);
+        xmax = fmaxf(xmax, fabsf((float)xs[s]));
+      }
       if (sizeof(LU) == 4) {
         // iterative refinement against FP64 residuals; a cell stops as soon as its correction
         // is below 1e-13 of the solution (well-conditioned cells need one step, the
         // ill-conditioned ones use up to `refine`); a cell whose last correction is still above
         // 1e-6 of its solution (the FP32 factor too poor a preconditioner for its block)
         // takes the FP64 factor below
-        float dlast = 0.f, xlast = 1.f;
+        float dlast = 0.f;
         for (int it = 0; it < refine; ++it) {
           double rr[10];
 #pragma unroll
@@ -130,21 +135,19 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
 #pragma unroll
           for (int s = 0; s < 10; ++s) ds[s] = to_lu<LU>(rr[s]);
           lus10_strided<LU, LU>(L, BS, piv, ds);
-          float dmax = 0.f, xmax = 0.f;
+          float dmax = 0.f;
 #pragma unroll
           for (int s = 0; s < 10; ++s) {
             x[s] += from_lu(ds[s]);
             dmax = fmaxf(dmax, fabsf((float)ds[s]));
-            xmax = fmaxf(xmax, fabsf((float)x[s]));
           }
           dlast = dmax;
-          xlast = xmax;
           if (dmax <= 1e-13f * xmax) break;
         }
         bool finite = true;
 #pragma unroll
         for (int s = 0; s < 10; ++s) finite = finite && isfinite(x[s]);
-        fp64_fallback = !finite || !(dlast <= 1e-6f * xlast);
+        fp64_fallback = !finite || !(dlast <= 1e-6f * xmax);
       }
     }
     if (fp64_fallback) {  // FP32 factor singular or out of range: factor the FP64 matrix,
