@@ -367,9 +367,9 @@ FP_COUNTS = {
     ("fp64", "chem_jac"): ("fp64", 957.0, "cell"),
     ("fp64", "block_lu_factor"): ("fp64", 759.0, "cell"),
     ("mixed", "face_flux"): ("fp32", 25990.0, "face"),
-    ("mixed", "chem_newton"): ("fp64", 1687.1, "cell"),
+    ("mixed", "chem_newton"): ("fp64", 1671.1, "cell"),
     ("mixed_fast", "face_flux"): ("fp32", 16190.0, "face"),
-    ("mixed_fast", "chem_newton"): ("fp64", 1687.1, "cell"),
+    ("mixed_fast", "chem_newton"): ("fp64", 1671.1, "cell"),
 }
 
 
@@ -379,9 +379,9 @@ FP_COUNTS = {
 DRAM_TRAFFIC = {
     ("fp64", "face_flux"): (248.2, "face"),    # mean of the x / y / z sweeps
     ("mixed", "face_flux"): (296.5, "face"),
-    ("mixed", "chem_newton"): (490.9, "cell"),
+    ("mixed", "chem_newton"): (471.4, "cell"),
     ("mixed_fast", "face_flux"): (355.6, "face"),
-    ("mixed_fast", "chem_newton"): (490.9, "cell"),
+    ("mixed_fast", "chem_newton"): (471.4, "cell"),
     ("fp64", "chem_rhs"): (357.3, "cell"),
 }
 

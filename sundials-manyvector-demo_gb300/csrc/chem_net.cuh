@@ -291,7 +291,9 @@ __device__ __forceinline__ double chem_ge_source_r(const ChemParams& P, const do
 // rates k and slopes dk at the cell temperature.  Each of the 64 nonzeros is handed to
 // put(row, col, value) once, already multiplied by the factors the reference applies to that
 // entry (1/mdensity on the ge row, dT/dge on the ge column); entries never put are zero.
-template <class Put>
+// Raw: those two factors are left out, for a caller that folds them into its own row and
+// column scaling (one multiply per cell instead of one per entry).
+template <bool Raw = false, class Put>
 __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double (&k)[kNRates],
                                               const double (&dk)[kNRates], const double (&y)[10],
                                               double T, double Tge, const ChemAux& A, Put&& put,
@@ -300,7 +302,7 @@ __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double 
                He_2 = y[6], He_3 = y[7], de = y[8];
   const double z = P.z, h2oda = A.h2, md = A.mdens, imd = A.imdens;
 #define SETJ(row, col, expr) put(row, col, (expr))
-#define SETG(col, expr) put(9, col, (expr) * imd)
+#define SETG(col, expr) put(9, col, Raw ? (expr) : (expr) * imd)
   const double H1sq = H_1 * H_1;
   SETJ(0, 0, -k[K11] * H_2 - k[K12] * de - k[K13] * H_1 + k[K21] * H1sq);
   SETJ(0, 1, k[K10] * H_1 + k[K19] * H_m0);
@@ -359,7 +361,7 @@ __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double 
     chem_fluxes(dk, y, r);
     chem_species(r, s);
 #pragma unroll
-    for (int q = 0; q < 9; ++q) put(q, 9, s[q] * Tge);
+    for (int q = 0; q < 9; ++q) put(q, 9, Raw ? s[q] : s[q] * Tge);
   }
   // four reciprocals serve every ge-row entry (the reference divides ~20 times)
   const GeRecip R = shared ? *shared : ge_recip(k, y);
@@ -388,12 +390,14 @@ __device__ __forceinline__ void chem_jacobian(const ChemParams& P, const double 
               k[COMPTON] * P.zp1_4 * (T - 2.73 * z - 2.73));
   const double dGn = -H2_1 * dk[GAH2] - H_1 * dk[GAHI] - H_2 * dk[GAHP] - He_1 * dk[GAHE] -
                      de * dk[GAEL];
-  put(9, 9, (-H2_1 * k[H2LTE] * h2oda * (-k[H2LTE] * dGn * (iG * iG) - dk[H2LTE] * iG) * (iD * iD) -
-             H2_1 * h2oda * dk[H2LTE] * iD +
-             0.5 * iF2 * Hf *
-                 (-1.0 * k[NCRN] * (-H2_1 * dk[NCRD2] - H_1 * dk[NCRD1]) * iN2 -
-                  1.0 * dk[NCRN] * iN) +
-             0.5 * iF * (-H2_1 * H_1 * dk[H2MCOOL] + H13 * dk[H2MHEAT])) * imd * Tge);
+  const double gg = -H2_1 * k[H2LTE] * h2oda * (-k[H2LTE] * dGn * (iG * iG) - dk[H2LTE] * iG) *
+                        (iD * iD) -
+                    H2_1 * h2oda * dk[H2LTE] * iD +
+                    0.5 * iF2 * Hf *
+                        (-1.0 * k[NCRN] * (-H2_1 * dk[NCRD2] - H_1 * dk[NCRD1]) * iN2 -
+                         1.0 * dk[NCRN] * iN) +
+                    0.5 * iF * (-H2_1 * H_1 * dk[H2MCOOL] + H13 * dk[H2MHEAT]);
+  put(9, 9, Raw ? gg : gg * imd * Tge);
 #undef SETG
 #undef SETJ
 }

@@ -74,15 +74,18 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
       }
 #pragma unroll
       for (int s = 0; s < 10; ++s) fout[j + s] = f[s];
-      // A = I - gamma * (J * inv_scale[row] * scale[col] * tunit), FP64 and a float copy
+      // A = I - gamma * (J * inv_scale[row] * scale[col] * tunit), FP64 and a float copy;
+      // the ge row's 1/mdensity and the ge column's dT/dge ride on the row and column factors
       double rf[10];  // -gamma * tunit * inv_scale[row]
 #pragma unroll
       for (int r = 0; r < 10; ++r) rf[r] = (-gamma * tunit) * isc[r];
+      rf[9] *= Ax.imdens;
+      const double sc9 = sc[9] * dTs;
 #pragma unroll
       for (int e = 0; e < 100; ++e) L[e * BS] = LU(0);  // structural zeros
       // every structural entry (the diagonal included) is put exactly once
-      chem_jacobian(P, k, dk, ya, Ts, dTs, Ax, [&](int row, int col, double v) {
-        const double a = (v * rf[row]) * sc[col] + (row == col ? 1.0 : 0.0);
+      chem_jacobian<true>(P, k, dk, ya, Ts, dTs, Ax, [&](int row, int col, double v) {
+        const double a = (v * rf[row]) * (col == 9 ? sc9 : sc[col]) + (row == col ? 1.0 : 0.0);
         if (kMixed) {
           const int e = kJacIndex[row][col];
           if (e >= 0) As[e * BS] = a;
