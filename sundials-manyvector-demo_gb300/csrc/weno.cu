@@ -9,8 +9,8 @@
 //      stored field-major so that the divergence pass reads them coalesced).
 //   2. divergence_kernel<NCHEM>: wdot = G - [(Fx+ - Fx-)/dx + (Fy+ - Fy-)/dy + (Fz+ - Fz-)/dz],
 //      with the legal-state check (src/euler3D.hpp:1405-1414) OR-ed into a status word.
-// The float-float form (weno_f2*.cu) shares pass 2.  Also here: the CFL wave speed, the pack1D
-// stencil gather and the conservation totals.
+// The float-float forms (weno_f2*.cu) use divergence_f2_kernel below as their pass 2.  Also
+// here: the CFL wave speed, the pack1D stencil gather and the conservation totals.
 #include "common.cuh"
 #include "weno_face.cuh"
 #include "weno_sweep.cuh"
@@ -113,18 +113,19 @@ int divergence(const Grid& g, const Fields& w, const Fields& wdot, double* const
 // Pass 2 of the float-float form: the same divergence over fluxes kept as float pairs.  On
 // GB300 the FP64 pipe runs at 1/64 of the FP32 rate, so the divergence's FP64 differences made
 // it FP64-bound (81 % of the pipe) at three times its HBM time; here the differences and the
-// 1/d scaling are float-float (FP32 pipes) and only G - div and the legal-state check are FP64.
+// 1/d scaling are float-float (FP32 pipes) and only G - div is FP64.  The legal-state flags of
+// the float-float forms are set by the primitives pass, which already has the pressure, so this
+// pass reads no state field and needs no division.
 template <int NCHEM>
-__global__ void __launch_bounds__(256) divergence_f2_kernel(Grid g, Fields w, Fields wdot,
+__global__ void __launch_bounds__(256) divergence_f2_kernel(Grid g, Fields wdot,
                                                             const float2* __restrict__ Fx,
                                                             const float2* __restrict__ Fy,
                                                             const float2* __restrict__ Fz,
-                                                            ForceTerm G, int* __restrict__ status) {
+                                                            ForceTerm G) {
   const long nx = g.n[0], ny = g.n[1], nz = g.n[2];
   const long nfx = (nx + 1) * ny * nz, nfy = nx * (ny + 1) * nz, nfz = nx * ny * (nz + 1);
   const f2 idx = f2_from_double(g.inv_d[0]), idy = f2_from_double(g.inv_d[1]),
            idz = f2_from_double(g.inv_d[2]);
-  int bad = 0;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < g.ncell;
        c += (long)gridDim.x * blockDim.x) {
     long i, j, k;
@@ -132,15 +133,6 @@ __global__ void __launch_bounds__(256) divergence_f2_kernel(Grid g, Fields w, Fi
     const long fx = i + (nx + 1) * (j + ny * k);
     const long fy = i + nx * (j + (ny + 1) * k);
     const long fz = c;
-    {
-      const double rho = w.f[0][c], mx = w.f[1][c], my = w.f[2][c], mz = w.f[3][c],
-                   et = w.f[4][c];
-      int s = 0;
-      if (!(rho > 0.0)) s |= 1;
-      if (!(et > 0.0)) s |= 2;
-      if (!(eos64(g.gamma, rho, mx, my, mz, et) > 0.0)) s |= 4;
-      bad |= s;
-    }
 #pragma unroll
     for (int v = 0; v < 5 + NCHEM; ++v) {
       const float2 a0 = Fx[v * nfx + fx], a1 = Fx[v * nfx + fx + 1];
@@ -154,18 +146,18 @@ __global__ void __launch_bounds__(256) divergence_f2_kernel(Grid g, Fields w, Fi
       *dst = base - f2_to_double(div);
     }
   }
-  bad = __reduce_or_sync(0xffffffffu, bad);
-  if (bad && (threadIdx.x & 31) == 0) atomicOr(status, bad);
 }
 
 int divergence_f2(const Grid& g, const Fields& w, const Fields& wdot, float2* const (&F)[3],
                   const ForceTerm& G, int* d_status, cudaStream_t s) {
+  (void)w;
+  (void)d_status;  // the legal-state flags are set by prims_f2
   ProfScope ps("divergence", s);
   const int b = sweep_blocks(g.ncell, 256);
   switch (g.nchem) {
-#define GBMV_DIV_F2(NC)                                                                     \
-  case NC:                                                                                 \
-    divergence_f2_kernel<NC><<<b, 256, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); \
+#define GBMV_DIV_F2(NC)                                                   \
+  case NC:                                                               \
+    divergence_f2_kernel<NC><<<b, 256, 0, s>>>(g, wdot, F[0], F[1], F[2], G); \
     break;
     GBMV_DIV_F2(0)
     GBMV_DIV_F2(2)

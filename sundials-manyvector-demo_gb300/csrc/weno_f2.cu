@@ -5,8 +5,10 @@
 namespace gbmv {
 
 __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2* __restrict__ Q2,
-                                                       const double* __restrict__ tscale) {
+                                                       const double* __restrict__ tscale,
+                                                       int* __restrict__ status) {
   const long n = g.ncell;
+  int bad = 0;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
        c += (long)gridDim.x * blockDim.x) {
     const double rho = w.f[0][c], mx = w.f[1][c], my = w.f[2][c], mz = w.f[3][c], et = w.f[4][c];
@@ -14,6 +16,10 @@ __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2*
     // of the reference's quotients, far inside the float-float representation error)
     const double ir = 1.0 / rho;
     const double p = (g.gamma - 1.0) * (et - (mx * mx + my * my + mz * mz) * 0.5 * ir);
+    // legal_state (src/euler3D.hpp:1398-1414) on this pressure: it differs from the quotient
+    // form only in the last bit, so only a state with p within rounding of zero can flag
+    // differently from the FP64 form
+    bad |= (!(rho > 0.0) ? 1 : 0) | (!(et > 0.0) ? 2 : 0) | (!(p > 0.0) ? 4 : 0);
     double q[kQ2Base] = {rho, mx, my, mz, et, p, mx * ir, my * ir, mz * ir,
                          sqrt0(g.gamma * p * ir)};
 #pragma unroll
@@ -28,11 +34,14 @@ __global__ void __launch_bounds__(256) prims_f2_kernel(Grid g, Fields w, float2*
       Q2[(kQ2Base + v) * n + c] = make_float2(x.hi, x.lo);
     }
   }
+  bad = __reduce_or_sync(0xffffffffu, bad);
+  if (bad && (threadIdx.x & 31) == 0) atomicOr(status, bad);
 }
 
-int prims_f2(const Grid& g, const Fields& w, float2* q2, const double* tscale, cudaStream_t s) {
+int prims_f2(const Grid& g, const Fields& w, float2* q2, const double* tscale, int* d_status,
+             cudaStream_t s) {
   ProfScope ps("prims", s);
-  prims_f2_kernel<<<sweep_blocks(g.ncell, 256), 256, 0, s>>>(g, w, q2, tscale);
+  prims_f2_kernel<<<sweep_blocks(g.ncell, 256), 256, 0, s>>>(g, w, q2, tscale, d_status);
   GBMV_LAUNCH_CHECK("prims_f2_kernel");
   return GBMV_OK;
 }

@@ -24,8 +24,9 @@ namespace gbmv {
 
 constexpr int kQ2Base = 10;  // index of the first tracer in Q2
 
-// Q2 from w (weno_f2.cu)
-int prims_f2(const Grid& g, const Fields& w, float2* q2, const double* tscale, cudaStream_t s);
+// Q2 from w, and the legal-state flags OR-ed into *d_status (weno_f2.cu)
+int prims_f2(const Grid& g, const Fields& w, float2* q2, const double* tscale, int* d_status,
+             cudaStream_t s);
 // the WV = 1 sweep (weno_f2_fast.cu)
 int feuler_f2_fast(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
                    double* scratch, float2* q2, const double* tscale, int* d_status,
@@ -152,7 +153,7 @@ int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTer
   face_counts(g, nf);
   float2* const F2 = reinterpret_cast<float2*>(scratch);  // 8 bytes per flux, as a double
   float2* F[3] = {F2, F2 + (long)(5 + NCHEM) * nf[0], F2 + (long)(5 + NCHEM) * (nf[0] + nf[1])};
-  int rc = prims_f2(g, w, q2, tscale, s);
+  int rc = prims_f2(g, w, q2, tscale, d_status, s);
   if (rc != GBMV_OK) return rc;
   {
     ProfScope ps("face_flux", s);
