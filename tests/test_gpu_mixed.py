@@ -51,6 +51,37 @@ def test_mixed_illegal_state_flagged(cuda):
     assert st == -1
 
 
+def _status_mask(torch, wl, precision):
+    import gbmv
+    nz, ny, nx = wl["fields"][0].shape
+    h = gbmv.Hydro((nx, ny, nz), wl["nchem"], wl["bc"], wl["gamma"], wl["force"])
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    wdot = [torch.zeros_like(f) for f in w]
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    h.fEuler_async(0.0, w, wdot, status, precision)
+    torch.cuda.synchronize()
+    return int(status.item())
+
+
+@pytest.mark.parametrize("plant", ["none", "rho", "et", "p", "rho_and_p"])
+def test_mixed_legal_state_mask_matches_fp64(cuda, plant):
+    """The float-float forms set the legal-state bits (1 density, 2 energy, 4 pressure;
+    legal_state, src/euler3D.hpp:1398-1414) in their primitives pass; the mask must equal the
+    FP64 form's for states away from p = 0 within rounding."""
+    wl = W.rayleigh_taylor(shape=(7, 6, 5), nchem=10, seed=W.SEED_BASE + 310)
+    rho, mx, my, mz, et = wl["fields"][:5]
+    ke = 0.5 * (mx * mx + my * my + mz * mz) / rho
+    if plant in ("rho", "rho_and_p"):
+        rho[1, 2, 3] = -1.0
+    if plant == "et":
+        et[4, 1, 2] = -0.5
+    if plant in ("p", "rho_and_p"):
+        et[2, 4, 1] = 0.25 * ke[2, 4, 1]  # positive energy below the kinetic energy
+    masks = [_status_mask(cuda, wl, prec) for prec in (0, 1, 2)]
+    expect = {"none": 0, "rho": 1, "et": 6, "p": 4, "rho_and_p": 5}[plant]
+    assert masks == [expect] * 3, masks
+
+
 def _chem_setup(torch, tables, n, seed):
     import gbmv
     y, _ = W.primordial(n, seed=seed)
