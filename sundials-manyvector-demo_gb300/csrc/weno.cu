@@ -148,15 +148,13 @@ __global__ void __launch_bounds__(256) divergence_f2_kernel(Grid g, Fields wdot,
   }
 }
 
-int divergence_f2(const Grid& g, const Fields& w, const Fields& wdot, float2* const (&F)[3],
-                  const ForceTerm& G, int* d_status, cudaStream_t s) {
-  (void)w;
-  (void)d_status;  // the legal-state flags are set by prims_f2
+int divergence_f2(const Grid& g, const Fields& wdot, float2* const (&F)[3], const ForceTerm& G,
+                  cudaStream_t s) {
   ProfScope ps("divergence", s);
   const int b = sweep_blocks(g.ncell, 256);
   switch (g.nchem) {
-#define GBMV_DIV_F2(NC)                                                   \
-  case NC:                                                               \
+#define GBMV_DIV_F2(NC)                                                     \
+  case NC:                                                                  \
     divergence_f2_kernel<NC><<<b, 256, 0, s>>>(g, wdot, F[0], F[1], F[2], G); \
     break;
     GBMV_DIV_F2(0)

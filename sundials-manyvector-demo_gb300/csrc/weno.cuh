@@ -24,8 +24,9 @@ int feuler_fp64(const Grid& g, const Fields& w, const Fields& wdot, const ForceT
 int divergence(const Grid& g, const Fields& w, const Fields& wdot, double* const (&F)[3],
                const ForceTerm& G, int* d_status, cudaStream_t s);
 // the same from fluxes stored as float pairs (hi, lo), differenced in float-float
-int divergence_f2(const Grid& g, const Fields& w, const Fields& wdot, float2* const (&F)[3],
-                  const ForceTerm& G, int* d_status, cudaStream_t s);
+// (no legal-state check: the float-float forms set those flags in prims_f2)
+int divergence_f2(const Grid& g, const Fields& wdot, float2* const (&F)[3], const ForceTerm& G,
+                  cudaStream_t s);
 
 int wave_speed_max(const Grid& g, const Fields& w, unsigned long long* d_out, cudaStream_t s);
 int pack1d(const Grid& g, const Fields& w, int dir, double* out, cudaStream_t s);

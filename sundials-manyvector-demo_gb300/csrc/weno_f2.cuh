@@ -173,7 +173,7 @@ int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTer
                                                                                 nf[2]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<z>");
   }
-  return divergence_f2(g, w, wdot, F, G, d_status, s);
+  return divergence_f2(g, wdot, F, G, s);
 }
 
 template <int WV>
