@@ -359,7 +359,7 @@ def algo_bytes(fam, n):
 
 # Arithmetic per unit of each kernel family, counted by ncu on these kernels
 # (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma} or {fadd,fmul,ffma}: adds + muls +
-# 2 x FMAs, per face or cell; profiles/fp_counts_112cube.md) -- the numerator of the compute
+# 2 x FMAs, per face or cell, on a 112^3 grid) -- the numerator of the compute
 # roofline; the denominator is the FMA rate measured by gbmv_diag_fma_rate.
 FP_COUNTS = {
     ("fp64", "face_flux"): ("fp64", 3841.3, "face"),
@@ -374,7 +374,7 @@ FP_COUNTS = {
 
 
 # DRAM bytes per unit of the dominant kernels, from ncu captures with the state larger than
-# L2 (dram__bytes_read.sum + dram__bytes_write.sum; profiles/fp_counts_112cube.md), scaled by
+# L2 (dram__bytes_read.sum + dram__bytes_write.sum per face or cell on a 112^3 grid), scaled by
 # the units of one 128^3 launch for the roofline's `traffic`.
 DRAM_TRAFFIC = {
     ("fp64", "face_flux"): (248.2, "face"),    # mean of the x / y / z sweeps

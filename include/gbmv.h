@@ -100,10 +100,13 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
  * cudaMalloc'ed buffers.
  *   Limit: (5+nchem) * [(nx+1)*ny*nz + nx*(ny+1)*nz + nx*ny*(nz+1)] <= 8388608 doubles
  *          (64 MiB, e.g. 56^3 at nchem=10, 82^3 at nchem=0); larger grids return GBMV_EINVAL
- *          with a message, nothing is launched.  Every GPU that loads this library keeps the
- *          64 MiB reserved until the process exits.
+ *          with a message, nothing is launched.  Bad grids, null fields: the codes and
+ *          messages of gbmv_hydro_create / gbmv_feuler.
  *   The first call on each device looks up the arrays' device addresses (with that device
- *   current); make that first call before any stream capture.
+ *   current).  Under CUDA's lazy module loading (the default) that lookup is also what commits
+ *   the 64 MiB on the device, which then stays committed until the process exits.  So make
+ *   the first call on each device before the caller's memory pool takes the device's free
+ *   memory, and before any stream capture; later calls commit nothing more.
  *   All calls share the one array and status word, which keep the last call's contents: the
  *   status word is cleared at the start of each call, but calls that overlap on the GPU
  *   (other streams, other host threads) race on the shared scratch -- serialise them.
@@ -324,7 +327,10 @@ double* gbmv_chem_state(gbmv_chem c, int which);
  * SUNLinSol_BDMPIMV (src/multirate_chem_hydro_main.cpp:1360-1369,
  * src/imex_chem_hydro_main.cpp:1123-1132): LU with partial pivoting of every 10x10 block of
  * A in place; pivots: 10 ints per block.  Returns 0, or a positive value (SUNLS_LUFACT_FAIL
- * style, recoverable) if some block is singular. */
+ * style, recoverable) if some block is singular.  Synchronous.  The singular-block flag is a
+ * device word of the calling host thread on the current device (allocated at that thread's
+ * first call there), so calls from different threads or on different devices do not share
+ * it. */
 int gbmv_block_lu_factor(long nblocks, double* A, int* pivots, void* stream);
 
 /* SUNLinSolSolve of the same (src/multirate_chem_hydro_main.cpp:1371-1395): x = A^{-1} b

@@ -95,7 +95,7 @@ struct gbmv_chem_s {
   int newton_bps = 0;                  // fused Newton: resident blocks per SM (0 = default)
 };
 
-static int check_grid(const gbmv_grid* g) {
+int gbmv::check_grid(const gbmv_grid* g) {
   if (!g) { set_error("null grid"); return GBMV_EINVAL; }
   if (g->nx < 3 || g->ny < 3 || g->nz < 3) {
     set_error("every extent must be >= 3 (got %ld x %ld x %ld)", g->nx, g->ny, g->nz);
@@ -671,15 +671,27 @@ int gbmv_chem_dirk_block(gbmv_chem c, int precision) {
 
 /* ------------------------------------------------------------------ block solve */
 
+// Status word of gbmv_block_lu_factor, which takes no handle: one word per (host thread,
+// device), allocated on that device at the thread's first factorisation there.  A call resets,
+// fills and reads its word before it returns, so calls of one thread never overlap, calls of
+// different threads use different words, and a word is never read on another device.
+// (4 bytes per thread and device stay allocated until the process exits.)
 static int* lu_info_buffer() {
-  static int* buf = nullptr;
-  static std::mutex m;
-  std::lock_guard<std::mutex> lk(m);
-  if (!buf && cudaMalloc(&buf, sizeof(int)) != cudaSuccess) {
+  constexpr int kMaxDev = 64;
+  static thread_local int* buf[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
     cudaGetLastError();
+    set_error("no usable current device for the block factorisation status word");
     return nullptr;
   }
-  return buf;
+  if (!buf[dev] && cudaMalloc(&buf[dev], sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    buf[dev] = nullptr;
+    set_error("device allocation of the block factorisation status word failed");
+    return nullptr;
+  }
+  return buf[dev];
 }
 
 int gbmv_block_lu_factor(long nblocks, double* A, int* pivots, void* stream) {

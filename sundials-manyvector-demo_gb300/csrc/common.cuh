@@ -12,6 +12,9 @@ namespace gbmv {
 void set_error(const char* fmt, ...);
 void count_launch(long n = 1);
 int check_cuda(cudaError_t e, const char* where);
+// Grid validation shared by every entry point that takes a gbmv_grid (capi.cu): 0, or
+// GBMV_EINVAL / GBMV_EUNSUPPORTED with the reason in gbmv_last_error().
+int check_grid(const gbmv_grid* g);
 
 #define GBMV_CUDA_TRY(expr)                                   \
   do {                                                        \

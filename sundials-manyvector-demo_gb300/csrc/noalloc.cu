@@ -9,8 +9,10 @@ namespace gbmv {
 namespace {
 
 // 64 MiB of flux scratch: enough for (5+nchem) * (face count of the three directions)
-// doubles, e.g. a 56^3 grid at NVAR=15 or an 82^3 grid at NVAR=5.  Every GPU on which the
-// library is loaded keeps this much memory reserved until the process exits.
+// doubles, e.g. a 56^3 grid at NVAR=15 or an 82^3 grid at NVAR=5.  This file has no kernel
+// of its own and is a module of its own, so under CUDA's lazy module loading (the default)
+// the memory is committed on a device when the first call there looks the arrays up, and
+// stays committed until the process exits.
 constexpr size_t kNoAllocScratchDoubles = size_t(8) << 20;
 
 __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
@@ -29,7 +31,8 @@ DeviceAddrs g_addr[kMaxDevices];
 
 // In host code the array names above are host-side stand-ins, not device addresses: passing
 // them to a kernel would fault.  Once per device, with that device current, look the real
-// addresses up with cudaGetSymbolAddress and keep them.
+// addresses up with cudaGetSymbolAddress (which also loads this module and commits its 64 MiB
+// on that device) and keep them.
 int device_addresses(DeviceAddrs* out) {
   int dev = 0;
   GBMV_CUDA_TRY(cudaGetDevice(&dev));
@@ -51,18 +54,6 @@ int device_addresses(DeviceAddrs* out) {
   return GBMV_OK;
 }
 
-int grid_ok(const gbmv_grid* g) {
-  if (!g || g->nx < 3 || g->ny < 3 || g->nz < 3) return 0;
-  if (!(g->nchem == 0 || g->nchem == 2 || g->nchem == 4 || g->nchem == 6 || g->nchem == 10))
-    return 0;
-  for (int a = 0; a < 3; ++a) {
-    const int lo = g->bc[2 * a], hi = g->bc[2 * a + 1];
-    if (lo < 0 || lo > 3 || hi < 0 || hi > 3) return 0;
-    if ((lo == GBMV_BC_PERIODIC) != (hi == GBMV_BC_PERIODIC)) return 0;
-  }
-  return g->dx > 0 && g->dy > 0 && g->dz > 0 && g->gamma > 1.0;
-}
-
 }  // namespace
 }  // namespace gbmv
 
@@ -71,10 +62,9 @@ using namespace gbmv;
 extern "C" int gbmv_feuler_noalloc(const gbmv_grid* grid, const double* force_host, double t,
                                    const double* const* w, double* const* wdot, void* stream) {
   (void)t;
-  if (!grid_ok(grid)) {
-    set_error("invalid grid for gbmv_feuler_noalloc");
-    return GBMV_EINVAL;
-  }
+  // the same checks, return codes and messages as gbmv_hydro_create
+  int rc = check_grid(grid);
+  if (rc) return rc;
   const Grid g = make_grid(*grid);
   const size_t need = feuler_fp64_scratch_doubles(g);
   if (need > kNoAllocScratchDoubles) {
@@ -83,13 +73,16 @@ extern "C" int gbmv_feuler_noalloc(const gbmv_grid* grid, const double* force_ho
               need, kNoAllocScratchDoubles);
     return GBMV_EINVAL;
   }
-  if (!w || !wdot) return GBMV_EINVAL;
-  for (int v = 0; v < 5; ++v)
-    if (!w[v] || !wdot[v]) return GBMV_EINVAL;
-  if (g.nchem && (!w[5] || !wdot[5])) return GBMV_EINVAL;
+  bool fields = w && wdot;
+  for (int v = 0; fields && v < 5; ++v) fields = w[v] && wdot[v];
+  if (fields && g.nchem) fields = w[5] && wdot[5];
+  if (!fields) {
+    set_error("gbmv_feuler_noalloc: null field pointer");
+    return GBMV_EINVAL;
+  }
 
   DeviceAddrs a;
-  int rc = device_addresses(&a);
+  rc = device_addresses(&a);
   if (rc) return rc;
 
   Fields W, Wd;

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import workloads as W
-from conftest import maxnorm_err
+from conftest import case_fields, feuler_case_names, maxnorm_err
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -30,7 +30,8 @@ def _ptrs(torch_list):
 def _call_noalloc(lib, wl, w, wdot, stream):
     import gbmv
     nz, ny, nx = wl["fields"][0].shape
-    g = gbmv.grid_struct((nx, ny, nz), wl["nchem"], wl["bc"], wl["gamma"])
+    g = gbmv.grid_struct((nx, ny, nz), wl["nchem"], wl["bc"], wl["gamma"],
+                         wl.get("domain", (0.0, 1.0, 0.0, 1.0, 0.0, 1.0)))
     force = None
     if wl["force"] is not None:
         fa = np.ascontiguousarray(wl["force"], dtype=np.float64)
@@ -100,3 +101,65 @@ def test_noalloc_rejects_grids_beyond_capacity(cuda):
                                  C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == -101
     assert b"scratch" in lib.gbmv_last_error()
+
+
+def test_noalloc_matches_reference_fixtures(cuda, golden_feuler):
+    """Against the outputs of the reference's own fEuler (tests/golden), every fixture case,
+    two calls in a row per case through the shared array."""
+    torch = cuda
+    import gbmv
+    lib = gbmv.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    g = golden_feuler
+    for name in feuler_case_names(g):
+        fields, nchem, bc, gamma, force = case_fields(g, name)
+        wl = dict(fields=fields, nchem=nchem, bc=bc, gamma=gamma,
+                  force=None if force is None or np.ndim(force) == 0 else force)
+        w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in fields]
+        for _ in range(2):
+            wdot = [torch.full_like(f, np.nan) for f in w]
+            rc = _call_noalloc(lib, wl, w, wdot, stream)
+            assert rc == int(g[f"{name}/status"]), (name, rc, lib.gbmv_last_error())
+            if rc:
+                continue
+            torch.cuda.synchronize()
+            for i, o in enumerate(wdot):
+                e = maxnorm_err(o.cpu().numpy(), g[f"{name}/wdot{i}"])
+                assert e <= TOL, (name, i, e)
+
+
+def test_noalloc_second_call_commits_no_memory(cuda):
+    """The first call on a device may commit the fixed array (lazy module loading); after it,
+    calls take no device memory: the device's free memory is the same before and after."""
+    torch = cuda
+    import gbmv
+    lib = gbmv.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    wl = W.rayleigh_taylor(shape=(20, 18, 16), nchem=10, seed=W.SEED_BASE + 204)
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    wdot = [torch.empty_like(f) for f in w]
+    assert _call_noalloc(lib, wl, w, wdot, stream) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert _call_noalloc(lib, wl, w, wdot, stream) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
+def test_noalloc_reports_refusals(cuda):
+    """Every refusal sets the message: bad grids as gbmv_hydro_create, null fields."""
+    torch = cuda
+    import gbmv
+    lib = gbmv.load()
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    dummy = torch.zeros(8, dtype=torch.float64, device="cuda")
+    arr = _ptrs([dummy] * 6)
+    g = gbmv.grid_struct((8, 8, 8), 3, (0,) * 6, 1.4)
+    assert lib.gbmv_feuler_noalloc(C.byref(g), None, C.c_double(0.0), arr, arr, s) == -104
+    assert b"nchem" in lib.gbmv_last_error()
+    g = gbmv.grid_struct((8, 8, 8), 0, (0,) * 6, 1.4)
+    empty = (C.c_void_p * 6)()
+    assert lib.gbmv_feuler_noalloc(C.byref(g), None, C.c_double(0.0), empty, arr, s) == -101
+    assert b"null field" in lib.gbmv_last_error()
