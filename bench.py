@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--newton-refine", type=int, default=None,
                    help="FP64-residual refinement cap of the fused Newton (default 2)")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-parity", action="store_true",
+                   help="skip the whole-grid comparisons with the oracle (all host cores)")
     p.add_argument("--dirk-n", type=int, default=64,
                    help="static-chemistry DIRK measurement on dirk_n^3 cells (0 = skip)")
     p.add_argument("--weno-n", default="128,256",
@@ -533,6 +535,9 @@ def run_gbmv(args):
         line["forms_maxnorm_err_vs_fp64"] = {f: float(f"{max(e.values()):.3e}")
                                              for f, e in all_errs.items()}
 
+    if not args.no_parity:
+        line["parity"] = fused_parity(wl, {f: r["out"] for f, r in res.items()}, head)
+
     if not args.no_e2e:
         fs = R["fs"] if R["fs"] is not None else make_fs(head)
         pin_in = [torch.from_numpy(a).pin_memory() for a in fs.host]
@@ -571,7 +576,8 @@ def run_gbmv(args):
             r["fs"] = None
         fs = None
         torch.cuda.empty_cache()
-        line["weno_rhs"] = run_weno(torch, gbmv, [int(x) for x in args.weno_n.split(",") if x])
+        line["weno_rhs"] = run_weno(torch, gbmv, [int(x) for x in args.weno_n.split(",") if x],
+                                    parity=not args.no_parity)
     if not args.no_sod:
         line["sod"] = run_sod(torch, gbmv, not args.no_cpu_baseline)
     if args.mri_n > 0:
@@ -603,13 +609,75 @@ def run_gbmv(args):
     print(json.dumps(line))
 
 
+# ----------------------------------------------------------------- whole-grid parity
+
+OUT_NAMES = ["rho", "mx", "my", "mz", "et", "chem", "fimpl", "newton_x"]
+
+
+def _maxnorm(a, b):
+    """max |a - b| / max |b| (NaN positions must coincide)."""
+    na, nb = np.isnan(a), np.isnan(b)
+    if not np.array_equal(na, nb):
+        return float("inf")
+    m = ~nb
+    if not m.any():
+        return 0.0
+    sc = float(np.max(np.abs(b[m])))
+    d = float(np.max(np.abs(a[m] - b[m])))
+    return d / sc if sc > 0 else d
+
+
+def _out_errs(outs, refs, names):
+    e = {}
+    for nm, a, b in zip(names, outs, refs):
+        if nm in ("chem", "fimpl", "newton_x"):
+            a2, b2 = a.reshape(-1, 10), b.reshape(-1, 10)
+            e[nm] = max(_maxnorm(a2[:, k], b2[:, k]) for k in range(10))
+        else:
+            e[nm] = _maxnorm(a, b)
+    return {k: float(f"{v:.3e}") for k, v in e.items()}
+
+
+def fused_parity(wl, form_outs, head):
+    """Every timed form's outputs of one stage at the full grid against the oracle's
+    composition of the same stage (fexpl + fimpl + Jimpl + block solve), evaluated on all
+    host cores (z-slabs and cell ranges on threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import h5tables
+    import oracle_py as O
+    t0 = time.time()
+    fields = [np.array(f, copy=True) for f in wl["fields"]]
+    oc = O.Chem(h5tables.load_table_block(TABLES), wl["scale"].reshape(-1))
+    st, ref = O.fused_chem_hydro_step(fields, wl["scale"], oc, wl["bc"], wl["gamma"],
+                                      wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"],
+                                      GAMMA_NEWTON, threads=0)
+    secs = time.time() - t0
+    if st != 0:
+        return {"error": f"oracle status {st}"}
+    errs = {f: _out_errs(o, ref, OUT_NAMES) for f, o in form_outs.items()}
+    out = {"what": ("one fused stage from the initial state, every output of every timed form "
+                    "against the CPU oracle at the full grid (per field max|gpu - oracle| / "
+                    "max|oracle|; chemistry, fimpl and the Newton update per species)"),
+           "oracle_threads": os.cpu_count(), "oracle_s": round(secs, 2),
+           "bars": {"fp64": "1e-12 (Newton update 1e-10)", "mixed forms": "1e-6"},
+           "maxnorm_err_vs_oracle": {f: max(e.values()) for f, e in errs.items()},
+           "per_output": {f: errs[f] for f in ("fp64", head) if f in errs}}
+    out["fp64_maxnorm_err_vs_oracle"] = out["maxnorm_err_vs_oracle"].get("fp64")
+    out["mixed_maxnorm_err_vs_oracle"] = out["maxnorm_err_vs_oracle"].get(head)
+    return out
+
+
 # ----------------------------------------------------------------- WENO RHS throughput (RT)
 
-def run_weno(torch, gbmv, grids, steps=3, warmup=2):
-    """Rayleigh-Taylor WENO RHS (fEuler alone) at NVAR 15, both forms: RHS evaluations per
-    second, cell updates per second, algorithmic HBM GB/s (read w + write wdot = 240 B/cell)
-    and the FP64 form's FP64-pipe fraction from the counted flops per face."""
+def run_weno(torch, gbmv, grids, steps=3, warmup=2, parity=True):
+    """Rayleigh-Taylor WENO RHS (fEuler alone) at NVAR 15, the FP64 and both mixed forms: RHS
+    evaluations per second, cell updates per second, algorithmic HBM GB/s (read w + write wdot
+    = 240 B/cell) and the FP64 form's FP64-pipe fraction from the counted flops per face; with
+    `parity`, each form's output against the CPU oracle at the full grid (all host cores)."""
     import workloads as W
+    if parity:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py as O
     fp64_peak = gbmv.fma_rate(True) / 1e12
     hbm_peak, peak_kind = measured_peaks()
     out = {"workload": "Rayleigh-Taylor: rho = 1.5 + 0.5 tanh((z-0.5)/0.02), hydrostatic p "
@@ -621,16 +689,27 @@ def run_weno(torch, gbmv, grids, steps=3, warmup=2):
         wl = W.rayleigh_taylor(n=n, nchem=10)
         h = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"], wl["force"])
         w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
-        del wl
         wdot = [torch.empty_like(f) for f in w]
+        ref = None
+        if parity:
+            t0 = time.time()
+            st, ref = O.feuler(wl["fields"], 10, wl["bc"], wl["gamma"], wl["force"], threads=0)
+            oracle_s = time.time() - t0
+            if st != 0:
+                raise RuntimeError("oracle: illegal state")
+        del wl
         ncell = n ** 3
         faces = 3 * (n + 1) * n * n
         g = {}
-        for name, prec in (("fp64", gbmv.FP64), ("mixed", gbmv.MIXED)):
+        perr = {}
+        for name, prec in (("fp64", gbmv.FP64), ("mixed", gbmv.MIXED),
+                           ("mixed_fast", gbmv.MIXED_FAST)):
             def rhs():
                 if h.fEuler(0.0, w, wdot, prec) != 0:
                     raise RuntimeError("fEuler failed")
             ms = time_steps(torch, rhs, steps, warmup)
+            if ref is not None:
+                perr[name] = float(f"{max(_maxnorm(a.cpu().numpy(), b) for a, b in zip(wdot, ref)):.3e}")
             r = {"ms_per_rhs": round(ms, 3), "rhs_per_s": round(1e3 / ms, 2),
                  "Mcell_updates_per_s": round(ncell / (ms * 1e-3) / 1e6, 2),
                  "algorithmic_GBps": round(240.0 * ncell / (ms * 1e-3) / 1e9, 1),
@@ -640,8 +719,14 @@ def run_weno(torch, gbmv, grids, steps=3, warmup=2):
                 r["fp64_pipe_frac"] = round(fl / (ms * 1e-3) / 1e12 / fp64_peak, 4)
             g[name] = r
         g["speedup_mixed_vs_fp64"] = round(g["fp64"]["ms_per_rhs"] / g["mixed"]["ms_per_rhs"], 3)
+        g["speedup_mixed_fast_vs_fp64"] = round(g["fp64"]["ms_per_rhs"] /
+                                                g["mixed_fast"]["ms_per_rhs"], 3)
+        if ref is not None:
+            g["parity"] = {"maxnorm_err_vs_oracle": perr, "oracle_threads": os.cpu_count(),
+                           "oracle_s": round(oracle_s, 2),
+                           "bars": {"fp64": 1e-12, "mixed": 1e-6, "mixed_fast": 1e-6}}
         out["grids"][f"{n}^3"] = g
-        del h, w, wdot
+        del h, w, wdot, ref
         torch.cuda.empty_cache()
     return out
 

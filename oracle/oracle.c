@@ -182,41 +182,48 @@ void orc_face_flux(const orc_grid* g, double* w1d, int idir, double* f_face) {
 }
 
 /* fEuler (src/utilities.cpp:17-253): forcing, all lower faces plus the upper boundary faces,
- * then wdot = G - [(Fx(i+1)-Fx(i))/dx + (Fy(j+1)-Fy(j))/dy + (Fz(k+1)-Fz(k))/dz]. */
-int orc_feuler(const orc_grid* g, const double* const* w, double* const* wdot,
-               const double* force) {
-  const long nx = g->nx, ny = g->ny, nz = g->nz, n = nx * ny * nz;
+ * then wdot = G - [(Fx(i+1)-Fx(i))/dx + (Fy(j+1)-Fy(j))/dy + (Fz(k+1)-Fz(k))/dz].
+ * This form evaluates the output planes k0 <= k < k1 only (the x and y faces of those planes
+ * and the z faces k0 .. k1), reading the whole input; each output value is computed exactly as
+ * in the whole-grid evaluation, so disjoint slabs can run on separate threads.  The legal-state
+ * test covers the slab's cells (the whole grid's status is the OR over the slabs). */
+int orc_feuler_slab(const orc_grid* g, const double* const* w, double* const* wdot,
+                    const double* force, long k0, long k1) {
+  const long nx = g->nx, ny = g->ny, nz = g->nz;
   const int nv = 5 + g->nchem;
-  int status = 0;
-  for (long c = 0; c < n; ++c)
-    if (legal_state(g->gamma, w[0][c], w[1][c], w[2][c], w[3][c], w[4][c])) status = -1;
-  if (status) return status;
+  if (k0 < 0) k0 = 0;
+  if (k1 > nz) k1 = nz;
+  if (k1 <= k0) return 0;
+  const long nk = k1 - k0;
+  for (long c = k0 * nx * ny; c < k1 * nx * ny; ++c)
+    if (legal_state(g->gamma, w[0][c], w[1][c], w[2][c], w[3][c], w[4][c])) return -1;
 
   double* fl[3];
-  const long fext[3][3] = {{nx + 1, ny, nz}, {nx, ny + 1, nz}, {nx, ny, nz + 1}};
+  /* face extents of the slab; face (i, j, kk) of direction d has global plane k0 + kk */
+  const long fext[3][3] = {{nx + 1, ny, nk}, {nx, ny + 1, nk}, {nx, ny, nk + 1}};
   for (int d = 0; d < 3; ++d)
     fl[d] = (double*)malloc(sizeof(double) * nv * fext[d][0] * fext[d][1] * fext[d][2]);
   double w1d[STS * MAXVAR];
   for (int d = 0; d < 3; ++d) {
     const long ex = fext[d][0], ey = fext[d][1], ez = fext[d][2];
-    for (long k = 0; k < ez; ++k)
+    for (long kk = 0; kk < ez; ++kk)
       for (long j = 0; j < ey; ++j)
         for (long i = 0; i < ex; ++i) {
           for (int l = 0; l < STS; ++l) {
-            long p[3] = {i, j, k};
+            long p[3] = {i, j, k0 + kk};
             p[d] += l - 3;
             for (int v = 0; v < nv; ++v) w1d[l * nv + v] = field_at(g, w, v, p);
           }
-          orc_face_flux(g, w1d, d, &fl[d][nv * (i + ex * (j + ey * k))]);
+          orc_face_flux(g, w1d, d, &fl[d][nv * (i + ex * (j + ey * kk))]);
         }
   }
   const double dd[3] = {g->dx, g->dy, g->dz};
-  for (long k = 0; k < nz; ++k)
+  for (long kk = 0; kk < nk; ++kk)
     for (long j = 0; j < ny; ++j)
       for (long i = 0; i < nx; ++i) {
-        const long c = i + nx * (j + ny * k);
-        const long lo[3] = {nv * (i + (nx + 1) * (j + ny * k)), nv * (i + nx * (j + (ny + 1) * k)),
-                            nv * (i + nx * (j + ny * k))};
+        const long c = i + nx * (j + ny * (k0 + kk));
+        const long lo[3] = {nv * (i + (nx + 1) * (j + ny * kk)), nv * (i + nx * (j + (ny + 1) * kk)),
+                            nv * (i + nx * (j + ny * kk))};
         const long hi[3] = {lo[0] + nv, lo[1] + nv * nx, lo[2] + nv * nx * ny};
         for (int v = 0; v < nv; ++v) {
           const double div = (fl[0][hi[0] + v] - fl[0][lo[0] + v]) / dd[0] +
@@ -231,6 +238,15 @@ int orc_feuler(const orc_grid* g, const double* const* w, double* const* wdot,
       }
   for (int d = 0; d < 3; ++d) free(fl[d]);
   return 0;
+}
+
+int orc_feuler(const orc_grid* g, const double* const* w, double* const* wdot,
+               const double* force) {
+  /* the whole grid's legal-state test comes first: nothing is written for an illegal state */
+  const long n = g->nx * g->ny * g->nz;
+  for (long c = 0; c < n; ++c)
+    if (legal_state(g->gamma, w[0][c], w[1][c], w[2][c], w[3][c], w[4][c])) return -1;
+  return orc_feuler_slab(g, w, wdot, force, 0, g->nz);
 }
 
 /* -------------------------------------------------------------- chemistry */

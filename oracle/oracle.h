@@ -43,6 +43,12 @@ typedef struct {
 int orc_feuler(const orc_grid* g, const double* const* w, double* const* wdot,
                const double* force);
 
+/* orc_feuler restricted to the output planes k0 <= k < k1 (reading the whole input): the same
+ * values the whole-grid call writes there, so disjoint slabs may run on separate threads.
+ * Returns -1 if a cell of the slab is an illegal state. */
+int orc_feuler_slab(const orc_grid* g, const double* const* w, double* const* wdot,
+                    const double* force, long k0, long k1);
+
 /* face_flux on one 6-point stencil w1d[6][nvar] (src/utilities.cpp:270-479). */
 void orc_face_flux(const orc_grid* g, double* w1d, int idir, double* f_face);
 

@@ -7,6 +7,7 @@ baseline legs, never by the product path.
 from __future__ import annotations
 
 import ctypes as C
+import concurrent.futures as cf
 import math
 import os
 import subprocess
@@ -92,9 +93,23 @@ def grid(shape, nchem, bc, gamma=1.4, domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
     return g
 
 
-def feuler(fields, nchem, bc, gamma=1.4, force=None, domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+def _threads(threads):
+    return max(1, os.cpu_count() or 1) if threads in (None, 0) else max(1, int(threads))
+
+
+def _chunks(n, parts):
+    """[(lo, hi)] splitting range(n) into at most `parts` near-equal pieces."""
+    parts = max(1, min(parts, n))
+    edges = [n * i // parts for i in range(parts + 1)]
+    return [(a, b) for a, b in zip(edges[:-1], edges[1:]) if b > a]
+
+
+def feuler(fields, nchem, bc, gamma=1.4, force=None, domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0),
+           threads=1):
     """fields: list of 5 arrays shaped (nz,ny,nx) and, if nchem>0, chem shaped (nz,ny,nx,nchem).
-    Returns (status, list of output arrays of the same shapes)."""
+    Returns (status, list of output arrays of the same shapes).  threads > 1 (0 = every core)
+    evaluates disjoint z-slabs of the output on that many threads (orc_feuler_slab; ctypes
+    releases the interpreter lock during the calls); the values are those of one call."""
     nz, ny, nx = fields[0].shape
     g = grid((nx, ny, nz), nchem, bc, gamma, domain)
     ins = [np.ascontiguousarray(f, dtype=np.float64) for f in fields]
@@ -105,7 +120,18 @@ def feuler(fields, nchem, bc, gamma=1.4, force=None, domain=(0.0, 1.0, 0.0, 1.0,
     if force is not None:
         fa = np.ascontiguousarray(force, dtype=np.float64)
         fc = _ptr(fa)
-    st = lib().orc_feuler(C.byref(g), inp, outp, fc)
+    nt = _threads(threads)
+    if nt == 1:
+        return lib().orc_feuler(C.byref(g), inp, outp, fc), outs
+    L = lib()
+    L.orc_feuler_slab.restype = C.c_int
+    with cf.ThreadPoolExecutor(nt) as ex:
+        sts = list(ex.map(lambda kk: L.orc_feuler_slab(C.byref(g), inp, outp, fc,
+                                                       C.c_long(kk[0]), C.c_long(kk[1])),
+                          _chunks(nz, 4 * nt)))
+    st = -1 if any(sts) else 0
+    if st:  # the whole-grid call writes nothing for an illegal state
+        outs = [np.zeros_like(f) for f in ins]
     return st, outs
 
 
@@ -128,21 +154,41 @@ class Chem:
         self.Ts = np.full(self.n, 1000.0)
         self.dTs_ge = np.zeros(self.n)
 
-    def rhs(self, y: np.ndarray) -> np.ndarray:
+    def _per_cell(self, fn, threads):
+        """fn(lo, hi) over cell ranges, on `threads` threads (0 = every core).  The network is
+        per cell (each cell reads and writes only its own entries), so chunks are disjoint."""
+        nt = _threads(threads)
+        if nt == 1:
+            fn(0, self.n)
+            return
+        with cf.ThreadPoolExecutor(nt) as ex:
+            list(ex.map(lambda r: fn(*r), _chunks(self.n, 4 * nt)))
+
+    def rhs(self, y: np.ndarray, threads=1) -> np.ndarray:
         y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
         yd = np.zeros_like(y)
-        lib().orc_chem_rhs(C.byref(self.c), C.c_long(self.n), _ptr(y), _ptr(self.scale),
-                           _ptr(self.inv_scale), _ptr(self.mdens), _ptr(self.imdens),
-                           _ptr(self.cie), _ptr(self.h2), _ptr(self.Ts), _ptr(self.dTs_ge),
-                           _ptr(yd))
+        L = lib()
+
+        def part(a, b):
+            L.orc_chem_rhs(C.byref(self.c), C.c_long(b - a), _ptr(y[10 * a:10 * b]),
+                           _ptr(self.scale[10 * a:10 * b]), _ptr(self.inv_scale[10 * a:10 * b]),
+                           _ptr(self.mdens[a:b]), _ptr(self.imdens[a:b]), _ptr(self.cie[a:b]),
+                           _ptr(self.h2[a:b]), _ptr(self.Ts[a:b]), _ptr(self.dTs_ge[a:b]),
+                           _ptr(yd[10 * a:10 * b]))
+        self._per_cell(part, threads)
         return yd
 
-    def jac(self, y: np.ndarray) -> np.ndarray:
+    def jac(self, y: np.ndarray, threads=1) -> np.ndarray:
         y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
         J = np.zeros(self.n * 100)
-        lib().orc_chem_jac(C.byref(self.c), C.c_long(self.n), _ptr(y), _ptr(self.scale),
-                           _ptr(self.inv_scale), _ptr(self.mdens), _ptr(self.cie),
-                           _ptr(self.h2), _ptr(self.Ts), _ptr(self.dTs_ge), _ptr(J))
+        L = lib()
+
+        def part(a, b):
+            L.orc_chem_jac(C.byref(self.c), C.c_long(b - a), _ptr(y[10 * a:10 * b]),
+                           _ptr(self.scale[10 * a:10 * b]), _ptr(self.inv_scale[10 * a:10 * b]),
+                           _ptr(self.mdens[a:b]), _ptr(self.cie[a:b]), _ptr(self.h2[a:b]),
+                           _ptr(self.Ts[a:b]), _ptr(self.dTs_ge[a:b]), _ptr(J[100 * a:100 * b]))
+        self._per_cell(part, threads)
         return J.reshape(self.n, 10, 10)  # [cell][col][row]
 
     def dirk_evolve(self, y: np.ndarray, t0: float, tout: float, tunit: float, forcing=(),
@@ -169,13 +215,59 @@ class Chem:
         return y, stats, int(nf)
 
 
-def block_newton_solve(J: np.ndarray, gamma: float, b: np.ndarray):
+def block_newton_solve(J: np.ndarray, gamma: float, b: np.ndarray, threads=1):
+    """(I - gamma J_i) x_i = b_i per 10x10 block; returns (0 or 1 + first singular block, x)."""
     J = np.ascontiguousarray(J, dtype=np.float64).reshape(-1)
     b = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
     x = np.zeros_like(b)
-    bad = lib().orc_block_newton_solve(C.c_long(b.size // 10), _ptr(J), C.c_double(gamma),
-                                       _ptr(b), _ptr(x))
-    return int(bad), x
+    n = b.size // 10
+    L = lib()
+    nt = _threads(threads)
+
+    def part(r):
+        a, e = r
+        bad = L.orc_block_newton_solve(C.c_long(e - a), _ptr(J[100 * a:100 * e]),
+                                       C.c_double(gamma), _ptr(b[10 * a:10 * e]),
+                                       _ptr(x[10 * a:10 * e]))
+        return a + bad if bad else 0
+    if nt == 1:
+        return int(part((0, n))), x
+    with cf.ThreadPoolExecutor(nt) as ex:
+        bads = [v for v in ex.map(part, _chunks(n, 4 * nt)) if v]
+    return (int(min(bads)) if bads else 0), x
+
+
+def fused_chem_hydro_step(fields, scale, chem, bc, gamma, energy_units, time_units,
+                          newton_gamma, threads=1):
+    """One fused chemistry-hydrodynamics stage over the oracle, the composition an IMEX /
+    multirate stage calls (and the GPU's fused-step benchmark times):
+      fexpl  (src/imex_chem_hydro_main.cpp:910-1000): physical chemistry = w5 * scale,
+             et = ge / EnergyUnits + |m|^2 / (2 rho) written into the state, fEuler of all
+             fields, the et tendency moved to the gas-energy slot (et tendency 0), w5 <-
+             physical / scale (the reference's in-place scale / unscale round trip);
+      fimpl  (:811-848) f = TimeUnits * f_chem(w5) (temperature state carried in `chem`);
+      Jimpl  (:850-908) J = TimeUnits * df/dy, solved per block with I - newton_gamma J
+             (the BDMPIMV solver, :1075-1194): x = (I - newton_gamma J)^{-1} f.
+    `fields`: the six state arrays (modified in place: et and the chemistry round trip, as the
+    GPU's FP64 form modifies them); `chem`: a Chem over `scale`.  Returns (status, [wdot_0..4,
+    wdot_5, f, x]) with wdot_5 the chemistry tendency of the physical densities."""
+    w = fields
+    phys = w[5] * scale
+    w[4][...] = phys[..., 9] * (1.0 / energy_units) + 0.5 / w[0] * (
+        w[1] * w[1] + w[2] * w[2] + w[3] * w[3])
+    st, out = feuler(list(w[:5]) + [phys], 10, bc, gamma, None, threads=threads)
+    if st != 0:
+        return st, None
+    out[5][..., 9] = out[4]
+    out[4][...] = 0.0
+    w[5][...] = phys / scale
+    y = w[5].reshape(-1)
+    f = chem.rhs(y, threads) * time_units
+    J = chem.jac(y, threads) * time_units
+    bad, x = block_newton_solve(J, newton_gamma, f, threads)
+    if bad:
+        return 1, None
+    return 0, out + [f, x]
 
 
 class ImexChemHydro:
