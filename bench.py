@@ -576,37 +576,51 @@ def run_gbmv(args):
             r["fs"] = None
         fs = None
         torch.cuda.empty_cache()
-        line["weno_rhs"] = run_weno(torch, gbmv, [int(x) for x in args.weno_n.split(",") if x],
+        line["weno_rhs"] = _guarded(run_weno, torch, gbmv,
+                                    [int(x) for x in args.weno_n.split(",") if x],
                                     parity=not args.no_parity)
     if not args.no_sod:
-        line["sod"] = run_sod(torch, gbmv, not args.no_cpu_baseline)
+        line["sod"] = _guarded(run_sod, torch, gbmv, not args.no_cpu_baseline)
     if args.mri_n > 0:
         for r in res.values():
             r["fs"] = None
         fs = None
         torch.cuda.empty_cache()
-        line["multirate"] = run_mri(torch, gbmv, args.mri_n)
+        line["multirate"] = _guarded(run_mri, torch, gbmv, args.mri_n)
     if args.imex_n > 0:
         for r in res.values():
             r["fs"] = None
         fs = None
         torch.cuda.empty_cache()
-        line["imex"] = run_imex(torch, gbmv, args.imex_n, args.imex_tf, not args.no_cpu_baseline)
+        line["imex"] = _guarded(run_imex, torch, gbmv, args.imex_n, args.imex_tf,
+                                not args.no_cpu_baseline)
     if args.ad_n > 0:
         for r in res.values():
             r["fs"] = None
         fs = None
         torch.cuda.empty_cache()
-        line["differentiation"] = run_ad(torch, gbmv, args.ad_n)
+        line["differentiation"] = _guarded(run_ad, torch, gbmv, args.ad_n)
     if args.dirk_n > 0:
         for k in ("fs",):
             for r in res.values():
                 r[k] = None
         fs = None
         torch.cuda.empty_cache()
-        line["chem_dirk"] = run_dirk(torch, gbmv, args.dirk_n, not args.no_cpu_baseline,
-                                     args.dirk_form)
+        line["chem_dirk"] = _guarded(run_dirk, torch, gbmv, args.dirk_n,
+                                     not args.no_cpu_baseline, args.dirk_form)
     print(json.dumps(line))
+
+
+def _guarded(fn, torch, *a, **kw):
+    """A secondary measurement: its failure is recorded in the line instead of losing it."""
+    try:
+        return fn(torch, *a, **kw)
+    except Exception as e:  # noqa: BLE001 (reported, not hidden)
+        import traceback
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return {"error": f"{type(e).__name__}: {e}",
+                "where": traceback.format_exc().strip().splitlines()[-3:]}
 
 
 # ----------------------------------------------------------------- whole-grid parity
@@ -733,11 +747,14 @@ def run_weno(torch, gbmv, grids, steps=3, warmup=2, parity=True):
 
 # ----------------------------------------------------------------- Sod whole run
 
+SOD_TABLE = 3  # ARKODE's default order-4 ERK (input_sod.txt: order = 4)
+
+
 def run_sod(torch, gbmv, with_cpu):
     """Sod shock tube 128x3x3 (reflecting x, periodic y,z, gamma 1.4) to t_f = 0.2 with the
-    adaptive Dormand-Prince ERK (rtol 1e-6, atol 1e-11) over the GPU FP64 RHS: time to t_f,
-    steps, L1 error of density against the exact Riemann solution; the oracle-driven run on
-    one host core beside it."""
+    adaptive ERK of the Sod inputs (order 4: ARKODE's Zonneveld 5-3-4, PID controller; rtol
+    1e-6, atol 1e-11) over the GPU FP64 RHS: time to t_f, steps, L1 error of density against
+    the exact Riemann solution; the oracle-driven run on one host core beside it."""
     import integrate as I
     import workloads as W
     nx = 128
@@ -757,7 +774,8 @@ def run_sod(torch, gbmv, with_cpu):
     y0 = np.stack([f.reshape(-1) for f in wl["fields"]])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    yg, st = I.erk_evolve(rhs_gpu, 0.0, 0.2, torch.from_numpy(y0).cuda(), 1e-6, 1e-11)
+    yg, st = I.erk_evolve(rhs_gpu, 0.0, 0.2, torch.from_numpy(y0).cuda(), 1e-6, 1e-11,
+                          table=SOD_TABLE)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     yg = yg.cpu().numpy()
@@ -765,7 +783,7 @@ def run_sod(torch, gbmv, with_cpu):
     r, _, _ = I.sod_exact(x, 0.2)
     rho = yg[0].reshape(shape)[1, 1]
     out = {"workload": "Sod 128x3x3, reflecting x / periodic y,z, gamma 1.4, t_f 0.2, "
-                       "adaptive DP5(4) rtol 1e-6 atol 1e-11, FP64 RHS",
+                       "adaptive Zonneveld 4(3) (order 4) rtol 1e-6 atol 1e-11, FP64 RHS",
            "s_to_tf": round(dt, 3), "steps": st.steps, "rhs_evals": st.nfe,
            "l1_density_err_vs_exact": float(f"{np.mean(np.abs(rho - r)):.3e}")}
     if with_cpu:
@@ -778,7 +796,7 @@ def run_sod(torch, gbmv, with_cpu):
             return np.stack([a.reshape(-1) for a in o])
 
         t0 = time.perf_counter()
-        yc, stc = I.erk_evolve(rhs_cpu, 0.0, 0.2, y0, 1e-6, 1e-11)
+        yc, stc = I.erk_evolve(rhs_cpu, 0.0, 0.2, y0, 1e-6, 1e-11, table=SOD_TABLE)
         dtc = time.perf_counter() - t0
         # max-normalised per field; fields that stay zero (the y, z momenta here) give 0
         diff = max(float(np.max(np.abs(yg[v] - yc[v]))) /
@@ -791,7 +809,7 @@ def run_sod(torch, gbmv, with_cpu):
 # ----------------------------------------------------------------- multirate time-to-t_f
 
 MRI_H, MRI_STEPS = 2e-6, 2   # slow step (code time units) and slow steps to t_f
-MRI_FAST = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01)
+MRI_FAST = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, table=112)
 
 
 def run_mri(torch, gbmv, n):
@@ -854,7 +872,8 @@ def run_mri(torch, gbmv, n):
 
 
 IMEX_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bias=2.0,
-                 growth=2.0)
+                 growth=2.0, adapt_method=2)  # the reference's primordial IMEX inputs
+IMEX_PAIR = (13, 112)  # ARK4(3)7L[2]SA: etable 13, itable 112 of those inputs
 
 
 def run_imex(torch, gbmv, n, tf, with_cpu):
@@ -871,9 +890,13 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
     wl = W.chem_hydro(n=n)
     eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
     tables = h5tables.load_table_block(TABLES)
-    out = {"workload": (f"chem_hydro {n}^3 x 15 to t_f = {tf} x 1e11 s, ARK3(2)4L[2]SA IMEX "
-                        "(WENO explicit, chemistry implicit), rtol 1e-6 atol 1e-10, maxcor 10, "
-                        "nlscoef 0.01, I controller safety 0.99 bias 2 growth 2"), "forms": {}}
+    table = integrate.ark_table(*IMEX_PAIR)
+    opts = dict(IMEX_OPTS, table=table)
+    out = {"workload": (f"chem_hydro {n}^3 x 15 to t_f = {tf} x 1e11 s, ARK4(3)7L[2]SA IMEX "
+                        "(etable 13 / itable 112; WENO explicit, chemistry implicit), rtol 1e-6 "
+                        "atol 1e-10, maxcor 10, nlscoef 0.01, I controller safety 0.99 bias 2 "
+                        "growth 2; fexpl chemistry tendency added unconverted, as the reference"),
+           "forms": {}}
     finals = {}
     # fp64 / mixed_fast: ARKODE's modified Newton over fimpl, Jimpl and the block LU;
     # mixed_fast_fused: full Newton stage corrections from the fused per-cell kernel (FP64
@@ -887,12 +910,12 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
         prob = integrate.ChemHydroImex(gbmv, hy, c, eu, tu, IMEX_OPTS["rtol"], IMEX_OPTS["atol"],
                                        prec, fused_newton=fused)
         wc = [x.clone() for x in w]  # warm-up on a copy (allocations)
-        integrate.ark_imex_evolve(prob, 0.0, tf * 1e-17, wc, **IMEX_OPTS)  # a few steps
+        integrate.ark_imex_evolve(prob, 0.0, tf * 1e-17, wc, **opts)  # a few steps
         c.state("Ts").fill_(1000.0)
         del wc
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st = integrate.ark_imex_evolve(prob, 0.0, tf, w, **IMEX_OPTS)
+        st = integrate.ark_imex_evolve(prob, 0.0, tf, w, **opts)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         finals[name] = [x.cpu().numpy() for x in w]
@@ -919,7 +942,7 @@ def run_imex(torch, gbmv, n, tf, with_cpu):
         prob = O.ImexChemHydro(sw, tables, sw["units"]["EnergyUnits"],
                                sw["units"]["TimeUnits"], IMEX_OPTS["rtol"], IMEX_OPTS["atol"])
         t0 = time.perf_counter()
-        st = integrate.ark_imex_evolve(prob, 0.0, tf, y, **IMEX_OPTS)
+        st = integrate.ark_imex_evolve(prob, 0.0, tf, y, **opts)
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"Mcell_steps_per_s": round(240 * st.steps / dt / 1e6, 6),
                                "s_to_tf": round(dt, 3), "steps": st.steps, "cores": 1,
@@ -1029,6 +1052,7 @@ def run_ad(torch, gbmv, n, ndir=16, h=1e-7, nsteps=50, every=10):
 
 DIRK_TOUT = 1e-3      # code time units (TimeUnits = 1e11 s): 1e8 s of chemistry
 DIRK_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01)  # Newton settings of the inputs
+DIRK_TABLE = 112  # ARK4(3)7L[2]SA, the `itable` of the reference's chemistry inputs
 
 
 def _dirk_summary(st):
@@ -1058,9 +1082,10 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
     scale = torch.from_numpy(y.reshape(-1).copy()).cuda()
     out = {"workload": (f"static primordial chemistry {n1}^3: uniform rho = 1e2 m_H, log-uniform "
                         "mass fractions in [1e-10, 1], log-uniform T in [10, 1e4] K; per-cell "
-                        "adaptive TR-BDF2 ESDIRK + modified Newton, rtol 1e-6, atol 1e-10, "
-                        f"maxcor 10, nlscoef 0.01, t in [0, {DIRK_TOUT}] x 1e11 s"),
-           "cells": n, "tout": DIRK_TOUT, "forms": {}}
+                        "adaptive ARK4(3)7L[2]SA ESDIRK (the inputs' itable 112) + modified "
+                        "Newton, rtol 1e-6, atol 1e-10, maxcor 10, nlscoef 0.01, "
+                        f"t in [0, {DIRK_TOUT}] x 1e11 s"),
+           "cells": n, "tout": DIRK_TOUT, "table": DIRK_TABLE, "forms": {}}
     finals = {}
     for name, prec in (("fp64", gbmv.FP64), ("mixed", gbmv.MIXED)):
         if forms not in ("both", name):
@@ -1071,7 +1096,7 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
         st = torch.zeros(8 * n, dtype=torch.int32, device="cuda")
         # warm-up call over the full interval: the block-size autotuner times its candidates
         # on this call's work, which must be representative of the timed one
-        c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, precision=prec, **DIRK_OPTS)
+        c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, precision=prec, table=DIRK_TABLE, **DIRK_OPTS)
         z.fill_(1.0)
         c.state("Ts").fill_(1000.0)
         torch.cuda.synchronize()
@@ -1079,7 +1104,8 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with ClockSampler(0) as clk:
             e0.record(s)
-            nf = c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, stats=st, precision=prec, **DIRK_OPTS)
+            nf = c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, stats=st, precision=prec,
+                               table=DIRK_TABLE, **DIRK_OPTS)
             e1.record(s)
             torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -1099,13 +1125,36 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
                                        "max": float(f"{e.max():.3e}")}
         out["speedup_mixed_vs_fp64"] = round(out["forms"]["fp64"]["ms"] /
                                              out["forms"]["mixed"]["ms"], 3)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as O
+    # both forms against a tight-tolerance FP64 solution (the oracle at rtol 1e-10) on a sample
+    # of cells: the error each form makes, and where the two forms part
+    ns_t = 512
+    t0 = time.perf_counter()
+    oc = O.Chem(tables, y[:ns_t].reshape(-1))
+    zt, _, nft = oc.dirk_evolve(np.ones(10 * ns_t), 0.0, DIRK_TOUT, 1e11, rtol=1e-10,
+                                atol=1e-14, maxcor=10, nlscoef=0.01, max_steps=500000,
+                                table=DIRK_TABLE)
+    zt = zt.reshape(ns_t, 10)
+    floor = DIRK_OPTS["atol"] / DIRK_OPTS["rtol"]
+    tight = {"sample": f"the first {ns_t} cells", "reference": "oracle FP64 at rtol 1e-10, "
+             "atol 1e-14", "reference_failed_cells": int(nft),
+             "oracle_s": round(time.perf_counter() - t0, 2)}
+    for name, z in finals.items():
+        e = (np.abs(z[:ns_t] - zt) / (np.abs(zt) + floor)).max(axis=1)
+        tight[f"{name}_relerr"] = {"median": float(f"{np.median(e):.3e}"),
+                                   "p99": float(f"{np.percentile(e, 99):.3e}"),
+                                   "max": float(f"{e.max():.3e}")}
+    if len(finals) == 2:
+        d = (np.abs(finals["mixed"][:ns_t] - finals["fp64"][:ns_t]) /
+             (np.abs(finals["fp64"][:ns_t]) + floor)).max(axis=1)
+        tight["mixed_vs_fp64_relerr_max"] = float(f"{d.max():.3e}")
+    out["vs_tight_tolerance_solution"] = tight
     if with_cpu:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle_py as O
         ns = 256
         oc = O.Chem(tables, y[:ns].reshape(-1))
         t0 = time.perf_counter()
-        oc.dirk_evolve(np.ones(10 * ns), 0.0, DIRK_TOUT, 1e11, **DIRK_OPTS)
+        oc.dirk_evolve(np.ones(10 * ns), 0.0, DIRK_TOUT, 1e11, table=DIRK_TABLE, **DIRK_OPTS)
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": round(ns / dt / 1e6, 6), "unit": "Mcells/s", "cores": 1,
                                "kind": "port",

@@ -264,6 +264,10 @@ typedef struct {
                         > 0 keeps an FP64 copy of the matrix (default 0: each Newton
                         iteration already refines against the FP64 nonlinear residual) */
   int block;         /* threads per block: 32, 64 or 128; 0 = autotuned (default 0) */
+  int table;         /* ARKODE DIRK table number (the `itable` input option): 112
+                        ARK437L2SA_DIRK_7_3_4 (the reference's chemistry inputs, default) or 102
+                        TRBDF2_3_3_2; any stiffly accurate ESDIRK of gbmv_butcher_table with an
+                        explicit first stage and one diagonal value is accepted */
 } gbmv_dirk_opts;
 
 /* Fill *o with the defaults above (rtol 1e-6, atol 1e-10). */
@@ -373,6 +377,37 @@ int gbmv_fexpl_async(gbmv_hydro h, gbmv_chem c, double t, double* const* w,
 /* PostprocessStep (src/imex_chem_hydro_main.cpp:1002-1051): et from ge and momenta. */
 int gbmv_postprocess_step(gbmv_hydro h, gbmv_chem c, double* const* w, double energy_units,
                           void* stream);
+
+/* ------------------------------------------------------------ Butcher tables */
+
+/* The Runge-Kutta tables the reference's input files select, by ARKODE table number (the
+ * `etable` / `itable` options of src/euler3D.hpp:126-172, given to ARKStepSetTableNum in
+ * src/euler3D_main.cpp:209-213, src/imex_chem_hydro_main.cpp:386 and
+ * src/multirate_chem_hydro_main.cpp:447), with the published coefficients:
+ *   explicit: 0 HEUN_EULER_2_1_2, 1 BOGACKI_SHAMPINE_4_2_3, 2 ARK324L2SA_ERK_4_2_3,
+ *             3 ZONNEVELD_5_3_4, 6 CASH_KARP_6_4_5, 8 DORMAND_PRINCE_7_4_5,
+ *             13 ARK437L2SA_ERK_7_3_4;
+ *   implicit: 102 TRBDF2_3_3_2, 104 ARK324L2SA_DIRK_4_2_3, 112 ARK437L2SA_DIRK_7_3_4.
+ * (2, 104) and (13, 112) are additive IMEX pairs (shared c and b).  Host-only: no device work. */
+#define GBMV_MAX_STAGES 7
+typedef struct {
+  int id;
+  int stages;   /* s */
+  int q;        /* method order */
+  int p;        /* embedding order */
+  double c[GBMV_MAX_STAGES];
+  double A[GBMV_MAX_STAGES][GBMV_MAX_STAGES]; /* row-major, diagonal included */
+  double b[GBMV_MAX_STAGES];
+  double bhat[GBMV_MAX_STAGES];
+  char name[32];
+} gbmv_butcher;
+
+/* Fill *out with table `id`; returns 0 or GBMV_EUNSUPPORTED (with a message). */
+int gbmv_butcher_table(int id, gbmv_butcher* out);
+
+/* ARKODE's default explicit table for an `order` (ARKStepSetOrder, the `order` input option,
+ * src/euler3D_main.cpp:207-209): 2 -> 0, 3 -> 1, 4 -> 3, 5 -> 6; -1 for other orders. */
+int gbmv_erk_default_table(int order);
 
 /* ----------------------------------------------------------------- utilities */
 

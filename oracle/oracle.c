@@ -648,11 +648,17 @@ long orc_block_newton_solve(long n, const double* J, double gamma, const double*
  * restatement applies ARKODE's Newton and step rules per cell (see oracle.h), except that no
  * Jacobian is kept between Newton-matrix setups (each setup evaluates J at the step's state)
  * and the WRMS weights are rounded to float, as the GPU kernel stores them.
- * TR-BDF2 ESDIRK pair: A = [[0,0,0],[gd,gd,0],[w,w,gd]], b = (w,w,gd),
- * bhat = ((1-w)/3, (3w+1)/3, gd/3) (Hosea & Shampine 1996). */
-#define DK_SQRT2 1.4142135623730951
-static const double dk_gd = (2.0 - DK_SQRT2) / 2.0;
-static const double dk_w = DK_SQRT2 / 4.0;
+ * The method is the stiffly accurate ESDIRK given in O (ARK4(3)7L[2]SA's implicit part, the
+ * reference inputs' itable 112, or TR-BDF2, itable 102): stage i of s solves
+ * z_i = y + h sum_{j<i} a_ij K_j + h gamma F(z_i) from the previous stage's value, y_{n+1} =
+ * z_s, and h sum_j e_j K_j (e = b - bhat) is the embedded error estimate of order p. */
+
+/* safety dsm^(-1/p) */
+static double dk_eta(double safety, double dsm, int p) {
+  if (p == 3) return safety / cbrt(dsm);
+  if (p == 2) return safety / sqrt(dsm);
+  return safety * pow(dsm, -1.0 / p);
+}
 
 static void dirk_F(const orc_chem* c, const double* X, const double* sc, const double* isc,
                    double md, double imd, double cie, double h2, const orc_dirk_opts* O,
@@ -690,14 +696,13 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
                           const double* inv_scale, const double* mdens, const double* imdens,
                           const double* cie_oda, const double* h2_oda, double* Ts, double* dTs_ge,
                           const orc_dirk_opts* O, int* stats) {
-  const double e1 = dk_w - (1.0 - dk_w) / 3.0, e2 = dk_w - (3.0 * dk_w + 1.0) / 3.0,
-               e3 = dk_gd - dk_gd / 3.0;
+  const int ns = O->s;
   long nfail = 0;
   for (long i = 0; i < n; ++i) {
     const long j = i * 10;
     const double *sc = scale + j, *isc = inv_scale + j;
     const double md = mdens[i], imd = imdens[i], cie = cie_oda[i], h2 = h2_oda[i];
-    double Y[10], K1[10], K2[10], Z[10], EW[10], f[10], A[100];
+    double Y[10], K1[10], KS[7][10], Z[10], EW[10], f[10], A[100];
     int piv[10];
     for (int s = 0; s < 10; ++s) Y[s] = y[j + s];
     double Tsc = Ts[i], dTsc = dTs_ge[i], Tsy, dTsy;
@@ -730,7 +735,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
           EW[s] = (double)(float)(1.0 / (O->rtol * fabs(Y[s]) + O->atol)); /* float weights */
           Z[s] = Y[s];
         }
-        const double gam = h * dk_gd;
+        const double gam = h * O->gamma;
         if (force_setup || nst >= nst_lp + O->msbp || !(fabs(gam / gp - 1.0) <= O->dgmax)) {
           /* no Jacobian is kept between setups: J at (Y, Ts(Y)) for every Newton matrix */
           double B[100];
@@ -758,20 +763,30 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
         break;
       }
       if (failed) break;
-      /* stages 2 and 3 by modified Newton */
+      /* implicit stages 1 .. s-1 by modified Newton */
       int conv = 1;
-      for (int stage = 2; stage <= 3 && conv; ++stage) {
-        const double gam = h * dk_gd, hw = h * dk_w;
-        const double tst = (stage == 2) ? t + (2.0 * dk_gd) * h : t + h;  /* c = (0, 2gd, 1) */
+      double tst = t;
+      for (int st = 1; st < ns && conv; ++st) {
+        const double gam = h * O->gamma;
+        double Bv[10];
+        const double c0 = h * O->a[st][0];
+        for (int s = 0; s < 10; ++s) {
+          Bv[s] = Y[s];
+          if (c0 != 0.0) Bv[s] += c0 * K1[s];
+        }
+        for (int q = 1; q < st; ++q) {
+          const double cq = h * O->a[st][q];
+          if (cq == 0.0) continue;
+          for (int s = 0; s < 10; ++s) Bv[s] += cq * KS[q][s];
+        }
+        tst = t + O->c[st] * h;
         int m = 0;
         conv = 0;
         for (;;) {
           dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, f);
           ++nfe;
           double dl[10];
-          for (int s = 0; s < 10; ++s)
-            dl[s] = (stage == 2) ? (Y[s] + gam * K1[s]) + gam * f[s] - Z[s]
-                                 : (Y[s] + hw * (K1[s] + K2[s])) + gam * f[s] - Z[s];
+          for (int s = 0; s < 10; ++s) dl[s] = Bv[s] + gam * f[s] - Z[s];
           lus10(A, piv, dl);
           if (gam != gp) {
             const double scl = 2.0 / (1.0 + gam / gp);
@@ -786,8 +801,8 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
           if ((m > 1 && del > 2.3 * delp) || m >= O->maxcor || !(del == del)) break;
           delp = del;
         }
-        if (conv && stage == 2) {
-          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, K2);
+        if (conv && st < ns - 1) {
+          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, KS[st]);
           ++nfe;
         }
       }
@@ -799,10 +814,15 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
         else force_setup = 1;
         continue;
       }
-      dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, t + h, &Tsc, &dTsc, f);
+      dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, f);
       ++nfe;
       double err[10];
-      for (int s = 0; s < 10; ++s) err[s] = h * ((e1 * K1[s] + e2 * K2[s]) + e3 * f[s]);
+      for (int s = 0; s < 10; ++s) {
+        double acc = O->e[0] * K1[s];
+        for (int q = 1; q < ns - 1; ++q)
+          if (O->e[q] != 0.0) acc += O->e[q] * KS[q][s];
+        err[s] = h * (acc + O->e[ns - 1] * f[s]);
+      }
       const double dsm = dk_wrms(err, EW);
       if (dsm <= 1.0) {
         ++nst;
@@ -814,7 +834,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
         Tsy = Tsc;
         dTsy = dTsc;
         jcur = 0;
-        double eta = (dsm > 0.0) ? O->safety / cbrt(dsm) : 1.0e300;
+        double eta = (dsm > 0.0) ? dk_eta(O->safety, dsm, O->p) : 1.0e300;
         eta = fmin(eta, nst == 1 ? O->etamx1 : O->growth);
         if (nef_s > 0 || ncf_s > 0) eta = fmin(eta, 1.0);
         h *= eta;
@@ -826,7 +846,7 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
         ++nef_s;
         ++netf;
         if (nef_s >= O->maxnef) { failed = 1; break; }
-        double eta = fmax(0.1, O->safety / cbrt(dsm));
+        double eta = fmax(0.1, dk_eta(O->safety, dsm, O->p));
         if (nef_s >= 2) eta = fmin(eta, 0.3);
         h *= eta;
       }

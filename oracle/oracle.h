@@ -95,9 +95,17 @@ typedef struct {
   int nforcing;
   double tshift, tscale;
   const double* fz[8];
+  /* the stiffly accurate ESDIRK: s stages, explicit first stage, diagonal gamma, stage i
+   * solves z_i = y + h sum_{j<i} a[i][j] K_j + h gamma F(z_i); e = b - bhat, embedding
+   * order p */
+  int s, p;
+  double gamma;
+  double c[7];
+  double a[7][7];
+  double e[7];
 } orc_dirk_opts;
 
-/* Per-cell adaptive TR-BDF2 ESDIRK integration of dz/dt = tunit * f_chem(z) (scaled
+/* Per-cell adaptive ESDIRK integration (the table in O) of dz/dt = tunit * f_chem(z) (scaled
  * variables, as orc_chem_rhs x tunit) from t0 to tout, modified Newton with ARKODE's
  * convergence, reuse and step rules (a fresh J at every Newton-matrix setup), FP64 LU; the algorithm of the GPU integrator
  * (gbmv_chem_dirk_evolve).  y, Ts, dTs_ge updated in place; stats (8 ints per cell, or NULL):

@@ -52,7 +52,54 @@ class OrcDirkOpts(C.Structure):
                                           "hmax")] + \
                [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf",
                                        "nforcing")] + \
-               [("tshift", C.c_double), ("tscale", C.c_double), ("fz", _P * 8)]
+               [("tshift", C.c_double), ("tscale", C.c_double), ("fz", _P * 8),
+                ("s", C.c_int), ("p", C.c_int), ("gamma", C.c_double), ("c", C.c_double * 7),
+                ("a", (C.c_double * 7) * 7), ("e", C.c_double * 7)]
+
+
+def _q(a, b):
+    return float(a) / float(b)
+
+
+def _dirk_tables():
+    """The oracle's own copy of the two stiffly accurate ESDIRKs, by ARKODE table number, from
+    the published coefficients (each rational as the double quotient of its integers):
+    112 ARK4(3)7L[2]SA implicit part (Kennedy & Carpenter, Appl. Numer. Math. 136 (2019)
+    183-205), 102 TR-BDF2 (Hosea & Shampine, Appl. Numer. Math. 20 (1996) 21-37).
+    Returned as dicts of s, p, A (rows incl. the diagonal), c, b, bhat."""
+    g = _q(1235, 10000)
+    b = [0.0, 0.0, _q(9164257142617, 17756377923965), _q(-10812980402763, 74029279521829),
+         _q(1335994250573, 5691609445217), _q(2273837961795, 8368240463276), _q(247, 2000)]
+    A = [[0.0] * 7 for _ in range(7)]
+    for i in range(1, 7):
+        A[i][i] = g
+    A[1][0] = g
+    A[2][0] = A[2][1] = _q(624185399699, 4186980696204)
+    A[3][0] = A[3][1] = _q(1258591069120, 10082082980243)
+    A[3][2] = _q(-322722984531, 8455138723562)
+    A[4][0] = A[4][1] = _q(-436103496990, 5971407786587)
+    A[4][2] = _q(-2689175662187, 11046760208243)
+    A[4][3] = _q(4431412449334, 12995360898505)
+    A[5][0] = A[5][1] = _q(-2207373168298, 14430576638973)
+    A[5][2] = _q(242511121179, 3358618340039)
+    A[5][3] = _q(3145666661981, 7780404714551)
+    A[5][4] = _q(5882073923981, 14490790706663)
+    A[6][:6] = b[:6]
+    ark437 = dict(s=7, p=3, A=A, b=b,
+                  c=[0.0, _q(247, 1000), _q(4276536705230, 10142255878289), _q(67, 200),
+                     _q(3, 40), _q(7, 10), 1.0],
+                  bhat=[0.0, 0.0, _q(4469248916618, 8635866897933),
+                        _q(-621260224600, 4094290005349), _q(696572312987, 2942599194819),
+                        _q(1532940081127, 5565293938103), _q(2441, 20000)])
+    rt2 = 1.4142135623730951
+    gd, w = (2.0 - rt2) / 2.0, rt2 / 4.0
+    trbdf2 = dict(s=3, p=3, A=[[0.0, 0.0, 0.0], [gd, gd, 0.0], [w, w, gd]], b=[w, w, gd],
+                  c=[0.0, 2.0 - rt2, 1.0],
+                  bhat=[(1.0 - w) / 3.0, (3.0 * w + 1.0) / 3.0, gd / 3.0])
+    return {112: ark437, 102: trbdf2}
+
+
+DIRK_TABLES = _dirk_tables()
 
 
 # defaults of gbmv_dirk_opts_default (include/gbmv.h)
@@ -192,12 +239,20 @@ class Chem:
         return J.reshape(self.n, 10, 10)  # [cell][col][row]
 
     def dirk_evolve(self, y: np.ndarray, t0: float, tout: float, tunit: float, forcing=(),
-                    tshift=0.0, tscale=1.0, **opts):
-        """Per-cell adaptive TR-BDF2 integration from t0 to tout (orc_chem_dirk_evolve), with
-        the MRI forcing sum_i tau^i forcing[i] (chemistry components) added to the RHS.
+                    tshift=0.0, tscale=1.0, table=112, **opts):
+        """Per-cell adaptive ESDIRK integration from t0 to tout (orc_chem_dirk_evolve) with the
+        table of ARKODE number `table` (112 ARK4(3)7L[2]SA, 102 TR-BDF2), with the MRI forcing
+        sum_i tau^i forcing[i] (chemistry components) added to the RHS.
         Returns (y(tout), stats[n, 8], number of failed cells); Ts / dTs_ge carried."""
         o = dict(DIRK_DEFAULTS, **opts)
         O = OrcDirkOpts()
+        T = DIRK_TABLES[table]
+        O.s, O.p, O.gamma = T["s"], T["p"], T["A"][1][1]
+        for i in range(T["s"]):
+            O.c[i] = T["c"][i]
+            O.e[i] = T["b"][i] - T["bhat"][i]
+            for j in range(T["s"]):
+                O.a[i][j] = T["A"][i][j]
         O.t0, O.tout, O.tunit = t0, tout, tunit
         keep = [np.ascontiguousarray(f, dtype=np.float64).reshape(-1) for f in forcing]
         O.nforcing, O.tshift, O.tscale = len(keep), tshift, tscale
@@ -276,12 +331,14 @@ class ImexChemHydro:
     fexpl (:910-1000: et from the physical gas energy, fEuler on the physical chemistry, the et
     tendency moved to the gas-energy slot, the in-place scale / unscale round trip of the
     chemistry component), its chemistry tendency converted to the scaled variables (species
-    / scale, gas energy x EnergyUnits / scale); fimpl (:811-848, TimeUnits x the source);
+    / scale, gas energy x EnergyUnits / scale) when forcing_units is "scaled", unconverted as
+    the reference adds it when "reference"; fimpl (:811-848, TimeUnits x the source);
     Jimpl (:850-908, TimeUnits x J) with I - gamma J solved per block by orc_block_newton_solve
     (the BDMPIMV solver, :1075-1194); PostprocessStep (:1002-1051); WRMS norms with weights
     1 / (rtol |y| + atol).  `wl` holds bc, gamma and the per-entry scale."""
 
-    def __init__(self, wl, tables, eu, tu, rtol, atol):
+    def __init__(self, wl, tables, eu, tu, rtol, atol, forcing_units="reference"):
+        self.forcing_units = forcing_units
         self.wl, self.eu, self.tu = wl, eu, tu
         self.rtol, self.atol = rtol, atol
         self.scale = wl["scale"]
@@ -303,8 +360,9 @@ class ImexChemHydro:
         out[5][..., 9] = out[4]
         out[4][:] = 0.0
         y[5][...] = phys / self.scale
-        out[5][..., :9] = out[5][..., :9] * self.inv[..., :9]
-        out[5][..., 9] = out[5][..., 9] * (self.inv[..., 9] * self.eu)
+        if self.forcing_units == "scaled":
+            out[5][..., :9] = out[5][..., :9] * self.inv[..., :9]
+            out[5][..., 9] = out[5][..., 9] * (self.inv[..., 9] * self.eu)
         return out
 
     def fi(self, t, y):

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "butcher.cuh"
 #include "chem.cuh"
 #include "weno.cuh"
 
@@ -92,6 +93,8 @@ struct gbmv_chem_s {
   int* d_nfail = nullptr;              //   [0] info, [1] failed cells,
   unsigned long long* d_next = nullptr;  //   [16] DIRK work counter
   int dirk_block[2] = {0, 0};          // autotuned block size per precision (0 = not yet)
+  double* dirk_k = nullptr;            // DIRK stage store (first DIRK call), dirk_k_lanes lanes
+  long dirk_k_lanes = 0;
   int newton_bps = 0;                  // fused Newton: resident blocks per SM (0 = default)
 };
 
@@ -379,6 +382,7 @@ int gbmv_chem_destroy(gbmv_chem c) {
   cudaFree(c->tab);
   cudaFree(c->cell);
   cudaFree(c->d_info);
+  cudaFree(c->dirk_k);
   delete c;
   return GBMV_OK;
 }
@@ -509,6 +513,57 @@ void gbmv_dirk_opts_default(gbmv_dirk_opts* o) {
   o->precision = GBMV_FP64;
   o->refine = 0;
   o->block = 0;
+  o->table = 0;
+}
+
+// The DIRK table of the options (0: ARK437L2SA_DIRK_7_3_4, the reference's chemistry inputs'
+// itable), checked to be a stiffly accurate ESDIRK with one diagonal value.
+static int dirk_table(int id, DirkTable* D) {
+  const int tid = id ? id : 112;
+  const ButcherTable* T = butcher_table(tid);
+  bool ok = T && T->s >= 2 && T->s <= kDirkMaxStages && T->A[0][0] == 0.0 && T->A[1][1] > 0.0;
+  for (int i = 1; ok && i < T->s; ++i) ok = T->A[i][i] == T->A[1][1];
+  for (int j = 0; ok && j < T->s; ++j) ok = T->b[j] == T->A[T->s - 1][j];
+  if (!ok) {
+    set_error("DIRK table %d is not a stiffly accurate ESDIRK of gbmv_butcher_table (use 112 "
+              "or 102)", tid);
+    return GBMV_EUNSUPPORTED;
+  }
+  memset(D, 0, sizeof *D);
+  D->s = T->s;
+  D->p = T->p;
+  D->gamma = T->A[1][1];
+  for (int i = 0; i < T->s; ++i) {
+    D->c[i] = T->c[i];
+    D->e[i] = T->b[i] - T->bhat[i];
+    for (int j = 0; j < T->s; ++j) D->a[i][j] = T->A[i][j];
+  }
+  return GBMV_OK;
+}
+
+
+// The stage store of the handle's DIRK (K_1 .. K_{s-2} of every lane), allocated at the first
+// call that needs it, for the most lanes any launch shape of the kernel runs.
+static int dirk_store(gbmv_chem c, DirkOpts* O, cudaStream_t s) {
+  if (O->T.s > 2 && !c->dirk_k) {
+    if (capturing(s)) {
+      set_error("the first DIRK call allocates its stage store: make it before any capture");
+      return GBMV_EINVAL;
+    }
+    const long lanes = chem_dirk_max_lanes();
+    if (lanes <= 0) return check_cuda(cudaGetLastError(), "DIRK occupancy query");
+    if (cudaMalloc(&c->dirk_k, sizeof(double) * 10 * (kDirkMaxStages - 2) * lanes) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      c->dirk_k = nullptr;
+      set_error("device allocation of the DIRK stage store (%ld lanes) failed", lanes);
+      return GBMV_ENOMEM;
+    }
+    c->dirk_k_lanes = lanes;
+  }
+  O->kstore = c->dirk_k;
+  O->kstore_lanes = c->dirk_k_lanes;
+  return GBMV_OK;
 }
 
 static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tunit, DirkOpts* O) {
@@ -547,7 +602,9 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
   O->tshift = 0.0;
   O->tscale = 1.0;
   for (int q = 0; q < 8; ++q) O->fz[q] = nullptr;
-  return GBMV_OK;
+  O->kstore = nullptr;
+  O->kstore_lanes = 0;
+  return dirk_table(o->table, &O->T);
 }
 
 static int ck(cudaError_t e, const char* where) {
@@ -616,6 +673,7 @@ static int dirk_launch(gbmv_chem c, double t0, double tout, double* y, double ti
   if (!c || !y || !d_nfail) { set_error("null argument"); return GBMV_EINVAL; }
   DirkOpts O;
   int rc = dirk_opts(opts, t0, tout, time_units, &O);
+  if (!rc) rc = dirk_store(c, &O, s);
   if (rc) return rc;
   const int mixed = opts->precision == GBMV_MIXED;
   int block = opts->block ? opts->block : c->dirk_block[mixed];
@@ -809,7 +867,9 @@ int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, doub
     return GBMV_EINVAL;
   }
   DirkOpts O;
+  cudaStream_t s = (cudaStream_t)stream;
   int rc = dirk_opts(opts, t0, tout, time_units, &O);
+  if (!rc) rc = dirk_store(c, &O, s);
   if (rc) return rc;
   ForcingSet Ff{};
   const double tau0 = nforcing > 0 ? (t0 - tshift) / tscale : 0.0;
@@ -828,7 +888,6 @@ int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, doub
   O.nforcing = nforcing;
   O.tshift = tshift;
   O.tscale = tscale;
-  cudaStream_t s = (cudaStream_t)stream;
   if (nforcing > 0) {
     DevFields6 D;
     for (int k = 0; k < 6; ++k) D.f[k] = w[k];

@@ -52,6 +52,18 @@ int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
                 cudaStream_t s, int blocks_per_sm = 0, const double* b = nullptr);
 
+// The stiffly accurate ESDIRK the persistent DIRK runs (explicit first stage, one diagonal
+// value gamma, b = last row of a): stage i of s solves z_i = y + h sum_{j<i} a_ij K_j
+// + h gamma F(z_i); e = b - bhat gives the embedded error estimate of order p.
+constexpr int kDirkMaxStages = 7;
+struct DirkTable {
+  int s, p;
+  double gamma;
+  double c[kDirkMaxStages];
+  double a[kDirkMaxStages][kDirkMaxStages];
+  double e[kDirkMaxStages];
+};
+
 // persistent per-cell DIRK integration from t0 to tout (chem_dirk.cu)
 struct DirkOpts {
   double t0, tout, tunit;
@@ -70,12 +82,20 @@ struct DirkOpts {
   int nforcing;
   double tshift, tscale;
   const double* fz[8];
+  DirkTable T;
+  // stage derivatives K_1 .. K_{s-2} of every lane (element-major [(j-1)*10 + species][lane]),
+  // kstore_lanes lanes; K_0 stays in shared memory
+  double* kstore;
+  long kstore_lanes;
 };
 constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
                                // matrix setups, Jacobians (= setups), F evaluations, failed
 int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,
               int lu_fp32, int block, unsigned long long* d_next, int* stats, int* d_nfail,
               cudaStream_t s);
+// Largest number of lanes (threads) any launch shape of chem_dirk runs on this device: the
+// stage store must hold kstore_lanes >= this many lanes.
+long chem_dirk_max_lanes();
 
 // batched 10x10 LU (blocklu.cu)
 int block_lu_factor(long nb, double* A, int* piv, int* d_info, cudaStream_t s);

@@ -6,16 +6,20 @@
 // src/primordial_ode_main.cpp, and the rank-local MRI inner stepper of
 // src/multirate_chem_hydro_main.cpp:1114-1224), carried to cell granularity.
 //
-// Method: TR-BDF2 written as an ESDIRK (explicit first stage, equal diagonal gd = 1 - 1/sqrt 2,
-// stiffly accurate, L-stable), its order-3 companion weights giving the embedded error
-// estimate (M. E. Hosea and L. F. Shampine, Appl. Numer. Math. 20 (1996) 21-37).  Each implicit
-// stage is solved by modified Newton with ARKODE's rules: Newton matrix A = I - gamma J reused
+// Method: a stiffly accurate ESDIRK from the table in DirkOpts (explicit first stage, one
+// diagonal value gamma, b = last row of a): ARK4(3)7L[2]SA's implicit part, the table the
+// reference's chemistry inputs select (`itable = 112`; C. A. Kennedy and M. H. Carpenter, Appl.
+// Numer. Math. 136 (2019) 183-205), or TR-BDF2 (`itable = 102`; M. E. Hosea and L. F. Shampine,
+// Appl. Numer. Math. 20 (1996) 21-37); the embedded weights give the error estimate.  Stage i
+// solves z_i = y + h sum_{j<i} a_ij K_j + h gamma F(z_i) from the previous stage's value.
+// Each implicit stage is solved by modified Newton with ARKODE's rules: Newton matrix A = I - gamma J reused
 // across steps (set up again when gamma moved by more than dgmax, after msbp steps, or after a
 // Newton failure with a matrix from an earlier step), correction scaled by
 // 2/(1 + gamma/gamma_p) when gamma differs from the factored one, WRMS convergence test with
 // rate estimate crate = max(0.3 crate, del/del_p), success when min(1, crate) del / nlscoef
 // <= 1, divergence when del > 2.3 del_p, at most maxcor iterations.  Step control: the error
-// estimate's WRMS norm dsm, eta = safety / cbrt(dsm) bounded by etamx1 on the first step,
+// estimate's WRMS norm dsm, eta = safety dsm^(-1/p) (p the embedding order) bounded by etamx1
+// on the first step,
 // growth after it, 1 right after a failure, and below by 0.1 (0.3 at most after repeated
 // error failures), h <= hmax; a Newton failure with a current J cuts the step by 0.25.
 // oracle/oracle.c (orc_chem_dirk_evolve) restates the same algorithm on the CPU.
@@ -41,16 +45,9 @@ namespace gbmv {
 
 namespace {
 
-// TR-BDF2 coefficients (ESDIRK form): A = [[0,0,0],[gd,gd,0],[w,w,gd]], b = (w, w, gd),
-// bhat = ((1-w)/3, (3w+1)/3, gd/3); e = b - bhat.
-constexpr double kSqrt2 = 1.4142135623730951;
-constexpr double kGd = (2.0 - kSqrt2) / 2.0;
-constexpr double kW = kSqrt2 / 4.0;
-constexpr double kE1 = kW - (1.0 - kW) / 3.0;
-constexpr double kE2 = kW - (3.0 * kW + 1.0) / 3.0;
-constexpr double kE3 = kGd - kGd / 3.0;
-
-enum : int { kPhK1 = 0, kPhNewton = 1, kPhK2 = 2, kPhK3 = 3 };
+// Lane state machine phases: F at the step start, a Newton iteration of the current stage,
+// F at a converged stage.
+enum : int { kPhK1 = 0, kPhNewton = 1, kPhStage = 2 };
 
 // F at a point given in the solver's scaled variables (strided shared-memory slice X) and
 // time tf: TimeUnits * f_chem plus the MRI forcing polynomial (ffast's order of summation).
@@ -107,10 +104,37 @@ __device__ __forceinline__ int eq_exponent(double x) {
   return max(-500, min(500, -ex));
 }
 
+// safety dsm^(-1/p): the step-size factor from the embedded error estimate of order p
+__device__ __forceinline__ double dirk_eta(double safety, double dsm, int p) {
+  return p == 3 ? safety / cbrt(dsm) : (p == 2 ? safety / sqrt(dsm)
+                                               : safety * pow(dsm, -1.0 / p));
+}
+
+// Base of stage i: B = Y + sum_{j<i} (h a_ij) K_j, K_0 from shared memory, K_1.. from the
+// stage store, terms added in j order (zero coefficients skipped, as the oracle does).
+template <int BS>
+__device__ __forceinline__ void dirk_stage_base(const DirkOpts& O, int i, double h,
+                                                const double* Y, const double* K1,
+                                                const double* KG, long kst, double* B) {
+  const double c0 = h * O.T.a[i][0];
+#pragma unroll
+  for (int s = 0; s < 10; ++s) {
+    double v = Y[s * BS];
+    if (c0 != 0.0) v += c0 * K1[s * BS];
+    B[s * BS] = v;
+  }
+  for (int j = 1; j < i; ++j) {
+    const double cj = h * O.T.a[i][j];
+    if (cj == 0.0) continue;
+#pragma unroll
+    for (int s = 0; s < 10; ++s) B[s * BS] += cj * KG[((j - 1) * 10 + s) * kst];
+  }
+}
+
 template <typename LU, bool REF, int BS>
 struct DirkLayout {
   // per-lane slices, element-major [element][BS]
-  static constexpr size_t kVec = 40 * sizeof(double);                   // Y, K1, K2, Z
+  static constexpr size_t kVec = 40 * sizeof(double);                   // Y, K1, B, Z
   static constexpr size_t kEw = 10 * sizeof(float);                     // weights
   static constexpr size_t kL = 100 * sizeof(LU);                        // factor
   static constexpr size_t kA = REF ? 100 * sizeof(double) : 0;          // FP64 matrix
@@ -205,7 +229,8 @@ __device__ __forceinline__ int dirk_setup(const ChemParams& P, const ChemState& 
 
 template <typename LU, bool REF, int BS>
 __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S, long n,
-                                                       double* __restrict__ y_io, DirkOpts O,
+                                                       double* __restrict__ y_io,
+                                                       const __grid_constant__ DirkOpts O,
                                                        unsigned long long* __restrict__ next,
                                                        int* __restrict__ stats,
                                                        int* __restrict__ nfail) {
@@ -215,9 +240,12 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
   const int lane = tid & 31;
   unsigned char* p = smem_raw;
   double* const Y = reinterpret_cast<double*>(p) + tid;  // state at the step start
-  double* const K1 = Y + 10 * BS;                         // F(Y)
-  double* const K2 = K1 + 10 * BS;                        // F(stage 2)
-  double* const Z = K2 + 10 * BS;                         // current stage iterate
+  double* const K1 = Y + 10 * BS;                         // K_0 = F(Y)
+  double* const B = K1 + 10 * BS;                         // base of the current stage
+  double* const Z = B + 10 * BS;                          // current stage iterate
+  // K_1 .. K_{s-2} of this lane in the stage store (L2-resident: lanes x 10 (s-2) doubles)
+  const long kst = O.kstore_lanes;
+  double* const KG = O.kstore + (long)blockIdx.x * BS + tid;
   p += Lay::kVec * BS;
   double* const A = reinterpret_cast<double*>(p) + tid;   // REF: FP64 Newton matrix
   p += Lay::kA * BS;
@@ -233,7 +261,8 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 
   long i = -1;
   bool exhausted = false;
-  int phase = kPhK1, stage = 2, m = 0;
+  const int ns = O.T.s;
+  int phase = kPhK1, stage = 1, m = 0;
   double t = 0.0, h = 0.0, gp = 0.0, crate = 1.0, delp = 0.0;
   double Tsy = 0.0, dTsy = 0.0, Tsc = 0.0, dTsc = 0.0;
   int nst = 0, nst_lp = 0, nef_s = 0, ncf_s = 0;
@@ -278,8 +307,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 
     // ---- one evaluation of F per pass (at Y for the first stage, else at the iterate)
     double f[10];
-    // stage abscissae of the ESDIRK: c = (0, 2 gd, 1)
-    const double tf = (phase == kPhK1) ? t : ((stage == 2) ? t + (2.0 * kGd) * h : t + h);
+    const double tf = (phase == kPhK1) ? t : t + O.T.c[stage] * h;
     dirk_F<BS>(P, S, i, phase == kPhK1 ? Y : Z, O, tf, mixed_temp, Tsc, dTsc, f);
     ++c_nfe;
 
@@ -302,18 +330,10 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       if (O.hmax > 0.0 && h > O.hmax) h = O.hmax;
       setup = true;
     } else if (phase == kPhNewton) {
-      const double gam = h * kGd;
+      const double gam = h * O.T.gamma;
       double g[10];
-      if (stage == 2) {
 #pragma unroll
-        for (int s = 0; s < 10; ++s)
-          g[s] = (Y[s * BS] + gam * K1[s * BS]) + gam * f[s] - Z[s * BS];
-      } else {
-        const double hw = h * kW;
-#pragma unroll
-        for (int s = 0; s < 10; ++s)
-          g[s] = (Y[s * BS] + hw * (K1[s * BS] + K2[s * BS])) + gam * f[s] - Z[s * BS];
-      }
+      for (int s = 0; s < 10; ++s) g[s] = B[s * BS] + gam * f[s] - Z[s * BS];
       int piv[10];
 #pragma unroll
       for (int s = 0; s < 10; ++s) piv[s] = PV[s * BS];
@@ -366,7 +386,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       if (m > 1) crate = fmax(0.3 * crate, del / delp);
       const double dcon = fmin(crate, 1.0) * del / O.nlscoef;
       if (dcon <= 1.0) {
-        phase = (stage == 2) ? kPhK2 : kPhK3;
+        phase = kPhStage;
       } else if ((m > 1 && del > 2.3 * delp) || m >= O.maxcor || !(del == del)) {
         // Newton failure: with a matrix from an earlier step set up a current one at the
         // same h, else cut the step
@@ -382,17 +402,29 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       } else {
         delp = del;
       }
-    } else if (phase == kPhK2) {
+    } else if (stage < ns - 1) {  // kPhStage, not the last stage: keep K_stage, next stage
 #pragma unroll
-      for (int s = 0; s < 10; ++s) K2[s * BS] = f[s];
-      stage = 3;  // predictor: the stage-2 value already in Z
+      for (int s = 0; s < 10; ++s) KG[((stage - 1) * 10 + s) * kst] = f[s];
+      ++stage;  // predictor: the converged value of this stage, already in Z
+      dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
       m = 0;
       phase = kPhNewton;
-    } else {  // kPhK3: error test
+    } else {  // kPhStage of the last stage: error test
+      double acc[10];
+      const double e0 = O.T.e[0];
+#pragma unroll
+      for (int s = 0; s < 10; ++s) acc[s] = e0 * K1[s * BS];
+      for (int j = 1; j < ns - 1; ++j) {
+        const double ej = O.T.e[j];
+        if (ej == 0.0) continue;
+#pragma unroll
+        for (int s = 0; s < 10; ++s) acc[s] += ej * KG[((j - 1) * 10 + s) * kst];
+      }
+      const double el = O.T.e[ns - 1];
       double s2 = 0.0;
 #pragma unroll
       for (int s = 0; s < 10; ++s) {
-        const double e = h * ((kE1 * K1[s * BS] + kE2 * K2[s * BS]) + kE3 * f[s]);
+        const double e = h * (acc[s] + el * f[s]);
         const double v = e * (double)EW[s * BS];
         s2 += v * v;
       }
@@ -408,7 +440,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         Tsy = Tsc;
         dTsy = dTsc;
         jcur = false;
-        double eta = (dsm > 0.0) ? O.safety / cbrt(dsm) : 1.0e300;
+        double eta = (dsm > 0.0) ? dirk_eta(O.safety, dsm, O.T.p) : 1.0e300;
         eta = fmin(eta, nst == 1 ? O.etamx1 : O.growth);
         if (nef_s > 0 || ncf_s > 0) eta = fmin(eta, 1.0);
         h *= eta;
@@ -423,7 +455,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         if (nef_s >= O.maxnef) {
           retire = failed = true;
         } else {
-          double eta = fmax(0.1, O.safety / cbrt(dsm));
+          double eta = fmax(0.1, dirk_eta(O.safety, dsm, O.T.p));
           if (nef_s >= 2) eta = fmin(eta, 0.3);
           h *= eta;
           setup = true;
@@ -443,7 +475,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         EW[s * BS] = (float)(1.0 / (O.rtol * fabs(ys) + O.atol));
         Z[s * BS] = ys;  // trivial predictor
       }
-      const double gam = h * kGd;
+      const double gam = h * O.T.gamma;
       if (force_setup || nst >= nst_lp + O.msbp || !(fabs(gam / gp - 1.0) <= O.dgmax)) {
         // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored (inline: an
         // out-of-line call measured 4 % slower in the mixed form)
@@ -469,7 +501,8 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           }
         }
       }
-      stage = 2;
+      stage = 1;
+      if (!retire) dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
       m = 0;
       phase = kPhNewton;
     }
@@ -497,20 +530,34 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
   }
 }
 
+// Resident blocks per SM of one instantiation (0 if it does not fit).
+template <typename LU, bool REF, int BS>
+static int dirk_blocks_per_sm(int* per_sm) {
+  const size_t shm = DirkLayout<LU, REF, BS>::bytes;
+  GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_dirk_kernel<LU, REF, BS>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+  GBMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      per_sm, chem_dirk_kernel<LU, REF, BS>, BS, shm));
+  return GBMV_OK;
+}
+
 template <typename LU, bool REF, int BS>
 static int launch_dirk(const ChemParams& P, const ChemState& S, long n, double* y,
                        const DirkOpts& O, unsigned long long* d_next, int* stats, int* d_nfail,
                        int nsm, cudaStream_t s) {
   const size_t shm = DirkLayout<LU, REF, BS>::bytes;
-  GBMV_CUDA_TRY(cudaFuncSetAttribute(chem_dirk_kernel<LU, REF, BS>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   int per_sm = 0;
-  GBMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, chem_dirk_kernel<LU, REF, BS>, BS, shm));
+  int rc = dirk_blocks_per_sm<LU, REF, BS>(&per_sm);
+  if (rc) return rc;
   if (per_sm < 1) return GBMV_EUNSUPPORTED;
   long blocks = (long)nsm * per_sm;
   const long need = (n + BS - 1) / BS;
   if (blocks > need) blocks = need;
+  if (O.T.s > 2 && (!O.kstore || blocks * BS > O.kstore_lanes)) {
+    set_error("DIRK stage store of %ld lanes is smaller than the launch (%ld lanes)",
+              O.kstore_lanes, blocks * BS);
+    return GBMV_EINVAL;
+  }
   chem_dirk_kernel<LU, REF, BS><<<(int)blocks, BS, shm, s>>>(P, S, n, y, O, d_next, stats,
                                                              d_nfail);
   GBMV_LAUNCH_CHECK("chem_dirk_kernel");
@@ -527,6 +574,35 @@ static int launch_dirk_bs(int block, const ChemParams& P, const ChemState& S, lo
     case 128: return launch_dirk<LU, REF, 128>(P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
     default: return GBMV_EINVAL;
   }
+}
+
+template <typename LU, bool REF>
+static int max_lanes_bs(int nsm, long* lanes) {
+  const int bs[3] = {32, 64, 128};
+  for (int k = 0; k < 3; ++k) {
+    int per_sm = 0;
+    int rc = k == 0 ? dirk_blocks_per_sm<LU, REF, 32>(&per_sm)
+                    : (k == 1 ? dirk_blocks_per_sm<LU, REF, 64>(&per_sm)
+                              : dirk_blocks_per_sm<LU, REF, 128>(&per_sm));
+    if (rc) return rc;
+    const long l = (long)nsm * per_sm * bs[k];
+    if (l > *lanes) *lanes = l;
+  }
+  return GBMV_OK;
+}
+
+long chem_dirk_max_lanes() {
+  int dev = 0, nsm = kSM;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  long lanes = 0;
+  if (max_lanes_bs<double, false>(nsm, &lanes) || max_lanes_bs<float, false>(nsm, &lanes) ||
+      max_lanes_bs<float, true>(nsm, &lanes))
+    return -1;
+  return lanes;
 }
 
 int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,

@@ -23,14 +23,26 @@ src/primordial_blast.cpp, ...); the caller passes `problem(inputs)`, returning a
           values (prepare_Dengo_scaling, src/primordial_static.cpp:227);
   force   optional constant external force, 5 + nchem values (external_forces).
 
-Methods: the reference selects SUNDIALS tables through order / etable / itable / mtable.
-SUNDIALS is absent here, so the host integrators of integrate.py stand in -- Dormand-Prince
-5(4) for ERK, ARK3(2)4L[2]SA for ARK-IMEX -- and for MRI the explicit coupling tables this
-package has, by SUNDIALS' ARKODE_MRITableID numbers: mtable -1 (MRIStep's default third-order
-explicit coupling) or 200 -> MIS-KW3, 201 -> MRI-GARK-ERK33a; other numbers are refused.
-Options the stand-in integrators do not have (dense_order, adapt_method, pq, k1-k3, mxhnil,
-hmin, predictor, fusedkernels, localreduce) are read and written back unchanged but do not
-alter the run; a zero option means "the integrator's default", as in the reference.
+Methods: the reference selects SUNDIALS tables through order / etable / itable / mtable, and
+so do these drivers, with the tables of gbmv_butcher_table (SUNDIALS is absent here; the host
+integrators of integrate.py run them):
+  run_euler      order != 0: ARKODE's default explicit table of that order (2 Heun-Euler,
+                 3 Bogacki-Shampine, 4 Zonneveld, 5 Cash-Karp); else etable >= 0: that table;
+                 else the order-4 default (src/euler3D_main.cpp:207-213);
+  run_imex       ARKStepSetTableNum(itable, etable) (src/imex_chem_hydro_main.cpp:386): both
+                 an additive pair (13 + 112 = ARK4(3)7L[2]SA, the primordial inputs'; 2 + 104 =
+                 ARK3(2)4L[2]SA), itable alone a DIRK on the chemistry only, etable alone an ERK;
+  run_multirate  the inner (fast) DIRK of itable (112 or 102; src/multirate_chem_hydro_main.
+                 cpp:446-449), the slow coupling of mtable by SUNDIALS' ARKODE_MRITableID
+                 numbers: -1 (MRIStep's default third-order explicit coupling) or 200 ->
+                 MIS-KW3, 201 -> MRI-GARK-ERK33a.
+Unknown table numbers are refused with ValueError.  adapt_method (0 PID, 1 PI, 2 I), k1-k3,
+pq, safety, bias, growth, etamx1, etamxf and maxnef set ARKODE's step controller.  Options the
+host integrators do not have (dense_order, mxhnil, hmin, predictor, fusedkernels,
+localreduce) are read and written back unchanged but do not alter the run; a zero option
+means "the integrator's default", as in the reference.  The chemistry drivers add the slow
+(fexpl / fslow) chemistry tendency to the scaled chemistry unconverted, as the reference does
+(forcing_units="reference"); forcing_units="scaled" converts it first (integrate.mri_evolve).
 """
 from __future__ import annotations
 
@@ -299,8 +311,8 @@ def run_euler(inp: Inputs, problem, outdir: str = ".", restart_dir: str | None =
     rtol, atol = o["rtol"], o["atol"]
     hmax = _opt(o["hmax"], math.inf)
     fixed = o["fixedstep"] != 0
-    common = dict(safety=_opt(o["safety"], 0.9), etamax=_opt(o["growth"], 5.0),
-                  max_steps=_opt(o["mxsteps"], 500), stability=stab)
+    common = dict(max_steps=_opt(o["mxsteps"], 500), stability=stab, table=erk_table(o),
+                  **_adapt(o))
 
     def evolve(t, tout, h):
         yt, st = I.erk_evolve(rhs, t, tout, y, rtol, atol, h0=h, hmax=hmax,
@@ -319,6 +331,31 @@ def run_euler(inp: Inputs, problem, outdir: str = ".", restart_dir: str | None =
                         transient if (fixed and o["htrans"] > 0.0) else None)
 
 
+def erk_table(o) -> int:
+    """The explicit table euler3D_main selects: `order` overrides `etable`
+    (src/euler3D_main.cpp:207-213); neither set -> ARKStep's order-4 default."""
+    import gbmv
+    if o["order"] != 0:
+        tid = gbmv.erk_default_table(o["order"])
+        if tid < 0:
+            raise ValueError(f"order {o['order']}: no explicit table of that order here (2-5)")
+        return tid
+    tid = o["etable"] if o["etable"] >= 0 else gbmv.erk_default_table(4)
+    gbmv.butcher_table(tid)  # refuses unknown numbers
+    return tid
+
+
+def _adapt(o) -> dict:
+    """ARKODE step-controller options of the inputs (zero = the controller's default)."""
+    kw = {"adapt_method": o["adapt_method"], "pq": o["pq"]}
+    for key in ("k1", "k2", "k3", "safety", "bias", "growth", "etamx1", "etamxf"):
+        if o[key] > 0:
+            kw[key] = o[key]
+    if o["maxnef"] > 0:
+        kw["maxnef"] = o["maxnef"]
+    return kw
+
+
 def _chem_setup(inp: Inputs, problem, restart_dir, tables):
     import numpy as np
     import torch
@@ -335,26 +372,25 @@ def _chem_setup(inp: Inputs, problem, restart_dir, tables):
 
 def run_imex(inp: Inputs, problem, tables, outdir: str = ".", restart_dir: str | None = None,
              precision: int | None = None, fused_newton: bool = False,
-             log=print) -> RunResult:
+             forcing_units: str = "reference", log=print) -> RunResult:
     """imex_chem_hydro_main: ARK-IMEX with fe = fexpl and fi = fimpl, the block-diagonal
-    direct solver, PostprocessStep after every step (integrate.ChemHydroImex); rtol, atol, h0,
-    hmax, fixedstep, safety, bias, growth, etamx1, etamxf, maxnef, maxniters (maxcor),
-    nlconvcoef (nlscoef) and mxsteps as ARKStep takes them.  tables: the 50 x 1024 rate table
-    block (h5tables.load_table_block)."""
+    direct solver, PostprocessStep after every step (integrate.ChemHydroImex), the method of
+    ARKStepSetTableNum(itable, etable); rtol, atol, h0, hmax, fixedstep, the controller options,
+    maxnef, maxniters (maxcor), nlconvcoef (nlscoef) and mxsteps as ARKStep takes them.
+    tables: the 50 x 1024 rate table block (h5tables.load_table_block)."""
     import gbmv
     o = inp.o
+    table = I.ark_table(o["etable"], o["itable"])  # refuses what ARKStepSetTableNum refuses
     t0, hydro, chem, w = _chem_setup(inp, problem, restart_dir or outdir, tables)
     u = inp.u
     eu = inp.field_units()[2]
     prec = gbmv.FP64 if precision is None else precision
     prob = I.ChemHydroImex(gbmv, hydro, chem, eu, u["TimeUnits"], o["rtol"], o["atol"], prec,
-                           fused_newton=fused_newton)
+                           fused_newton=fused_newton, forcing_units=forcing_units)
     kw = dict(rtol=o["rtol"], atol=o["atol"], hmax=_opt(o["hmax"], math.inf),
               fixed_h=o["hmax"] if o["fixedstep"] else 0.0,
-              max_steps=_opt(o["mxsteps"], 500))
-    for key, name in (("safety", "safety"), ("bias", "bias"), ("growth", "growth"),
-                      ("etamx1", "etamx1"), ("etamxf", "etamxf"), ("maxnef", "maxnef"),
-                      ("maxniters", "maxcor"), ("nlconvcoef", "nlscoef")):
+              max_steps=_opt(o["mxsteps"], 500), table=table, **_adapt(o))
+    for key, name in (("maxniters", "maxcor"), ("nlconvcoef", "nlscoef")):
         if o[key] > 0:
             kw[name] = o[key]
 
@@ -377,16 +413,21 @@ MRI_TABLES = {-1: I.MRI_KW3, 200: I.MRI_KW3, 201: I.MRI_ERK33A}
 
 def run_multirate(inp: Inputs, problem, tables, outdir: str = ".",
                   restart_dir: str | None = None, precision: int | None = None,
-                  log=print) -> RunResult:
+                  forcing_units: str = "reference", log=print) -> RunResult:
     """multirate_chem_hydro_main: MRI with a fixed slow step h0 (dTout when h0 is 0,
     src/multirate_chem_hydro_main.cpp:222), slow RHS fexpl, fast stages by
     gbmv_mri_fast_evolve (per-cell DIRK with rtol, atol, maxniters, nlconvcoef, hmax, safety,
     growth, etamx1, maxnef, mxsteps as the inner ARKStep takes them).  A slow step that would
     pass an output time is shortened to end on it, as MRIStep's stop time does.  The inner
-    integrator's fixed-step mode (fixedstep) is not available and is refused."""
+    integrator's fixed-step mode (fixedstep) is not available and is refused.  The inner DIRK
+    is the one of itable (112 ARK4(3)7L[2]SA, as the reference's multirate inputs select, or
+    102 TR-BDF2); itable -1 (ARKODE's default inner DIRK, SDIRK 5(3)4) is not available and is
+    refused."""
     o, u = inp.o, inp.u
     if o["mtable"] not in MRI_TABLES:
         raise ValueError(f"mtable {o['mtable']} is not available (-1, 200 MIS-KW3, 201 ERK33a)")
+    if o["itable"] not in (102, 112):
+        raise ValueError(f"itable {o['itable']}: the inner DIRK must be 112 or 102")
     if o["fixedstep"]:
         raise ValueError("fixedstep: the per-cell fast integrator has adaptive steps only")
     import gbmv
@@ -396,7 +437,7 @@ def run_multirate(inp: Inputs, problem, tables, outdir: str = ".",
     prec = gbmv.FP64 if precision is None else precision
     dtout = (u["tf"] - t0) / u["nout"]
     hslow = o["h0"] if o["h0"] > 0 else dtout
-    fast = dict(rtol=o["rtol"], atol=o["atol"])
+    fast = dict(rtol=o["rtol"], atol=o["atol"], table=o["itable"])
     for key, name in (("maxniters", "maxcor"), ("nlconvcoef", "nlscoef"), ("hmax", "hmax"),
                       ("safety", "safety"), ("growth", "growth"), ("etamx1", "etamx1"),
                       ("maxnef", "maxnef"), ("mxsteps", "max_steps")):
@@ -409,12 +450,12 @@ def run_multirate(inp: Inputs, problem, tables, outdir: str = ".",
         tm = t + nfull * hslow
         if nfull >= 1:
             r = I.mri_evolve(gbmv, hydro, chem, w, t, tm, hslow, eu, u["TimeUnits"], table,
-                             prec, **fast)
+                             prec, forcing_units=forcing_units, **fast)
             steps, failed = r.slow_steps, r.fast_failed_cells
         rem = tout - tm
         if rem > 1e-12 * max(abs(tout), hslow):
             r = I.mri_evolve(gbmv, hydro, chem, w, tm, tout, rem, eu, u["TimeUnits"], table,
-                             prec, **fast)
+                             prec, forcing_units=forcing_units, **fast)
             steps, failed = steps + r.slow_steps, failed + r.fast_failed_cells
         if failed:
             raise RuntimeError(f"fast integration failed in {failed} cells")

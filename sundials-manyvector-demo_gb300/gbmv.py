@@ -44,7 +44,18 @@ class _DirkOpts(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("rtol", "atol", "nlscoef", "h0", "safety", "dgmax",
                                           "growth", "etamx1", "hmax")] + \
                [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf",
-                                       "precision", "refine", "block")]
+                                       "precision", "refine", "block", "table")]
+
+
+MAX_STAGES = 7
+
+
+class _Butcher(C.Structure):
+    """gbmv_butcher (include/gbmv.h)."""
+    _fields_ = [("id", C.c_int), ("stages", C.c_int), ("q", C.c_int), ("p", C.c_int),
+                ("c", C.c_double * MAX_STAGES), ("A", (C.c_double * MAX_STAGES) * MAX_STAGES),
+                ("b", C.c_double * MAX_STAGES), ("bhat", C.c_double * MAX_STAGES),
+                ("name", C.c_char * 32)]
 
 
 _P = C.POINTER(C.c_double)
@@ -108,6 +119,8 @@ SIGNATURES = [
     ("gbmv_ffast", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
                              C.c_int, C.POINTER(_VP), C.c_double, C.c_double, _VP]),
     ("gbmv_postprocess_step", C.c_int, [_VP, _VP, C.POINTER(_VP), C.c_double, _VP]),
+    ("gbmv_butcher_table", C.c_int, [C.c_int, C.POINTER(_Butcher)]),
+    ("gbmv_erk_default_table", C.c_int, [C.c_int]),
     ("gbmv_version", C.c_char_p, []),
     ("gbmv_last_error", C.c_char_p, []),
     ("gbmv_launch_count", C.c_long, []),
@@ -380,6 +393,24 @@ def dirk_opts(**kw) -> _DirkOpts:
             raise GbmvError(f"unknown DIRK option {k}")
         setattr(o, k, v)
     return o
+
+
+def butcher_table(table_id: int) -> dict:
+    """The Runge-Kutta table of ARKODE number `table_id` (gbmv_butcher_table): dict with name,
+    s, q (method order), p (embedding order), c, A (rows, diagonal included), b, bhat.
+    Host-only (no GPU needed)."""
+    t = _Butcher()
+    _check(load().gbmv_butcher_table(int(table_id), C.byref(t)), "gbmv_butcher_table")
+    s = t.stages
+    return {"id": t.id, "name": t.name.decode(), "s": s, "q": t.q, "p": t.p,
+            "c": [t.c[i] for i in range(s)],
+            "A": [[t.A[i][j] for j in range(s)] for i in range(s)],
+            "b": [t.b[i] for i in range(s)], "bhat": [t.bhat[i] for i in range(s)]}
+
+
+def erk_default_table(order: int) -> int:
+    """ARKODE's default explicit table number for an order (-1 if none)."""
+    return load().gbmv_erk_default_table(int(order))
 
 
 def _wrap_device(ptr: int, n: int):

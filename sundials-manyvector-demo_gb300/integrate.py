@@ -1,32 +1,86 @@
-"""Host time integration for whole-run checks (SUNDIALS is not available here).
+"""Host time integration over the drop-in entry points (SUNDIALS is not available here).
 
-An adaptive explicit Runge-Kutta driver with ARKODE's error control conventions -- WRMS norm
-of the embedded error with weights 1 / (rtol |y| + atol), step accepted when the norm is
-<= 1, step-size update h * min(etamax, max(etamin, safety * err^(-1/q))) -- running the
-Dormand-Prince 5(4) pair (FSAL).  The driver is array-library agnostic: `y` may be a numpy
-array or a torch tensor (the GPU RHS keeps everything on the device); `rhs(t, y)` returns
-dy/dt of the same kind.  It plays the role of ARKStep in euler3D_main.cpp's pure-hydro runs;
-its step sequence is not SUNDIALS', so whole-run comparisons are made within the integration
-tolerance.
+The ARKStep / MRIStep configurations the reference's main programs select, array-library
+agnostic (`y` may be numpy arrays or torch tensors; the GPU problems keep everything on the
+device):
+
+  erk_evolve        adaptive (or fixed-step) explicit Runge-Kutta, any explicit table of
+                    gbmv_butcher_table (ARKStepSetOrder / ARKStepSetTableNum with an explicit
+                    table, src/euler3D_main.cpp:207-213);
+  ark_imex_evolve   additive Runge-Kutta with modified Newton on the implicit stages, any
+                    explicit / implicit / additive pair (ARKStepSetTableNum,
+                    src/imex_chem_hydro_main.cpp:386);
+  mri_gark_evolve   explicit MRI-GARK slow stepping over an inner fast integrator (MRIStep,
+                    src/multirate_chem_hydro_main.cpp:529-560).
+
+Error control is ARKODE's: WRMS norm of the embedded difference with weights
+1 / (rtol |y| + atol), accepted when <= 1, step factor from its adaptivity controllers (PID,
+PI or I, `adapt_method` 0 / 1 / 2, with its default gains, safety, bias and growth bounds).
+The Butcher tables come from the library (gbmv_butcher_table), the single copy of the
+coefficients the GPU integrator uses too.
 """
 from __future__ import annotations
 
 import math
 
-# Dormand-Prince 5(4) (J. R. Dormand, P. J. Prince, J. Comput. Appl. Math. 6 (1980) 19-26)
-_C = [0.0, 1 / 5, 3 / 10, 4 / 5, 8 / 9, 1.0, 1.0]
-_A = [
-    [],
-    [1 / 5],
-    [3 / 40, 9 / 40],
-    [44 / 45, -56 / 15, 32 / 9],
-    [19372 / 6561, -25360 / 2187, 64448 / 6561, -212 / 729],
-    [9017 / 3168, -355 / 33, 46732 / 5247, 49 / 176, -5103 / 18656],
-    [35 / 384, 0.0, 500 / 1113, 125 / 192, -2187 / 6784, 11 / 84],
-]
-_B = [35 / 384, 0.0, 500 / 1113, 125 / 192, -2187 / 6784, 11 / 84, 0.0]
-_BSTAR = [5179 / 57600, 0.0, 7571 / 16695, 393 / 640, -92097 / 339200, 187 / 2100, 1 / 40]
-_E = [b - bs for b, bs in zip(_B, _BSTAR)]
+def butcher(table_id):
+    """Table `table_id` of the library (a dict of name, s, q, p, c, A, b, bhat)."""
+    import gbmv
+    return gbmv.butcher_table(table_id)
+
+
+# ARKODE's adaptivity controllers (arkode_adapt.c): eta = safety * e_n^(-k1/k) e_{n-1}^(k2/k)
+# e_{n-2}^(-k3/k), e = bias * dsm, k the embedding order, with the default gains of each
+# method: 0 PID (0.58, 0.21, 0.10), 1 PI (0.8, 0.31), 2 I (1.0)
+_ADAPT_GAINS = {0: (0.58, 0.21, 0.10), 1: (0.8, 0.31, 0.0), 2: (1.0, 0.0, 0.0)}
+
+
+class Controller:
+    """ARKODE's step-size adaptivity for an embedded pair of order p (ARKStep defaults:
+    safety 0.96, bias 1.5, growth 20, etamx1 10^4 on the first step, etamxf 0.3 after small_nef
+    error failures in one step, step factor kept at 1 inside [1, 1.5) to keep the Newton
+    matrix, at least 0.1).  adapt_method 0 PID (default), 1 PI, 2 I; k1..k3 0 = the method's
+    default gains; pq = 1 uses the method order q instead of p."""
+
+    def __init__(self, p, q=None, adapt_method=0, k1=0.0, k2=0.0, k3=0.0, pq=0, safety=0.96,
+                 bias=1.5, growth=20.0, etamx1=1e4, etamxf=0.3, small_nef=2):
+        if adapt_method not in _ADAPT_GAINS:
+            raise ValueError(f"adapt_method {adapt_method} is not available (0 PID, 1 PI, 2 I)")
+        g = _ADAPT_GAINS[adapt_method]
+        self.k = [k1 or g[0], (k2 or g[1]) if adapt_method < 2 else 0.0,
+                  (k3 or g[2]) if adapt_method == 0 else 0.0]
+        self.ord = q if (pq and q) else p
+        self.safety, self.bias, self.growth = safety, bias, growth
+        self.etamx1, self.etamxf, self.small_nef = etamx1, etamxf, small_nef
+        self.ehist = [1.0, 1.0]  # bias * dsm of the last two accepted steps
+
+    def _eta(self, dsm):
+        e1 = max(self.bias * dsm, 1e-10)
+        k = self.ord
+        eta = e1 ** (-self.k[0] / k)
+        if self.k[1]:
+            eta *= self.ehist[0] ** (self.k[1] / k)
+        if self.k[2]:
+            eta *= self.ehist[1] ** (-self.k[2] / k)
+        return self.safety * eta
+
+    def accepted(self, dsm, first, after_failure):
+        """Step factor after an accepted step with error norm dsm."""
+        eta = min(self._eta(dsm), self.etamx1 if first else self.growth)
+        if after_failure:
+            eta = min(eta, 1.0)
+        if 1.0 <= eta < 1.5:
+            eta = 1.0
+        eta = max(eta, 0.1)
+        self.ehist = [max(self.bias * dsm, 1e-10), self.ehist[0]]
+        return eta
+
+    def rejected(self, dsm, nef):
+        """Step factor after the nef-th error-test failure of a step."""
+        eta = max(0.1, min(1.0, self.safety * max(self.bias * dsm, 1e-10) ** (-1.0 / self.ord)))
+        if nef >= self.small_nef:
+            eta = min(eta, self.etamxf)
+        return eta
 
 
 def _wrms(e, y, rtol, atol):
@@ -43,22 +97,31 @@ class ERKResult:
         self.h_next = 0.0  # the step the controller proposes after the last one
 
 
-def erk_evolve(rhs, t0, tf, y0, rtol=1e-6, atol=1e-11, h0=0.0, safety=0.9, etamax=5.0,
-               etamin=0.2, hmax=math.inf, max_steps=100000, fixed_h=0.0, stability=None):
-    """Integrate dy/dt = rhs(t, y) from t0 to tf; returns (y(tf), stats).  fixed_h > 0: steps
-    of fixed_h (the last one shortened to reach tf) without error control, as ARKStep's fixed
-    step mode.  stability(t, y): an explicitly stable step bound applied to every adaptive
-    step (ARKStepSetStabilityFn, as the reference's CFL function `stability` is used)."""
+def erk_evolve(rhs, t0, tf, y0, rtol=1e-6, atol=1e-11, h0=0.0, hmax=math.inf,
+               max_steps=100000, fixed_h=0.0, stability=None, table=8, maxnef=7, **adapt):
+    """Integrate dy/dt = rhs(t, y) from t0 to tf with the explicit table `table` (an ARKODE
+    table number of gbmv_butcher_table, or a table dict; default Dormand-Prince 5(4)); returns
+    (y(tf), stats).  A table whose last row is b with c = 1 reuses its last stage derivative
+    as the next step's first (FSAL).  fixed_h > 0: steps of fixed_h (the last one shortened to
+    reach tf) without error control, as ARKStep's fixed step mode.  stability(t, y): an
+    explicitly stable step bound applied to every adaptive step (ARKStepSetStabilityFn, as
+    the reference's CFL function `stability` is used).  adapt: Controller options
+    (adapt_method, k1, k2, k3, pq, safety, bias, growth, etamx1, etamxf, small_nef)."""
+    T = butcher(table) if not isinstance(table, dict) else table
+    A, b, c, bh = T["A"], T["b"], T["c"], T["bhat"]
+    ns = T["s"]
+    e = [bi - bhi for bi, bhi in zip(b, bh)]
+    fsal = c[-1] == 1.0 and list(A[-1][:ns - 1]) == list(b[:ns - 1]) and b[-1] == 0.0
+    ctl = Controller(T["p"], T["q"], **adapt)
     st = ERKResult()
     y = y0.clone() if hasattr(y0, "clone") else y0.copy()
     t = t0
     k1 = rhs(t, y)
     st.nfe += 1
-    if h0 <= 0.0:  # initial step from the derivative size (ARKODE estimates similarly)
-        d0 = _wrms(y, y, rtol, atol)
-        d1 = _wrms(k1, y, rtol, atol)
-        h0 = 0.01 * d0 / d1 if d0 > 1e-5 and d1 > 1e-5 else 1e-6
+    if h0 <= 0.0:  # ARKODE's initial-step rule, on the explicit problem
+        h0 = _initial_step(_ExplicitProblem(rhs, rtol, atol), t0, tf, [y], [k1], atol)
     h = fixed_h if fixed_h > 0.0 else min(h0, tf - t0, hmax)
+    first, nef_s = True, 0
     while t < tf:
         if st.steps + st.fails > max_steps:
             raise RuntimeError("erk_evolve: too many steps")
@@ -71,40 +134,64 @@ def erk_evolve(rhs, t0, tf, y0, rtol=1e-6, atol=1e-11, h0=0.0, safety=0.9, etama
             t = tf
             break
         ks = [k1]
-        for s in range(1, 7):
+        for i in range(1, ns):
             ys = y
-            for j, a in enumerate(_A[s]):
-                if a != 0.0:
-                    ys = ys + (h * a) * ks[j]
-            ks.append(rhs(t + _C[s] * h, ys))
+            for j in range(i):
+                if A[i][j] != 0.0:
+                    ys = ys + (h * A[i][j]) * ks[j]
+            ks.append(rhs(t + c[i] * h, ys))
             st.nfe += 1
         ynew = y
-        for b, k in zip(_B, ks):
-            if b != 0.0:
-                ynew = ynew + (h * b) * k
+        for bj, k in zip(b, ks):
+            if bj != 0.0:
+                ynew = ynew + (h * bj) * k
         err = None
-        for e, k in zip(_E, ks):
-            if e != 0.0:
-                err = (h * e) * k if err is None else err + (h * e) * k
-        en = 0.0 if fixed_h > 0.0 else _wrms(err, ynew, rtol, atol)
+        for ej, k in zip(e, ks):
+            if ej != 0.0:
+                err = (h * ej) * k if err is None else err + (h * ej) * k
+        en = 0.0 if (fixed_h > 0.0 or err is None) else _wrms(err, y, rtol, atol)
         if not math.isfinite(en):
             en = 1e10
         if en <= 1.0:
             t = tf if h == tf - t else t + h
             y = ynew
-            k1 = ks[6]  # FSAL
+            k1 = ks[-1] if fsal else rhs(t, y)
+            if not fsal:
+                st.nfe += 1
             st.steps += 1
+            if fixed_h > 0.0:
+                h = fixed_h
+                st.h_next = fixed_h
+                continue
+            eta = ctl.accepted(en, first, nef_s > 0)
+            first, nef_s = False, 0
+            h = min(h * eta, hmax)
+            # a step cut short to land on tf does not shrink the proposal for the next interval
+            st.h_next = max(h, hp) if cut else h
         else:
             st.fails += 1
-        if fixed_h > 0.0:
-            h = fixed_h
-            st.h_next = fixed_h
-            continue
-        fac = etamax if en == 0.0 else min(etamax, max(etamin, safety * en ** (-1.0 / 5.0)))
-        h = min(h * fac, hmax)
-        # a step cut short to land on tf does not shrink the proposal for the next interval
-        st.h_next = max(h, hp) if (cut and en <= 1.0) else h
+            nef_s += 1
+            if nef_s >= maxnef:
+                raise RuntimeError("erk_evolve: too many error-test failures in one step")
+            h *= ctl.rejected(en, nef_s)
+            st.h_next = h
     return y, st
+
+
+class _ExplicitProblem:
+    """The problem protocol of _initial_step for one explicit right-hand side."""
+
+    def __init__(self, rhs, rtol, atol):
+        self.rhs, self.rtol, self.atol = rhs, rtol, atol
+
+    def fe(self, t, y):
+        return [self.rhs(t, y[0])]
+
+    def fi(self, t, y):
+        return [None]
+
+    def norm(self, v, y):
+        return _wrms(v[0], y[0], self.rtol, self.atol)
 
 
 def sod_exact(x, t, gamma=1.4, left=(1.0, 0.0, 1.0), right=(0.125, 0.0, 0.1), x0=0.5):
@@ -229,8 +316,11 @@ def mri_gark_evolve(slow_rhs, fast_evolve, t0, tf, y, h, table=MRI_ERK22B):
     return res
 
 
+FORCING_UNITS = ("reference", "scaled")
+
+
 def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=MRI_KW3,
-               precision=0, slow_rhs=None, **fast_opts):
+               precision=0, slow_rhs=None, forcing_units="reference", **fast_opts):
     """Multirate chemistry-hydrodynamics integration (the MRIStep driver of
     src/multirate_chem_hydro_main.cpp) with a fixed slow step h and an explicit MRI-GARK
     coupling `table`, by default MIS-KW3, MRIStep's default third-order explicit coupling that
@@ -243,11 +333,16 @@ def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=
     Units of the slow chemistry forcing: fexpl returns the chemistry tendency of the physical
     densities, with the total-energy tendency (code units) in the gas-energy slot, as the
     reference's fslow does (src/multirate_chem_hydro_main.cpp:1061-1074, TUnitScale = 1),
-    while the fast variables are the scaled ones (chemistry / scale).  The reference adds the
-    two as they are; here the forcing is converted to the scaled variables first -- species
-    tendencies divided by scale, the gas-energy slot EnergyUnits * etdot / scale -- so that the
-    coupling is dimensionally consistent (`scaled_forcing`)."""
+    while the fast variables are the scaled ones (chemistry / scale).  forcing_units
+    "reference" (the default) adds the two as they are, as the reference does;
+    "scaled" converts the forcing to the scaled variables first -- species tendencies divided
+    by scale, the gas-energy slot EnergyUnits * etdot / scale (`scaled_forcing`) -- which makes
+    the coupling dimensionally consistent, a departure from the reference to select
+    explicitly.  fast_opts: gbmv_dirk_opts fields of the inner DIRK (table = the inputs'
+    itable, 112 by default)."""
     import torch
+    if forcing_units not in FORCING_UNITS:
+        raise ValueError(f"forcing_units must be one of {FORCING_UNITS}")
     fs0 = slow_rhs or (lambda t, y, out: gbmv.fexpl(hydro, chem, t, y, out, energy_units,
                                                     precision))
     inv_scale = chem.state("inv_scale").view(-1, 10)
@@ -256,7 +351,8 @@ def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=
         out = [torch.empty_like(x) for x in y]
         if fs0(t, y, out) != 0:
             raise RuntimeError("slow RHS failed (illegal state)")
-        scaled_forcing(out[5].view(-1, 10), inv_scale, energy_units)
+        if forcing_units == "scaled":
+            scaled_forcing(out[5].view(-1, 10), inv_scale, energy_units)
         return out
 
     def fast(ta, tb, y, forcing, tshift, tscale):
@@ -267,40 +363,46 @@ def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=
 
 
 def mri_erk22b_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units,
-                      precision=0, slow_rhs=None, **fast_opts):
+                      precision=0, slow_rhs=None, **kw):
     """mri_evolve with the second-order MRI-GARK-ERK22b coupling (explicit midpoint: forcings
     g1 = fs(Y1) on [t, t+h/2] and g2 = 2 fs(Y2) - fs(Y1) on [t+h/2, t+h])."""
     return mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, MRI_ERK22B,
-                      precision, slow_rhs, **fast_opts)
+                      precision, slow_rhs, **kw)
 
 
 # ---------------------------------------------------------------------------- ARK-IMEX
-#
-# ARK3(2)4L[2]SA, the additive Runge-Kutta pair of C. A. Kennedy and M. H. Carpenter,
-# Appl. Numer. Math. 44 (2003) 139-181: explicit ERK and stiffly accurate ESDIRK sharing the
-# abscissae c and the weights b, third order with a second-order embedding, diagonal gamma
-# = 1767732205903 / 4055673282236.  Rows of AI include the diagonal entry.
-_AG = 1767732205903 / 4055673282236
-ARK324 = {
-    "name": "ARK3(2)4L[2]SA",
-    "q": 3,  # method order
-    "p": 2,  # embedding order
-    "c": [0.0, 1767732205903 / 2027836641118, 3 / 5, 1.0],
-    "ae": [[],
-           [1767732205903 / 2027836641118],
-           [5535828885825 / 10492691773637, 788022342437 / 10882634858940],
-           [6485989280629 / 16251701735622, -4246266847089 / 9704473918619,
-            10755448449292 / 10357097424841]],
-    "ai": [[0.0],
-           [_AG, _AG],
-           [2746238789719 / 10658868560708, -640167445237 / 6845629431997, _AG],
-           [1471266399579 / 7840856788654, -4482444167858 / 7529755066697,
-            11266239266428 / 11593286722821, _AG]],
-    "b": [1471266399579 / 7840856788654, -4482444167858 / 7529755066697,
-          11266239266428 / 11593286722821, _AG],
-    "bhat": [2756255671327 / 12835298489170, -10771552573575 / 22201958757719,
-             9247589265047 / 10645013368117, 2193209047091 / 5459859503100],
-}
+
+
+def ark_table(etable=2, itable=104):
+    """The additive method ARKStepSetTableNum(itable, etable) selects (src/imex_chem_hydro_main.
+    cpp:386): both >= 0 an IMEX pair (they must share c, b and bhat: ARK3(2)4L[2]SA = (2, 104),
+    ARK4(3)7L[2]SA = (13, 112)), only itable >= 0 a DIRK on fi alone, only etable >= 0 an ERK
+    on fe alone.  Returns a dict with name, q, p, c, b, bhat, ae (strictly lower rows), ai
+    (rows with the diagonal), explicit, implicit."""
+    if etable < 0 and itable < 0:
+        raise ValueError("at least one of etable / itable must name a table")
+    E = butcher(etable) if etable >= 0 else None
+    Im = butcher(itable) if itable >= 0 else None
+    for T, kind in ((E, "explicit"), (Im, "implicit")):
+        if T is None:
+            continue
+        A = T["A"]
+        diag = [A[i][i] for i in range(T["s"])]
+        if kind == "explicit" and any(diag):
+            raise ValueError(f"table {T['id']} is not explicit")
+        if kind == "implicit" and not (diag[0] == 0.0 and all(d == diag[1] for d in diag[1:])
+                                       and diag[1] > 0.0):
+            raise ValueError(f"table {T['id']} is not an ESDIRK with one diagonal value")
+    if E is not None and Im is not None and (E["c"] != Im["c"] or E["b"] != Im["b"] or
+                                             E["bhat"] != Im["bhat"]):
+        raise ValueError(f"tables {etable} and {itable} are not an additive pair")
+    B = E if E is not None else Im
+    s = B["s"]
+    return {"name": "+".join(T["name"] for T in (E, Im) if T is not None),
+            "q": B["q"], "p": B["p"], "c": B["c"], "b": B["b"], "bhat": B["bhat"],
+            "ae": [list(E["A"][i][:i]) if E else [0.0] * i for i in range(s)],
+            "ai": [list(Im["A"][i][:i + 1]) if Im else [0.0] * (i + 1) for i in range(s)],
+            "explicit": E is not None, "implicit": Im is not None}
 
 
 class ImexResult:
@@ -329,6 +431,31 @@ def _combo(base, terms):
                 acc = coef * v if acc is None else acc + coef * v
         out.append(acc)
     return out
+
+
+def _fsum(fe_, fi_):
+    """fe + fi over ManyVector component lists, either may be None (absent part)."""
+    if fe_ is None:
+        return fi_
+    if fi_ is None:
+        return fe_
+    return _combo(fe_, [(1.0, fi_)])
+
+
+class _PartProblem:
+    """fe / fi of a problem with the absent part of the method's table returning None."""
+
+    def __init__(self, prob, use_e, use_i):
+        self.p, self.use_e, self.use_i = prob, use_e, use_i
+
+    def fe(self, t, y):
+        return self.p.fe(t, y) if self.use_e else [None] * len(y)
+
+    def fi(self, t, y):
+        return self.p.fi(t, y) if self.use_i else [None] * len(y)
+
+    def norm(self, v, y):
+        return self.p.norm(v, y)
 
 
 def _clone(x):
@@ -373,9 +500,9 @@ def _initial_step(prob, t0, tf, y, f0, atol):
 
 
 def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.inf,
-                    fixed_h=0.0, safety=0.96, bias=1.5, growth=20.0, etamx1=1e4, etamxf=0.3,
-                    small_nef=2, etacf=0.25, maxnef=7, maxncf=10, maxcor=3, nlscoef=0.1,
-                    crdown=0.3, rdiv=2.3, dgmax=0.2, msbp=20, max_steps=5000, table=ARK324):
+                    fixed_h=0.0, etacf=0.25, maxnef=7, maxncf=10, maxcor=3, nlscoef=0.1,
+                    crdown=0.3, rdiv=2.3, dgmax=0.2, msbp=20, max_steps=5000, table=None,
+                    **adapt):
     """Adaptive additive Runge-Kutta (IMEX) integration of y' = fe(t, y) + fi(t, y) from t0 to
     tf, the ARKStep configuration of src/imex_chem_hydro_main.cpp:337-475 (fexpl explicit,
     fimpl implicit, the block-diagonal direct solver on the chemistry subvector, a
@@ -403,21 +530,23 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
     iterations; a failure with a current matrix cuts the step by etacf.  With
     prob.fused_newton the stage iterations are full Newton steps from prob.correction (the
     matrix current at every iterate, so no setups, lagging or gamma-ratio scaling) under the
-    same convergence test.  Error control: WRMS
-    norm dsm of the embedded difference with weights from y_n, accepted when dsm <= 1; I
-    controller eta = safety (bias dsm)^(-1/p) (p the embedding order, ARKODE's convention),
-    bounded by etamx1 on the first step and growth after, kept at 1 inside [1, 1.5) (the
-    matrix-reuse window) and after a failure, at least 0.1, at most etamxf after small_nef
-    error failures in one step; h <= hmax.  fixed_h > 0 takes fixed steps without error
-    control.  Defaults are ARKODE's; the reference's IMEX inputs use safety 0.99, bias 2,
-    growth 2, maxcor 10, nlscoef 0.01.  Returns an ImexResult; raises RuntimeError when a step
-    cannot be completed."""
+    same convergence test.  Error control: WRMS norm dsm of the embedded difference with
+    weights from y_n, accepted when dsm <= 1, the step factor from ARKODE's controller
+    (`Controller`, adapt options adapt_method, k1-k3, pq, safety, bias, growth, etamx1,
+    etamxf, small_nef); h <= hmax.  fixed_h > 0 takes fixed steps without error control.
+    table: ark_table(...) (default ARK3(2)4L[2]SA, ARKStep's default IMEX method); with an
+    explicit-only table fi, setup and solve are not used, with an implicit-only one fe is
+    not.  Defaults are ARKODE's; the reference's IMEX inputs use safety 0.99, bias 2, growth
+    2, maxcor 10, nlscoef 0.01 and the ARK4(3)7L[2]SA pair.  Returns an ImexResult; raises
+    RuntimeError when a step cannot be completed."""
     st = ImexResult()
+    table = table if table is not None else ark_table(2, 104)
     ae, ai, c = table["ae"], table["ai"], table["c"]
     b, bh = table["b"], table["bhat"]
     e = [x - xh for x, xh in zip(b, bh)]
     ns = len(c)
-    kexp = -1.0 / table["p"]
+    use_e, use_i = table.get("explicit", True), table.get("implicit", True)
+    ctl = Controller(table["p"], table.get("q"), **adapt)
     post = getattr(prob, "postprocess", None)
     fused = bool(getattr(prob, "fused_newton", False))
     t = t0
@@ -431,11 +560,12 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
         if st.attempts >= max_steps:
             raise RuntimeError("ark_imex_evolve: max_steps attempts reached")
         if F0 is None:
-            F0 = (prob.fe(t, y), prob.fi(t, y))
-            st.nfe += 1
-            st.nfi += 1
+            F0 = (prob.fe(t, y) if use_e else None, prob.fi(t, y) if use_i else None)
+            st.nfe += int(use_e)
+            st.nfi += int(use_i)
         if h <= 0.0:
-            h = _initial_step(prob, t, tf, y, _combo(F0[0], [(1.0, F0[1])]), atol)
+            h = _initial_step(_PartProblem(prob, use_e, use_i), t, tf, y,
+                              _fsum(F0[0], F0[1]), atol)
         h = min(h, hmax)
         last = tf - t <= h * (1.0 + 1e-8)  # stretch a step by a rounding sliver onto tf
         if last:
@@ -446,8 +576,13 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
         for i in range(1, ns):
             ti = t + c[i] * h
             gam = h * ai[i][i]
-            a = _combo(y, [(h * ae[i][j], Fe[j]) for j in range(i)] +
-                       [(h * ai[i][j], Fi[j]) for j in range(i)])
+            a = _combo(y, [(h * ae[i][j], Fe[j]) for j in range(i) if Fe[j] is not None] +
+                       [(h * ai[i][j], Fi[j]) for j in range(i) if Fi[j] is not None])
+            if not use_i:  # explicit stage
+                Fe.append(prob.fe(ti, a))
+                Fi.append(None)
+                st.nfe += 1
+                continue
             z = [_clone(x) for x in y]  # trivial predictor
             m, delp = 0, 0.0
             if fused:
@@ -491,9 +626,9 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
                 delp = dn
             if conv_fail:
                 break
-            Fe.append(prob.fe(ti, z))
+            Fe.append(prob.fe(ti, z) if use_e else None)
             Fi.append(prob.fi(ti, z))
-            st.nfe += 1
+            st.nfe += int(use_e)
             st.nfi += 1
         if conv_fail:
             st.ncf += 1
@@ -507,7 +642,7 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
             else:
                 force_setup = True
             continue
-        F = [_combo(fe_, [(1.0, fi_)]) for fe_, fi_ in zip(Fe, Fi)]
+        F = [_fsum(fe_, fi_) for fe_, fi_ in zip(Fe, Fi)]
         ynew = _combo(y, [(h * b[j], F[j]) for j in range(ns)])
         if fixed_h > 0.0:
             dsm = 0.0
@@ -532,14 +667,7 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
             if fixed_h > 0.0:
                 h = fixed_h
             else:
-                eta = safety * max(bias * dsm, 1e-10) ** kexp
-                eta = min(eta, etamx1 if first else growth)
-                if nef_s > 0 or ncf_s > 0:
-                    eta = min(eta, 1.0)
-                if 1.0 <= eta < 1.5:
-                    eta = 1.0
-                eta = max(eta, 0.1)
-                h = min(h * eta, hmax)
+                h = min(h * ctl.accepted(dsm, first, nef_s > 0 or ncf_s > 0), hmax)
             first = False
             nef_s = ncf_s = 0
         else:
@@ -547,10 +675,7 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
             nef_s += 1
             if nef_s >= maxnef:
                 raise RuntimeError("ark_imex_evolve: too many error-test failures in one step")
-            eta = max(0.1, min(1.0, safety * max(bias * dsm, 1e-10) ** kexp))
-            if nef_s >= small_nef:
-                eta = min(eta, etamxf)
-            h *= eta
+            h *= ctl.rejected(dsm, nef_s)
     st.h_next = h
     return st
 
@@ -558,8 +683,9 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
 class ChemHydroImex:
     """The reference's IMEX splitting (src/imex_chem_hydro_main.cpp) over the drop-in entry
     points, all on the device: fe = fexpl (WENO flux divergence of every field and the
-    gas-energy coupling, :910-1000; its chemistry tendency converted to the scaled variables
-    by `scaled_forcing`, as the multirate driver does), fi = fimpl (TimeUnits x the chemistry
+    gas-energy coupling, :910-1000; with forcing_units "reference" (the default) its
+    chemistry tendency is added to the scaled chemistry unconverted, as the reference does,
+    with "scaled" converted by `scaled_forcing` first), fi = fimpl (TimeUnits x the chemistry
     source on component 5, zero on the fluid, :811-848), the Newton matrix I - gamma Jimpl
     (:850-908) from gbmv_chem_jac + gbmv_block_form_newton, factored and solved by the
     block-diagonal LU (SUNLinSol_BDMPIMV, :1075-1194), PostprocessStep after every step
@@ -568,8 +694,11 @@ class ChemHydroImex:
     kernel's full Newton corrections."""
 
     def __init__(self, gbmv, hydro, chem, energy_units, time_units, rtol, atol, precision=0,
-                 fused_newton=False, lu_precision=1, refine=4):
+                 fused_newton=False, lu_precision=1, refine=4, forcing_units="reference"):
         import torch
+        if forcing_units not in FORCING_UNITS:
+            raise ValueError(f"forcing_units must be one of {FORCING_UNITS}")
+        self.forcing_units = forcing_units
         self.g, self.hydro, self.chem = gbmv, hydro, chem
         # fused_newton: stage corrections from gbmv_chem_newton_stage (source, Jacobian and
         # factor per cell and per iterate, no Jacobian in HBM), by default with the FP32 factor
@@ -591,7 +720,8 @@ class ChemHydroImex:
         out = [torch.empty_like(x) for x in y]
         if self.g.fexpl(self.hydro, self.chem, t, y, out, self.eu, self.precision) != 0:
             raise RuntimeError("fexpl: illegal state")
-        scaled_forcing(out[5].view(-1, 10), self.inv_scale, self.eu)
+        if self.forcing_units == "scaled":
+            scaled_forcing(out[5].view(-1, 10), self.inv_scale, self.eu)
         return out
 
     def fi(self, t, y):

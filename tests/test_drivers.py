@@ -73,9 +73,9 @@ def test_refusals(tmp_path):
         D.load_inputs(TimeUnits=0.0)
     # MRI coupling numbers this package does not have, and inner fixed steps
     with pytest.raises(ValueError, match="mtable"):
-        D.run_multirate(D.load_inputs(mtable=202), None, None)
+        D.run_multirate(D.load_inputs(mtable=202, itable=112), None, None)
     with pytest.raises(ValueError, match="fixedstep"):
-        D.run_multirate(D.load_inputs(fixedstep=1, hmax=1e-3), None, None)
+        D.run_multirate(D.load_inputs(fixedstep=1, hmax=1e-3, itable=112), None, None)
 
 
 def test_restart_parameters_round_trip(tmp_path):
@@ -99,3 +99,28 @@ def test_scan_matches_sscanf_rules():
     assert D._scan("1e-3 # c", False) == 1e-3 and D._scan("-.5", False) == -0.5
     assert D._scan("5e", False) == 5.0 and math.isinf(D._scan("inf", False))
     assert D._match("xlbc = 1", "xl") is None and D._match("xl= 3", "xl").strip() == "3"
+
+
+def test_method_selection_follows_the_inputs():
+    """order overrides etable for the hydro driver (ARKODE's default table of each order);
+    the chemistry drivers take ARKStepSetTableNum(itable, etable); unknown numbers refused."""
+    import integrate as I
+    assert D.erk_table(D.load_inputs(order=4).o) == 3          # Zonneveld 5-3-4
+    assert D.erk_table(D.load_inputs(order=5).o) == 6          # Cash-Karp 6-4-5
+    assert D.erk_table(D.load_inputs(order=0, etable=13).o) == 13
+    assert D.erk_table(D.load_inputs(order=0, etable=8).o) == 8
+    assert D.erk_table(D.load_inputs(order=0).o) == 3
+    for bad in (dict(order=7), dict(order=0, etable=5)):
+        with pytest.raises(Exception):
+            D.erk_table(D.load_inputs(**bad).o)
+    # the primordial inputs' IMEX pair and static-chemistry DIRK-only setting
+    t = I.ark_table(13, 112)
+    assert t["name"] == "ARK437L2SA_ERK_7_3_4+ARK437L2SA_DIRK_7_3_4"
+    assert not I.ark_table(-1, 112)["explicit"]
+    with pytest.raises(ValueError):
+        D.run_imex(D.load_inputs(etable=-1, itable=-1), None, None)
+    with pytest.raises(ValueError, match="itable"):
+        D.run_multirate(D.load_inputs(itable=-1), None, None)
+    # the controller options reach the integrators
+    kw = D._adapt(D.load_inputs(adapt_method=2, safety=0.99, bias=2.0, growth=2.0).o)
+    assert kw == {"adapt_method": 2, "pq": 0, "safety": 0.99, "bias": 2.0, "growth": 2.0}

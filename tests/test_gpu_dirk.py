@@ -44,12 +44,15 @@ def _relerr(a, b, floor):
     return np.abs(a - b) / (np.abs(b) + floor)
 
 
-def test_dirk_fp64_matches_oracle(cuda, tables):
+@pytest.mark.parametrize("table", [112, 102])
+def test_dirk_fp64_matches_oracle(cuda, tables, table):
+    """Both ESDIRK tables (112 = ARK4(3)7L[2]SA, the inputs' itable; 102 = TR-BDF2)."""
     n, tout = 256, 1e-3
     scale = _cells(n, W.SEED_BASE + 500)
-    zg, sg, nfg, _ = _gpu_run(cuda, tables, scale, tout, precision=0, block=64, **OPTS)
+    zg, sg, nfg, _ = _gpu_run(cuda, tables, scale, tout, precision=0, block=64, table=table,
+                              **OPTS)
     oc = O.Chem(tables, scale)
-    zo, so, nfo = oc.dirk_evolve(np.ones(10 * n), 0.0, tout, TU, **OPTS)
+    zo, so, nfo = oc.dirk_evolve(np.ones(10 * n), 0.0, tout, TU, table=table, **OPTS)
     zo = zo.reshape(n, 10)
     assert nfg == nfo == 0
     same = np.all(sg[:, :7] == so[:, :7], axis=1)
@@ -121,7 +124,7 @@ def test_dirk_every_cell_retired_once_and_histogram(cuda, tables):
     z, st, nf, c = _gpu_run(torch, tables, scale, tout, precision=1, block=64, **OPTS)
     assert nf == 0
     assert np.all(st[:, 0] >= 1) and np.all(st[:, 7] == 0)
-    assert np.all(st[:, 1] >= 2 * st[:, 0])     # two implicit stages per accepted step
+    assert np.all(st[:, 1] >= 6 * st[:, 0])     # six implicit stages per accepted step
     assert np.all(st[:, 6] >= st[:, 1])         # an F evaluation per Newton iteration
     assert np.all(np.isfinite(z)) and not np.any(np.all(z == 1.0, axis=1))
     hist = np.bincount(st[:, 1])
@@ -149,7 +152,7 @@ def test_dirk_options_rejected(cuda, tables):
     c = gbmv.Chem(16, tables)
     z = torch.ones(160, dtype=torch.float64, device="cuda")
     for bad in (dict(rtol=0.0), dict(block=48), dict(refine=9), dict(precision=3),
-                dict(maxcor=0)):
+                dict(maxcor=0), dict(table=13), dict(table=104 + 1000), dict(table=8)):
         with pytest.raises(gbmv.GbmvError):
             c.dirk_evolve(0.0, 1e-3, z, TU, **bad)
     with pytest.raises(gbmv.GbmvError):

@@ -16,8 +16,11 @@ import workloads as W
 
 pytestmark = pytest.mark.gpu
 
+# order 4 -> Zonneveld 5-3-4 (input_sod.txt's method); the I controller (adapt_method 2) keeps
+# no error history, so a restart from the saved step size continues the step sequence exactly
+# (the PID default would restart its history, as a restarted reference run does)
 SOD = dict(nx=128, ny=3, nz=3, xlbc=3, xrbc=3, gamma=1.4, tf=0.2, nout=4, rtol=1e-6,
-           atol=1e-11, showstats=1)
+           atol=1e-11, showstats=1, order=4, adapt_method=2)
 
 
 def _sod_problem(inp):
@@ -62,10 +65,12 @@ def test_euler_driver_sod_and_restart(cuda, tmp_path):
 def _chem_inputs(wl, **kw):
     nz, ny, nx = wl["fields"][0].shape
     u = wl["units"]
+    # the method and controller settings of the reference's primordial inputs
+    # (input_primordial_blast_imex.txt / _mr.txt): ARK4(3)7L[2]SA, I controller
     base = dict(nx=nx, ny=ny, nz=nz, xlbc=3, xrbc=3, gamma=wl["gamma"], tf=4e-6, nout=2,
                 rtol=1e-6, atol=1e-10, MassUnits=u["MassUnits"], LengthUnits=u["LengthUnits"],
                 TimeUnits=u["TimeUnits"], maxniters=10, nlconvcoef=0.01, safety=0.99, bias=2.0,
-                growth=2.0, showstats=1)
+                growth=2.0, showstats=1, order=0, etable=13, itable=112, adapt_method=2)
     base.update(kw)
     return D.load_inputs(**base)
 
@@ -104,7 +109,7 @@ def test_multirate_driver_matches_direct_run(cuda, tables, tmp_path):
     wl = W.chem_hydro(shape=(8, 6, 5))
     inp = _chem_inputs(wl, h0=1e-6, showstats=0)
     fast = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, growth=2.0,
-                max_steps=5000)
+                max_steps=5000, table=112)
     r = D.run_multirate(inp, _chem_problem(wl), tables, str(tmp_path), log=lambda s: None)
     assert len(r.outputs) == 3 and r.steps == 4
     _, f = _fields(r.outputs[-1], 10, inp)

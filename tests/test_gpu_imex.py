@@ -50,17 +50,26 @@ def test_wrms_norm_matches_numpy(cuda):
         hy.wrms_norm(zero, zero, 0.0, 0.0)
 
 
-def test_imex_fp64_matches_oracle_driven_run(cuda, tables):
+@pytest.mark.parametrize("pair,units,adapt", [((2, 104), "scaled", 0),
+                                               ((13, 112), "reference", 2),
+                                               ((13, 112), "scaled", 0)],
+                         ids=["ark324-scaled-pid", "ark437-reference-i", "ark437-scaled-pid"])
+def test_imex_fp64_matches_oracle_driven_run(cuda, tables, pair, units, adapt):
+    """ARK3(2)4L[2]SA and the primordial inputs' ARK4(3)7L[2]SA (etable 13, itable 112), the
+    fexpl chemistry tendency unconverted as the reference adds it or converted to the scaled
+    variables, the PID and I controllers."""
     torch = cuda
     import integrate
     wl = W.chem_hydro(shape=(8, 6, 5))
     eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
     tf = 4e-6
+    opts = dict(OPTS, table=integrate.ark_table(*pair), adapt_method=adapt)
     y_ref = [f.copy() for f in wl["fields"]]
-    oracle_prob = O.ImexChemHydro(wl, tables, eu, tu, OPTS["rtol"], OPTS["atol"])
-    st_ref = integrate.ark_imex_evolve(oracle_prob, 0.0, tf, y_ref, **OPTS)
-    _, prob, w = _gpu_problem(torch, wl, tables, eu, tu)
-    st = integrate.ark_imex_evolve(prob, 0.0, tf, w, **OPTS)
+    oracle_prob = O.ImexChemHydro(wl, tables, eu, tu, OPTS["rtol"], OPTS["atol"],
+                                  forcing_units=units)
+    st_ref = integrate.ark_imex_evolve(oracle_prob, 0.0, tf, y_ref, **opts)
+    _, prob, w = _gpu_problem(torch, wl, tables, eu, tu, forcing_units=units)
+    st = integrate.ark_imex_evolve(prob, 0.0, tf, w, **opts)
     torch.cuda.synchronize()
     got = [x.cpu().numpy() for x in w]
     # the same step sequence, then the same states to well inside the tolerance

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 FAST = dict(rtol=1e-8, atol=1e-12, maxcor=10, nlscoef=0.01)
 
 
-def _oracle_fexpl(wl_state, wl, eu):
+def _oracle_fexpl(wl_state, wl, eu, units):
     f = [x.copy() for x in wl_state]
     scale = wl["scale"]
     phys = f[5] * scale
@@ -24,13 +24,13 @@ def _oracle_fexpl(wl_state, wl, eu):
     out[5][..., 9] = out[4]
     out[4][:] = 0.0
     f[5] = phys / scale
-    # slow chemistry forcing in the scaled fast variables (integrate.scaled_forcing)
-    out[5][..., :9] = out[5][..., :9] * (1.0 / scale[..., :9])
-    out[5][..., 9] = out[5][..., 9] * ((1.0 / scale[..., 9]) * eu)
+    if units == "scaled":  # slow chemistry forcing in the scaled fast variables
+        out[5][..., :9] = out[5][..., :9] * (1.0 / scale[..., :9])
+        out[5][..., 9] = out[5][..., 9] * ((1.0 / scale[..., 9]) * eu)
     return out, f
 
 
-def _oracle_mri(wl, tables, t0, h, nsteps, eu, tu, table):
+def _oracle_mri(wl, tables, t0, h, nsteps, eu, tu, table, units):
     """The explicit MRI-GARK step written out over the oracle: stage i's forcing polynomial
     r(tau) = sum_k tau^k sum_j G[k][i-1][j] / dc F_j, tau = (t - ta) / (dc h)."""
     y = [x.copy() for x in wl["fields"]]
@@ -52,7 +52,7 @@ def _oracle_mri(wl, tables, t0, h, nsteps, eu, tu, table):
         t = t0 + s * h
         Fs = []
         for i in range(1, len(c)):
-            f, y = _oracle_fexpl(y, wl, eu)
+            f, y = _oracle_fexpl(y, wl, eu, units)
             Fs.append(f)
             dc = c[i] - c[i - 1]
             g = [[sum(Gk[i - 1][j] / dc * Fs[j][k] for j in range(i)) for k in range(6)]
@@ -61,7 +61,8 @@ def _oracle_mri(wl, tables, t0, h, nsteps, eu, tu, table):
     return y, n
 
 
-def _gpu_mri(torch, wl, tables, t0, h, nsteps, eu, tu, precision, table=None):
+def _gpu_mri(torch, wl, tables, t0, h, nsteps, eu, tu, precision, table=None,
+             units="reference"):
     import gbmv
     import integrate
     nz, ny, nx = wl["fields"][0].shape
@@ -71,10 +72,11 @@ def _gpu_mri(torch, wl, tables, t0, h, nsteps, eu, tu, precision, table=None):
     w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
     if table is None:
         r = integrate.mri_erk22b_evolve(gbmv, hy, c, w, t0, t0 + nsteps * h, h, eu, tu,
-                                        precision=precision, block=64, **FAST)
+                                        precision=precision, forcing_units=units, block=64,
+                                        **FAST)
     else:
         r = integrate.mri_evolve(gbmv, hy, c, w, t0, t0 + nsteps * h, h, eu, tu, table,
-                                 precision=precision, block=64, **FAST)
+                                 precision=precision, forcing_units=units, block=64, **FAST)
     torch.cuda.synchronize()
     assert r.fast_failed_cells == 0 and r.slow_steps == nsteps
     return [x.cpu().numpy() for x in w]
@@ -85,15 +87,19 @@ def _tables():
     return [None, integrate.MRI_KW3, integrate.MRI_ERK33A]
 
 
-@pytest.mark.parametrize("which", [0, 1, 2], ids=["erk22b", "kw3", "erk33a"])
-def test_mri_fp64_matches_oracle_driven_scheme(cuda, tables, which):
+@pytest.mark.parametrize("which,units", [(0, "scaled"), (1, "scaled"), (2, "scaled"),
+                                         (1, "reference")],
+                         ids=["erk22b", "kw3", "erk33a", "kw3-reference-units"])
+def test_mri_fp64_matches_oracle_driven_scheme(cuda, tables, which, units):
+    """Both forcing units: "reference" adds fexpl's chemistry tendency unconverted (the
+    reference's fslow), "scaled" converts it to the scaled fast variables first."""
     import integrate
     table = _tables()[which]
     wl = W.chem_hydro(shape=(8, 6, 5))
     eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
     t0, h, ns = 0.0, 2e-6, 2
-    ref, n = _oracle_mri(wl, tables, t0, h, ns, eu, tu, table or integrate.MRI_ERK22B)
-    got = _gpu_mri(cuda, wl, tables, t0, h, ns, eu, tu, 0, table)
+    ref, n = _oracle_mri(wl, tables, t0, h, ns, eu, tu, table or integrate.MRI_ERK22B, units)
+    got = _gpu_mri(cuda, wl, tables, t0, h, ns, eu, tu, 0, table, units)
     for k in range(5):
         assert maxnorm_err(got[k], ref[k]) <= 1e-10, k
     a, b = got[5].reshape(n, 10), ref[5].reshape(n, 10)

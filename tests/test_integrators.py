@@ -10,8 +10,8 @@ import pytest
 import integrate as I
 
 
-def _tables():
-    t = I.ARK324
+def _tables(etable=2, itable=104):
+    t = I.ark_table(etable, itable)
     n = len(t["c"])
     AE = np.zeros((n, n))
     AI = np.zeros((n, n))
@@ -35,7 +35,7 @@ def test_ark324_order_conditions():
     assert abs(bh @ c ** 2 - 1 / 3) > 1e-3 or abs(bh @ (AE @ c) - 1 / 6) > 1e-3
     # explicit part strictly lower triangular; implicit part ESDIRK, stiffly accurate
     assert np.all(np.triu(AE) == 0)
-    assert AI[0, 0] == 0 and np.allclose(np.diag(AI)[1:], I.ARK324["ai"][1][1])
+    assert AI[0, 0] == 0 and np.allclose(np.diag(AI)[1:], AI[1, 1])
     assert np.array_equal(AI[-1], b)
     # L-stability of the implicit part: R(z) = det(I - zA + z 1 b^T) / det(I - zA) decays
     # like 1/z as z -> -inf
@@ -46,17 +46,15 @@ def test_ark324_order_conditions():
         assert abs(R) < 5.0 / abs(z)
 
 
-def test_dormand_prince_order_conditions():
-    A = np.zeros((7, 7))
-    for i, row in enumerate(I._A):
-        A[i, :len(row)] = row
-    c, b, bs = np.array(I._C), np.array(I._B), np.array(I._BSTAR)
-    assert np.allclose(A.sum(axis=1), c, atol=1e-15)
-    for k in range(5):  # quadrature conditions up to order 5
-        assert abs(b @ c ** k - 1 / (k + 1)) < 1e-14
-    for k in range(4):
-        assert abs(bs @ c ** k - 1 / (k + 1)) < 1e-14
-    assert abs(b @ (A @ c) - 1 / 6) < 1e-14 and abs(b @ (A @ c ** 2) - 1 / 12) < 1e-14
+def test_ark_table_selection_rules():
+    """ARKStepSetTableNum's rules: both numbers an IMEX pair, one of them a pure method,
+    neither refused; mismatched pairs and wrong kinds refused."""
+    t = I.ark_table(13, 112)
+    assert t["explicit"] and t["implicit"] and t["q"] == 4 and t["p"] == 3
+    assert not I.ark_table(-1, 112)["explicit"] and not I.ark_table(13, -1)["implicit"]
+    for bad in ((-1, -1), (13, 104), (112, -1), (-1, 13)):
+        with pytest.raises((ValueError, Exception)):
+            I.ark_table(*bad)
 
 
 class SplitProblem:
@@ -118,7 +116,7 @@ def test_imex_adaptive_error_tracks_tolerance():
     errs, steps = [], []
     for rtol in (1e-4, 1e-6, 1e-8):
         p = SplitProblem(-1e4, rtol=rtol, atol=rtol * 1e-3)
-        y, st = _run(p, T)
+        y, st = _run(p, T, max_steps=20000)
         errs.append(max(abs(y[0][0] - math.sin(T)), abs(y[1][0] - math.cos(T))))
         steps.append(st.steps)
         assert p.post == st.steps  # PostprocessStep after every accepted step
@@ -231,3 +229,79 @@ def test_mri_gark_tables_order(table):
     errs = [_mri_linear(table, h) for h in (0.1, 0.05, 0.025)]
     orders = [math.log2(errs[k] / errs[k + 1]) for k in range(2)]
     assert min(orders) > table["order"] - 0.25, (errs, orders)
+
+
+@pytest.mark.parametrize("table,order", [(3, 4), (13, 4), (8, 5), (6, 5), (1, 3)])
+def test_erk_tables_fixed_step_order(table, order):
+    """The explicit tables the inputs select (order 4 -> Zonneveld, etable 13, the
+    Dormand-Prince and Cash-Karp pairs, Bogacki-Shampine) converge at their order."""
+    def rhs(t, y):
+        return np.array([y[1], -y[0] + 0.1 * math.sin(t) * y[0] ** 2])
+    ref, _ = I.erk_evolve(rhs, 0.0, 2.0, np.array([0.2, 1.0]), table=8, fixed_h=1e-3)
+    errs = []
+    for h in (0.2, 0.1, 0.05):
+        y, st = I.erk_evolve(rhs, 0.0, 2.0, np.array([0.2, 1.0]), table=table, fixed_h=h)
+        errs.append(np.max(np.abs(y - ref)))
+    orders = [math.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert min(orders) > order - 0.4, (errs, orders)
+
+
+@pytest.mark.parametrize("am", [0, 1, 2])
+def test_erk_adaptivity_controllers(am):
+    def rhs(t, y):
+        return np.array([y[1], -y[0]])
+    for rtol in (1e-6, 1e-9):
+        y, st = I.erk_evolve(rhs, 0.0, 5.0, np.array([0.0, 1.0]), rtol, rtol * 1e-3, table=3,
+                             adapt_method=am)
+        err = max(abs(y[0] - math.sin(5.0)), abs(y[1] - math.cos(5.0)))
+        assert err < 100 * rtol and st.steps > 5
+    with pytest.raises(ValueError):
+        I.erk_evolve(rhs, 0.0, 1.0, np.array([0.0, 1.0]), adapt_method=4)
+
+
+def test_imex_ark437_fixed_step_order():
+    """ARK4(3)7L[2]SA (etable 13, itable 112): fourth order on the nonstiff split problem."""
+    T = 2.0
+    errs = []
+    for h in (0.2, 0.1, 0.05):
+        y, st = _run(SplitProblem(-2.0), T, fixed_h=h, maxcor=10, nlscoef=1e-4,
+                     table=I.ark_table(13, 112))
+        errs.append(max(abs(y[0][0] - math.sin(T)), abs(y[1][0] - math.cos(T))))
+    orders = [math.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert min(orders) > 3.6, (errs, orders)
+
+
+class StiffOnly:
+    """y' = lam (y - cos t) - sin t (implicit part only): y = cos t."""
+
+    def __init__(self, lam):
+        self.lam, self.rtol, self.atol, self.g = lam, 1e-8, 1e-12, None
+
+    def fe(self, t, y):
+        raise AssertionError("an implicit-only table evaluates no explicit part")
+
+    def fi(self, t, y):
+        return [self.lam * (y[0] - math.cos(t)) - math.sin(t)]
+
+    def setup(self, t, y, gamma):
+        self.g = gamma
+        return 0
+
+    def solve(self, b):
+        return [b[0] / (1.0 - self.g * self.lam)]
+
+    def norm(self, v, y):
+        return float(abs(v[0][0]) / (self.rtol * abs(y[0][0]) + self.atol))
+
+
+def test_imex_implicit_only_and_explicit_only_tables():
+    p = StiffOnly(-1e5)
+    y = [np.ones(1)]
+    st = I.ark_imex_evolve(p, 0.0, 1.0, y, rtol=p.rtol, atol=p.atol, maxcor=10,
+                           table=I.ark_table(-1, 112))
+    assert abs(y[0][0] - math.cos(1.0)) < 1e-7 and st.nfe == 0 and st.steps < 200
+    y = [np.zeros(1), np.ones(1)]
+    prob = SplitProblem(0.0)
+    st = I.ark_imex_evolve(prob, 0.0, 2.0, y, rtol=1e-8, atol=1e-12,
+                           table=I.ark_table(13, -1))
+    assert abs(y[0][0] - math.sin(2.0)) < 1e-6 and st.nni == 0 and st.nsetups == 0
