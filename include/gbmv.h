@@ -135,6 +135,15 @@ int gbmv_feuler_jvp(gbmv_hydro h, double t, const double* const* w, const double
 int gbmv_feuler_vjp(gbmv_hydro h, double t, const double* const* w, const double* const* v,
                     double* const* u, void* stream);
 
+/* Cells where a central difference of fEuler along dw crosses a kink (no counterpart in the
+ * reference; for derivative tests): mask[cell] = 1 (device, ncells bytes) when one of the
+ * cell's six faces changes its Lax-Friedrichs branch -- the stencil point that maximises
+ * |u| + c, or the sign of that point's velocity -- between w - eps dw, w and w + eps dw;
+ * elsewhere (f(w + eps dw) - f(w - eps dw)) / (2 eps) differentiates one smooth branch and
+ * converges to gbmv_feuler_jvp.  Asynchronous. */
+int gbmv_feuler_kink_mask(gbmv_hydro h, const double* const* w, const double* const* dw,
+                          double eps, unsigned char* mask, void* stream);
+
 /* pack1D_x / pack1D_y / pack1D_z and their _bdry variants (EulerData, src/euler3D.hpp:
  * 1197-1378), for all faces at once: the six-point stencils the face fluxes of direction dir
  * (0 x, 1 y, 2 z) read, after the periodic wrap and the boundary ghost rules.  out (device):
@@ -310,6 +319,16 @@ int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, doub
                          double tshift, double tscale, const gbmv_dirk_opts* opts, int* stats,
                          void* stream);
 
+/* Same, asynchronous and CUDA-graph capturable (the stage of a captured MRI slow step): the
+ * failed-cell count is added to *d_nfail (device int, caller-zeroed); opts->block must be set
+ * or tuned by an earlier synchronous call, and the first call on the handle (which allocates
+ * the DIRK stage store) must come before any capture. */
+int gbmv_mri_fast_evolve_async(gbmv_hydro h, gbmv_chem c, double t0, double tout,
+                               double* const* w, double time_units, int nforcing,
+                               const double* const* forcing, double tshift, double tscale,
+                               const gbmv_dirk_opts* opts, int* stats, int* d_nfail,
+                               void* stream);
+
 /* Block size the autotuner chose for a precision (0 = not tuned yet). */
 int gbmv_chem_dirk_block(gbmv_chem c, int precision);
 
@@ -408,6 +427,58 @@ int gbmv_butcher_table(int id, gbmv_butcher* out);
 /* ARKODE's default explicit table for an `order` (ARKStepSetOrder, the `order` input option,
  * src/euler3D_main.cpp:207-209): 2 -> 0, 3 -> 1, 4 -> 3, 5 -> 6; -1 for other orders. */
 int gbmv_erk_default_table(int order);
+
+/* ------------------------------------------------ device-resident step control */
+
+/* Adaptive time stepping whose every step is a CUDA graph (the stages, the error norm and
+ * these calls captured once and replayed): the accept / reject decision and the step-size
+ * controller run on the device, so the host reads nothing back between steps.  No
+ * counterpart in the reference, whose ARKStep decides on the host after a synchronising norm;
+ * the controller is ARKODE's (ARKStepSetAdaptivityMethod's PID / PI / I with k1, k2, k3,
+ * safety, bias, growth, etamx1, etamxf, small_nef; src/euler3D.hpp:126-172 options).
+ * The state is GBMV_STEP_STATE doubles of device memory at the indices below; initialise it
+ * with t = t0, tf, h = the first step, first = 1, e1 = e2 = 1, everything else 0 (a graph
+ * captured over these calls serves any interval: the interval lives in the state). */
+#define GBMV_ST_T 0        /* current time */
+#define GBMV_ST_H 1        /* proposed next step */
+#define GBMV_ST_HUSED 2    /* the step of the attempt in flight (0 when done) */
+#define GBMV_ST_ACCEPT 3   /* 1 if the last attempt was accepted */
+#define GBMV_ST_DONE 4     /* 1 once t reached tf or the run failed */
+#define GBMV_ST_E1 5       /* bias * dsm of the last accepted step */
+#define GBMV_ST_E2 6       /* ... and of the one before */
+#define GBMV_ST_FIRST 7    /* 1 before the first accepted step */
+#define GBMV_ST_NEF 8      /* error-test failures of the step in progress */
+#define GBMV_ST_STEPS 9    /* accepted steps */
+#define GBMV_ST_ATTEMPTS 10
+#define GBMV_ST_FAILS 11   /* error-test failures */
+#define GBMV_ST_STATUS 12  /* 0, -1 maxnef failures in one step, -2 max_attempts reached */
+#define GBMV_ST_LAST 13    /* 1 if the attempt in flight ends on tf */
+#define GBMV_ST_HPROP 14   /* the proposal before the cut to tf */
+#define GBMV_ST_TF 15      /* end of the integration interval */
+#define GBMV_STEP_STATE 16
+
+typedef struct {
+  double hmax;           /* largest step (0: none) */
+  double safety, bias, growth, etamx1, etamxf;
+  double k1, k2, k3;     /* controller gains (k2 = k3 = 0: I controller; k3 = 0: PI) */
+  int order;             /* the order k in the exponents (the embedding order) */
+  int small_nef, maxnef, max_attempts;
+  int fixed;             /* 1: fixed steps of h, no error control */
+} gbmv_step_params;
+
+/* Start an attempt: h_used = min(h, hmax, tf - t) (0 and done = 1 when nothing is left). */
+int gbmv_step_begin(double* d_state, const gbmv_step_params* p, void* stream);
+/* Finish it with the WRMS error norm *d_dsm (device): accept (t += h_used) or reject, next h
+ * from the controller; failures set status and done. */
+int gbmv_step_end(double* d_state, const double* d_dsm, const gbmv_step_params* p, void* stream);
+/* y = ynew over n doubles if the last attempt was accepted (else nothing). */
+int gbmv_step_select(long n, const double* d_state, double* y, const double* ynew, void* stream);
+
+/* gbmv_wrms_norm with the result in device memory (*d_norm) and no synchronisation, for
+ * step graphs; the handle's reduction scratch must exist already (any earlier synchronous
+ * reduction call on the handle, or one call of this outside a capture). */
+int gbmv_wrms_norm_async(gbmv_hydro h, const double* const* v, const double* const* y,
+                         double rtol, double atol, double* d_norm, void* stream);
 
 /* ----------------------------------------------------------------- utilities */
 

@@ -854,10 +854,12 @@ int gbmv_ffast(gbmv_hydro h, gbmv_chem c, double t, const double* const* w, doub
   return mri_forcing(c->n, F, nforcing, D, true, 6, s);
 }
 
-int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, double* const* w,
-                         double time_units, int nforcing, const double* const* forcing,
-                         double tshift, double tscale, const gbmv_dirk_opts* opts, int* stats,
-                         void* stream) {
+// The fast evolve shared by gbmv_mri_fast_evolve (synchronous, may tune the DIRK block size)
+// and gbmv_mri_fast_evolve_async (graph-capturable: failures added to *d_nfail).
+static int mri_fast_launch(gbmv_hydro h, gbmv_chem c, double t0, double tout, double* const* w,
+                           double time_units, int nforcing, const double* const* forcing,
+                           double tshift, double tscale, const gbmv_dirk_opts* opts, int* stats,
+                           int* d_nfail, cudaStream_t s, bool may_tune) {
   if (!h || !c || h->g.nchem != 10 || c->n != h->g.ncell || !fields_ok(w, 10)) {
     set_error("mri_fast_evolve needs a 10-species hydro grid matching the chemistry cells");
     return GBMV_EINVAL;
@@ -867,7 +869,6 @@ int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, doub
     return GBMV_EINVAL;
   }
   DirkOpts O;
-  cudaStream_t s = (cudaStream_t)stream;
   int rc = dirk_opts(opts, t0, tout, time_units, &O);
   if (!rc) rc = dirk_store(c, &O, s);
   if (rc) return rc;
@@ -888,28 +889,52 @@ int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, doub
   O.nforcing = nforcing;
   O.tshift = tshift;
   O.tscale = tscale;
-  if (nforcing > 0) {
-    DevFields6 D;
-    for (int k = 0; k < 6; ++k) D.f[k] = w[k];
-    rc = mri_forcing(c->n, Ff, nforcing, D, false, 5, s);  // components 0-4 only
-    if (rc) return rc;
-  }
   const int mixed = opts->precision == GBMV_MIXED;
   int block = opts->block ? opts->block : c->dirk_block[mixed];
   if (!block) {
+    if (!may_tune || capturing(s)) {
+      set_error("DIRK block size not tuned yet: set opts->block or make a synchronous call first");
+      return GBMV_EINVAL;
+    }
     O.nforcing = 0;  // tune on the unforced problem (same work per evaluation within a few %)
     rc = dirk_autotune(c, w[5], O, mixed, s);
     if (rc) return rc;
     O.nforcing = nforcing;
     block = c->dirk_block[mixed];
   }
+  if (nforcing > 0) {
+    DevFields6 D;
+    for (int k = 0; k < 6; ++k) D.f[k] = w[k];
+    rc = mri_forcing(c->n, Ff, nforcing, D, false, 5, s);  // components 0-4 only
+    if (rc) return rc;
+  }
+  return chem_dirk(c->P, c->S, c->n, w[5], O, mixed, block, c->d_next, stats, d_nfail, s);
+}
+
+int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, double* const* w,
+                         double time_units, int nforcing, const double* const* forcing,
+                         double tshift, double tscale, const gbmv_dirk_opts* opts, int* stats,
+                         void* stream) {
+  if (!c) { set_error("null handle"); return GBMV_EINVAL; }
+  cudaStream_t s = (cudaStream_t)stream;
   GBMV_CUDA_TRY(cudaMemsetAsync(c->d_nfail, 0, sizeof(int), s));
-  rc = chem_dirk(c->P, c->S, c->n, w[5], O, mixed, block, c->d_next, stats, c->d_nfail, s);
+  int rc = mri_fast_launch(h, c, t0, tout, w, time_units, nforcing, forcing, tshift, tscale,
+                           opts, stats, c->d_nfail, s, true);
   if (rc) return rc;
   int nf = 0;
   GBMV_CUDA_TRY(cudaMemcpyAsync(&nf, c->d_nfail, sizeof(int), cudaMemcpyDeviceToHost, s));
   GBMV_CUDA_TRY(cudaStreamSynchronize(s));
   return nf;
+}
+
+int gbmv_mri_fast_evolve_async(gbmv_hydro h, gbmv_chem c, double t0, double tout,
+                               double* const* w, double time_units, int nforcing,
+                               const double* const* forcing, double tshift, double tscale,
+                               const gbmv_dirk_opts* opts, int* stats, int* d_nfail,
+                               void* stream) {
+  if (!d_nfail) { set_error("null failure counter"); return GBMV_EINVAL; }
+  return mri_fast_launch(h, c, t0, tout, w, time_units, nforcing, forcing, tshift, tscale,
+                         opts, stats, d_nfail, (cudaStream_t)stream, false);
 }
 
 static bool capturing(cudaStream_t s) {
@@ -1056,6 +1081,45 @@ int gbmv_wrms_norm(gbmv_hydro h, const double* const* v, const double* const* y,
   GBMV_CUDA_TRY(cudaMemcpyAsync(norm, h->cons + conservation_scratch_doubles() - 2,
                                 sizeof(double), cudaMemcpyDeviceToHost, s));
   GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBMV_OK;
+}
+
+int gbmv_feuler_kink_mask(gbmv_hydro h, const double* const* w, const double* const* dw,
+                          double eps, unsigned char* mask, void* stream) {
+  if (!h || !fields_ok(w, h->g.nchem) || !fields_ok(dw, h->g.nchem) || !mask ||
+      !(eps >= 0.0)) {
+    set_error("null handle, field or mask pointer, or eps < 0");
+    return GBMV_EINVAL;
+  }
+  Fields W, D;
+  for (int k = 0; k < 6; ++k) {
+    W.f[k] = const_cast<double*>(w[k]);
+    D.f[k] = const_cast<double*>(dw[k]);
+  }
+  return feuler_kink_mask(h->g, W, D, eps, mask, (cudaStream_t)stream);
+}
+
+int gbmv_wrms_norm_async(gbmv_hydro h, const double* const* v, const double* const* y,
+                         double rtol, double atol, double* d_norm, void* stream) {
+  if (!h || !fields_ok(v, h->g.nchem) || !fields_ok(y, h->g.nchem) || !d_norm) {
+    set_error("null handle, field or output pointer");
+    return GBMV_EINVAL;
+  }
+  if (!(rtol >= 0.0) || !(atol >= 0.0) || !(rtol > 0.0 || atol > 0.0)) {
+    set_error("rtol, atol must be >= 0 and not both 0");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (int rc = reduction_scratch(h, s, "gbmv_wrms_norm_async")) return rc;
+  Fields V, Y;
+  for (int k = 0; k < 6; ++k) {
+    V.f[k] = const_cast<double*>(v[k]);
+    Y.f[k] = const_cast<double*>(y[k]);
+  }
+  int rc = wrms_norm(h->g, V, Y, rtol, atol, h->cons, s);
+  if (rc) return rc;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(d_norm, h->cons + conservation_scratch_doubles() - 2,
+                                sizeof(double), cudaMemcpyDeviceToDevice, s));
   return GBMV_OK;
 }
 

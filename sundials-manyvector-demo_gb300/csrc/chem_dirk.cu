@@ -227,6 +227,54 @@ __device__ __forceinline__ int dirk_setup(const ChemParams& P, const ChemState& 
   return lu10_strided<LU>(L, BS, piv);
 }
 
+// FP64-residual refinement steps of the FP32 form's per-cell fallback (below).
+constexpr int kFallbackRefine = 2;
+
+// The FP32 form's fallback for a cell whose Newton iteration failed with a current matrix: its
+// later linear solves are refined against FP64 residuals of the Newton matrix
+// I - gp tunit J(Y, Ts(Y)) at the step's state, the Jacobian entries evaluated on the fly
+// (the FP32 layout keeps no FP64 copy of the matrix), the FP32 factor as the preconditioner.
+// Out of line: it runs for a handful of cells and stays out of the common path's code.
+struct RefineIO {
+  double g[10];   // Newton residual (right-hand side)
+  double dl[10];  // correction, refined in place
+  int piv[10];
+};
+
+template <int BS>
+__device__ __noinline__ void dirk_refine_fp64(const ChemParams& P, const ChemState& S, long i,
+                                              const DirkOpts& O, const double* Y,
+                                              const float* L, const short* EQ, double gp,
+                                              double Tsy, double dTsy, RefineIO& io) {
+  const int (&piv)[10] = io.piv;
+  const double (&g)[10] = io.g;
+  double (&dl)[10] = io.dl;
+  const long j = i * 10;
+  double ya[10];
+#pragma unroll
+  for (int s = 0; s < 10; ++s) ya[s] = Y[s * BS] * S.scale[j + s];
+  double k[kNRates], dk[kNRates];
+  chem_rates<true>(P, Tsy, k, dk);
+  const ChemAux Ax{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
+  const double* __restrict__ sc = S.scale + j;
+  const double* __restrict__ isc = S.inv_scale + j;
+  const double mg = -gp * O.tunit;
+  for (int it = 0; it < kFallbackRefine; ++it) {
+    double r[10];
+#pragma unroll
+    for (int s = 0; s < 10; ++s) r[s] = g[s];
+    chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
+      r[row] -= ((row == col ? 1.0 : 0.0) + mg * ((v * isc[row]) * sc[col])) * dl[col];
+    });
+    float u[10];
+#pragma unroll
+    for (int s = 0; s < 10; ++s) u[s] = to_lu<float>(r[s] * pow2(EQ[s * BS]));
+    lus10_strided<float, float>(L, BS, piv, u);
+#pragma unroll
+    for (int s = 0; s < 10; ++s) dl[s] += from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
+  }
+}
+
 template <typename LU, bool REF, int BS>
 __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S, long n,
                                                        double* __restrict__ y_io,
@@ -268,6 +316,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
   int nst = 0, nst_lp = 0, nef_s = 0, ncf_s = 0;
   int c_nni = 0, c_netf = 0, c_ncf = 0, c_nsetup = 0, c_nfe = 0;
   bool jcur = false, force_setup = true, last = false;
+  bool fp64ref = false;  // FP32 form: this cell's solves refined in FP64 (after a failure)
 
   while (true) {
     // ---- refill: lanes without a cell take the next indices (one atomic per warp)
@@ -297,6 +346,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           jcur = false;
           force_setup = true;
           last = false;
+          fp64ref = false;
         } else {
           exhausted = true;
         }
@@ -366,6 +416,20 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
             for (int s = 0; s < 10; ++s) dl[s] += from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
           }
+        } else if (fp64ref) {
+          if constexpr (sizeof(LU) == 4) {
+            // copies in and out keep the common path's vectors in registers
+            RefineIO io;
+#pragma unroll
+            for (int s = 0; s < 10; ++s) {
+              io.g[s] = g[s];
+              io.dl[s] = dl[s];
+              io.piv[s] = piv[s];
+            }
+            dirk_refine_fp64<BS>(P, S, i, O, Y, L, EQ, gp, Tsy, dTsy, io);
+#pragma unroll
+            for (int s = 0; s < 10; ++s) dl[s] = io.dl[s];
+          }
         }
       }
       if (gam != gp) {
@@ -395,8 +459,12 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         if (ncf_s >= O.maxncf) {
           retire = failed = true;
         } else {
-          if (jcur) h *= 0.25;
-          else force_setup = true;
+          if (jcur) {
+            h *= 0.25;
+            fp64ref = sizeof(LU) == 4 && !REF;  // the FP32 factor is not enough for this cell
+          } else {
+            force_setup = true;
+          }
           setup = true;
         }
       } else {

@@ -50,6 +50,11 @@ int feuler_jvp(const Grid& g, const Fields& w, const Fields& dw, const Fields& o
 int feuler_vjp(const Grid& g, const Fields& w, const Fields& v, const Fields& out, double* A,
                cudaStream_t s);
 
+// cells one of whose six faces changes its Lax-Friedrichs branch (maximising stencil point,
+// sign of its velocity) between w - h dw, w and w + h dw: mask[cell] = 1 (weno_kinks.cu)
+int feuler_kink_mask(const Grid& g, const Fields& w, const Fields& dw, double h,
+                     unsigned char* mask, cudaStream_t s);
+
 // float-float form (weno_f2.cu)
 size_t feuler_f2_prims_floats(const Grid& g);
 // tscale: null, or the per-entry scale of a chemistry component held in scaled units

@@ -437,7 +437,7 @@ def run_multirate(inp: Inputs, problem, tables, outdir: str = ".",
     prec = gbmv.FP64 if precision is None else precision
     dtout = (u["tf"] - t0) / u["nout"]
     hslow = o["h0"] if o["h0"] > 0 else dtout
-    fast = dict(rtol=o["rtol"], atol=o["atol"], table=o["itable"])
+    fast = dict(rtol=o["rtol"], atol=o["atol"], itable=o["itable"])
     for key, name in (("maxniters", "maxcor"), ("nlconvcoef", "nlscoef"), ("hmax", "hmax"),
                       ("safety", "safety"), ("growth", "growth"), ("etamx1", "etamx1"),
                       ("maxnef", "maxnef"), ("mxsteps", "max_steps")):

@@ -58,6 +58,18 @@ class _Butcher(C.Structure):
                 ("name", C.c_char * 32)]
 
 
+class _StepParams(C.Structure):
+    """gbmv_step_params (include/gbmv.h)."""
+    _fields_ = [(k, C.c_double) for k in ("hmax", "safety", "bias", "growth", "etamx1",
+                                          "etamxf", "k1", "k2", "k3")] + \
+               [(k, C.c_int) for k in ("order", "small_nef", "maxnef", "max_attempts", "fixed")]
+
+
+# indices of the device step state (GBMV_ST_* of include/gbmv.h)
+ST = dict(t=0, h=1, h_used=2, accept=3, done=4, e1=5, e2=6, first=7, nef=8, steps=9,
+          attempts=10, fails=11, status=12, last=13, h_prop=14, tf=15)
+STEP_STATE = 16
+
 _P = C.POINTER(C.c_double)
 _VP = C.c_void_p
 
@@ -116,9 +128,19 @@ SIGNATURES = [
     ("gbmv_mri_fast_evolve", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.POINTER(_VP),
                                        C.c_double, C.c_int, C.POINTER(_VP), C.c_double,
                                        C.c_double, C.POINTER(_DirkOpts), _VP, _VP]),
+    ("gbmv_mri_fast_evolve_async", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.POINTER(_VP),
+                                             C.c_double, C.c_int, C.POINTER(_VP), C.c_double,
+                                             C.c_double, C.POINTER(_DirkOpts), _VP, _VP, _VP]),
     ("gbmv_ffast", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
                              C.c_int, C.POINTER(_VP), C.c_double, C.c_double, _VP]),
     ("gbmv_postprocess_step", C.c_int, [_VP, _VP, C.POINTER(_VP), C.c_double, _VP]),
+    ("gbmv_step_begin", C.c_int, [_VP, C.POINTER(_StepParams), _VP]),
+    ("gbmv_step_end", C.c_int, [_VP, _VP, C.POINTER(_StepParams), _VP]),
+    ("gbmv_step_select", C.c_int, [C.c_long, _VP, _VP, _VP, _VP]),
+    ("gbmv_feuler_kink_mask", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.c_double, _VP,
+                                        _VP]),
+    ("gbmv_wrms_norm_async", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
+                                       C.c_double, _VP, _VP]),
     ("gbmv_butcher_table", C.c_int, [C.c_int, C.POINTER(_Butcher)]),
     ("gbmv_erk_default_table", C.c_int, [C.c_int]),
     ("gbmv_version", C.c_char_p, []),
@@ -248,6 +270,21 @@ class Hydro:
         _check(load().gbmv_wrms_norm(self.h, _vec(v), _vec(y), rtol, atol, out,
                                      _stream_ptr(stream)), "gbmv_wrms_norm")
         return out[0]
+
+    def kink_mask(self, w, dw, eps, mask, stream=None):
+        """gbmv_feuler_kink_mask into `mask` (CUDA uint8 tensor of ncells): 1 where a central
+        difference of fEuler along dw with step eps crosses a Lax-Friedrichs branch."""
+        import torch
+        ncell = self.shape[0] * self.shape[1] * self.shape[2]
+        if mask.dtype != torch.uint8 or not mask.is_cuda or mask.numel() != ncell:
+            raise GbmvError("mask must be a CUDA uint8 tensor of ncells")
+        _check(load().gbmv_feuler_kink_mask(self.h, _vec(w), _vec(dw), eps, mask.data_ptr(),
+                                            _stream_ptr(stream)), "gbmv_feuler_kink_mask")
+
+    def wrms_norm_async(self, v, y, rtol, atol, out, stream=None):
+        """gbmv_wrms_norm_async: the norm into the 1-element CUDA float64 tensor `out`."""
+        _check(load().gbmv_wrms_norm_async(self.h, _vec(v), _vec(y), rtol, atol, _dev_ptr(out),
+                                           _stream_ptr(stream)), "gbmv_wrms_norm_async")
 
     def print_stats(self, w, units=(1.0, 1.0, 1.0), stream=None):
         """Per-field RMS over the grid as print_stats (src/io.cpp:552) computes it; units =
@@ -395,6 +432,33 @@ def dirk_opts(**kw) -> _DirkOpts:
     return o
 
 
+def step_params(order, hmax=0.0, safety=0.96, bias=1.5, growth=20.0, etamx1=1e4,
+                etamxf=0.3, k1=0.58, k2=0.21, k3=0.1, small_nef=2, maxnef=7,
+                max_attempts=100000, fixed=False) -> _StepParams:
+    """gbmv_step_params (ARKODE's defaults: the PID controller)."""
+    p = _StepParams()
+    p.hmax, p.safety, p.bias, p.growth = hmax, safety, bias, growth
+    p.etamx1, p.etamxf, p.k1, p.k2, p.k3 = etamx1, etamxf, k1, k2, k3
+    p.order, p.small_nef, p.maxnef, p.max_attempts = order, small_nef, maxnef, max_attempts
+    p.fixed = int(bool(fixed))
+    return p
+
+
+def step_begin(state, params, stream=None):
+    _check(load().gbmv_step_begin(_dev_ptr(state), C.byref(params), _stream_ptr(stream)),
+           "gbmv_step_begin")
+
+
+def step_end(state, dsm, params, stream=None):
+    _check(load().gbmv_step_end(_dev_ptr(state), _dev_ptr(dsm), C.byref(params),
+                                _stream_ptr(stream)), "gbmv_step_end")
+
+
+def step_select(state, y, ynew, stream=None):
+    _check(load().gbmv_step_select(y.numel(), _dev_ptr(state), _dev_ptr(y), _dev_ptr(ynew),
+                                   _stream_ptr(stream)), "gbmv_step_select")
+
+
 def butcher_table(table_id: int) -> dict:
     """The Runge-Kutta table of ARKODE number `table_id` (gbmv_butcher_table): dict with name,
     s, q (method order), p (embedding order), c, A (rows, diagonal included), b, bhat.
@@ -512,6 +576,22 @@ def mri_fast_evolve(hydro: Hydro, chem: Chem, t0, tout, w, time_units, forcing=(
                                               stats.data_ptr() if stats is not None else None,
                                               _stream_ptr(stream)),
                   "gbmv_mri_fast_evolve", allow=range(0, chem.n + 1))
+
+
+def mri_fast_evolve_async(hydro: Hydro, chem: Chem, t0, tout, w, time_units, nfail, forcing=(),
+                          tshift=0.0, tscale=1.0, stats=None, stream=None, **opts) -> int:
+    """gbmv_mri_fast_evolve_async: graph-capturable; failed cells added to nfail (CUDA int32);
+    opts must fix `block` (or an earlier synchronous call must have tuned it)."""
+    nf = len(forcing)
+    arr = (_VP * max(1, 6 * nf))()
+    for i, fv in enumerate(forcing):
+        for k, comp in enumerate(fv):
+            arr[6 * i + k] = _dev_ptr(comp)
+    o = dirk_opts(**opts)
+    return _check(load().gbmv_mri_fast_evolve_async(
+        hydro.h, chem.c, t0, tout, _vec(w), time_units, nf, arr if nf else None, tshift, tscale,
+        C.byref(o), stats.data_ptr() if stats is not None else None, nfail.data_ptr(),
+        _stream_ptr(stream)), "gbmv_mri_fast_evolve_async")
 
 
 def PostprocessStep(hydro: Hydro, chem: Chem, w, energy_units, stream=None):

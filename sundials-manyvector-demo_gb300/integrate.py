@@ -178,6 +178,127 @@ def erk_evolve(rhs, t0, tf, y0, rtol=1e-6, atol=1e-11, h0=0.0, hmax=math.inf,
     return y, st
 
 
+class GraphERK:
+    """erk_evolve with every step one CUDA graph: the stages (right-hand sides and linear
+    combinations), the embedded error's WRMS norm, ARKODE's controller and the accept / reject
+    selection all run on the device (gbmv_step_begin / _end / _select, gbmv_wrms_norm_async),
+    captured once and replayed; the host replays `batch` steps at a time and reads the step
+    state (16 doubles) between batches, so no step waits for the host.
+
+      rhs_async(y, out)        enqueue out = f(y) on the current stream (flat CUDA float64
+                               tensors; graph-capturable; illegal states reported through
+                               the caller's own device status word, read by `status()`)
+      norm_async(v, y, out)    enqueue the WRMS norm of v with weights from y into out[0]
+    `y` (a flat CUDA float64 tensor) is advanced in place.  The table is any explicit table
+    of gbmv_butcher_table (default ARKODE's order-4 Zonneveld 5-3-4); the stage derivative at
+    the step start is evaluated in every step graph (no FSAL reuse).  adapt: Controller
+    options (adapt_method, k1, k2, k3, pq, safety, bias, growth, etamx1, etamxf, small_nef).
+    Replays after the end time are no-ops apart from their launches (at most batch - 1).
+    The graph is captured at the first `evolve` (its first step run eagerly outside the
+    capture) and reused by later calls with the same controller settings, whatever the
+    interval."""
+
+    def __init__(self, rhs_async, norm_async, y, table=3, hmax=0.0, fixed_h=0.0, batch=16,
+                 max_attempts=100000, maxnef=7, status=None, **adapt):
+        import torch
+        import gbmv
+        self.g, self.torch = gbmv, torch
+        self.T = butcher(table) if not isinstance(table, dict) else table
+        T = self.T
+        ctl = Controller(T["p"], T["q"], **adapt)
+        self.rhs, self.norm, self.y, self.batch = rhs_async, norm_async, y, batch
+        self.status_fn = status
+        self.fixed_h, self.hmax = fixed_h, hmax
+        self.ctl, self.max_attempts, self.maxnef = ctl, max_attempts, maxnef
+        s = T["s"]
+        coef = [T["A"][i][j] for i in range(s) for j in range(s)] + list(T["b"]) + \
+               [bi - bhi for bi, bhi in zip(T["b"], T["bhat"])]
+        dev = y.device
+        self.coef = torch.tensor(coef, dtype=torch.float64, device=dev)
+        self.hc = torch.empty_like(self.coef)
+        self.k = [torch.empty_like(y) for _ in range(s)]
+        self.ys, self.ynew, self.err = (torch.empty_like(y) for _ in range(3))
+        self.dsm = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.state = torch.zeros(gbmv.STEP_STATE, dtype=torch.float64, device=dev)
+        self.graph, self.params = None, None
+
+    def _body(self):
+        g, T, s = self.g, self.T, self.T["s"]
+        A, b = T["A"], T["b"]
+        e = [bi - bhi for bi, bhi in zip(T["b"], T["bhat"])]
+        g.step_begin(self.state, self.params)
+        ST = g.ST
+        self.torch.mul(self.coef, self.state[ST["h_used"]:ST["h_used"] + 1], out=self.hc)
+        hc = self.hc
+        self.rhs(self.y, self.k[0])
+        for i in range(1, s):
+            self.ys.copy_(self.y)
+            for j in range(i):
+                if A[i][j] != 0.0:
+                    self.ys.addcmul_(self.k[j], hc[i * s + j])
+            self.rhs(self.ys, self.k[i])
+        self.ynew.copy_(self.y)
+        for j in range(s):
+            if b[j] != 0.0:
+                self.ynew.addcmul_(self.k[j], hc[s * s + j])
+        self.err.zero_()
+        for j in range(s):
+            if e[j] != 0.0:
+                self.err.addcmul_(self.k[j], hc[s * s + s + j])
+        self.norm(self.err, self.y, self.dsm)
+        g.step_end(self.state, self.dsm, self.params)
+        g.step_select(self.state, self.y, self.ynew)
+
+    def evolve(self, t0, tf, h0):
+        """Advance y from t0 to tf starting with step h0 (> 0); returns an ERKResult."""
+        torch, g = self.torch, self.g
+        c = self.ctl
+        fixed = self.fixed_h > 0.0
+        p = g.step_params(c.ord, hmax=self.hmax if self.hmax < math.inf else 0.0,
+                          safety=c.safety, bias=c.bias, growth=c.growth, etamx1=c.etamx1,
+                          etamxf=c.etamxf, k1=c.k[0], k2=c.k[1], k3=c.k[2],
+                          small_nef=c.small_nef, maxnef=self.maxnef,
+                          max_attempts=self.max_attempts, fixed=fixed)
+        st0 = [0.0] * g.STEP_STATE
+        ST = g.ST
+        st0[ST["t"]], st0[ST["tf"]] = t0, tf
+        st0[ST["h"]] = self.fixed_h if fixed else h0
+        st0[ST["first"]], st0[ST["e1"]], st0[ST["e2"]] = 1.0, 1.0, 1.0
+        self.state.copy_(torch.tensor(st0, dtype=torch.float64))
+        if self.graph is None or self.params is None or \
+                bytes(self.params) != bytes(p):  # (re)capture for these parameters
+            self.params = p
+            y_save = self.y.clone()
+            self._body()  # eager first step: first-use allocations happen outside the capture
+            torch.cuda.synchronize()
+            self.y.copy_(y_save)
+            self.state.copy_(torch.tensor(st0, dtype=torch.float64))
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=side):
+                self._body()
+            torch.cuda.synchronize()
+        res = ERKResult()
+        while True:
+            for _ in range(self.batch):
+                self.graph.replay()
+            st = self.state.cpu().tolist()
+            if self.status_fn is not None and self.status_fn():
+                raise RuntimeError("right-hand side reported an illegal state")
+            if st[ST["status"]] < 0:
+                raise RuntimeError("GraphERK: " + ("too many error-test failures in one step"
+                                                   if st[ST["status"]] == -1 else
+                                                   "max_attempts reached"))
+            if st[ST["done"]] != 0.0:
+                break
+        res.steps = int(st[ST["steps"]])
+        res.fails = int(st[ST["fails"]])
+        res.nfe = int(st[ST["attempts"]]) * self.T["s"]
+        res.h_next = st[ST["h"]]
+        return res
+
+
 class _ExplicitProblem:
     """The problem protocol of _initial_step for one explicit right-hand side."""
 
@@ -320,7 +441,8 @@ FORCING_UNITS = ("reference", "scaled")
 
 
 def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=MRI_KW3,
-               precision=0, slow_rhs=None, forcing_units="reference", **fast_opts):
+               precision=0, slow_rhs=None, forcing_units="reference", itable=112,
+               **fast_opts):
     """Multirate chemistry-hydrodynamics integration (the MRIStep driver of
     src/multirate_chem_hydro_main.cpp) with a fixed slow step h and an explicit MRI-GARK
     coupling `table`, by default MIS-KW3, MRIStep's default third-order explicit coupling that
@@ -338,8 +460,8 @@ def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=
     "scaled" converts the forcing to the scaled variables first -- species tendencies divided
     by scale, the gas-energy slot EnergyUnits * etdot / scale (`scaled_forcing`) -- which makes
     the coupling dimensionally consistent, a departure from the reference to select
-    explicitly.  fast_opts: gbmv_dirk_opts fields of the inner DIRK (table = the inputs'
-    itable, 112 by default)."""
+    explicitly.  itable: the inner DIRK's table (the inputs' itable: 112 ARK4(3)7L[2]SA or 102
+    TR-BDF2); fast_opts: the other gbmv_dirk_opts fields of the inner DIRK."""
     import torch
     if forcing_units not in FORCING_UNITS:
         raise ValueError(f"forcing_units must be one of {FORCING_UNITS}")
@@ -357,9 +479,118 @@ def mri_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units, table=
 
     def fast(ta, tb, y, forcing, tshift, tscale):
         return gbmv.mri_fast_evolve(hydro, chem, ta, tb, y, time_units, forcing, tshift, tscale,
-                                    precision=precision, **fast_opts)
+                                    precision=precision, table=itable, **fast_opts)
 
     return mri_gark_evolve(fs, fast, t0, tf, w, h, table)
+
+
+class GraphMRI:
+    """mri_evolve with every slow step one CUDA graph: the slow right-hand sides
+    (gbmv_fexpl_async), the stage forcing polynomials (linear combinations into preallocated
+    ManyVectors) and the fast evolves (gbmv_mri_fast_evolve_async, the persistent DIRK) of all
+    stages are captured once and replayed per slow step; illegal states and failed cells land
+    in device words read once per `evolve` call.  The chemistry network is autonomous, so each
+    stage's inner problem runs on local time [0, dc h] with tshift 0 and tscale dc h (the same
+    forcing polynomial as tau = (t - T_{i-1}) / (dc h)), which makes every slow step's graph
+    the same.  Options as mri_evolve; fast_opts must allow the DIRK block size to be tuned
+    by the eager first step (block 0) or fix it."""
+
+    def __init__(self, gbmv, hydro, chem, w, h, energy_units, time_units, table=MRI_KW3,
+                 precision=0, forcing_units="reference", itable=112, **fast_opts):
+        import torch
+        if forcing_units not in FORCING_UNITS:
+            raise ValueError(f"forcing_units must be one of {FORCING_UNITS}")
+        self.g, self.torch = gbmv, torch
+        self.hydro, self.chem, self.w, self.h = hydro, chem, w, h
+        self.eu, self.tu, self.table, self.precision = energy_units, time_units, table, precision
+        self.units, self.fast_opts = forcing_units, dict(fast_opts, table=itable)
+        dev = w[0].device
+        sizes = [x.numel() for x in w]
+        self.sizes = sizes
+        ns = len(table["c"])
+
+        def mv():
+            flat = torch.empty(sum(sizes), dtype=torch.float64, device=dev)
+            return flat, [v.view(x.shape) for v, x in zip(torch.split(flat, sizes), w)]
+        self.F = [mv() for _ in range(ns - 1)]
+        self.force = [[mv() for _ in table["G"]] for _ in range(ns)]
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.nfail = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.inv9 = chem.state("inv_scale").view(-1, 10)[:, :9]
+        self.inv_ge = chem.state("inv_scale").view(-1, 10)[:, 9] * energy_units
+        self.graph = None
+
+    def _slow(self, j):
+        flat, comps = self.F[j]
+        self.g.fexpl_async(self.hydro, self.chem, 0.0, self.w, comps, self.eu, self.status,
+                           self.precision)
+        if self.units == "scaled":
+            c5 = comps[5].view(-1, 10)
+            c5[:, :9].mul_(self.inv9)
+            c5[:, 9].mul_(self.inv_ge)
+
+    def _body(self):
+        c, G, h = self.table["c"], self.table["G"], self.h
+        ns = len(c)
+        self._slow(0)
+        for i in range(1, ns):
+            dc = c[i] - c[i - 1]
+            forcing = []
+            for q, Gk in enumerate(G):
+                row = Gk[i - 1]
+                flat, comps = self.force[i][q]
+                flat.zero_()
+                for j in range(len(row)):
+                    if row[j] != 0.0:
+                        flat.add_(self.F[j][0], alpha=row[j] / dc)
+                forcing.append(comps)
+            while len(forcing) > 1 and all(v == 0.0 for v in G[len(forcing) - 1][i - 1]):
+                forcing.pop()  # drop vanishing top powers for this stage
+            self.g.mri_fast_evolve_async(self.hydro, self.chem, 0.0, dc * h, self.w, self.tu,
+                                         self.nfail, forcing, 0.0, dc * h,
+                                         precision=self.precision, **self.fast_opts)
+            if i < ns - 1:
+                self._slow(i)
+
+    def evolve(self, t0, tf):
+        """Advance w by whole slow steps from t0 to tf; returns an MRIResult."""
+        torch = self.torch
+        nsteps = int(round((tf - t0) / self.h))
+        if nsteps < 1 or abs(nsteps * self.h - (tf - t0)) > 1e-12 * max(abs(tf), 1.0):
+            raise ValueError("tf - t0 must be a whole number of slow steps")
+        res = MRIResult()
+        ns = len(self.table["c"])
+        start = 0
+        if self.graph is None:
+            # the first step eagerly: the DIRK block-size tuning and first-use allocations
+            # happen outside the capture
+            if not self.fast_opts.get("block"):  # tune on copies of the state
+                keep = [self.chem.state(k).clone() for k in ("Ts", "dTs_ge")]
+                self.g.mri_fast_evolve(self.hydro, self.chem, 0.0, self.h * 1e-6,
+                                       [x.clone() for x in self.w], self.tu,
+                                       precision=self.precision, **self.fast_opts)
+                for k, v in zip(("Ts", "dTs_ge"), keep):
+                    self.chem.state(k).copy_(v)
+                self.fast_opts["block"] = self.chem.dirk_block(self.precision)
+            self._body()
+            torch.cuda.synchronize()
+            start = 1
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=side):
+                self._body()
+            torch.cuda.synchronize()
+        for _ in range(start, nsteps):
+            self.graph.replay()
+        st, nf = int(self.status.item()), int(self.nfail.item())
+        if st:
+            raise RuntimeError(f"slow RHS: illegal state (mask {st})")
+        res.slow_steps = nsteps
+        res.slow_rhs = nsteps * (ns - 1)
+        res.fast_failed_cells = nf
+        self.nfail.zero_()
+        return res
 
 
 def mri_erk22b_evolve(gbmv, hydro, chem, w, t0, tf, h, energy_units, time_units,

