@@ -361,6 +361,18 @@ int gbmv_block_lu_factor(long nblocks, double* A, int* pivots, void* stream);
 int gbmv_block_lu_solve(long nblocks, const double* LU, const int* pivots, const double* b,
                         double* x, void* stream);
 
+/* The same solver as a handle that owns its pivots (10 ints per block) and its own
+ * singular-block word, the content a SUNLinearSolver built over these calls keeps
+ * (SUNLinSol_RankLocalLS / SUNLinSol_BDMPIMV's block solver, src/multirate_chem_hydro_main.cpp:
+ * 1312-1411).  setup factors A in place (synchronous, returns 0 or 1 for a singular block);
+ * solve is asynchronous. */
+typedef struct gbmv_block_ls_s* gbmv_block_ls;
+int gbmv_block_ls_create(long nblocks, gbmv_block_ls* out);
+int gbmv_block_ls_destroy(gbmv_block_ls ls);
+int gbmv_block_ls_setup(gbmv_block_ls ls, double* A, void* stream);
+int gbmv_block_ls_solve(gbmv_block_ls ls, const double* LU, const double* b, double* x,
+                        void* stream);
+
 /* ARKLS's Newton matrix A = I - gamma*J (SUNMatScaleAddI) for dense blocks, in place. */
 int gbmv_block_form_newton(long nblocks, double* J, double gamma, void* stream);
 

@@ -767,6 +767,58 @@ int gbmv_block_lu_factor(long nblocks, double* A, int* pivots, void* stream) {
   return GBMV_OK;
 }
 
+// Block linear solver handle: owns the pivots and its own singular-block word.
+struct gbmv_block_ls_s {
+  long nblocks = 0;
+  int* pivots = nullptr;
+  int* d_info = nullptr;
+};
+
+int gbmv_block_ls_create(long nblocks, gbmv_block_ls* out) {
+  if (!out || nblocks <= 0) { set_error("bad block solver arguments"); return GBMV_EINVAL; }
+  *out = nullptr;
+  gbmv_block_ls L = new (std::nothrow) gbmv_block_ls_s();
+  if (!L) return GBMV_ENOMEM;
+  L->nblocks = nblocks;
+  if (cudaMalloc(&L->pivots, sizeof(int) * 10 * nblocks) != cudaSuccess ||
+      cudaMalloc(&L->d_info, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(L->pivots);
+    delete L;
+    set_error("device allocation of the block solver's pivots failed");
+    return GBMV_ENOMEM;
+  }
+  *out = L;
+  return GBMV_OK;
+}
+
+int gbmv_block_ls_destroy(gbmv_block_ls L) {
+  if (!L) return GBMV_OK;
+  cudaFree(L->pivots);
+  cudaFree(L->d_info);
+  delete L;
+  return GBMV_OK;
+}
+
+int gbmv_block_ls_setup(gbmv_block_ls L, double* A, void* stream) {
+  if (!L || !A) { set_error("null block solver or matrix"); return GBMV_EINVAL; }
+  cudaStream_t s = (cudaStream_t)stream;
+  GBMV_CUDA_TRY(cudaMemsetAsync(L->d_info, 0, sizeof(int), s));
+  int rc = block_lu_factor(L->nblocks, A, L->pivots, L->d_info, s);
+  if (rc) return rc;
+  int h = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&h, L->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h) { set_error("singular block"); return 1; }
+  return GBMV_OK;
+}
+
+int gbmv_block_ls_solve(gbmv_block_ls L, const double* LU, const double* b, double* x,
+                        void* stream) {
+  if (!L || !LU || !b || !x) { set_error("bad block solve arguments"); return GBMV_EINVAL; }
+  return block_lu_solve(L->nblocks, LU, L->pivots, b, x, (cudaStream_t)stream);
+}
+
 int gbmv_block_lu_solve(long nblocks, const double* LU, const int* pivots, const double* b,
                         double* x, void* stream) {
   if (nblocks <= 0 || !LU || !pivots || !b || !x) { set_error("bad solve arguments"); return GBMV_EINVAL; }

@@ -461,7 +461,9 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         } else {
           if (jcur) {
             h *= 0.25;
-            fp64ref = sizeof(LU) == 4 && !REF;  // the FP32 factor is not enough for this cell
+            // a second failure with a current matrix in one step: the FP32 factor is not
+            // enough for this cell; refine its solves in FP64 from now on
+            if (ncf_s >= 2) fp64ref = sizeof(LU) == 4 && !REF;
           } else {
             force_setup = true;
           }

@@ -97,13 +97,14 @@ __global__ void __launch_bounds__(256) divergence_kernel(Grid g, Fields w, Field
 int divergence(const Grid& g, const Fields& w, const Fields& wdot, double* const (&F)[3],
                const ForceTerm& G, int* d_status, cudaStream_t s) {
   ProfScope ps("divergence", s);
-  const int b = sweep_blocks(g.ncell, 256);
+  const int t = spread_threads(g.ncell, 256);
+  const int b = sweep_blocks(g.ncell, t);
   switch (g.nchem) {
-    case 0: divergence_kernel<0><<<b, 256, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
-    case 2: divergence_kernel<2><<<b, 256, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
-    case 4: divergence_kernel<4><<<b, 256, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
-    case 6: divergence_kernel<6><<<b, 256, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
-    case 10: divergence_kernel<10><<<b, 256, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
+    case 0: divergence_kernel<0><<<b, t, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
+    case 2: divergence_kernel<2><<<b, t, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
+    case 4: divergence_kernel<4><<<b, t, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
+    case 6: divergence_kernel<6><<<b, t, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
+    case 10: divergence_kernel<10><<<b, t, 0, s>>>(g, w, wdot, F[0], F[1], F[2], G, d_status); break;
     default: set_error("nchem=%d not compiled (0,2,4,6,10)", g.nchem); return GBMV_EUNSUPPORTED;
   }
   GBMV_LAUNCH_CHECK("divergence_kernel");
@@ -178,17 +179,20 @@ static int launch_fp64(const Grid& g, const Fields& w, const Fields& wdot, const
                   scratch + (long)(5 + NCHEM) * (nf[0] + nf[1])};
   {
     ProfScope ps("face_flux", s);
-    face_flux_kernel<NCHEM, 0><<<sweep_blocks(nf[0], 128), 128, 0, s>>>(g, w, F[0], nf[0]);
+    const int t = spread_threads(nf[0], 128);
+    face_flux_kernel<NCHEM, 0><<<sweep_blocks(nf[0], t), t, 0, s>>>(g, w, F[0], nf[0]);
     GBMV_LAUNCH_CHECK("face_flux_kernel<x>");
   }
   {
     ProfScope ps("face_flux", s);
-    face_flux_kernel<NCHEM, 1><<<sweep_blocks(nf[1], 128), 128, 0, s>>>(g, w, F[1], nf[1]);
+    const int t = spread_threads(nf[1], 128);
+    face_flux_kernel<NCHEM, 1><<<sweep_blocks(nf[1], t), t, 0, s>>>(g, w, F[1], nf[1]);
     GBMV_LAUNCH_CHECK("face_flux_kernel<y>");
   }
   {
     ProfScope ps("face_flux", s);
-    face_flux_kernel<NCHEM, 2><<<sweep_blocks(nf[2], 128), 128, 0, s>>>(g, w, F[2], nf[2]);
+    const int t = spread_threads(nf[2], 128);
+    face_flux_kernel<NCHEM, 2><<<sweep_blocks(nf[2], t), t, 0, s>>>(g, w, F[2], nf[2]);
     GBMV_LAUNCH_CHECK("face_flux_kernel<z>");
   }
   return divergence(g, w, wdot, F, G, d_status, s);

@@ -80,6 +80,17 @@ inline int sweep_blocks(long n, int t) {
   return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
+// Threads per block of a one-item-per-thread pass over n items whose kernel allows up to
+// tmax: the largest of tmax, tmax/2, ..., 32 that still gives every SM two blocks, so that a
+// small grid (the Sod tube's ~1200 faces) spreads over as many SMs as it can fill instead of
+// queueing its FP64 work on a few of them; large grids keep tmax.  Each item is computed by
+// one thread independently, so the results do not depend on the choice.
+inline int spread_threads(long n, int tmax) {
+  int t = tmax;
+  while (t > 32 && n < 2L * kSM * t) t /= 2;
+  return t;
+}
+
 // faces normal to x, y, z
 inline void face_counts(const Grid& g, long (&nf)[3]) {
   const long nx = g.n[0], ny = g.n[1], nz = g.n[2];

@@ -110,6 +110,10 @@ SIGNATURES = [
     ("gbmv_block_lu_factor", C.c_int, [C.c_long, _VP, _VP, _VP]),
     ("gbmv_block_lu_solve", C.c_int, [C.c_long, _VP, _VP, _VP, _VP, _VP]),
     ("gbmv_block_form_newton", C.c_int, [C.c_long, _VP, C.c_double, _VP]),
+    ("gbmv_block_ls_create", C.c_int, [C.c_long, C.POINTER(_VP)]),
+    ("gbmv_block_ls_destroy", C.c_int, [_VP]),
+    ("gbmv_block_ls_setup", C.c_int, [_VP, _VP, _VP]),
+    ("gbmv_block_ls_solve", C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     ("gbmv_fexpl", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.c_double,
                              C.c_int, _VP]),
     ("gbmv_fexpl_async", C.c_int, [_VP, _VP, C.c_double, C.POINTER(_VP), C.POINTER(_VP),
@@ -492,26 +496,31 @@ def _wrap_device(ptr: int, n: int):
 
 class BlockLinearSolver:
     """Block-diagonal direct solver on the chemistry subvector (SUNLinSol_RankLocalLS /
-    SUNLinSol_BDMPIMV over the batched dense LU): setup factors A in place."""
+    SUNLinSol_BDMPIMV over the batched dense LU, gbmv_block_ls): setup factors A in place;
+    the handle owns the pivots and its singular-block word."""
 
     def __init__(self, nblocks: int):
-        import torch
         self.nb = nblocks
-        self.piv = torch.zeros(nblocks * 10, dtype=torch.int32, device="cuda")
+        h = _VP()
+        _check(load().gbmv_block_ls_create(nblocks, C.byref(h)), "gbmv_block_ls_create")
+        self.ls = h
         self.last_flag = 0
 
+    def __del__(self):
+        if getattr(self, "ls", None) and _lib is not None:
+            _lib.gbmv_block_ls_destroy(self.ls)
+            self.ls = None
+
     def setup(self, A, stream=None) -> int:
-        self.last_flag = _check(load().gbmv_block_lu_factor(self.nb, _dev_ptr(A),
-                                                            self.piv.data_ptr(),
-                                                            _stream_ptr(stream)),
-                                "gbmv_block_lu_factor", allow=(0, 1))
+        self.last_flag = _check(load().gbmv_block_ls_setup(self.ls, _dev_ptr(A),
+                                                           _stream_ptr(stream)),
+                                "gbmv_block_ls_setup", allow=(0, 1))
         return self.last_flag
 
     def solve(self, A, x, b, tol=0.0, stream=None) -> int:
-        self.last_flag = _check(load().gbmv_block_lu_solve(self.nb, _dev_ptr(A), self.piv.data_ptr(),
-                                                           _dev_ptr(b), _dev_ptr(x),
-                                                           _stream_ptr(stream)),
-                                "gbmv_block_lu_solve")
+        self.last_flag = _check(load().gbmv_block_ls_solve(self.ls, _dev_ptr(A), _dev_ptr(b),
+                                                           _dev_ptr(x), _stream_ptr(stream)),
+                                "gbmv_block_ls_solve")
         return self.last_flag
 
 

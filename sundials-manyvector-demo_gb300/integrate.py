@@ -911,6 +911,65 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
     return st
 
 
+def batched_gmres(matvec, b, m=10, rtol=1e-13):
+    """Matrix-free GMRES on many independent small systems at once: b is [ncell, k] (one
+    right-hand side of k entries per cell), matvec(v) applies every cell's operator to the
+    rows of v ([ncell, k]).  Each cell builds its own Krylov basis (Arnoldi with modified
+    Gram-Schmidt and one re-orthogonalisation, Givens rotations on its Hessenberg matrix), all
+    cells advancing together, one matvec per iteration for all of them; at most m iterations
+    (m = k solves each system exactly in exact arithmetic), fewer once every cell's residual
+    is below rtol times its |b|.  Returns (x [ncell, k], iterations)."""
+    import torch
+    n, k = b.shape
+    m = min(m, k)
+    dt = b.dtype
+    beta = torch.linalg.vector_norm(b, dim=1)
+    safe = torch.where(beta > 0, beta, torch.ones_like(beta))
+    V = [b / safe[:, None]]
+    H = torch.zeros(n, m + 1, m, dtype=dt, device=b.device)
+    cs = torch.zeros(n, m, dtype=dt, device=b.device)
+    sn = torch.zeros(n, m, dtype=dt, device=b.device)
+    g = torch.zeros(n, m + 1, dtype=dt, device=b.device)
+    g[:, 0] = beta
+    it = 0
+    for j in range(m):
+        w = matvec(V[j])
+        for _ in range(2):  # modified Gram-Schmidt, twice
+            for i in range(j + 1):
+                hij = (w * V[i]).sum(dim=1)
+                H[:, i, j] += hij
+                w = w - hij[:, None] * V[i]
+        hn = torch.linalg.vector_norm(w, dim=1)
+        H[:, j + 1, j] = hn
+        V.append(w / torch.where(hn > 0, hn, torch.ones_like(hn))[:, None])
+        for i in range(j):  # earlier rotations on the new column
+            a, c = H[:, i, j].clone(), H[:, i + 1, j].clone()
+            H[:, i, j] = cs[:, i] * a + sn[:, i] * c
+            H[:, i + 1, j] = -sn[:, i] * a + cs[:, i] * c
+        a, c = H[:, j, j], H[:, j + 1, j]
+        r = torch.sqrt(a * a + c * c)
+        rs = torch.where(r > 0, r, torch.ones_like(r))
+        cs[:, j] = torch.where(r > 0, a / rs, torch.ones_like(r))
+        sn[:, j] = torch.where(r > 0, c / rs, torch.zeros_like(r))
+        H[:, j, j] = r
+        H[:, j + 1, j] = 0.0
+        g[:, j + 1] = -sn[:, j] * g[:, j]
+        g[:, j] = cs[:, j] * g[:, j]
+        it = j + 1
+        if bool((g[:, j + 1].abs() <= rtol * beta).all()):
+            break
+    R = H[:, :it, :it]
+    diag = torch.diagonal(R, dim1=1, dim2=2)
+    dead = diag == 0  # a cell whose Krylov space closed earlier: those components are 0
+    R = R + torch.diag_embed(dead.to(dt))
+    gy = torch.where(dead, torch.zeros_like(g[:, :it]), g[:, :it])
+    y = torch.linalg.solve_triangular(R, gy[:, :, None], upper=True)[:, :, 0]
+    x = torch.zeros_like(b)
+    for i in range(it):
+        x = x + y[:, i:i + 1] * V[i]
+    return x, it
+
+
 class ChemHydroImex:
     """The reference's IMEX splitting (src/imex_chem_hydro_main.cpp) over the drop-in entry
     points, all on the device: fe = fexpl (WENO flux divergence of every field and the
@@ -925,10 +984,19 @@ class ChemHydroImex:
     kernel's full Newton corrections."""
 
     def __init__(self, gbmv, hydro, chem, energy_units, time_units, rtol, atol, precision=0,
-                 fused_newton=False, lu_precision=1, refine=4, forcing_units="reference"):
+                 fused_newton=False, lu_precision=1, refine=4, forcing_units="reference",
+                 linear_solver="direct"):
         import torch
         if forcing_units not in FORCING_UNITS:
             raise ValueError(f"forcing_units must be one of {FORCING_UNITS}")
+        if linear_solver not in ("direct", "gmres"):
+            raise ValueError("linear_solver must be 'direct' or 'gmres'")
+        # "gmres": matrix-free Newton-Krylov -- each stage correction solves
+        # (I - gamma J(z)) x = b per cell by batched GMRES whose Jacobian actions are
+        # gbmv_chem_jvp at the current iterate (the temperature state of the fi call that
+        # precedes every solve), no Jacobian formed or factored
+        self.linear_solver = linear_solver
+        self.krylov_iters = 0
         self.forcing_units = forcing_units
         self.g, self.hydro, self.chem = gbmv, hydro, chem
         # fused_newton: stage corrections from gbmv_chem_newton_stage (source, Jacobian and
@@ -959,15 +1027,29 @@ class ChemHydroImex:
         import torch
         f = torch.empty_like(y[5])
         self.chem.calculate_rhs_cvklu(t, y[5].view(-1), f.view(-1), self.tu)
+        self._z5 = y[5].reshape(-1)  # the iterate whose temperature state J v uses (GMRES)
         return [None] * 5 + [f]
 
     def setup(self, t, y, gamma):
+        if self.linear_solver == "gmres":
+            self.gamma, self.t_lin = gamma, t
+            return 0
         self.chem.calculate_jacobian_cvklu(t, y[5].view(-1), self.J, self.tu)
         self.g.form_newton_matrix(self.J, gamma)
         return self.ls.setup(self.J)
 
-    def solve(self, b):
+    def solve(self, b, z=None):
         import torch
+        if self.linear_solver == "gmres":
+            y = self._z5
+            jv = torch.empty(y.numel(), dtype=torch.float64, device=y.device)
+
+            def matvec(v):
+                self.chem.jvp(self.t_lin, y, v.reshape(-1), jv, self.tu)
+                return v - self.gamma * jv.view(-1, 10)
+            x, it = batched_gmres(matvec, b[5].reshape(-1, 10))
+            self.krylov_iters += it
+            return list(b[:5]) + [x.view(b[5].shape)]
         x = torch.empty_like(b[5])
         self.ls.solve(self.J, x.view(-1), b[5].view(-1))
         return list(b[:5]) + [x]
