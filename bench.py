@@ -172,6 +172,14 @@ class FusedStep:
         self.status = torch.zeros(2, dtype=torch.int32, device="cuda")
         self.graph = None
         torch.cuda.synchronize()
+        # the library's launch-shape autotuners on this state (results do not depend on them):
+        # the face sweeps' threads per block, and the fused Newton's grid where it runs alone
+        self.tuned = {"sweep_threads": self.hydro.autotune(self.w, self.precision)}
+        if form != "fp64" and not concurrent:
+            self.tuned["newton_blocks_per_sm"] = self.chem.newton_autotune(
+                self.w[5].view(-1), GAMMA_NEWTON, self.units["TimeUnits"], gbmv.MIXED,
+                NEWTON_REFINE)
+        torch.cuda.synchronize()
         if form != "fp64":  # the whole stage as one CUDA graph (asynchronous entry points)
             self.chem_stream = torch.cuda.Stream()
             if concurrent:  # persistent Newton grid leaving room for the WENO sweep beside it
@@ -186,8 +194,9 @@ class FusedStep:
                 self._stage_async()
             torch.cuda.synchronize()
             # the captured launches keep their grid; eager calls (the per-kernel timings) use
-            # the default deep grid again
-            self.chem.set_newton_occupancy(0)
+            # the tuned (or default) grid again
+            if concurrent:
+                self.chem.set_newton_occupancy(0)
 
     def _stage_async(self, t=0.0):
         g, torch = self.gbmv, self.torch
@@ -443,7 +452,7 @@ def run_gbmv(args):
         fs.step()
         torch.cuda.synchronize()
         res[form] = dict(fs=fs, ms=ms, fam=fam, fam_steps=fam_steps, launches=launches, clocks=clk,
-                         out=fs.outputs())
+                         out=fs.outputs(), tuned=fs.tuned)
         if form != forms[-1]:
             del fs.J
             res[form]["fs"] = None
@@ -521,7 +530,8 @@ def run_gbmv(args):
         "gpu_launches": int(R["launches"]),
         "clocks": R["clocks"],
         "forms": {f: {"ms_per_step": round(r["ms"], 4),
-                      "value": round(ncell / (r["ms"] * 1e-3) / 1e6, 3)} for f, r in res.items()},
+                      "value": round(ncell / (r["ms"] * 1e-3) / 1e6, 3),
+                      "autotuned": r["tuned"]} for f, r in res.items()},
     }
     if head.endswith("_concurrent"):
         line["config"]["schedule"] = (

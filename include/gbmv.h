@@ -114,6 +114,15 @@ int gbmv_feuler_async(gbmv_hydro h, double t, const double* const* w, double* co
 int gbmv_feuler_noalloc(const gbmv_grid* grid, const double* force_host, double t,
                         const double* const* w, double* const* wdot, void* stream);
 
+/* Autotuner of the face sweeps' launch shape (no counterpart in the reference): times the
+ * flux divergence of `precision` on the state w with 32, 64 and 128 threads per block and
+ * keeps the fastest for this handle and precision (*threads, host, may be NULL, receives it).
+ * Each face is computed by one thread on its own, so the choice changes no result.  Without a
+ * call the sweeps use 128 threads, fewer on grids too small to give every SM two blocks.
+ * Synchronous; allocates a temporary output; not during a stream capture. */
+int gbmv_hydro_autotune(gbmv_hydro h, const double* const* w, int precision, int* threads,
+                        void* stream);
+
 /* stability (src/utilities.cpp:483-528): dt_stab = cfl * min(dx,dy,dz) / max(|mx/rho| + c),
  * including the reference's use of |mx/rho| for all three directions.  *dt_stab is host. */
 int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,
@@ -338,6 +347,15 @@ int gbmv_chem_dirk_block(gbmv_chem c, int precision);
  * the same stage: the chemistry and the flux divergence of a stage are independent and load
  * different pipes, FP64 and FP32).  Returns 0 or GBMV_EINVAL. */
 int gbmv_chem_set_newton_occupancy(gbmv_chem c, int blocks_per_sm);
+
+/* Autotuner of gbmv_chem_newton's launch shape: times the fused Newton on y (gamma,
+ * time_units, lu_precision, refine as the caller will use them) on the deep grid-stride grid
+ * and on persistent grids of 2-8 one-warp blocks per SM, restores the temperature state, and
+ * keeps the fastest as the handle's Newton occupancy (as gbmv_chem_set_newton_occupancy;
+ * *blocks_per_sm, host, may be NULL, receives it, 0 = the deep grid).  Per-cell work does not
+ * depend on the launch shape, so results are unchanged.  Synchronous; not during a capture. */
+int gbmv_chem_newton_autotune(gbmv_chem c, const double* y, double gamma, double time_units,
+                              int lu_precision, int refine, int* blocks_per_sm, void* stream);
 
 /* Device pointers of the persistent per-cell state (for checkpoint/restart and tests):
  * which: 0 Ts, 1 dTs_ge, 2 mdensity, 3 inv_mdensity, 4 cie optical depth, 5 h2 optical depth,

@@ -462,3 +462,45 @@ class RefChem:
         J = np.zeros(self.n * 100)
         self.L.ref_chem_jac(C.c_double(0.0), _ptr(y), _ptr(J), None)
         return J.reshape(self.n, 10, 10)
+
+
+class RefGlue:
+    """The reference's IMEX-program glue compiled from its own source (oracle/_ref/
+    libref_glue.so, see ref_glue.cpp): fexpl, PostprocessStep and the static problem's Dengo
+    scaling on one grid.  `scale` (10 per cell, the physical chemistry) goes through
+    prepare_Dengo_structures; fields are [rho, mx, my, mz, et, chem] arrays."""
+
+    def __init__(self, shape, bc, gamma, units, scale, table_dir):
+        path = os.path.join(REF, "libref_glue.so")
+        self.L = C.CDLL(path)
+        self.L.ref_glue_energy_units.restype = C.c_double
+        nz, ny, nx = shape
+        phys = np.ascontiguousarray(scale, dtype=np.float64).reshape(-1).copy()
+        st = self.L.ref_glue_setup(C.c_long(nx), C.c_long(ny), C.c_long(nz),
+                                   (C.c_int * 6)(*bc), C.c_double(gamma),
+                                   C.c_double(units["MassUnits"]),
+                                   C.c_double(units["LengthUnits"]),
+                                   C.c_double(units["TimeUnits"]), table_dir.encode(),
+                                   _ptr(phys))
+        if st != 0:
+            raise RuntimeError(f"ref_glue_setup failed ({st})")
+        self.prepared_chem = phys  # ones, as prepare_Dengo_structures leaves the solution
+
+    @staticmethod
+    def _arr(fields):
+        return (C.c_void_p * 6)(*[f.ctypes.data for f in fields])
+
+    def energy_units(self):
+        return self.L.ref_glue_energy_units()
+
+    def fexpl(self, t, fields):
+        """(status, wdot); `fields` modified in place as the reference modifies them."""
+        out = [np.zeros_like(f) for f in fields]
+        st = self.L.ref_glue_fexpl(C.c_double(t), self._arr(fields), self._arr(out))
+        return st, out
+
+    def postprocess(self, t, fields):
+        return self.L.ref_glue_postprocess(C.c_double(t), self._arr(fields))
+
+    def scaling(self, fields, apply):
+        return self.L.ref_glue_scaling(self._arr(fields), int(bool(apply)))

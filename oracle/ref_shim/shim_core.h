@@ -51,6 +51,8 @@ struct shim_nvector {
 typedef struct shim_nvector* N_Vector;
 
 double* N_VGetSubvectorArrayPointer_MPIManyVector(N_Vector v, int k);
+/* a one-component view of component k (defined in shim_glue.c, for the main programs' glue) */
+N_Vector N_VGetSubvector_MPIManyVector(N_Vector v, sunindextype k);
 double* N_VGetArrayPointer(N_Vector v);
 void N_VConst(double c, N_Vector v);
 

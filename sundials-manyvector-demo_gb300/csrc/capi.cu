@@ -81,6 +81,7 @@ struct gbmv_hydro_s {
   double* adj = nullptr;   // per-face stencil cotangents of the VJP (first use)
   double* cons = nullptr;  // conservation-sum partials (first use)
   int* d_status = nullptr;
+  int sweep_threads[3] = {0, 0, 0};  // face-sweep threads per block per precision (0: by size)
 };
 
 struct gbmv_chem_s {
@@ -128,6 +129,32 @@ static bool fields_ok(const double* const* w, int nchem) {
   for (int v = 0; v < 5; ++v)
     if (!w[v]) return false;
   return nchem == 0 || w[5] != nullptr;
+}
+
+// Median of five event-timed runs of fn (after one untimed run), in ms; < 0 on error.
+template <class Fn>
+static float time_runs(cudaStream_t s, Fn fn) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    return -1.f;
+  }
+  float ms[5] = {0, 0, 0, 0, 0};
+  int rc = fn();
+  for (int k = 0; k < 5 && !rc; ++k) {
+    cudaEventRecord(e0, s);
+    rc = fn();
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = GBMV_ECUDA;
+    else cudaEventElapsedTime(&ms[k], e0, e1);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return -1.f;
+  for (int a = 0; a < 5; ++a)
+    for (int b = a + 1; b < 5; ++b)
+      if (ms[b] < ms[a]) { float t = ms[a]; ms[a] = ms[b]; ms[b] = t; }
+  return ms[2];
 }
 
 extern "C" {
@@ -242,7 +269,9 @@ static int feuler_dispatch(gbmv_hydro h, const double* const* w, double* const* 
   if (!h->g.nchem) W.f[5] = nullptr;
   ForceTerm G = h->force;
   G.in_wdot = (flags & GBMV_FORCE_IN_WDOT) ? 1 : 0;
-  if (precision == GBMV_FP64) return feuler_fp64(h->g, W, Wd, G, h->scratch, d_status, s);
+  Grid g = h->g;
+  g.sweep_threads = h->sweep_threads[precision];
+  if (precision == GBMV_FP64) return feuler_fp64(g, W, Wd, G, h->scratch, d_status, s);
   if (!h->prims) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
@@ -258,8 +287,47 @@ static int feuler_dispatch(gbmv_hydro h, const double* const* w, double* const* 
       return GBMV_ENOMEM;
     }
   }
-  return feuler_f2(h->g, W, Wd, G, h->scratch, h->prims, tscale, d_status, s,
+  return feuler_f2(g, W, Wd, G, h->scratch, h->prims, tscale, d_status, s,
                    precision == GBMV_MIXED_FAST);
+}
+
+int gbmv_hydro_autotune(gbmv_hydro h, const double* const* w, int precision, int* threads,
+                        void* stream) {
+  if (!h || !fields_ok(w, h->g.nchem) ||
+      (precision != GBMV_FP64 && precision != GBMV_MIXED && precision != GBMV_MIXED_FAST)) {
+    set_error("null handle or field, or unknown precision");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (capturing(s)) {
+    set_error("the face-sweep autotuner times launches: call it outside any stream capture");
+    return GBMV_EINVAL;
+  }
+  const long n = h->g.ncell;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * (5 + h->g.nchem) * n) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("autotune output allocation failed");
+    return GBMV_ENOMEM;
+  }
+  double* wd[6];
+  for (int k = 0; k < 6; ++k) wd[k] = (k < 5 || h->g.nchem) ? out + (long)k * n : nullptr;
+  const int cand[3] = {32, 64, 128};
+  int best = 0, rc = GBMV_OK;
+  float best_ms = 0.f;
+  for (int c = 0; c < 3 && !rc; ++c) {
+    h->sweep_threads[precision] = cand[c];
+    const float ms = time_runs(s, [&]() {
+      return feuler_dispatch(h, w, wd, precision, 0, h->d_status, s, nullptr);
+    });
+    if (ms < 0.f) { rc = GBMV_ECUDA; break; }
+    if (best == 0 || ms < best_ms) { best = cand[c]; best_ms = ms; }
+  }
+  cudaFree(out);
+  h->sweep_threads[precision] = rc ? 0 : best;
+  if (rc) return rc;
+  if (threads) *threads = best;
+  return GBMV_OK;
 }
 
 int gbmv_feuler(gbmv_hydro h, double t, const double* const* w, double* const* wdot,
@@ -719,6 +787,54 @@ int gbmv_chem_set_newton_occupancy(gbmv_chem c, int blocks_per_sm) {
     return GBMV_EINVAL;
   }
   c->newton_bps = blocks_per_sm;
+  return GBMV_OK;
+}
+
+int gbmv_chem_newton_autotune(gbmv_chem c, const double* y, double gamma, double time_units,
+                              int lu_precision, int refine, int* blocks_per_sm, void* stream) {
+  if (!c || !y || (lu_precision != GBMV_FP64 && lu_precision != GBMV_MIXED) || refine < 0) {
+    set_error("bad Newton autotune arguments");
+    return GBMV_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (capturing(s)) {
+    set_error("the Newton autotuner times launches: call it outside any stream capture");
+    return GBMV_EINVAL;
+  }
+  const long n = c->n;
+  double *buf = nullptr;  // f, x, saved Ts and dTs/dge
+  if (cudaMalloc(&buf, sizeof(double) * 22 * n) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("autotune buffer allocation failed");
+    return GBMV_ENOMEM;
+  }
+  double *f = buf, *x = buf + 10 * n, *ts = buf + 20 * n;
+  int rc = ck(cudaMemcpyAsync(ts, c->S.Ts, sizeof(double) * n, cudaMemcpyDeviceToDevice, s),
+              "autotune save");
+  if (!rc) rc = ck(cudaMemcpyAsync(ts + n, c->S.dTs_ge, sizeof(double) * n,
+                                   cudaMemcpyDeviceToDevice, s), "autotune save");
+  const int cand[7] = {0, 2, 3, 4, 5, 6, 8};  // 0: the deep grid-stride grid
+  int best = -1;
+  float best_ms = 0.f;
+  for (int k = 0; k < 7 && !rc; ++k) {
+    const float ms = time_runs(s, [&]() {
+      GBMV_CUDA_TRY(cudaMemcpyAsync(c->S.Ts, ts, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                    s));
+      return chem_newton(c->P, c->S, n, y, f, x, gamma, time_units,
+                         lu_precision == GBMV_MIXED, refine, c->d_info, s, cand[k]);
+    });
+    if (ms < 0.f) { rc = GBMV_ECUDA; break; }
+    if (best < 0 || ms < best_ms) { best = cand[k]; best_ms = ms; }
+  }
+  if (!rc) rc = ck(cudaMemcpyAsync(c->S.Ts, ts, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                   s), "autotune restore");
+  if (!rc) rc = ck(cudaMemcpyAsync(c->S.dTs_ge, ts + n, sizeof(double) * n,
+                                   cudaMemcpyDeviceToDevice, s), "autotune restore");
+  if (!rc) rc = ck(cudaStreamSynchronize(s), "autotune restore");
+  cudaFree(buf);
+  if (rc) return rc;
+  c->newton_bps = best;
+  if (blocks_per_sm) *blocks_per_sm = best;
   return GBMV_OK;
 }
 

@@ -172,7 +172,9 @@ __global__ void energy_sync_kernel(const double* __restrict__ scale, double* __r
       ge = c[nchem - 1];
     }
     const double r = rho[i], a = mx[i], b = my[i], d = mz[i];
-    et[i] = ge * eunit_scale + 0.5 / r * (a * a + b * b + d * d);
+    // the reference's expression with its roundings (no FMA contraction): bit-equal et
+    const double m2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(d, d));
+    et[i] = __dadd_rn(__dmul_rn(ge, eunit_scale), __dmul_rn(0.5 / r, m2));
     if (restore == 1)
       for (int v = 0; v < nchem; ++v) c[v] /= s[v];
   }

@@ -51,6 +51,7 @@ struct Grid {
   double gamma;
   double inv_d[3]; // 1/dx, 1/dy, 1/dz
   double d[3];
+  int sweep_threads;  // threads per block of the face sweeps (0: by size, spread_threads)
 };
 
 inline Grid make_grid(const gbmv_grid& g) {
@@ -62,6 +63,7 @@ inline Grid make_grid(const gbmv_grid& g) {
   G.gamma = g.gamma;
   G.d[0] = g.dx; G.d[1] = g.dy; G.d[2] = g.dz;
   for (int i = 0; i < 3; ++i) G.inv_d[i] = 1.0 / G.d[i];
+  G.sweep_threads = 0;
   return G;
 }
 

@@ -179,19 +179,19 @@ static int launch_fp64(const Grid& g, const Fields& w, const Fields& wdot, const
                   scratch + (long)(5 + NCHEM) * (nf[0] + nf[1])};
   {
     ProfScope ps("face_flux", s);
-    const int t = spread_threads(nf[0], 128);
+    const int t = sweep_threads(g, nf[0], 128);
     face_flux_kernel<NCHEM, 0><<<sweep_blocks(nf[0], t), t, 0, s>>>(g, w, F[0], nf[0]);
     GBMV_LAUNCH_CHECK("face_flux_kernel<x>");
   }
   {
     ProfScope ps("face_flux", s);
-    const int t = spread_threads(nf[1], 128);
+    const int t = sweep_threads(g, nf[1], 128);
     face_flux_kernel<NCHEM, 1><<<sweep_blocks(nf[1], t), t, 0, s>>>(g, w, F[1], nf[1]);
     GBMV_LAUNCH_CHECK("face_flux_kernel<y>");
   }
   {
     ProfScope ps("face_flux", s);
-    const int t = spread_threads(nf[2], 128);
+    const int t = sweep_threads(g, nf[2], 128);
     face_flux_kernel<NCHEM, 2><<<sweep_blocks(nf[2], t), t, 0, s>>>(g, w, F[2], nf[2]);
     GBMV_LAUNCH_CHECK("face_flux_kernel<z>");
   }

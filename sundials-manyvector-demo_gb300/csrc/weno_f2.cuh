@@ -157,20 +157,23 @@ int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTer
   if (rc != GBMV_OK) return rc;
   {
     ProfScope ps("face_flux", s);
-    face_flux_f2_kernel<NCHEM, 0, WV><<<sweep_blocks(nf[0], 128), 128, 0, s>>>(g, w, q2, F[0],
-                                                                                nf[0]);
+    const int t = sweep_threads(g, nf[0], 128);
+    face_flux_f2_kernel<NCHEM, 0, WV><<<sweep_blocks(nf[0], t), t, 0, s>>>(g, w, q2, F[0],
+                                                                            nf[0]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<x>");
   }
   {
     ProfScope ps("face_flux", s);
-    face_flux_f2_kernel<NCHEM, 1, WV><<<sweep_blocks(nf[1], 128), 128, 0, s>>>(g, w, q2, F[1],
-                                                                                nf[1]);
+    const int t = sweep_threads(g, nf[1], 128);
+    face_flux_f2_kernel<NCHEM, 1, WV><<<sweep_blocks(nf[1], t), t, 0, s>>>(g, w, q2, F[1],
+                                                                            nf[1]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<y>");
   }
   {
     ProfScope ps("face_flux", s);
-    face_flux_f2_kernel<NCHEM, 2, WV><<<sweep_blocks(nf[2], 128), 128, 0, s>>>(g, w, q2, F[2],
-                                                                                nf[2]);
+    const int t = sweep_threads(g, nf[2], 128);
+    face_flux_f2_kernel<NCHEM, 2, WV><<<sweep_blocks(nf[2], t), t, 0, s>>>(g, w, q2, F[2],
+                                                                            nf[2]);
     GBMV_LAUNCH_CHECK("face_flux_f2_kernel<z>");
   }
   return divergence_f2(g, wdot, F, G, s);

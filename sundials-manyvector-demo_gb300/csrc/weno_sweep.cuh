@@ -91,6 +91,12 @@ inline int spread_threads(long n, int tmax) {
   return t;
 }
 
+// the face sweeps' threads per block: the tuned value, else by size
+inline int sweep_threads(const Grid& g, long n, int tmax) {
+  return g.sweep_threads > 0 && g.sweep_threads <= tmax ? g.sweep_threads
+                                                        : spread_threads(n, tmax);
+}
+
 // faces normal to x, y, z
 inline void face_counts(const Grid& g, long (&nf)[3]) {
   const long nx = g.n[0], ny = g.n[1], nz = g.n[2];

@@ -84,6 +84,9 @@ SIGNATURES = [
     ("gbmv_feuler_noalloc", C.c_int, [C.POINTER(_Grid), _P, C.c_double, C.POINTER(_VP),
                                       C.POINTER(_VP), _VP]),
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
+    ("gbmv_hydro_autotune", C.c_int, [_VP, C.POINTER(_VP), C.c_int, C.POINTER(C.c_int), _VP]),
+    ("gbmv_chem_newton_autotune", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.c_int, C.c_int,
+                                            C.POINTER(C.c_int), _VP]),
     ("gbmv_pack1d", C.c_int, [_VP, C.POINTER(_VP), C.c_int, _VP, _VP]),
     ("gbmv_conservation", C.c_int, [_VP, C.POINTER(_VP), C.c_double, C.c_double, _P, _VP]),
     ("gbmv_wrms_norm", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.c_double, C.c_double,
@@ -275,6 +278,13 @@ class Hydro:
                                      _stream_ptr(stream)), "gbmv_wrms_norm")
         return out[0]
 
+    def autotune(self, w, precision=FP64, stream=None) -> int:
+        """gbmv_hydro_autotune: the face sweeps' threads per block for this precision."""
+        t = C.c_int()
+        _check(load().gbmv_hydro_autotune(self.h, _vec(w), precision, C.byref(t),
+                                          _stream_ptr(stream)), "gbmv_hydro_autotune")
+        return t.value
+
     def kink_mask(self, w, dw, eps, mask, stream=None):
         """gbmv_feuler_kink_mask into `mask` (CUDA uint8 tensor of ncells): 1 where a central
         difference of fEuler along dw with step eps crosses a Lax-Friedrichs branch."""
@@ -411,6 +421,17 @@ class Chem:
             self.c, t0, tout, _dev_ptr(y), time_units, C.byref(o),
             stats.data_ptr() if stats is not None else None, nfail.data_ptr(),
             _stream_ptr(stream)), "gbmv_chem_dirk_evolve_async")
+
+    def newton_autotune(self, y, gamma, time_units=1.0, lu_precision=MIXED, refine=2,
+                        stream=None) -> int:
+        """gbmv_chem_newton_autotune: the fused Newton's resident blocks per SM (0 = deep
+        grid), kept as the handle's Newton occupancy."""
+        b = C.c_int()
+        _check(load().gbmv_chem_newton_autotune(self.c, _dev_ptr(y), gamma, time_units,
+                                                lu_precision, refine, C.byref(b),
+                                                _stream_ptr(stream)),
+               "gbmv_chem_newton_autotune")
+        return b.value
 
     def set_newton_occupancy(self, blocks_per_sm: int):
         """Resident blocks per SM of the fused Newton kernel (0 = default deep grid)."""

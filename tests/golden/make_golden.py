@@ -1,12 +1,14 @@
 """Generate the golden fixtures in this directory from the reference's own code.
 
 The reference ships no golden vectors, so they are produced by running its hot-path sources
-(src/utilities.cpp, src/euler3D.hpp, src/raja_primordial_network.cpp), compiled unmodified
+(src/utilities.cpp, src/euler3D.hpp, src/raja_primordial_network.cpp, and the IMEX program's
+glue with the static problem's Dengo scaling: src/imex_chem_hydro_main.cpp,
+src/primordial_static.cpp), compiled unmodified
 against the one-rank shims by oracle/build_ref.sh, on seeded synthetic inputs.  This needs the
 reference tree (it runs only where it exists); the fixtures it writes are committed and the
 tests read only them.
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT] [--glue-only]
 """
 from __future__ import annotations
 
@@ -103,8 +105,63 @@ def main(ref_root=None):
         ch[f"dTs_ge{call}"] = s["dTs_ge"]
         ch[f"J{call}"] = J
     np.savez_compressed(os.path.join(HERE, "chem_cases.npz"), **ch)
-    print("wrote feuler_cases.npz and chem_cases.npz")
+    glue_fixtures()
+    print("wrote feuler_cases.npz, chem_cases.npz and glue_cases.npz")
+
+
+def glue_fixtures():
+    """The IMEX program's glue run from the reference's own source (oracle/_ref/
+    libref_glue.so): prepare_Dengo_structures, fexpl (twice in a row: the state it rewrites
+    feeds the second call), PostprocessStep, apply / unapply_Dengo_scaling, on two
+    chemistry-hydrodynamics grids."""
+    g = {}
+    cases = [("ch_8x6x5", W.chem_hydro(shape=(8, 6, 5)), None),
+             ("ch_7x5x6_mixedbc", W.chem_hydro(shape=(7, 5, 6), seed=W.SEED_BASE + 90),
+              (1, 3, 0, 0, 3, 3))]
+    rng = np.random.Generator(np.random.PCG64(W.SEED_BASE + 91))
+    for name, wl, bc in cases:
+        if bc is not None:
+            wl["bc"] = bc
+        u = wl["units"]
+        ref = O.RefGlue(wl["fields"][0].shape, wl["bc"], wl["gamma"], u, wl["scale"], HERE)
+        g[f"{name}/bc"] = np.array(wl["bc"])
+        g[f"{name}/gamma"] = np.array(wl["gamma"])
+        for k in ("MassUnits", "LengthUnits", "TimeUnits"):
+            g[f"{name}/{k}"] = np.array(u[k])
+        g[f"{name}/EnergyUnits"] = np.array(ref.energy_units())
+        g[f"{name}/scale"] = wl["scale"].copy()
+        g[f"{name}/prepared_chem"] = ref.prepared_chem.copy()
+        f = [np.ascontiguousarray(x.copy()) for x in wl["fields"]]
+        for i, x in enumerate(f):
+            g[f"{name}/w{i}"] = x.copy()
+        for call in range(2):
+            st, out = ref.fexpl(0.0, f)
+            assert st == 0
+            for i in range(6):
+                g[f"{name}/fexpl{call}_wdot{i}"] = out[i]
+                g[f"{name}/fexpl{call}_w{i}"] = f[i].copy()
+        p = [np.ascontiguousarray(x.copy()) for x in wl["fields"]]
+        p[4] = p[4] * (1.0 + rng.uniform(-0.1, 0.1, size=p[4].shape))  # stale et
+        p[5] = p[5] * (1.0 + rng.uniform(-0.01, 0.01, size=p[5].shape))
+        for i, x in enumerate(p):
+            g[f"{name}/post_in{i}"] = x.copy()
+        assert ref.postprocess(0.0, p) == 0
+        for i, x in enumerate(p):
+            g[f"{name}/post_out{i}"] = x.copy()
+        s = [np.ascontiguousarray(x.copy()) for x in wl["fields"]]
+        assert ref.scaling(s, True) == 0
+        g[f"{name}/applied_chem"] = s[5].copy()
+        assert ref.scaling(s, False) == 0
+        g[f"{name}/unapplied_chem"] = s[5].copy()
+    g["cases"] = np.array([c[0] for c in cases])
+    np.savez_compressed(os.path.join(HERE, "glue_cases.npz"), **g)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else None)
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if "--glue-only" in sys.argv:  # keep the other fixtures, (re)write glue_cases.npz
+        cmd = [os.path.join(ROOT, "oracle", "build_ref.sh")] + args[:1]
+        subprocess.check_call(cmd)
+        glue_fixtures()
+    else:
+        main(args[0] if args else None)

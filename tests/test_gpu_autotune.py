@@ -1,0 +1,51 @@
+"""The launch-shape autotuners (gbmv_hydro_autotune: the face sweeps' threads per block per
+precision; gbmv_chem_newton_autotune: the fused Newton's resident blocks per SM; the DIRK's
+block size is tuned inside gbmv_chem_dirk_evolve and tested with it): each picks one of its
+candidates, and the results after tuning equal the untuned results bit for bit (one face or
+cell per thread, independent of the launch shape)."""
+import numpy as np
+import pytest
+
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_sweep_autotune_keeps_results(cuda):
+    torch = cuda
+    import gbmv
+    wl = W.rayleigh_taylor(shape=(40, 36, 32), nchem=10, seed=W.SEED_BASE + 800)
+    nz, ny, nx = wl["fields"][0].shape
+    w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+    for prec in (gbmv.FP64, gbmv.MIXED, gbmv.MIXED_FAST):
+        h = gbmv.Hydro((nx, ny, nz), 10, wl["bc"], wl["gamma"], wl["force"])
+        a = [torch.empty_like(x) for x in w]
+        b = [torch.empty_like(x) for x in w]
+        assert h.fEuler(0.0, w, a, prec) == 0
+        t = h.autotune(w, prec)
+        assert t in (32, 64, 128)
+        assert h.fEuler(0.0, w, b, prec) == 0
+        torch.cuda.synchronize()
+        assert all(torch.equal(x, y) for x, y in zip(a, b)), prec
+
+
+def test_newton_autotune_keeps_results_and_state(cuda, tables):
+    torch = cuda
+    import gbmv
+    n = 20000
+    y, _ = W.primordial(n, seed=W.SEED_BASE + 801)
+    c = gbmv.Chem(n, tables)
+    c.set_scale(torch.from_numpy(y.reshape(-1).copy()).cuda())
+    z = torch.ones(10 * n, dtype=torch.float64, device="cuda")
+    f1, x1 = torch.empty_like(z), torch.empty_like(z)
+    f2, x2 = torch.empty_like(z), torch.empty_like(z)
+    ts0 = c.state("Ts").clone()
+    bps = c.newton_autotune(z, 1e-4, 1e11, gbmv.MIXED, 2)
+    assert bps in (0, 2, 3, 4, 5, 6, 8)
+    assert torch.equal(c.state("Ts"), ts0)  # the temperature state restored
+    assert c.newton_iteration(0.0, z, f1, x1, 1e-4, 1e11, lu_precision=gbmv.MIXED) == 0
+    c.state("Ts").copy_(ts0)
+    c.set_newton_occupancy(0)
+    assert c.newton_iteration(0.0, z, f2, x2, 1e-4, 1e11, lu_precision=gbmv.MIXED) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(f1, f2) and torch.equal(x1, x2)

@@ -177,3 +177,48 @@ def test_print_stats_rms(cuda, nchem):
             ref = math.sqrt(math.fsum((wl["fields"][5][..., v] ** 2).ravel()) / n)
             assert abs(rms[5 + v] - ref) <= 1e-14 * ref, v
         assert h.print_stats(w, units) == rms
+
+
+def test_glue_matches_the_reference_program(cuda, tables):
+    """gbmv_fexpl (FP64), gbmv_postprocess_step and the Dengo scaling entries against the
+    reference's own IMEX-program fexpl / PostprocessStep and the static problem's
+    prepare / apply / unapply_Dengo_scaling compiled from its source
+    (tests/golden/glue_cases.npz): fexpl <= 1e-12 per field over two calls in a row (the state
+    it rewrites included), the others bit for bit."""
+    import os
+    torch = cuda
+    import gbmv
+    from conftest import GOLDEN
+    g = np.load(os.path.join(GOLDEN, "glue_cases.npz"))
+    for name in [str(c) for c in g["cases"]]:
+        w0 = g[f"{name}/w0"]
+        nz, ny, nx = w0.shape
+        n = nx * ny * nz
+        bc = tuple(int(b) for b in g[f"{name}/bc"])
+        eu = float(g[f"{name}/EnergyUnits"])
+        h = gbmv.Hydro((nx, ny, nz), 10, bc, float(g[f"{name}/gamma"]))
+        c = gbmv.Chem(n, tables)
+        phys = torch.from_numpy(g[f"{name}/scale"].reshape(-1).copy()).cuda()
+        c.prepare_Dengo_structures(phys)  # scale = chem, chem = 1 (prepare_Dengo_structures)
+        torch.cuda.synchronize()
+        assert torch.equal(phys, torch.ones_like(phys))
+        w = [torch.from_numpy(g[f"{name}/w{i}"].copy()).cuda() for i in range(6)]
+        for call in range(2):
+            out = [torch.empty_like(x) for x in w]
+            assert gbmv.fexpl(h, c, 0.0, w, out, eu, gbmv.FP64) == 0
+            for i in range(6):
+                e = maxnorm_err(out[i].cpu().numpy(), g[f"{name}/fexpl{call}_wdot{i}"])
+                assert e <= 1e-12, (name, call, i, e)
+                assert np.array_equal(w[i].cpu().numpy(), g[f"{name}/fexpl{call}_w{i}"]), \
+                    (name, call, "state", i)
+        q = [torch.from_numpy(g[f"{name}/post_in{i}"].copy()).cuda() for i in range(6)]
+        assert gbmv.PostprocessStep(h, c, q, eu) == 0
+        for i in range(6):
+            assert np.array_equal(q[i].cpu().numpy(), g[f"{name}/post_out{i}"]), (name, i)
+        s5 = torch.from_numpy(g[f"{name}/w5"].copy()).cuda()
+        c.apply_Dengo_scaling(s5.view(-1))
+        torch.cuda.synchronize()
+        assert np.array_equal(s5.cpu().numpy(), g[f"{name}/applied_chem"])
+        c.unapply_Dengo_scaling(s5.view(-1))
+        torch.cuda.synchronize()
+        assert np.array_equal(s5.cpu().numpy(), g[f"{name}/unapplied_chem"])

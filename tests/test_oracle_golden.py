@@ -76,3 +76,38 @@ def test_block_solve_singular_flagged():
     J[2] = np.eye(10)  # I - 1*I = 0 -> singular block 2
     bad, _ = O.block_newton_solve(J, 1.0, np.ones(40))
     assert bad == 3
+
+
+def _glue_cases():
+    import os
+    from conftest import GOLDEN
+    g = np.load(os.path.join(GOLDEN, "glue_cases.npz"))
+    return g, [str(c) for c in g["cases"]]
+
+
+def test_oracle_glue_matches_the_reference_program(tables):
+    """The oracle's composition of the IMEX program's callbacks (oracle_py.ImexChemHydro with
+    the reference's unconverted forcing) against the program's own fexpl and PostprocessStep
+    and the static problem's Dengo scaling, compiled from the reference's source
+    (tests/golden/glue_cases.npz): bit for bit, two fexpl calls in a row (the state the first
+    rewrites feeds the second)."""
+    g, cases = _glue_cases()
+    for name in cases:
+        w = [g[f"{name}/w{i}"].copy() for i in range(6)]
+        wl = {"bc": tuple(int(b) for b in g[f"{name}/bc"]), "gamma": float(g[f"{name}/gamma"]),
+              "scale": g[f"{name}/scale"]}
+        eu, tu = float(g[f"{name}/EnergyUnits"]), float(g[f"{name}/TimeUnits"])
+        assert np.all(g[f"{name}/prepared_chem"] == 1.0)
+        p = O.ImexChemHydro(wl, tables, eu, tu, 1e-6, 1e-10, forcing_units="reference")
+        for call in range(2):
+            out = p.fe(0.0, w)
+            for i in range(6):
+                assert np.array_equal(out[i], g[f"{name}/fexpl{call}_wdot{i}"]), (name, call, i)
+                assert np.array_equal(w[i], g[f"{name}/fexpl{call}_w{i}"]), (name, call, i)
+        q = [g[f"{name}/post_in{i}"].copy() for i in range(6)]
+        p.postprocess(0.0, q)
+        for i in range(6):
+            assert np.array_equal(q[i], g[f"{name}/post_out{i}"]), (name, "post", i)
+        chem = g[f"{name}/w5"] * wl["scale"]
+        assert np.array_equal(chem, g[f"{name}/applied_chem"])
+        assert np.array_equal(chem / wl["scale"], g[f"{name}/unapplied_chem"])
