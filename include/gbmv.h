@@ -338,6 +338,14 @@ int gbmv_mri_fast_evolve_async(gbmv_hydro h, gbmv_chem c, double t0, double tout
                                const gbmv_dirk_opts* opts, int* stats, int* d_nfail,
                                void* stream);
 
+/* The GBMV_MIXED DIRK (refine 0) runs two passes: every cell in FP32-LU arithmetic, then the
+ * cells that pass could not finish (Newton iterations that keep failing on an FP32 factor too
+ * poor for the block) again from their start state in FP64, so they get exactly the FP64
+ * form's result.  This returns how many cells the last GBMV_MIXED call on the handle sent to
+ * the FP64 pass, and copies up to max_cells of their indices (host) into cells (may be NULL).
+ * Synchronous. */
+int gbmv_chem_dirk_retried(gbmv_chem c, int* cells, int max_cells, void* stream);
+
 /* Block size the autotuner chose for a precision (0 = not tuned yet). */
 int gbmv_chem_dirk_block(gbmv_chem c, int precision);
 

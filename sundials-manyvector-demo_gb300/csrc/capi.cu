@@ -96,6 +96,8 @@ struct gbmv_chem_s {
   int dirk_block[2] = {0, 0};          // autotuned block size per precision (0 = not yet)
   double* dirk_k = nullptr;            // DIRK stage store (first DIRK call), dirk_k_lanes lanes
   long dirk_k_lanes = 0;
+  double* dirk_retry = nullptr;        // FP32 DIRK's second pass: start state, Ts, cell list
+  DirkRetry retry{};
   int newton_bps = 0;                  // fused Newton: resident blocks per SM (0 = default)
 };
 
@@ -451,6 +453,7 @@ int gbmv_chem_destroy(gbmv_chem c) {
   cudaFree(c->cell);
   cudaFree(c->d_info);
   cudaFree(c->dirk_k);
+  cudaFree(c->dirk_retry);
   delete c;
   return GBMV_OK;
 }
@@ -631,6 +634,24 @@ static int dirk_store(gbmv_chem c, DirkOpts* O, cudaStream_t s) {
   }
   O->kstore = c->dirk_k;
   O->kstore_lanes = c->dirk_k_lanes;
+  if (!c->dirk_retry) {  // the FP32 form's second pass: start state, Ts, failed-cell list
+    if (capturing(s)) {
+      set_error("the first DIRK call allocates its buffers: make it before any capture");
+      return GBMV_EINVAL;
+    }
+    const long n = c->n;
+    if (cudaMalloc(&c->dirk_retry, sizeof(double) * 12 * n + sizeof(int) * (n + 1)) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      c->dirk_retry = nullptr;
+      set_error("device allocation of the DIRK retry buffers failed");
+      return GBMV_ENOMEM;
+    }
+    c->retry.y0 = c->dirk_retry;
+    c->retry.ts0 = c->dirk_retry + 10 * n;
+    c->retry.list = reinterpret_cast<int*>(c->dirk_retry + 12 * n);
+    c->retry.count = c->retry.list + n;
+  }
   return GBMV_OK;
 }
 
@@ -672,6 +693,12 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
   for (int q = 0; q < 8; ++q) O->fz[q] = nullptr;
   O->kstore = nullptr;
   O->kstore_lanes = 0;
+  O->list_in = nullptr;
+  O->list_in_n = nullptr;
+  O->y_init = nullptr;
+  O->Ts_init = nullptr;
+  O->list_out = nullptr;
+  O->list_out_n = nullptr;
   return dirk_table(o->table, &O->T);
 }
 
@@ -756,7 +783,8 @@ static int dirk_launch(gbmv_chem c, double t0, double tout, double* y, double ti
     if (rc) return rc;
     block = c->dirk_block[mixed];
   }
-  rc = chem_dirk(c->P, c->S, c->n, y, O, mixed, block, c->d_next, stats, d_nfail, s);
+  rc = chem_dirk(c->P, c->S, c->n, y, O, mixed, block, c->d_next, stats, d_nfail, s,
+                 &c->retry);
   if (rc == GBMV_EUNSUPPORTED) set_error("DIRK block of %d threads does not fit on an SM", block);
   return rc;
 }
@@ -836,6 +864,21 @@ int gbmv_chem_newton_autotune(gbmv_chem c, const double* y, double gamma, double
   c->newton_bps = best;
   if (blocks_per_sm) *blocks_per_sm = best;
   return GBMV_OK;
+}
+
+int gbmv_chem_dirk_retried(gbmv_chem c, int* cells, int max_cells, void* stream) {
+  if (!c) { set_error("null handle"); return GBMV_EINVAL; }
+  if (!c->dirk_retry) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  int count = 0;
+  GBMV_CUDA_TRY(cudaMemcpyAsync(&count, c->retry.count, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  const int k = cells ? (count < max_cells ? count : max_cells) : 0;
+  if (k > 0) {
+    GBMV_CUDA_TRY(cudaMemcpyAsync(cells, c->retry.list, sizeof(int) * k, cudaMemcpyDeviceToHost, s));
+    GBMV_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return count;
 }
 
 int gbmv_chem_dirk_block(gbmv_chem c, int precision) {
@@ -1076,7 +1119,8 @@ static int mri_fast_launch(gbmv_hydro h, gbmv_chem c, double t0, double tout, do
     rc = mri_forcing(c->n, Ff, nforcing, D, false, 5, s);  // components 0-4 only
     if (rc) return rc;
   }
-  return chem_dirk(c->P, c->S, c->n, w[5], O, mixed, block, c->d_next, stats, d_nfail, s);
+  return chem_dirk(c->P, c->S, c->n, w[5], O, mixed, block, c->d_next, stats, d_nfail, s,
+                   &c->retry);
 }
 
 int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, double* const* w,

@@ -87,12 +87,31 @@ struct DirkOpts {
   // kstore_lanes lanes; K_0 stays in shared memory
   double* kstore;
   long kstore_lanes;
+  // cell lists.  list_in: null = cells 0..n-1, else the *list_in_n cells list_in[...], each
+  // started from y_init / Ts_init (Ts at [cell], dTs/dge at [n + cell]) instead of the in-out
+  // state.  list_out: null = failed cells are counted in nfail, else appended to list_out.
+  const int* list_in;
+  const int* list_in_n;
+  const double* y_init;
+  const double* Ts_init;
+  int* list_out;
+  int* list_out_n;
+};
+
+// Buffers of the FP32 form's second pass: the cells the FP32 pass could not finish are
+// integrated again from their start state in FP64 (chem_dirk).
+struct DirkRetry {
+  double* y0;   // 10 n: the start state
+  double* ts0;  // 2 n: Ts, dTs/dge at the start
+  int* list;    // n: failed cells of the FP32 pass
+  int* count;   // 1
 };
 constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
                                // matrix setups, Jacobians (= setups), F evaluations, failed
+// retry: null, or (FP32 form without refinement) the buffers of the FP64 second pass
 int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,
               int lu_fp32, int block, unsigned long long* d_next, int* stats, int* d_nfail,
-              cudaStream_t s);
+              cudaStream_t s, const DirkRetry* retry = nullptr);
 // Largest number of lanes (threads) any launch shape of chem_dirk runs on this device: the
 // stage store must hold kstore_lanes >= this many lanes.
 long chem_dirk_max_lanes();

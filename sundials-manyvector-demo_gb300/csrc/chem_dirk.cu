@@ -227,54 +227,6 @@ __device__ __forceinline__ int dirk_setup(const ChemParams& P, const ChemState& 
   return lu10_strided<LU>(L, BS, piv);
 }
 
-// FP64-residual refinement steps of the FP32 form's per-cell fallback (below).
-constexpr int kFallbackRefine = 2;
-
-// The FP32 form's fallback for a cell whose Newton iteration failed with a current matrix: its
-// later linear solves are refined against FP64 residuals of the Newton matrix
-// I - gp tunit J(Y, Ts(Y)) at the step's state, the Jacobian entries evaluated on the fly
-// (the FP32 layout keeps no FP64 copy of the matrix), the FP32 factor as the preconditioner.
-// Out of line: it runs for a handful of cells and stays out of the common path's code.
-struct RefineIO {
-  double g[10];   // Newton residual (right-hand side)
-  double dl[10];  // correction, refined in place
-  int piv[10];
-};
-
-template <int BS>
-__device__ __noinline__ void dirk_refine_fp64(const ChemParams& P, const ChemState& S, long i,
-                                              const DirkOpts& O, const double* Y,
-                                              const float* L, const short* EQ, double gp,
-                                              double Tsy, double dTsy, RefineIO& io) {
-  const int (&piv)[10] = io.piv;
-  const double (&g)[10] = io.g;
-  double (&dl)[10] = io.dl;
-  const long j = i * 10;
-  double ya[10];
-#pragma unroll
-  for (int s = 0; s < 10; ++s) ya[s] = Y[s * BS] * S.scale[j + s];
-  double k[kNRates], dk[kNRates];
-  chem_rates<true>(P, Tsy, k, dk);
-  const ChemAux Ax{S.mdens[i], S.imdens[i], S.cie[i], S.h2[i]};
-  const double* __restrict__ sc = S.scale + j;
-  const double* __restrict__ isc = S.inv_scale + j;
-  const double mg = -gp * O.tunit;
-  for (int it = 0; it < kFallbackRefine; ++it) {
-    double r[10];
-#pragma unroll
-    for (int s = 0; s < 10; ++s) r[s] = g[s];
-    chem_jacobian(P, k, dk, ya, Tsy, dTsy, Ax, [&](int row, int col, double v) {
-      r[row] -= ((row == col ? 1.0 : 0.0) + mg * ((v * isc[row]) * sc[col])) * dl[col];
-    });
-    float u[10];
-#pragma unroll
-    for (int s = 0; s < 10; ++s) u[s] = to_lu<float>(r[s] * pow2(EQ[s * BS]));
-    lus10_strided<float, float>(L, BS, piv, u);
-#pragma unroll
-    for (int s = 0; s < 10; ++s) dl[s] += from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
-  }
-}
-
 template <typename LU, bool REF, int BS>
 __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S, long n,
                                                        double* __restrict__ y_io,
@@ -316,7 +268,6 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
   int nst = 0, nst_lp = 0, nef_s = 0, ncf_s = 0;
   int c_nni = 0, c_netf = 0, c_ncf = 0, c_nsetup = 0, c_nfe = 0;
   bool jcur = false, force_setup = true, last = false;
-  bool fp64ref = false;  // FP32 form: this cell's solves refined in FP64 (after a failure)
 
   while (true) {
     // ---- refill: lanes without a cell take the next indices (one atomic per warp)
@@ -330,13 +281,16 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       if (want) {
         const unsigned long long mine =
             base + (unsigned long long)__popc(wm & ((1u << lane) - 1u));
-        if (mine < (unsigned long long)n) {
-          i = (long)mine;
+        const unsigned long long count =
+            O.list_in ? (unsigned long long)*O.list_in_n : (unsigned long long)n;
+        if (mine < count) {
+          i = O.list_in ? (long)O.list_in[mine] : (long)mine;
           const long j = i * 10;
+          const double* __restrict__ y0 = O.y_init ? O.y_init : y_io;
 #pragma unroll
-          for (int s = 0; s < 10; ++s) Y[s * BS] = y_io[j + s];
-          Tsc = S.Ts[i];
-          dTsc = S.dTs_ge[i];
+          for (int s = 0; s < 10; ++s) Y[s * BS] = y0[j + s];
+          Tsc = O.Ts_init ? O.Ts_init[i] : S.Ts[i];
+          dTsc = O.Ts_init ? O.Ts_init[n + i] : S.dTs_ge[i];
           t = O.t0;
           h = O.h0;
           gp = 0.0;
@@ -346,7 +300,6 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           jcur = false;
           force_setup = true;
           last = false;
-          fp64ref = false;
         } else {
           exhausted = true;
         }
@@ -416,20 +369,6 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
             for (int s = 0; s < 10; ++s) dl[s] += from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
           }
-        } else if (fp64ref) {
-          if constexpr (sizeof(LU) == 4) {
-            // copies in and out keep the common path's vectors in registers
-            RefineIO io;
-#pragma unroll
-            for (int s = 0; s < 10; ++s) {
-              io.g[s] = g[s];
-              io.dl[s] = dl[s];
-              io.piv[s] = piv[s];
-            }
-            dirk_refine_fp64<BS>(P, S, i, O, Y, L, EQ, gp, Tsy, dTsy, io);
-#pragma unroll
-            for (int s = 0; s < 10; ++s) dl[s] = io.dl[s];
-          }
         }
       }
       if (gam != gp) {
@@ -459,14 +398,8 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         if (ncf_s >= O.maxncf) {
           retire = failed = true;
         } else {
-          if (jcur) {
-            h *= 0.25;
-            // a second failure with a current matrix in one step: the FP32 factor is not
-            // enough for this cell; refine its solves in FP64 from now on
-            if (ncf_s >= 2) fp64ref = sizeof(LU) == 4 && !REF;
-          } else {
-            force_setup = true;
-          }
+          if (jcur) h *= 0.25;
+          else force_setup = true;
           setup = true;
         }
       } else {
@@ -594,7 +527,10 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         st[6] = c_nfe;
         st[7] = failed ? 1 : 0;
       }
-      if (failed) atomicAdd(nfail, 1);
+      if (failed) {
+        if (O.list_out) O.list_out[atomicAdd(O.list_out_n, 1)] = (int)i;  // retried in FP64
+        else atomicAdd(nfail, 1);
+      }
       i = -1;
     }
   }
@@ -677,7 +613,7 @@ long chem_dirk_max_lanes() {
 
 int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,
               int lu_fp32, int block, unsigned long long* d_next, int* stats, int* d_nfail,
-              cudaStream_t s) {
+              cudaStream_t s, const DirkRetry* retry) {
   GBMV_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), s));
   int dev = 0, nsm = kSM;
   GBMV_CUDA_TRY(cudaGetDevice(&dev));
@@ -687,7 +623,32 @@ int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const 
     return launch_dirk_bs<double, false>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
   if (O.refine > 0)
     return launch_dirk_bs<float, true>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
-  return launch_dirk_bs<float, false>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
+  if (!retry)
+    return launch_dirk_bs<float, false>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
+  // FP32 pass over every cell, its start state kept; a cell it cannot finish (its Newton
+  // iterations keep failing on an FP32 factor too poor for the block) is listed, and an FP64
+  // pass integrates the listed cells again from their start state.  Both passes are
+  // asynchronous launches; the second finds an empty list when nothing failed.
+  GBMV_CUDA_TRY(cudaMemcpyAsync(retry->y0, y, sizeof(double) * 10 * n, cudaMemcpyDeviceToDevice,
+                                s));
+  GBMV_CUDA_TRY(cudaMemcpyAsync(retry->ts0, S.Ts, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                s));
+  GBMV_CUDA_TRY(cudaMemcpyAsync(retry->ts0 + n, S.dTs_ge, sizeof(double) * n,
+                                cudaMemcpyDeviceToDevice, s));
+  GBMV_CUDA_TRY(cudaMemsetAsync(retry->count, 0, sizeof(int), s));
+  DirkOpts Om = O;
+  Om.list_out = retry->list;
+  Om.list_out_n = retry->count;
+  int rc = launch_dirk_bs<float, false>(block, P, S, n, y, Om, d_next, stats, d_nfail, nsm, s);
+  if (rc) return rc;
+  GBMV_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), s));
+  DirkOpts Of = O;
+  Of.list_in = retry->list;
+  Of.list_in_n = retry->count;
+  Of.y_init = retry->y0;
+  Of.Ts_init = retry->ts0;
+  Of.mixed_temp = 0;
+  return launch_dirk<double, false, 64>(P, S, n, y, Of, d_next, stats, d_nfail, nsm, s);
 }
 
 }  // namespace gbmv

@@ -131,6 +131,7 @@ SIGNATURES = [
     ("gbmv_chem_dirk_evolve_async", C.c_int, [_VP, C.c_double, C.c_double, _VP, C.c_double,
                                               C.POINTER(_DirkOpts), _VP, _VP, _VP]),
     ("gbmv_chem_dirk_block", C.c_int, [_VP, C.c_int]),
+    ("gbmv_chem_dirk_retried", C.c_int, [_VP, C.POINTER(C.c_int), C.c_int, _VP]),
     ("gbmv_chem_set_newton_occupancy", C.c_int, [_VP, C.c_int]),
     ("gbmv_mri_fast_evolve", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.POINTER(_VP),
                                        C.c_double, C.c_int, C.POINTER(_VP), C.c_double,
@@ -436,6 +437,14 @@ class Chem:
     def set_newton_occupancy(self, blocks_per_sm: int):
         """Resident blocks per SM of the fused Newton kernel (0 = default deep grid)."""
         _check(load().gbmv_chem_set_newton_occupancy(self.c, blocks_per_sm), "set_newton_occupancy")
+
+    def dirk_retried(self, max_cells=1 << 20, stream=None):
+        """Cells the last GBMV_MIXED DIRK call integrated again in FP64 (gbmv_chem_dirk_retried):
+        their indices as a numpy array."""
+        buf = (C.c_int * max_cells)()
+        n = _check(load().gbmv_chem_dirk_retried(self.c, buf, max_cells, _stream_ptr(stream)),
+                   "gbmv_chem_dirk_retried", allow=range(0, 1 << 31))
+        return np.array(buf[:min(n, max_cells)], dtype=np.int64)
 
     def dirk_block(self, precision=FP64) -> int:
         """Block size the autotuner picked for a precision (0 = not tuned yet)."""

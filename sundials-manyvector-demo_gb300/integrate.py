@@ -911,15 +911,27 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
     return st
 
 
-def batched_gmres(matvec, b, m=10, rtol=1e-13):
+def batched_gmres(matvec, b, m=10, rtol=1e-13, precond=None, cycles=1):
     """Matrix-free GMRES on many independent small systems at once: b is [ncell, k] (one
     right-hand side of k entries per cell), matvec(v) applies every cell's operator to the
     rows of v ([ncell, k]).  Each cell builds its own Krylov basis (Arnoldi with modified
     Gram-Schmidt and one re-orthogonalisation, Givens rotations on its Hessenberg matrix), all
     cells advancing together, one matvec per iteration for all of them; at most m iterations
     (m = k solves each system exactly in exact arithmetic), fewer once every cell's residual
-    is below rtol times its |b|.  Returns (x [ncell, k], iterations)."""
+    is below rtol times its |b|.  precond: None, or per-row factors d [ncell, k] for left
+    (Jacobi) preconditioning, GMRES then running on diag(d) A x = diag(d) b.  cycles > 1
+    restarts from the residual b - A x (restarted GMRES(m)).
+    Returns (x [ncell, k], total iterations)."""
     import torch
+    if cycles > 1:
+        x, its = batched_gmres(matvec, b, m, rtol, precond)
+        for _ in range(cycles - 1):
+            dx, it = batched_gmres(matvec, b - matvec(x), m, rtol, precond)
+            x, its = x + dx, its + it
+        return x, its
+    if precond is not None:
+        d = precond
+        return batched_gmres(lambda v: d * matvec(v), d * b, m, rtol)
     n, k = b.shape
     m = min(m, k)
     dt = b.dtype
@@ -1032,7 +1044,22 @@ class ChemHydroImex:
 
     def setup(self, t, y, gamma):
         if self.linear_solver == "gmres":
+            # Jacobi preconditioner: 1 / diag(I - gamma J) at the setup state, the diagonal
+            # probed by ten Jacobian actions along the species unit vectors (the scaled
+            # chemistry Jacobian spans many decades: unpreconditioned Krylov loses digits)
+            import torch
             self.gamma, self.t_lin = gamma, t
+            y5 = y[5].reshape(-1)
+            n = y5.numel() // 10
+            e = torch.zeros_like(y5)
+            jv = torch.empty_like(y5)
+            diag = torch.empty(n, 10, dtype=y5.dtype, device=y5.device)
+            for sp in range(10):
+                e.zero_()
+                e.view(n, 10)[:, sp] = 1.0
+                self.chem.jvp(t, y5, e, jv, self.tu)
+                diag[:, sp] = 1.0 - gamma * jv.view(n, 10)[:, sp]
+            self.precond = torch.where(diag != 0, 1.0 / diag, torch.ones_like(diag))
             return 0
         self.chem.calculate_jacobian_cvklu(t, y[5].view(-1), self.J, self.tu)
         self.g.form_newton_matrix(self.J, gamma)
@@ -1047,7 +1074,8 @@ class ChemHydroImex:
             def matvec(v):
                 self.chem.jvp(self.t_lin, y, v.reshape(-1), jv, self.tu)
                 return v - self.gamma * jv.view(-1, 10)
-            x, it = batched_gmres(matvec, b[5].reshape(-1, 10))
+            x, it = batched_gmres(matvec, b[5].reshape(-1, 10), precond=self.precond,
+                                  cycles=2)
             self.krylov_iters += it
             return list(b[:5]) + [x.view(b[5].shape)]
         x = torch.empty_like(b[5])

@@ -202,3 +202,22 @@ def test_mri_fast_evolve_with_forcing(cuda, tables):
     oc2 = O.Chem(tables, wl["scale"].reshape(-1))
     zu, _, _ = oc2.dirk_evolve(wl["fields"][5].reshape(-1), t0, tout, TU, **OPTS)
     assert np.max(np.abs(zu.reshape(n, 10) - zo)) > 1e-8
+
+
+def test_mixed_dirk_second_pass_gives_the_fp64_result(cuda, tables):
+    """The FP32-LU DIRK sends the cells it cannot finish to an FP64 second pass from their
+    start state: on the 64^3 static-chemistry inputs (where a few cells' Newton iterations
+    keep failing on their FP32 factor) no cell fails, and every retried cell ends with exactly
+    the FP64 form's state and statistics."""
+    torch = cuda
+    import gbmv
+    n, tout = 64 ** 3, 1e-3
+    y, _ = W.primordial(n, seed=W.SEED_BASE + 2)
+    scale = y.reshape(-1)
+    zm, sm, nfm, cm = _gpu_run(torch, tables, scale, tout, precision=1, block=64, **OPTS)
+    retried = cm.dirk_retried()
+    z64, s64, nf64, _ = _gpu_run(torch, tables, scale, tout, precision=0, block=64, **OPTS)
+    assert nfm == 0 and nf64 == 0
+    assert len(retried) >= 1  # the inputs have cells the FP32 pass cannot finish
+    assert np.array_equal(zm[retried], z64[retried])
+    assert np.array_equal(sm[retried], s64[retried])
