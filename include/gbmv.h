@@ -292,10 +292,12 @@ typedef struct {
 void gbmv_dirk_opts_default(gbmv_dirk_opts* o);
 
 /* Integrate every cell's chemistry dz/dt = time_units * f_chem(z) (scaled variables, as
- * gbmv_chem_rhs) from t0 to tout with an adaptive TR-BDF2 ESDIRK and modified Newton on
- * per-cell 10x10 systems, each cell on its own step sequence, in one persistent launch that
- * retires finished cells and pulls new ones.  It replaces the fast-stage integration of the
- * chemistry drivers: ARKStep DIRK + Jfast/Jimpl + the block solver
+ * gbmv_chem_rhs) from t0 to tout with the adaptive ESDIRK of opts->table and modified Newton
+ * on per-cell 10x10 systems, each cell on its own step sequence, in one persistent launch
+ * that retires finished cells and pulls new ones.  In the GBMV_MIXED form the cells whose
+ * FP32 pass fails are integrated again from their start state by a second, FP64 launch over
+ * just those cells (counted by gbmv_chem_dirk_retried).  It replaces the fast-stage
+ * integration of the chemistry drivers: ARKStep DIRK + Jfast/Jimpl + the block solver
  * (src/primordial_ode_main.cpp) and the rank-local MRI inner stepper's evolve
  * (src/multirate_chem_hydro_main.cpp:1114-1224), with per-cell instead of rank-wide step
  * control.  y: 10 * ncells device doubles, updated in place; the temperature state is
