@@ -286,6 +286,12 @@ typedef struct {
                         ARK437L2SA_DIRK_7_3_4 (the reference's chemistry inputs, default) or 102
                         TRBDF2_3_3_2; any stiffly accurate ESDIRK of gbmv_butcher_table with an
                         explicit first stage and one diagonal value is accepted */
+  int setup_batch;   /* Newton-matrix setups are gathered per warp: a cell that needs one waits
+                        (no F evaluation) until this many cells of its warp wait, or every
+                        active cell of the warp waits, or one has waited 4 x setup_batch
+                        passes, or no cell is left to start; then they set up together.  1 =
+                        every cell sets up at once.  Every cell runs the same computation
+                        whatever the value: only the interleaving changes (default 8) */
 } gbmv_dirk_opts;
 
 /* Fill *o with the defaults above (rtol 1e-6, atol 1e-10). */

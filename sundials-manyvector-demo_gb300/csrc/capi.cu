@@ -585,6 +585,7 @@ void gbmv_dirk_opts_default(gbmv_dirk_opts* o) {
   o->refine = 0;
   o->block = 0;
   o->table = 0;
+  o->setup_batch = 8;
 }
 
 // The DIRK table of the options (0: ARK437L2SA_DIRK_7_3_4, the reference's chemistry inputs'
@@ -662,9 +663,9 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
       o->maxnef < 1 || o->maxncf < 1 || o->refine < 0 || o->refine > 8 ||
       (o->precision != GBMV_FP64 && o->precision != GBMV_MIXED) ||
       (o->block != 0 && o->block != 32 && o->block != 64 && o->block != 128) ||
-      !(tout > t0) || !(tunit > 0.0)) {
+      o->setup_batch < 1 || o->setup_batch > 32 || !(tout > t0) || !(tunit > 0.0)) {
     set_error("bad DIRK options (tolerances > 0, growth >= 1, hmax >= 0, counts >= 1, refine 0-8, "
-              "block 0/32/64/128, tout > t0, time_units > 0)");
+              "block 0/32/64/128, setup_batch 1-32, tout > t0, time_units > 0)");
     return GBMV_EINVAL;
   }
   O->t0 = t0;
@@ -686,6 +687,7 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
   O->maxnef = o->maxnef;
   O->maxncf = o->maxncf;
   O->refine = o->precision == GBMV_MIXED ? o->refine : 0;
+  O->setup_batch = o->setup_batch;
   O->mixed_temp = o->precision == GBMV_MIXED;
   O->nforcing = 0;
   O->tshift = 0.0;

@@ -76,6 +76,7 @@ struct DirkOpts {
   double growth, etamx1, hmax;  // step growth bounds (after the first step / on it); hmax <= 0: none
   int maxcor, max_steps, msbp, maxnef, maxncf;
   int refine;      // FP32 LU: refinement steps per Newton solve
+  int setup_batch; // waiting lanes of a warp that trigger its matrix setups (1: no waiting)
   int mixed_temp;  // temperature iterations 1-8 in FP32
   // MRI forcing added to F: sum_i tau^i fz[i] (chemistry components, 10 per cell),
   // tau = (t - tshift) / tscale

@@ -268,6 +268,12 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
   int nst = 0, nst_lp = 0, nef_s = 0, ncf_s = 0;
   int c_nni = 0, c_netf = 0, c_ncf = 0, c_nsetup = 0, c_nfe = 0;
   bool jcur = false, force_setup = true, last = false;
+  // step start requested / Newton-matrix setup pending (the lane waits for its warp's setup
+  // pass) / passes waited
+  bool setup = false, pend = false;
+  int waited = 0;
+  const int batch = O.setup_batch;
+  const int max_wait = 4 * O.setup_batch;
 
   while (true) {
     // ---- refill: lanes without a cell take the next indices (one atomic per warp)
@@ -300,173 +306,18 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           jcur = false;
           force_setup = true;
           last = false;
+          setup = pend = false;
         } else {
           exhausted = true;
         }
       }
     }
     if (__all_sync(full, i < 0)) break;
-    if (i < 0) continue;
+    bool retire = false, failed = false;
 
-    // ---- one evaluation of F per pass (at Y for the first stage, else at the iterate)
-    double f[10];
-    const double tf = (phase == kPhK1) ? t : t + O.T.c[stage] * h;
-    dirk_F<BS>(P, S, i, phase == kPhK1 ? Y : Z, O, tf, mixed_temp, Tsc, dTsc, f);
-    ++c_nfe;
-
-    bool setup = false, retire = false, failed = false;
-    if (phase == kPhK1) {
-#pragma unroll
-      for (int s = 0; s < 10; ++s) K1[s * BS] = f[s];
-      Tsy = Tsc;
-      dTsy = dTsc;
-      if (h <= 0.0) {  // initial step from the derivative size
-        double s2 = 0.0;
-#pragma unroll
-        for (int s = 0; s < 10; ++s) {
-          const double v = f[s] / (O.rtol * fabs(Y[s * BS]) + O.atol);
-          s2 += v * v;
-        }
-        const double fn = sqrt(s2 / 10.0);
-        h = (fn > 0.0) ? O.h0fac / fn : O.tout - t;
-      }
-      if (O.hmax > 0.0 && h > O.hmax) h = O.hmax;
-      setup = true;
-    } else if (phase == kPhNewton) {
-      const double gam = h * O.T.gamma;
-      double g[10];
-#pragma unroll
-      for (int s = 0; s < 10; ++s) g[s] = B[s * BS] + gam * f[s] - Z[s * BS];
-      int piv[10];
-#pragma unroll
-      for (int s = 0; s < 10; ++s) piv[s] = PV[s * BS];
-      double dl[10];
-      if (sizeof(LU) == 8) {
-#pragma unroll
-        for (int s = 0; s < 10; ++s) dl[s] = g[s];
-        lus10_strided<LU, double>(L, BS, piv, dl);
-      } else {
-        // equilibrated FP32 solve: (R A C) u = R g, dl = C u
-        LU u[10];
-#pragma unroll
-        for (int s = 0; s < 10; ++s) u[s] = to_lu<LU>(g[s] * pow2(EQ[s * BS]));
-        lus10_strided<LU, LU>(L, BS, piv, u);
-#pragma unroll
-        for (int s = 0; s < 10; ++s) dl[s] = from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
-        if (REF) {
-          for (int it = 0; it < O.refine; ++it) {  // r = g - A dl in FP64, solve, update
-            double r[10];
-#pragma unroll
-            for (int s = 0; s < 10; ++s) r[s] = g[s];
-#pragma unroll
-            for (int e = 0; e < 64; ++e) {
-              const int row = kJacPattern[e][0], col = kJacPattern[e][1];
-              r[row] -= A[(col * 10 + row) * BS] * dl[col];
-            }
-#pragma unroll
-            for (int s = 0; s < 10; ++s) u[s] = to_lu<LU>(r[s] * pow2(EQ[s * BS]));
-            lus10_strided<LU, LU>(L, BS, piv, u);
-#pragma unroll
-            for (int s = 0; s < 10; ++s) dl[s] += from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
-          }
-        }
-      }
-      if (gam != gp) {
-        const double sc = 2.0 / (1.0 + gam / gp);
-#pragma unroll
-        for (int s = 0; s < 10; ++s) dl[s] *= sc;
-      }
-      double s2 = 0.0;
-#pragma unroll
-      for (int s = 0; s < 10; ++s) {
-        Z[s * BS] += dl[s];
-        const double v = dl[s] * (double)EW[s * BS];
-        s2 += v * v;
-      }
-      const double del = sqrt(s2 / 10.0);
-      ++m;
-      ++c_nni;
-      if (m > 1) crate = fmax(0.3 * crate, del / delp);
-      const double dcon = fmin(crate, 1.0) * del / O.nlscoef;
-      if (dcon <= 1.0) {
-        phase = kPhStage;
-      } else if ((m > 1 && del > 2.3 * delp) || m >= O.maxcor || !(del == del)) {
-        // Newton failure: with a matrix from an earlier step set up a current one at the
-        // same h, else cut the step
-        ++ncf_s;
-        ++c_ncf;
-        if (ncf_s >= O.maxncf) {
-          retire = failed = true;
-        } else {
-          if (jcur) h *= 0.25;
-          else force_setup = true;
-          setup = true;
-        }
-      } else {
-        delp = del;
-      }
-    } else if (stage < ns - 1) {  // kPhStage, not the last stage: keep K_stage, next stage
-#pragma unroll
-      for (int s = 0; s < 10; ++s) KG[((stage - 1) * 10 + s) * kst] = f[s];
-      ++stage;  // predictor: the converged value of this stage, already in Z
-      dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
-      m = 0;
-      phase = kPhNewton;
-    } else {  // kPhStage of the last stage: error test
-      double acc[10];
-      const double e0 = O.T.e[0];
-#pragma unroll
-      for (int s = 0; s < 10; ++s) acc[s] = e0 * K1[s * BS];
-      for (int j = 1; j < ns - 1; ++j) {
-        const double ej = O.T.e[j];
-        if (ej == 0.0) continue;
-#pragma unroll
-        for (int s = 0; s < 10; ++s) acc[s] += ej * KG[((j - 1) * 10 + s) * kst];
-      }
-      const double el = O.T.e[ns - 1];
-      double s2 = 0.0;
-#pragma unroll
-      for (int s = 0; s < 10; ++s) {
-        const double e = h * (acc[s] + el * f[s]);
-        const double v = e * (double)EW[s * BS];
-        s2 += v * v;
-      }
-      const double dsm = sqrt(s2 / 10.0);
-      if (dsm <= 1.0) {
-        ++nst;
-        t = last ? O.tout : t + h;
-#pragma unroll
-        for (int s = 0; s < 10; ++s) {
-          Y[s * BS] = Z[s * BS];
-          K1[s * BS] = f[s];  // stiffly accurate: F(stage 3) = F(y_{n+1})
-        }
-        Tsy = Tsc;
-        dTsy = dTsc;
-        jcur = false;
-        double eta = (dsm > 0.0) ? dirk_eta(O.safety, dsm, O.T.p) : 1.0e300;
-        eta = fmin(eta, nst == 1 ? O.etamx1 : O.growth);
-        if (nef_s > 0 || ncf_s > 0) eta = fmin(eta, 1.0);
-        h *= eta;
-        if (O.hmax > 0.0 && h > O.hmax) h = O.hmax;
-        nef_s = ncf_s = 0;
-        if (last) retire = true;
-        else if (nst >= O.max_steps) retire = failed = true;
-        else setup = true;
-      } else {
-        ++nef_s;
-        ++c_netf;
-        if (nef_s >= O.maxnef) {
-          retire = failed = true;
-        } else {
-          double eta = fmax(0.1, dirk_eta(O.safety, dsm, O.T.p));
-          if (nef_s >= 2) eta = fmin(eta, 0.3);
-          h *= eta;
-          setup = true;
-        }
-      }
-    }
-
-    while (setup && !retire) {  // start (or restart) a step at (t, Y)
+    // ---- step start (or restart) at (t, Y): weights, predictor; a lane whose Newton matrix
+    // must be set up waits for the warp's setup pass below
+    if (i >= 0 && setup) {
       setup = false;
       last = (t + h >= O.tout);
       if (last) h = O.tout - t;
@@ -480,34 +331,221 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
       }
       const double gam = h * O.T.gamma;
       if (force_setup || nst >= nst_lp + O.msbp || !(fabs(gam / gp - 1.0) <= O.dgmax)) {
-        // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored (inline: an
-        // out-of-line call measured 4 % slower in the mixed form)
-        int piv[10];
-        const int info = dirk_setup<LU, REF, BS>(P, S, i, O, Y, A, L, EQ, gam, Tsy, dTsy, piv);
+        pend = true;
+        waited = 0;
+      } else {
+        stage = 1;
+        dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
+        m = 0;
+        phase = kPhNewton;
+      }
+    }
+
+    // ---- the warp's setup pass: the waiting lanes set up together once enough of them wait
+    // (a setup costs about two F evaluations and every lane of the warp pays for it in time,
+    // so one lane setting up alone stalls the other 31)
+    const unsigned pm = __ballot_sync(full, pend);
+    if (pm) {
+      const int npend = __popc(pm);
+      const int nact = __popc(__ballot_sync(full, i >= 0));
+      const int wmax = __reduce_max_sync(full, pend ? waited : 0);
+      const bool drained = __any_sync(full, exhausted);
+      if (npend >= batch || npend == nact || wmax >= max_wait || drained) {
+        if (pend) {
+          pend = false;
+          // Newton matrix I - gamma J with J evaluated at (Y, Ts(Y)), factored (inline: an
+          // out-of-line call measured 4 % slower in the mixed form)
+          const double gam = h * O.T.gamma;
+          int piv[10];
+          const int info =
+              dirk_setup<LU, REF, BS>(P, S, i, O, Y, A, L, EQ, gam, Tsy, dTsy, piv);
 #pragma unroll
-        for (int s = 0; s < 10; ++s) PV[s * BS] = (signed char)piv[s];
-        gp = gam;
-        nst_lp = nst;
-        crate = 1.0;
-        jcur = true;
-        force_setup = false;
-        ++c_nsetup;
-        if (info) {  // singular Newton matrix: a recoverable failure, cut the step and retry
+          for (int s = 0; s < 10; ++s) PV[s * BS] = (signed char)piv[s];
+          gp = gam;
+          nst_lp = nst;
+          crate = 1.0;
+          jcur = true;
+          force_setup = false;
+          ++c_nsetup;
+          if (info) {  // singular Newton matrix: a recoverable failure, cut the step and retry
+            ++ncf_s;
+            ++c_ncf;
+            if (ncf_s >= O.maxncf) {
+              retire = failed = true;
+            } else {
+              h *= 0.25;
+              force_setup = true;
+              setup = true;
+            }
+          } else {
+            stage = 1;
+            dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
+            m = 0;
+            phase = kPhNewton;
+          }
+        }
+      } else if (pend) {
+        ++waited;
+      }
+    }
+
+    // ---- one evaluation of F per pass (at Y for the first stage, else at the iterate)
+    if (i >= 0 && !pend && !setup && !retire) {
+      double f[10];
+      const double tf = (phase == kPhK1) ? t : t + O.T.c[stage] * h;
+      dirk_F<BS>(P, S, i, phase == kPhK1 ? Y : Z, O, tf, mixed_temp, Tsc, dTsc, f);
+      ++c_nfe;
+
+      if (phase == kPhK1) {
+#pragma unroll
+        for (int s = 0; s < 10; ++s) K1[s * BS] = f[s];
+        Tsy = Tsc;
+        dTsy = dTsc;
+        if (h <= 0.0) {  // initial step from the derivative size
+          double s2 = 0.0;
+#pragma unroll
+          for (int s = 0; s < 10; ++s) {
+            const double v = f[s] / (O.rtol * fabs(Y[s * BS]) + O.atol);
+            s2 += v * v;
+          }
+          const double fn = sqrt(s2 / 10.0);
+          h = (fn > 0.0) ? O.h0fac / fn : O.tout - t;
+        }
+        if (O.hmax > 0.0 && h > O.hmax) h = O.hmax;
+        setup = true;
+      } else if (phase == kPhNewton) {
+        const double gam = h * O.T.gamma;
+        double g[10];
+#pragma unroll
+        for (int s = 0; s < 10; ++s) g[s] = B[s * BS] + gam * f[s] - Z[s * BS];
+        int piv[10];
+#pragma unroll
+        for (int s = 0; s < 10; ++s) piv[s] = PV[s * BS];
+        double dl[10];
+        if (sizeof(LU) == 8) {
+#pragma unroll
+          for (int s = 0; s < 10; ++s) dl[s] = g[s];
+          lus10_strided<LU, double>(L, BS, piv, dl);
+        } else {
+          // equilibrated FP32 solve: (R A C) u = R g, dl = C u
+          LU u[10];
+#pragma unroll
+          for (int s = 0; s < 10; ++s) u[s] = to_lu<LU>(g[s] * pow2(EQ[s * BS]));
+          lus10_strided<LU, LU>(L, BS, piv, u);
+#pragma unroll
+          for (int s = 0; s < 10; ++s) dl[s] = from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
+          if (REF) {
+            for (int it = 0; it < O.refine; ++it) {  // r = g - A dl in FP64, solve, update
+              double r[10];
+#pragma unroll
+              for (int s = 0; s < 10; ++s) r[s] = g[s];
+#pragma unroll
+              for (int e = 0; e < 64; ++e) {
+                const int row = kJacPattern[e][0], col = kJacPattern[e][1];
+                r[row] -= A[(col * 10 + row) * BS] * dl[col];
+              }
+#pragma unroll
+              for (int s = 0; s < 10; ++s) u[s] = to_lu<LU>(r[s] * pow2(EQ[s * BS]));
+              lus10_strided<LU, LU>(L, BS, piv, u);
+#pragma unroll
+              for (int s = 0; s < 10; ++s) dl[s] += from_lu(u[s]) * pow2(EQ[(10 + s) * BS]);
+            }
+          }
+        }
+        if (gam != gp) {
+          const double sc = 2.0 / (1.0 + gam / gp);
+#pragma unroll
+          for (int s = 0; s < 10; ++s) dl[s] *= sc;
+        }
+        double s2 = 0.0;
+#pragma unroll
+        for (int s = 0; s < 10; ++s) {
+          Z[s * BS] += dl[s];
+          const double v = dl[s] * (double)EW[s * BS];
+          s2 += v * v;
+        }
+        const double del = sqrt(s2 / 10.0);
+        ++m;
+        ++c_nni;
+        if (m > 1) crate = fmax(0.3 * crate, del / delp);
+        const double dcon = fmin(crate, 1.0) * del / O.nlscoef;
+        if (dcon <= 1.0) {
+          phase = kPhStage;
+        } else if ((m > 1 && del > 2.3 * delp) || m >= O.maxcor || !(del == del)) {
+          // Newton failure: with a matrix from an earlier step set up a current one at the
+          // same h, else cut the step
           ++ncf_s;
           ++c_ncf;
           if (ncf_s >= O.maxncf) {
             retire = failed = true;
           } else {
-            h *= 0.25;
-            force_setup = true;
+            if (jcur) h *= 0.25;
+            else force_setup = true;
+            setup = true;
+          }
+        } else {
+          delp = del;
+        }
+      } else if (stage < ns - 1) {  // kPhStage, not the last stage: keep K_stage, next stage
+#pragma unroll
+        for (int s = 0; s < 10; ++s) KG[((stage - 1) * 10 + s) * kst] = f[s];
+        ++stage;  // predictor: the converged value of this stage, already in Z
+        dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
+        m = 0;
+        phase = kPhNewton;
+      } else {  // kPhStage of the last stage: error test
+        double acc[10];
+        const double e0 = O.T.e[0];
+#pragma unroll
+        for (int s = 0; s < 10; ++s) acc[s] = e0 * K1[s * BS];
+        for (int j = 1; j < ns - 1; ++j) {
+          const double ej = O.T.e[j];
+          if (ej == 0.0) continue;
+#pragma unroll
+          for (int s = 0; s < 10; ++s) acc[s] += ej * KG[((j - 1) * 10 + s) * kst];
+        }
+        const double el = O.T.e[ns - 1];
+        double s2 = 0.0;
+#pragma unroll
+        for (int s = 0; s < 10; ++s) {
+          const double e = h * (acc[s] + el * f[s]);
+          const double v = e * (double)EW[s * BS];
+          s2 += v * v;
+        }
+        const double dsm = sqrt(s2 / 10.0);
+        if (dsm <= 1.0) {
+          ++nst;
+          t = last ? O.tout : t + h;
+#pragma unroll
+          for (int s = 0; s < 10; ++s) {
+            Y[s * BS] = Z[s * BS];
+            K1[s * BS] = f[s];  // stiffly accurate: F(last stage) = F(y_{n+1})
+          }
+          Tsy = Tsc;
+          dTsy = dTsc;
+          jcur = false;
+          double eta = (dsm > 0.0) ? dirk_eta(O.safety, dsm, O.T.p) : 1.0e300;
+          eta = fmin(eta, nst == 1 ? O.etamx1 : O.growth);
+          if (nef_s > 0 || ncf_s > 0) eta = fmin(eta, 1.0);
+          h *= eta;
+          if (O.hmax > 0.0 && h > O.hmax) h = O.hmax;
+          nef_s = ncf_s = 0;
+          if (last) retire = true;
+          else if (nst >= O.max_steps) retire = failed = true;
+          else setup = true;
+        } else {
+          ++nef_s;
+          ++c_netf;
+          if (nef_s >= O.maxnef) {
+            retire = failed = true;
+          } else {
+            double eta = fmax(0.1, dirk_eta(O.safety, dsm, O.T.p));
+            if (nef_s >= 2) eta = fmin(eta, 0.3);
+            h *= eta;
             setup = true;
           }
         }
       }
-      stage = 1;
-      if (!retire) dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
-      m = 0;
-      phase = kPhNewton;
     }
 
     if (retire) {
@@ -532,6 +570,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         else atomicAdd(nfail, 1);
       }
       i = -1;
+      setup = pend = false;
     }
   }
 }

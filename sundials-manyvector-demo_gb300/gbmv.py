@@ -44,7 +44,8 @@ class _DirkOpts(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("rtol", "atol", "nlscoef", "h0", "safety", "dgmax",
                                           "growth", "etamx1", "hmax")] + \
                [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf",
-                                       "precision", "refine", "block", "table")]
+                                       "precision", "refine", "block", "table",
+                                       "setup_batch")]
 
 
 MAX_STAGES = 7

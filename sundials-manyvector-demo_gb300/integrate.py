@@ -911,27 +911,54 @@ def ark_imex_evolve(prob, t0, tf, y, rtol=1e-6, atol=1e-10, h0=0.0, hmax=math.in
     return st
 
 
-def batched_gmres(matvec, b, m=10, rtol=1e-13, precond=None, cycles=1):
+def batched_equilibrate(A, sweeps=10):
+    """Row and column factors (r, c), each [ncell, k], that equilibrate every block of A
+    ([ncell, k, k]): diag(r) A diag(c) has the maxima of its rows and columns near 1 (Ruiz's
+    iteration: each sweep divides the rows, then the columns, by
+    the square roots of their maxima; D. Ruiz, "A scaling algorithm to equilibrate both rows
+    and columns norms in matrices", RAL-TR-2001-034).  Zero rows or columns keep factor 1.
+    The scaling for batched_gmres (precond=r, right=c) on badly scaled blocks."""
+    import torch
+    B = A.abs()
+    r = torch.ones(A.shape[:2], dtype=A.dtype, device=A.device)
+    c = torch.ones_like(r)
+    for _ in range(sweeps):
+        mr = B.amax(dim=2)
+        dr = torch.where(mr > 0, torch.rsqrt(mr), torch.ones_like(mr))
+        B = B * dr[:, :, None]
+        r = r * dr
+        mc = B.amax(dim=1)
+        dc = torch.where(mc > 0, torch.rsqrt(mc), torch.ones_like(mc))
+        B = B * dc[:, None, :]
+        c = c * dc
+    return r, c
+
+
+def batched_gmres(matvec, b, m=10, rtol=1e-13, precond=None, right=None, cycles=1):
     """Matrix-free GMRES on many independent small systems at once: b is [ncell, k] (one
     right-hand side of k entries per cell), matvec(v) applies every cell's operator to the
     rows of v ([ncell, k]).  Each cell builds its own Krylov basis (Arnoldi with modified
     Gram-Schmidt and one re-orthogonalisation, Givens rotations on its Hessenberg matrix), all
     cells advancing together, one matvec per iteration for all of them; at most m iterations
     (m = k solves each system exactly in exact arithmetic), fewer once every cell's residual
-    is below rtol times its |b|.  precond: None, or per-row factors d [ncell, k] for left
-    (Jacobi) preconditioning, GMRES then running on diag(d) A x = diag(d) b.  cycles > 1
-    restarts from the residual b - A x (restarted GMRES(m)).
-    Returns (x [ncell, k], total iterations)."""
+    is below rtol times its |b|.  A cell stops using its basis at its own convergence or at a
+    breakdown of its Arnoldi process (a zero new vector: its Krylov space is invariant), so
+    later iterations of the other cells leave its solution alone.  Scaling: precond, None or per-row factors dl [ncell, k] (left), and
+    right, None or per-column factors dr (right): GMRES then runs on diag(dl) A diag(dr) u =
+    diag(dl) b and returns x = diag(dr) u.  cycles > 1 restarts from the residual b - A x
+    (restarted GMRES(m)).  Returns (x [ncell, k], total iterations)."""
     import torch
     if cycles > 1:
-        x, its = batched_gmres(matvec, b, m, rtol, precond)
+        x, its = batched_gmres(matvec, b, m, rtol, precond, right)
         for _ in range(cycles - 1):
-            dx, it = batched_gmres(matvec, b - matvec(x), m, rtol, precond)
+            dx, it = batched_gmres(matvec, b - matvec(x), m, rtol, precond, right)
             x, its = x + dx, its + it
         return x, its
-    if precond is not None:
-        d = precond
-        return batched_gmres(lambda v: d * matvec(v), d * b, m, rtol)
+    if precond is not None or right is not None:
+        dl = precond if precond is not None else torch.ones_like(b)
+        dr = right if right is not None else torch.ones_like(b)
+        u, it = batched_gmres(lambda v: dl * matvec(dr * v), dl * b, m, rtol)
+        return dr * u, it
     n, k = b.shape
     m = min(m, k)
     dt = b.dtype
@@ -943,6 +970,9 @@ def batched_gmres(matvec, b, m=10, rtol=1e-13, precond=None, cycles=1):
     sn = torch.zeros(n, m, dtype=dt, device=b.device)
     g = torch.zeros(n, m + 1, dtype=dt, device=b.device)
     g[:, 0] = beta
+    # columns of the basis each cell uses: it stops at convergence or breakdown
+    kc = torch.where(beta > 0, torch.full_like(beta, m, dtype=torch.long),
+                     torch.zeros_like(beta, dtype=torch.long))
     it = 0
     for j in range(m):
         w = matvec(V[j])
@@ -968,12 +998,16 @@ def batched_gmres(matvec, b, m=10, rtol=1e-13, precond=None, cycles=1):
         g[:, j + 1] = -sn[:, j] * g[:, j]
         g[:, j] = cs[:, j] * g[:, j]
         it = j + 1
-        if bool((g[:, j + 1].abs() <= rtol * beta).all()):
+        done = (g[:, j + 1].abs() <= rtol * beta) | (hn == 0)
+        kc = torch.where(done & (kc > j + 1), torch.full_like(kc, j + 1), kc)
+        if bool((kc <= j + 1).all()):
             break
     R = H[:, :it, :it]
+    cols = torch.arange(it, device=b.device)
+    unused = cols[None, :] >= kc[:, None]  # basis columns past the cell's own stop
     diag = torch.diagonal(R, dim1=1, dim2=2)
-    dead = diag == 0  # a cell whose Krylov space closed earlier: those components are 0
-    R = R + torch.diag_embed(dead.to(dt))
+    dead = unused | (diag == 0)
+    R = torch.where(dead[:, None, :], torch.zeros_like(R), R) + torch.diag_embed(dead.to(dt))
     gy = torch.where(dead, torch.zeros_like(g[:, :it]), g[:, :it])
     y = torch.linalg.solve_triangular(R, gy[:, :, None], upper=True)[:, :, 0]
     x = torch.zeros_like(b)
@@ -1044,22 +1078,26 @@ class ChemHydroImex:
 
     def setup(self, t, y, gamma):
         if self.linear_solver == "gmres":
-            # Jacobi preconditioner: 1 / diag(I - gamma J) at the setup state, the diagonal
-            # probed by ten Jacobian actions along the species unit vectors (the scaled
-            # chemistry Jacobian spans many decades: unpreconditioned Krylov loses digits)
+            # two-sided diagonal scaling at the setup state: ten Jacobian actions along the
+            # species unit vectors give the columns e_k - gamma J e_k of every block, which are
+            # equilibrated (batched_equilibrate) and then dropped; the Krylov iterations apply
+            # J only through gbmv_chem_jvp.  The blocks' columns and rows span many decades
+            # (2-norm condition numbers up to 1e32 on the chem-hydro state, a few 1e9 once
+            # equilibrated): row (Jacobi) scaling alone, or one row and column sweep, leaves
+            # GMRES's residual norm blind to the small components.
             import torch
             self.gamma, self.t_lin = gamma, t
             y5 = y[5].reshape(-1)
             n = y5.numel() // 10
             e = torch.zeros_like(y5)
             jv = torch.empty_like(y5)
-            diag = torch.empty(n, 10, dtype=y5.dtype, device=y5.device)
+            A = torch.empty(n, 10, 10, dtype=y5.dtype, device=y5.device)
             for sp in range(10):
                 e.zero_()
                 e.view(n, 10)[:, sp] = 1.0
                 self.chem.jvp(t, y5, e, jv, self.tu)
-                diag[:, sp] = 1.0 - gamma * jv.view(n, 10)[:, sp]
-            self.precond = torch.where(diag != 0, 1.0 / diag, torch.ones_like(diag))
+                A[:, :, sp] = e.view(n, 10) - gamma * jv.view(n, 10)
+            self.precond, self.right = batched_equilibrate(A)
             return 0
         self.chem.calculate_jacobian_cvklu(t, y[5].view(-1), self.J, self.tu)
         self.g.form_newton_matrix(self.J, gamma)
@@ -1075,7 +1113,7 @@ class ChemHydroImex:
                 self.chem.jvp(self.t_lin, y, v.reshape(-1), jv, self.tu)
                 return v - self.gamma * jv.view(-1, 10)
             x, it = batched_gmres(matvec, b[5].reshape(-1, 10), precond=self.precond,
-                                  cycles=2)
+                                  right=self.right, cycles=2)
             self.krylov_iters += it
             return list(b[:5]) + [x.view(b[5].shape)]
         x = torch.empty_like(b[5])

@@ -116,6 +116,27 @@ def test_dirk_block_sizes_bitwise_equal_and_autotune(cuda, tables):
     assert np.array_equal(z, ref[0]) and np.array_equal(st, ref[1])
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_dirk_setup_batching_bitwise_equal(cuda, tables, precision):
+    """Gathering a warp's Newton-matrix setups (setup_batch lanes wait, skipping their F
+    evaluations, until they set up together) changes only the interleaving of the lanes'
+    work: every cell's state, temperature and counters are identical for any setup_batch."""
+    torch = cuda
+    n, tout = 6000, 2e-4   # more cells than resident lanes at 32 threads per block
+    scale = _cells(n, W.SEED_BASE + 505)
+    ref = None
+    for sb in (1, 6, 32):
+        z, st, nf, c = _gpu_run(torch, tables, scale, tout, precision=precision, block=32,
+                                setup_batch=sb, **OPTS)
+        Ts = c.state("Ts").cpu().numpy()
+        assert nf == 0
+        if ref is None:
+            ref = (z, st, Ts)
+        else:
+            assert np.array_equal(z, ref[0]) and np.array_equal(st, ref[1]), sb
+            assert np.array_equal(Ts, ref[2]), sb
+
+
 def test_dirk_every_cell_retired_once_and_histogram(cuda, tables):
     torch = cuda
     import gbmv
@@ -152,7 +173,8 @@ def test_dirk_options_rejected(cuda, tables):
     c = gbmv.Chem(16, tables)
     z = torch.ones(160, dtype=torch.float64, device="cuda")
     for bad in (dict(rtol=0.0), dict(block=48), dict(refine=9), dict(precision=3),
-                dict(maxcor=0), dict(table=13), dict(table=104 + 1000), dict(table=8)):
+                dict(maxcor=0), dict(table=13), dict(table=104 + 1000), dict(table=8),
+                dict(setup_batch=0), dict(setup_batch=33)):
         with pytest.raises(gbmv.GbmvError):
             c.dirk_evolve(0.0, 1e-3, z, TU, **bad)
     with pytest.raises(gbmv.GbmvError):
