@@ -5,8 +5,10 @@
 //     sqrt(gamma p / rho) -- then every field and primitive split into float pairs (hi, lo):
 //     Q2[q][cell], q = rho, mx, my, mz, et, p, ux, uy, uz, c, tracers...;
 //   face_flux_f2_kernel<NCHEM, DIR>: the face flux in float-float arithmetic from Q2 (no FP64
-//     instruction on the common path); faces whose states leave the float range, or touch a
-//     non-positive density (homogeneous Dirichlet ghosts), are computed in FP64 from w;
+//     instruction on the common path), the two Lax-Friedrichs sides of every reconstruction
+//     evaluated together on the paired FP32 instructions (df64x2.cuh); faces whose states
+//     leave the float range, or touch a non-positive density (homogeneous Dirichlet ghosts),
+//     are computed in FP64 from w;
 //   divergence_f2: the FP64 form's divergence pass over fluxes kept as float pairs, the
 //     differences in float-float, the final G - div in FP64 (weno.cu).
 //
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(128, WV == 1 ? GBMV_F2_FAST_MINB : 1)
     if (ok) {
       // characteristic fields keep float-float weights in every mixed form: the reference's
       // eigenbasis (conditioning ~1/c^2) amplifies weight rounding in the back-projection
-      fluid_face_flux<f2, true, 0>(W, g.gamma, S, o, &pre);
+      fluid_face_flux_f2v(W, g.gamma, S, o, pre);
     } else {  // FP64, exactly the FP64 form's arithmetic
       double Wd[6][5];
 #pragma unroll
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(128, WV == 1 ? GBMV_F2_FAST_MINB : 1)
         const float2 t = __ldg(Q2 + (kQ2Base + c) * n + cell[l]);
         cv[l] = nall[l] ? f2(-t.x, -t.y) : f2(t.x, t.y);
       }
-      const f2 r = tracer_face_flux<f2, WV>(S, cv);
+      const f2 r = tracer_face_flux_f2v<WV>(S, cv);
       F[(5 + c) * nfaces + f] = make_float2(r.hi, r.lo);
     }
   }

@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "df64.cuh"
+#include "df64x2.cuh"
 
 namespace gbmv {
 
@@ -211,6 +212,75 @@ __device__ __forceinline__ T weno_pick(T f0, T f1, T f2_, T f3, T f4) {
   else return weno_safe<Plus>(f0, f1, f2_, f3, f4);
 }
 
+// Paired reconstructions (df64x2.cuh): both Lax-Friedrichs sides of a face in one pass, lane x
+// the plus side from f0..f4, lane y the minus side with its stencil reversed -- the minus
+// formula on g0..g4 is the plus formula on g4..g0 (the candidates, linear weights and
+// smoothness indicators map onto each other under the reversal) -- so one instruction stream
+// serves both.  Lane x returns exactly weno_side_f2<true>'s value; lane y the minus side's
+// value up to the rounding of the mirrored evaluation order.
+static __device__ __noinline__ f2v weno_plus_f2v(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
+  const f2v D01 = f0 - f1, D12 = f1 - f2_, D23 = f2_ - f3, D34 = f3 - f4;
+  const f2v dA = D23 - D34, dB = D12 - D23, dC = D01 - D12;  // second differences
+  const f2v eA = dA + f2v_scale(D23, 2.f), eB = D12 + D23, eC = dC - f2v_scale(D12, 2.f);
+  const f2v b13(f2(13.0 / 12.0)), sixth(f2(1.0 / 6.0)), eps(f2(1e-6));
+  const f2v aA = eps + (b13 * f2v_sqr(dA) + f2v_scale(f2v_sqr(eA), 0.25f));
+  const f2v aB = eps + (b13 * f2v_sqr(dB) + f2v_scale(f2v_sqr(eB), 0.25f));
+  const f2v aC = eps + (b13 * f2v_sqr(dC) + f2v_scale(f2v_sqr(eC), 0.25f));
+  const f2v qA = f3 + sixth * (f2v_scale(D23, 2.f) + D34);
+  const f2v qB = f2_ - sixth * (D12 + f2v_scale(D23, 2.f));
+  const f2v qC = f2_ + sixth * (f2v_scale(D01, 2.f) - f2v(f2(5.0)) * D12);
+  const f2v m = f2v_min(f2v_min(aA, aB), aC);
+  const f2v rA = m / aA, rB = m / aB, rC = m / aC;
+  const f2v tA = f2v(f2(0.3)) * f2v_sqr(rA), tB = f2v(f2(0.6)) * f2v_sqr(rB),
+            tC = f2v(f2(0.1)) * f2v_sqr(rC);
+  return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
+}
+// the correction form of weno_side_f2d (species fields of GBMV_MIXED_FAST), paired
+static __device__ __noinline__ f2v weno_plus_f2dv(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
+  const float2 D01 = (f0 - f1).to_float(), D12 = (f1 - f2_).to_float(),
+               D23 = (f2_ - f3).to_float(), D34 = (f3 - f4).to_float();
+  const float2 dA = sub2(D23, D34), dB = sub2(D12, D23), dC = sub2(D01, D12);
+  const float2 eA = fma2(v2(2.f), D23, dA), eB = add2(D12, D23), eC = fma2(v2(-2.f), D12, dC);
+  const float2 b13 = v2(13.f / 12.f), q = v2(0.25f), sixth = v2(1.f / 6.f);
+  const float2 aA = add2(v2(1e-6f), fma2(b13, mul2(dA, dA), mul2(q, mul2(eA, eA))));
+  const float2 aB = add2(v2(1e-6f), fma2(b13, mul2(dB, dB), mul2(q, mul2(eB, eB))));
+  const float2 aC = add2(v2(1e-6f), fma2(b13, mul2(dC, dC), mul2(q, mul2(eC, eC))));
+  // candidate minus central point (plus side: linear weights 0.3, 0.6, 0.1)
+  const float2 cA = mul2(fma2(v2(-4.f), D23, D34), sixth);
+  const float2 cB = mul2(fma2(v2(2.f), D23, D12), v2(-1.f / 6.f));
+  const float2 cC = mul2(fma2(v2(-5.f), D12, mul2(v2(2.f), D01)), sixth);
+  const float2 m = make_float2(fminf(fminf(aA.x, aB.x), aC.x), fminf(fminf(aA.y, aB.y), aC.y));
+  // ratios in (0, 1] and a sum of weights above 0.1: the fast reciprocal is accurate here
+  const float2 rA = make_float2(__fdividef(m.x, aA.x), __fdividef(m.y, aA.y));
+  const float2 rB = make_float2(__fdividef(m.x, aB.x), __fdividef(m.y, aB.y));
+  const float2 rC = make_float2(__fdividef(m.x, aC.x), __fdividef(m.y, aC.y));
+  const float2 tA = mul2(v2(0.3f), mul2(rA, rA)), tB = mul2(v2(0.6f), mul2(rB, rB)),
+               tC = mul2(v2(0.1f), mul2(rC, rC));
+  const float2 num = fma2(tA, cA, fma2(tB, cB, mul2(tC, cC)));
+  const float2 den = add2(add2(tA, tB), tC);
+  const float2 corr = make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+  return f2_ + f2v(corr, make_float2(0.f, 0.f));
+}
+// both sides of a face: lane x the plus side from f0..f4, lane y the minus side whose stencil
+// g0..g4 is held reversed (f0.y = g4, ..., f4.y = g0); values beyond 1e18 in magnitude (where
+// float squares would overflow) go to the per-side FP64 fallback
+template <int WV>
+__device__ __forceinline__ f2v weno_pair(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
+  float mx = 0.f;
+  mx = fmaxf(mx, fmaxf(fabsf(f0.hi.x), fabsf(f0.hi.y)));
+  mx = fmaxf(mx, fmaxf(fabsf(f1.hi.x), fabsf(f1.hi.y)));
+  mx = fmaxf(mx, fmaxf(fabsf(f2_.hi.x), fabsf(f2_.hi.y)));
+  mx = fmaxf(mx, fmaxf(fabsf(f3.hi.x), fabsf(f3.hi.y)));
+  mx = fmaxf(mx, fmaxf(fabsf(f4.hi.x), fabsf(f4.hi.y)));
+  if (mx < 1e18f) {
+    if constexpr (WV == 1) return weno_plus_f2dv(f0, f1, f2_, f3, f4);
+    else return weno_plus_f2v(f0, f1, f2_, f3, f4);
+  }
+  const f2 rx = weno_side_f2_fallback<true>(f0.x(), f1.x(), f2_.x(), f3.x(), f4.x());
+  const f2 ry = weno_side_f2_fallback<false>(f4.y(), f3.y(), f2_.y(), f1.y(), f0.y());
+  return f2v(rx, ry);
+}
+
 // Face-local data shared by the fluid and tracer parts.
 template <typename T>
 struct FaceState {
@@ -328,6 +398,96 @@ __device__ __forceinline__ T tracer_face_flux(const FaceState<T>& S, const T (&c
   r = r + weno_pick<false, WV>(cv[1] * S.hm[1], cv[2] * S.hm[2], cv[3] * S.hm[3],
                                cv[4] * S.hm[4], cv[5] * S.hm[5]);
   return r;
+}
+
+// Float-float fluid part with both Lax-Friedrichs sides paired (df64x2.cuh): the same
+// arithmetic as fluid_face_flux<f2, true> up to the rounding of the mirrored minus side.
+// Pair k holds side 0 at stencil point k in lane x and side 1 at point 5 - k in lane y, so the
+// projected pairs feed weno_pair directly; the split fluxes are formed per pair from the point
+// values (no per-point flux arrays are kept).
+__device__ __forceinline__ void fluid_face_flux_f2v(const f2 (&W)[6][5], double gamma_d,
+                                                    FaceState<f2>& S, f2 (&out)[5],
+                                                    const PointPrims<f2>& pre) {
+  const f2 gm = f2_from_double(gamma_d - 1.0);
+  const f2 half(0.5), one(1.0);
+  // Roe average at the face (src/utilities.cpp:298-304)
+  const f2 sL = sqrt0(W[2][0]), sR = sqrt0(W[3][0]);
+  const f2 sbar = half * (sL + sR);
+  const f2 isL = one / sL, isR = one / sR, hs = half / sbar;
+  const f2 u = (W[2][1] * isL + W[3][1] * isR) * hs;
+  const f2 v = (W[2][2] * isL + W[3][2] * isR) * hs;
+  const f2 ww = (W[2][3] * isL + W[3][3] * isR) * hs;
+  const f2 H = ((pre.p[2] + W[2][4]) * isL + (pre.p[3] + W[3][4]) * isR) * hs;
+  const f2 qsq = u * u + v * v + ww * ww;
+  const f2 c = gm * (H - half * qsq);  // the reference's "csnd" (src/utilities.cpp:309)
+  const f2 ci = one / c;
+  // nonzero entries of the left eigenvector rows (src/utilities.cpp:342-364)
+  const f2 hgc = half * gm * ci, hc = half * ci;
+  const f2v L00(hc * (u + half * gm * qsq)), L01(-hc * (gm * u + one)), L02(-v * hgc),
+      L03(-ww * hgc), L04(hgc);
+  const f2 gc = gm * ci;
+  const f2v L30(-gc * (qsq - H)), L31(u * gc), L32(v * gc), L33(ww * gc), L34(-gc);
+  const f2v L40(-hc * (u - half * gm * qsq)), L41(-hc * (gm * u - one));
+  const f2v vv(v), wv(ww);
+  // Lax-Friedrichs speed (src/utilities.cpp:368-380)
+  f2 alpha(0.0);
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const f2 s = f2_fabs(pre.u[j]) + pre.c[j];
+    alpha = (alpha < s) ? s : alpha;
+  }
+  const f2 ha = half * alpha;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    S.hp[j] = half * pre.u[j] + ha;
+    S.hm[j] = half * pre.u[j] - ha;
+  }
+  const f2v sa(ha, -ha);
+  const f2v hv(half);
+  f2v P[5][5];  // [pair][characteristic component]
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int a = k, b = 5 - k;
+    const f2v uj(pre.u[a], pre.u[b]), pj(pre.p[a], pre.p[b]);
+    f2v Wj[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) Wj[m] = f2v(W[a][m], W[b][m]);
+    // halved point flux plus (or minus) 0.5 alpha w, as fluid_face_flux forms it
+    f2v fs[5];
+    fs[0] = sa * Wj[0] + hv * Wj[1];
+    fs[1] = sa * Wj[1] + hv * (uj * Wj[1] + pj);
+    fs[2] = sa * Wj[2] + hv * (uj * Wj[2]);
+    fs[3] = sa * Wj[3] + hv * (uj * Wj[3]);
+    fs[4] = sa * Wj[4] + hv * (uj * (Wj[4] + pj));
+    P[k][0] = L00 * fs[0] + L01 * fs[1] + L02 * fs[2] + L03 * fs[3] + L04 * fs[4];
+    P[k][1] = fs[2] - vv * fs[0];
+    P[k][2] = fs[3] - wv * fs[0];
+    P[k][3] = L30 * fs[0] + L31 * fs[1] + L32 * fs[2] + L33 * fs[3] + L34 * fs[4];
+    P[k][4] = L40 * fs[0] + L41 * fs[1] + L02 * fs[2] + L03 * fs[3] + L04 * fs[4];
+  }
+  f2 ff[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const f2v r = weno_pair<0>(P[0][i], P[1][i], P[2][i], P[3][i], P[4][i]);
+    ff[i] = r.x() + r.y();
+  }
+  // right eigenvector columns (src/utilities.cpp:318-340)
+  out[0] = ff[0] + ff[3] + ff[4];
+  out[1] = (u - c) * ff[0] + u * ff[3] + (u + c) * ff[4];
+  out[2] = v * ff[0] + ff[1] + v * ff[3] + v * ff[4];
+  out[3] = ww * ff[0] + ff[2] + ww * ff[3] + ww * ff[4];
+  out[4] = (H - u * c) * ff[0] + v * ff[1] + ww * ff[2] + (half * qsq) * ff[3] + (H + u * c) * ff[4];
+}
+
+// Float-float tracer part with both sides paired: pair k holds c_k hp_k (lane x) and
+// c_{5-k} hm_{5-k} (lane y).
+template <int WV>
+__device__ __forceinline__ f2 tracer_face_flux_f2v(const FaceState<f2>& S, const f2 (&cv)[6]) {
+  f2v a[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) a[k] = f2v(cv[k], cv[5 - k]) * f2v(S.hp[k], S.hm[5 - k]);
+  const f2v r = weno_pair<WV>(a[0], a[1], a[2], a[3], a[4]);
+  return r.x() + r.y();
 }
 
 }  // namespace gbmv
