@@ -86,11 +86,14 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
   dTs_ge = 1.0 / dge_dT;
 }
 
-// The same ten-iteration Newton solve with the first `nfloat` iterations in FP32 (table
-// lookups on float copies of the four adiabatic-index tables, value and slope per bin, rounded
-// once at setup exactly as the iterations would round the FP64 entries) and the rest in FP64.  From the converged basin the
-// FP64 iterations restore full accuracy (Newton's quadratic convergence), so the result
-// matches chem_temperature's to rounding whenever the reference's ten iterations converge.
+// The same Newton solve with up to `nfloat` iterations in FP32 (table lookups on float copies
+// of the four adiabatic-index tables, value and slope per bin, rounded once at setup exactly
+// as the iterations would round the FP64 entries) and two in FP64.  The FP32 stage stops early
+// once its step is below 1e-5 T: Newton's error after such a step is ~1e-10 T, inside the
+// basin where the two FP64 iterations restore full accuracy (quadratic convergence), so the
+// result matches chem_temperature's to rounding whenever the reference's ten iterations
+// converge.  From the carried temperature of a nearby state (successive stages, Newton
+// iterates) one FP32 iteration usually suffices.
 __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, const double (&y)[10],
                                                        double& Ts, double& dTs_ge, int nfloat) {
   const float kb = 1.3806504e-16f, mh = 1.67e-24f, gm1 = 1.5f;
@@ -120,7 +123,9 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
                        gm1 * (H_1 + H_2 + H_m0 + He_1 + He_2 + He_3 + de);
     const float dge_dT = kdm * (T * (-H2_1 * i1 * i1 * dg1 - H2_2 * i2 * i2 * dg2) + nsum);
     const float dge = kdm * T * nsum - ge;
-    T = T - dge / dge_dT;
+    const float dT = dge / dge_dT;
+    T = T - dT;
+    if (fabsf(dT) <= 1e-5f * T) break;
   }
   Ts = (double)T;
   // remaining iterations (and dT/dge) in FP64: exactly chem_temperature's loop body
