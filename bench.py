@@ -145,7 +145,7 @@ class FusedStep:
                   FP64-residual refinement, no Jacobian in HBM), the whole stage captured as
                   one CUDA graph and replayed."""
 
-    def __init__(self, torch, n, form, wl=None, concurrent=False, newton_bps=4):
+    def __init__(self, torch, n, form, wl=None, concurrent=False, newton_bps=None):
         import gbmv
         import h5tables
         import workloads as W
@@ -182,21 +182,51 @@ class FusedStep:
         torch.cuda.synchronize()
         if form != "fp64":  # the whole stage as one CUDA graph (asynchronous entry points)
             self.chem_stream = torch.cuda.Stream()
-            if concurrent:  # persistent Newton grid leaving room for the WENO sweep beside it
+            if concurrent:  # persistent Newton grid leaving room for the WENO sweep beside it,
+                # and sweeps sized to share the SMs with it
+                self.hydro.set_sweep_budget(True)
+                self.tuned["sweeps"] = "shared"
+                if newton_bps is None:  # the Newton's resident blocks per SM, by timing the
+                    # two-branch graph (the state is restored after each trial)
+                    trials = {b: self._graph_ms(b) for b in NEWTON_BPS_CANDIDATES}
+                    newton_bps = min(trials, key=trials.get)
+                    self.tuned["newton_blocks_per_sm_trials_ms"] = trials
+                self.tuned["newton_blocks_per_sm"] = newton_bps
                 self.chem.set_newton_occupancy(newton_bps)
-            self._stage_async()
-            torch.cuda.synchronize()
-            self.check_status()
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            self.graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self.graph, stream=side):
-                self._stage_async()
-            torch.cuda.synchronize()
+            self.graph = self._capture()
             # the captured launches keep their grid; eager calls (the per-kernel timings) use
             # the tuned (or default) grid again
             if concurrent:
                 self.chem.set_newton_occupancy(0)
+
+    def _capture(self):
+        torch = self.torch
+        self._stage_async()
+        torch.cuda.synchronize()
+        self.check_status()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side):
+            self._stage_async()
+        torch.cuda.synchronize()
+        return graph
+
+    def _graph_ms(self, bps, reps=6):
+        """Mean time of one replay of the concurrent stage with `bps` Newton blocks per SM."""
+        torch = self.torch
+        self.chem.set_newton_occupancy(bps)
+        graph = self._capture()
+        graph.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        del graph
+        self.reset()
+        return round(e0.elapsed_time(e1) / reps, 3)
 
     def _stage_async(self, t=0.0):
         g, torch = self.gbmv, self.torch
@@ -914,6 +944,9 @@ def run_mri(torch, gbmv, n):
     out["speedup_mixed_vs_fp64"] = round(out["forms"]["fp64"]["s_to_tf"] /
                                          out["forms"]["mixed"]["s_to_tf"], 3)
     return out
+
+
+NEWTON_BPS_CANDIDATES = (3, 4, 5, 6)  # the concurrent stage's Newton blocks per SM, by timing
 
 
 IMEX_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bias=2.0,

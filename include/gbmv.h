@@ -123,6 +123,17 @@ int gbmv_feuler_noalloc(const gbmv_grid* grid, const double* force_host, double 
 int gbmv_hydro_autotune(gbmv_hydro h, const double* const* w, int precision, int* threads,
                         void* stream);
 
+/* Register budget of the GBMV_MIXED_FAST face sweeps (no counterpart in the reference):
+ * GBMV_SWEEPS_ALONE (default) sizes them to run alone on the GPU (3 resident 128-thread blocks
+ * per SM); GBMV_SWEEPS_SHARED for running beside another kernel on the same SMs, e.g. the
+ * chemistry Newton on a second stream of the same CUDA graph (5 blocks per SM: fewer registers
+ * a thread, so the other kernel's warps fit beside them).  The sweeps compute the same values
+ * bit for bit under either budget; only the speed differs.  Takes effect at the next launch
+ * (a captured graph keeps the budget it was captured with). */
+#define GBMV_SWEEPS_ALONE 0
+#define GBMV_SWEEPS_SHARED 1
+int gbmv_hydro_set_sweep_budget(gbmv_hydro h, int budget);
+
 /* stability (src/utilities.cpp:483-528): dt_stab = cfl * min(dx,dy,dz) / max(|mx/rho| + c),
  * including the reference's use of |mx/rho| for all three directions.  *dt_stab is host. */
 int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,

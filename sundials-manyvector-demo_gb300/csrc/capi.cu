@@ -82,6 +82,7 @@ struct gbmv_hydro_s {
   double* cons = nullptr;  // conservation-sum partials (first use)
   int* d_status = nullptr;
   int sweep_threads[3] = {0, 0, 0};  // face-sweep threads per block per precision (0: by size)
+  int sweep_shared = 0;               // GBMV_SWEEPS_SHARED register budget
 };
 
 struct gbmv_chem_s {
@@ -273,6 +274,7 @@ static int feuler_dispatch(gbmv_hydro h, const double* const* w, double* const* 
   G.in_wdot = (flags & GBMV_FORCE_IN_WDOT) ? 1 : 0;
   Grid g = h->g;
   g.sweep_threads = h->sweep_threads[precision];
+  g.sweep_shared = h->sweep_shared;
   if (precision == GBMV_FP64) return feuler_fp64(g, W, Wd, G, h->scratch, d_status, s);
   if (!h->prims) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -329,6 +331,15 @@ int gbmv_hydro_autotune(gbmv_hydro h, const double* const* w, int precision, int
   h->sweep_threads[precision] = rc ? 0 : best;
   if (rc) return rc;
   if (threads) *threads = best;
+  return GBMV_OK;
+}
+
+int gbmv_hydro_set_sweep_budget(gbmv_hydro h, int budget) {
+  if (!h || (budget != GBMV_SWEEPS_ALONE && budget != GBMV_SWEEPS_SHARED)) {
+    set_error("null handle or unknown sweep budget (GBMV_SWEEPS_ALONE, GBMV_SWEEPS_SHARED)");
+    return GBMV_EINVAL;
+  }
+  h->sweep_shared = budget == GBMV_SWEEPS_SHARED;
   return GBMV_OK;
 }
 

@@ -52,6 +52,7 @@ struct Grid {
   double inv_d[3]; // 1/dx, 1/dy, 1/dz
   double d[3];
   int sweep_threads;  // threads per block of the face sweeps (0: by size, spread_threads)
+  int sweep_shared;   // GBMV_MIXED_FAST sweeps sized to share the SMs with another kernel
 };
 
 inline Grid make_grid(const gbmv_grid& g) {
@@ -64,6 +65,7 @@ inline Grid make_grid(const gbmv_grid& g) {
   G.d[0] = g.dx; G.d[1] = g.dy; G.d[2] = g.dz;
   for (int i = 0; i < 3; ++i) G.inv_d[i] = 1.0 / G.d[i];
   G.sweep_threads = 0;
+  G.sweep_shared = 0;
   return G;
 }
 

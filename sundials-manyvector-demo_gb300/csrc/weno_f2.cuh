@@ -34,15 +34,16 @@ int feuler_f2_fast(const Grid& g, const Fields& w, const Fields& wdot, const For
                    double* scratch, float2* q2, const double* tscale, int* d_status,
                    cudaStream_t s);
 
-// WV = 1 (fewer instructions per face) runs faster at 3 resident blocks per SM even with the
-// register cap's spills (measured 6.11 -> 5.63 ms per 128^3 RHS); WV = 0 is faster at 2.
-// GBMV_F2_FAST_MINB: the WV = 1 residency target, a build-time tuning knob (register
-// allocation only: results are the same bit for bit at any value).
-#ifndef GBMV_F2_FAST_MINB
-#define GBMV_F2_FAST_MINB 3
-#endif
-template <int NCHEM, int DIR, int WV>
-__global__ void __launch_bounds__(128, WV == 1 ? GBMV_F2_FAST_MINB : 1)
+// Register budget (residency target, 128-thread blocks per SM; register allocation only:
+// results are the same bit for bit).  WV = 1 (fewer instructions per face) runs fastest alone
+// at 3 resident blocks per SM even with the register cap's spills (6.11 -> 5.63 ms per 128^3
+// RHS against 2); WV = 0 at 1-2.  Beside the chemistry Newton on a second stream (255
+// registers a thread) a WV = 1 sweep capped at 5 blocks per SM leaves the Newton warps room:
+// the concurrent 128^3 stage measured 8.21 ms against 9.14 at 3 (Grid::sweep_shared).
+constexpr int kF2FastMinB = 3;
+constexpr int kF2FastSharedMinB = 5;
+template <int NCHEM, int DIR, int WV, int MINB>
+__global__ void __launch_bounds__(128, MINB)
     face_flux_f2_kernel(Grid g, Fields w, const float2* __restrict__ Q2,
                         float2* __restrict__ F, long nfaces) {
   const long nx = g.n[0], ny = g.n[1], n = g.ncell;
@@ -148,36 +149,51 @@ __global__ void __launch_bounds__(128, WV == 1 ? GBMV_F2_FAST_MINB : 1)
   }
 }
 
+// the three face sweeps of one register budget
+template <int NCHEM, int WV, int MINB>
+int sweeps_f2(const Grid& g, const Fields& w, const float2* q2, float2* const (&F)[3],
+              const long (&nf)[3], cudaStream_t s) {
+  {
+    ProfScope ps("face_flux", s);
+    const int t = sweep_threads(g, nf[0], 128);
+    face_flux_f2_kernel<NCHEM, 0, WV, MINB><<<sweep_blocks(nf[0], t), t, 0, s>>>(g, w, q2, F[0],
+                                                                                  nf[0]);
+    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<x>");
+  }
+  {
+    ProfScope ps("face_flux", s);
+    const int t = sweep_threads(g, nf[1], 128);
+    face_flux_f2_kernel<NCHEM, 1, WV, MINB><<<sweep_blocks(nf[1], t), t, 0, s>>>(g, w, q2, F[1],
+                                                                                  nf[1]);
+    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<y>");
+  }
+  {
+    ProfScope ps("face_flux", s);
+    const int t = sweep_threads(g, nf[2], 128);
+    face_flux_f2_kernel<NCHEM, 2, WV, MINB><<<sweep_blocks(nf[2], t), t, 0, s>>>(g, w, q2, F[2],
+                                                                                  nf[2]);
+    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<z>");
+  }
+  return GBMV_OK;
+}
+
 template <int NCHEM, int WV>
 int launch_f2(const Grid& g, const Fields& w, const Fields& wdot, const ForceTerm& G,
               double* scratch, float2* q2, const double* tscale, int* d_status, cudaStream_t s) {
   long nf[3];
   face_counts(g, nf);
   float2* const F2 = reinterpret_cast<float2*>(scratch);  // 8 bytes per flux, as a double
-  float2* F[3] = {F2, F2 + (long)(5 + NCHEM) * nf[0], F2 + (long)(5 + NCHEM) * (nf[0] + nf[1])};
+  float2* const F[3] = {F2, F2 + (long)(5 + NCHEM) * nf[0],
+                        F2 + (long)(5 + NCHEM) * (nf[0] + nf[1])};
   int rc = prims_f2(g, w, q2, tscale, d_status, s);
   if (rc != GBMV_OK) return rc;
-  {
-    ProfScope ps("face_flux", s);
-    const int t = sweep_threads(g, nf[0], 128);
-    face_flux_f2_kernel<NCHEM, 0, WV><<<sweep_blocks(nf[0], t), t, 0, s>>>(g, w, q2, F[0],
-                                                                            nf[0]);
-    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<x>");
+  if constexpr (WV == 1) {
+    rc = g.sweep_shared ? sweeps_f2<NCHEM, WV, kF2FastSharedMinB>(g, w, q2, F, nf, s)
+                        : sweeps_f2<NCHEM, WV, kF2FastMinB>(g, w, q2, F, nf, s);
+  } else {
+    rc = sweeps_f2<NCHEM, WV, 1>(g, w, q2, F, nf, s);
   }
-  {
-    ProfScope ps("face_flux", s);
-    const int t = sweep_threads(g, nf[1], 128);
-    face_flux_f2_kernel<NCHEM, 1, WV><<<sweep_blocks(nf[1], t), t, 0, s>>>(g, w, q2, F[1],
-                                                                            nf[1]);
-    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<y>");
-  }
-  {
-    ProfScope ps("face_flux", s);
-    const int t = sweep_threads(g, nf[2], 128);
-    face_flux_f2_kernel<NCHEM, 2, WV><<<sweep_blocks(nf[2], t), t, 0, s>>>(g, w, q2, F[2],
-                                                                            nf[2]);
-    GBMV_LAUNCH_CHECK("face_flux_f2_kernel<z>");
-  }
+  if (rc != GBMV_OK) return rc;
   return divergence_f2(g, wdot, F, G, s);
 }
 

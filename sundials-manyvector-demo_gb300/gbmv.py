@@ -26,6 +26,7 @@ LIB_PATH = os.path.join(PKG, "_build", "libgbmv.so")
 
 BC_PERIODIC, BC_NEUMANN, BC_DIRICHLET, BC_REFLECTING = 0, 1, 2, 3
 FP64, MIXED, MIXED_FAST = 0, 1, 2
+SWEEPS_ALONE, SWEEPS_SHARED = 0, 1  # gbmv_hydro_set_sweep_budget
 FORCE_IN_WDOT = 1
 
 
@@ -86,6 +87,7 @@ SIGNATURES = [
                                       C.POINTER(_VP), _VP]),
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
     ("gbmv_hydro_autotune", C.c_int, [_VP, C.POINTER(_VP), C.c_int, C.POINTER(C.c_int), _VP]),
+    ("gbmv_hydro_set_sweep_budget", C.c_int, [_VP, C.c_int]),
     ("gbmv_chem_newton_autotune", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.c_int, C.c_int,
                                             C.POINTER(C.c_int), _VP]),
     ("gbmv_pack1d", C.c_int, [_VP, C.POINTER(_VP), C.c_int, _VP, _VP]),
@@ -286,6 +288,13 @@ class Hydro:
         _check(load().gbmv_hydro_autotune(self.h, _vec(w), precision, C.byref(t),
                                           _stream_ptr(stream)), "gbmv_hydro_autotune")
         return t.value
+
+    def set_sweep_budget(self, shared: bool) -> None:
+        """gbmv_hydro_set_sweep_budget: GBMV_MIXED_FAST face sweeps sized to run alone (False)
+        or beside another kernel on the same SMs (True)."""
+        _check(load().gbmv_hydro_set_sweep_budget(self.h, SWEEPS_SHARED if shared
+                                                  else SWEEPS_ALONE),
+               "gbmv_hydro_set_sweep_budget")
 
     def kink_mask(self, w, dw, eps, mask, stream=None):
         """gbmv_feuler_kink_mask into `mask` (CUDA uint8 tensor of ncells): 1 where a central

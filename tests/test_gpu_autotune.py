@@ -29,6 +29,28 @@ def test_sweep_autotune_keeps_results(cuda):
         assert all(torch.equal(x, y) for x, y in zip(a, b)), prec
 
 
+def test_sweep_budget_keeps_results(cuda):
+    """The shared register budget (sweeps sized to run beside the Newton) computes the same
+    tendencies bit for bit, every tracer count, every precision (FP64 and GBMV_MIXED ignore it)."""
+    torch = cuda
+    import gbmv
+    for nchem in (0, 4, 10):
+        wl = W.rayleigh_taylor(shape=(24, 20, 18), nchem=nchem, seed=W.SEED_BASE + 801 + nchem)
+        nz, ny, nx = wl["fields"][0].shape
+        w = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in wl["fields"]]
+        h = gbmv.Hydro((nx, ny, nz), nchem, wl["bc"], wl["gamma"], wl["force"])
+        for prec in (gbmv.FP64, gbmv.MIXED, gbmv.MIXED_FAST):
+            a = [torch.empty_like(x) for x in w]
+            b = [torch.empty_like(x) for x in w]
+            h.set_sweep_budget(False)
+            assert h.fEuler(0.0, w, a, prec) == 0
+            h.set_sweep_budget(True)
+            assert h.fEuler(0.0, w, b, prec) == 0
+            torch.cuda.synchronize()
+            assert all(torch.equal(x, y) for x, y in zip(a, b)), (nchem, prec)
+    assert gbmv.load().gbmv_hydro_set_sweep_budget(h.h, 2) == -101  # GBMV_EINVAL
+
+
 def test_newton_autotune_keeps_results_and_state(cuda, tables):
     torch = cuda
     import gbmv
