@@ -109,6 +109,13 @@ __device__ __forceinline__ double dirk_eta(double safety, double dsm, int p) {
   return p == 3 ? safety / cbrt(dsm) : (p == 2 ? safety / sqrt(dsm)
                                                : safety * pow(dsm, -1.0 / p));
 }
+// The same in FP32 (the mixed form): a step-size factor needs a few digits, and the FP64
+// root and division cost ~40 FP64-rate instructions, issued in almost every pass of a warp
+// for the one or two lanes that finish a step there
+__device__ __forceinline__ double dirk_eta_f(double safety, float dsm, int p) {
+  const float e = p == 3 ? cbrtf(dsm) : (p == 2 ? sqrtf(dsm) : powf(dsm, 1.f / p));
+  return safety * (double)(1.f / e);
+}
 
 // Base of stage i: B = Y + sum_{j<i} (h a_ij) K_j, K_0 from shared memory, K_1.. from the
 // stage store, terms added in j order (zero coefficients skipped, as the oracle does).
@@ -457,14 +464,26 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
 #pragma unroll
           for (int s = 0; s < 10; ++s) dl[s] *= sc;
         }
-        double s2 = 0.0;
+        double del;
+        if (sizeof(LU) == 4) {  // the convergence measure in FP32 (a decision quantity)
+          float s2 = 0.f;
 #pragma unroll
-        for (int s = 0; s < 10; ++s) {
-          Z[s * BS] += dl[s];
-          const double v = dl[s] * (double)EW[s * BS];
-          s2 += v * v;
+          for (int s = 0; s < 10; ++s) {
+            Z[s * BS] += dl[s];
+            const float v = (float)dl[s] * EW[s * BS];
+            s2 = fmaf(v, v, s2);
+          }
+          del = (double)sqrtf(0.1f * s2);
+        } else {
+          double s2 = 0.0;
+#pragma unroll
+          for (int s = 0; s < 10; ++s) {
+            Z[s * BS] += dl[s];
+            const double v = dl[s] * (double)EW[s * BS];
+            s2 += v * v;
+          }
+          del = sqrt(s2 / 10.0);
         }
-        const double del = sqrt(s2 / 10.0);
         ++m;
         ++c_nni;
         if (m > 1) crate = fmax(0.3 * crate, del / delp);
@@ -505,14 +524,27 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           for (int s = 0; s < 10; ++s) acc[s] += ej * KG[((j - 1) * 10 + s) * kst];
         }
         const double el = O.T.e[ns - 1];
-        double s2 = 0.0;
+        double dsm;
+        float dsmf = 0.f;
+        if (sizeof(LU) == 4) {  // the error norm in FP32 (an accept test and a step factor)
+          float s2 = 0.f;
 #pragma unroll
-        for (int s = 0; s < 10; ++s) {
-          const double e = h * (acc[s] + el * f[s]);
-          const double v = e * (double)EW[s * BS];
-          s2 += v * v;
+          for (int s = 0; s < 10; ++s) {
+            const float v = (float)(h * (acc[s] + el * f[s])) * EW[s * BS];
+            s2 = fmaf(v, v, s2);
+          }
+          dsmf = sqrtf(0.1f * s2);
+          dsm = (double)dsmf;
+        } else {
+          double s2 = 0.0;
+#pragma unroll
+          for (int s = 0; s < 10; ++s) {
+            const double e = h * (acc[s] + el * f[s]);
+            const double v = e * (double)EW[s * BS];
+            s2 += v * v;
+          }
+          dsm = sqrt(s2 / 10.0);
         }
-        const double dsm = sqrt(s2 / 10.0);
         if (dsm <= 1.0) {
           ++nst;
           t = last ? O.tout : t + h;
@@ -524,7 +556,9 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           Tsy = Tsc;
           dTsy = dTsc;
           jcur = false;
-          double eta = (dsm > 0.0) ? dirk_eta(O.safety, dsm, O.T.p) : 1.0e300;
+          double eta = !(dsm > 0.0) ? 1.0e300
+                       : (sizeof(LU) == 4 ? dirk_eta_f(O.safety, dsmf, O.T.p)
+                                          : dirk_eta(O.safety, dsm, O.T.p));
           eta = fmin(eta, nst == 1 ? O.etamx1 : O.growth);
           if (nef_s > 0 || ncf_s > 0) eta = fmin(eta, 1.0);
           h *= eta;
@@ -539,7 +573,8 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           if (nef_s >= O.maxnef) {
             retire = failed = true;
           } else {
-            double eta = fmax(0.1, dirk_eta(O.safety, dsm, O.T.p));
+            double eta = fmax(0.1, sizeof(LU) == 4 ? dirk_eta_f(O.safety, dsmf, O.T.p)
+                                                   : dirk_eta(O.safety, dsm, O.T.p));
             if (nef_s >= 2) eta = fmin(eta, 0.3);
             h *= eta;
             setup = true;
