@@ -13,6 +13,7 @@
 #include "chem.cuh"
 #include "chem_net.cuh"
 #include "chem_lu.cuh"
+#include "df64.cuh"
 
 namespace gbmv {
 
@@ -47,11 +48,12 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
 #pragma unroll
     for (int s = 0; s < 10; ++s) ya[s] = y[j + s] * sc[s];
     double Ts = S.Ts[i], dTs = 0.0;
-    // mixed form: 8 FP32 + 2 FP64 iterations.  (Stopping after one FP64 iteration where its
-    // correction is below 1e-7 T measured 0.9 % faster but left the carried temperature up to
-    // 1.2e-10 off the FP64 form's ten-iteration value on slowly converging cells.)
+    // mixed form: up to 8 FP32 iterations, then one FP64 iteration if the FP32 stage
+    // converged (its last step below 1e-5 T), else two.  (Cutting the FP64 stage on the size of
+    // its own first correction instead left the carried temperature up to 1.2e-10 off the FP64
+    // form's ten-iteration value on slowly converging cells.)
     if (sizeof(LU) == 4)
-      chem_temperature_mixed(P, ya, Ts, dTs, 8);
+      chem_temperature_mixed(P, ya, Ts, dTs, 8, true);
     else
       chem_temperature(P, ya, Ts, dTs);
     S.Ts[i] = Ts;
@@ -89,9 +91,18 @@ __global__ void __launch_bounds__(BS) chem_newton_kernel(ChemParams P, ChemState
         if (kMixed) {
           const int e = kJacIndex[row][col];
           if (e >= 0) As[e * BS] = a;
+        } else {
+          L[(col * 10 + row) * BS] = to_lu<LU>(a);
         }
-        L[(col * 10 + row) * BS] = to_lu<LU>(a);
       }, &Rg);
+      if constexpr (kMixed) {  // the FP32 factor's entries, converted with integer
+        // instructions after the Jacobian (off the FP64 pipe, which bounds this kernel, and off
+        // the Jacobian's dependency chains: 5.45 -> 5.34 ms per 128^3 call; converting inside
+        // the entry loop had measured 1 % slower)
+#pragma unroll
+        for (int e = 0; e < 64; ++e)
+          L[(kJacPattern[e][1] * 10 + kJacPattern[e][0]) * BS] = f32_of_f64(As[e * BS]);
+      }
     }
 #pragma unroll
     for (int s = 0; s < 10; ++s) f[s] = fout[j + s];
