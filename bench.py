@@ -11,7 +11,7 @@ per-step host->device copies of the state from pinned memory and device->host co
 outputs (tendency vector and Newton update) through the public Python API.
 
   python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl gbmv|reference]
-                  [--form best|fp64|mixed|mixed_fast|mixed_fast_concurrent]
+                  [--form best|fp64|mixed|mixed_fast|mixed_fast_concurrent|mixed_fast_queue]
 --form best (default) times the plain FP64 form and the mixed-precision forms (the last with
 the chemistry Newton on a second stream beside the WENO sweep inside the step's graph), checks
 each mixed form's outputs against the FP64 form's (max-normalised per field), and reports the
@@ -50,7 +50,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gbmv", choices=["gbmv", "reference"])
     p.add_argument("--form", default="best",
-                   choices=["best", "fp64", "mixed", "mixed_fast", "mixed_fast_concurrent"])
+                   choices=["best", "fp64", "mixed", "mixed_fast", "mixed_fast_concurrent",
+                            "mixed_fast_queue"])
     p.add_argument("--n", type=int, default=N)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--newton-refine", type=int, default=None,
@@ -186,13 +187,15 @@ class FusedStep:
                 # and sweeps sized to share the SMs with it
                 self.hydro.set_sweep_budget(True)
                 self.tuned["sweeps"] = "shared"
+                if concurrent == "queue":
+                    self.queue = torch.zeros(1, dtype=torch.int64, device="cuda")
                 if newton_bps is None:  # the Newton's resident blocks per SM, by timing the
                     # two-branch graph (the state is restored after each trial)
                     trials = {b: self._graph_ms(b) for b in NEWTON_BPS_CANDIDATES}
                     newton_bps = min(trials, key=trials.get)
                     self.tuned["newton_blocks_per_sm_trials_ms"] = trials
                 self.tuned["newton_blocks_per_sm"] = newton_bps
-                self.chem.set_newton_occupancy(newton_bps)
+                self._set_narrow(newton_bps)
             self.graph = self._capture()
             # the captured launches keep their grid; eager calls (the per-kernel timings) use
             # the tuned (or default) grid again
@@ -212,10 +215,16 @@ class FusedStep:
         torch.cuda.synchronize()
         return graph
 
+    def _set_narrow(self, bps):
+        if self.concurrent == "queue":
+            self.narrow_bps = bps
+        else:
+            self.chem.set_newton_occupancy(bps)
+
     def _graph_ms(self, bps, reps=6):
         """Mean time of one replay of the concurrent stage with `bps` Newton blocks per SM."""
         torch = self.torch
-        self.chem.set_newton_occupancy(bps)
+        self._set_narrow(bps)
         graph = self._capture()
         graph.replay()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -241,14 +250,28 @@ class FusedStep:
         # two independent branches of the stage: the chemistry (FP64 pipe) beside the WENO
         # sweep (FP32 pipes); the mixed fexpl never writes w[5], so both may read it
         main = torch.cuda.current_stream()
+        queue = self.concurrent == "queue"
+        if queue:
+            self.queue.zero_()
         fork = torch.cuda.Event()
         fork.record(main)
         self.chem_stream.wait_event(fork)
-        g.chem_newton_async(self.chem, t, self.w[5].view(-1), self.f, self.x, GAMMA_NEWTON, TU,
-                            self.status[1:2], lu_precision=g.MIXED, refine=NEWTON_REFINE,
-                            stream=self.chem_stream)
+        y = self.w[5].view(-1)
+        if queue:  # a narrow launch beside the sweep, a full-width one after it: one pass
+            g.chem_newton_queue_async(self.chem, t, y, self.f, self.x, GAMMA_NEWTON, TU,
+                                      self.status[1:2], self.queue, self.narrow_bps,
+                                      lu_precision=g.MIXED, refine=NEWTON_REFINE,
+                                      stream=self.chem_stream)
+        else:
+            g.chem_newton_async(self.chem, t, y, self.f, self.x, GAMMA_NEWTON, TU,
+                                self.status[1:2], lu_precision=g.MIXED, refine=NEWTON_REFINE,
+                                stream=self.chem_stream)
         g.fexpl_async(self.hydro, self.chem, t, self.w, self.wdot, EU, self.status[0:1],
                       self.precision)
+        if queue:
+            g.chem_newton_queue_async(self.chem, t, y, self.f, self.x, GAMMA_NEWTON, TU,
+                                      self.status[1:2], self.queue, 0, lu_precision=g.MIXED,
+                                      refine=NEWTON_REFINE)
         join = torch.cuda.Event()
         join.record(self.chem_stream)
         main.wait_event(join)
@@ -455,14 +478,15 @@ def run_gbmv(args):
     global NEWTON_REFINE
     if args.newton_refine is not None:
         NEWTON_REFINE = args.newton_refine
-    forms = (["fp64", "mixed", "mixed_fast", "mixed_fast_concurrent"] if args.form == "best"
-             else [args.form])
+    forms = (["fp64", "mixed", "mixed_fast", "mixed_fast_concurrent", "mixed_fast_queue"]
+             if args.form == "best" else [args.form])
     if args.concurrent and "mixed" in forms:
         forms.append("mixed_concurrent")
 
     def make_fs(form):
-        base = form.replace("_concurrent", "")
-        return FusedStep(torch, args.n, base, wl, concurrent=form.endswith("_concurrent"))
+        base = form.replace("_concurrent", "").replace("_queue", "")
+        mode = "queue" if form.endswith("_queue") else form.endswith("_concurrent")
+        return FusedStep(torch, args.n, base, wl, concurrent=mode)
 
     res = {}
     for form in forms:
@@ -514,7 +538,7 @@ def run_gbmv(args):
     fp64_peak = gbmv.fma_rate(True) / 1e12
     dt_ms, nl = fam[dom]
     avg_ms = dt_ms / max(nl, 1)
-    hform = head.replace("_concurrent", "")
+    hform = head.replace("_concurrent", "").replace("_queue", "")
     key = "face_flux_mx" if (dom == "face_flux" and hform != "fp64") else dom
     achieved = algo_bytes(key, args.n) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     traffic, traffic_note = None, None
@@ -563,12 +587,17 @@ def run_gbmv(args):
                       "value": round(ncell / (r["ms"] * 1e-3) / 1e6, 3),
                       "autotuned": r["tuned"]} for f, r in res.items()},
     }
-    if head.endswith("_concurrent"):
+    if head.endswith("_concurrent") or head.endswith("_queue"):
+        bps = R["tuned"].get("newton_blocks_per_sm")
         line["config"]["schedule"] = (
             "one CUDA graph per step with two branches: the chemistry Newton on a second stream "
-            "(persistent grid, 4 one-warp blocks per SM) beside the WENO sweep; outputs "
-            "bit-identical to the serial graph; kernel_ms_per_step and roofline time each "
-            "kernel alone (eager, serial), so their sum exceeds ms_per_step by the overlap")
+            f"(persistent grid, {bps} one-warp blocks per SM, chosen by timing the graph) beside "
+            "the WENO sweep (its register budget sized to share the SMs)"
+            + ("; both Newton launches take 32-cell chunks from one counter, the second, a full-"
+               "width launch after the sweep, drains what the first has not taken"
+               if head.endswith("_queue") else "")
+            + "; outputs bit-identical to the serial graph; kernel_ms_per_step and roofline time "
+            "each kernel alone (eager, serial), so their sum exceeds ms_per_step by the overlap")
     if errs is not None:
         line["mixed_vs_fp64_maxnorm_err"] = {k: float(f"{v:.3e}") for k, v in errs.items()}
         line["speedup_vs_fp64_form"] = round(res["fp64"]["ms"] / res[head]["ms"], 3)
@@ -968,7 +997,7 @@ def run_mri(torch, gbmv, n):
     return out
 
 
-NEWTON_BPS_CANDIDATES = (3, 4, 5, 6)  # the concurrent stage's Newton blocks per SM, by timing
+NEWTON_BPS_CANDIDATES = (2, 3, 4, 5, 6)  # the concurrent stage's Newton blocks per SM, timed
 
 
 IMEX_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bias=2.0,

@@ -261,6 +261,19 @@ int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, do
                            double gamma, double time_units, int lu_precision, int refine,
                            int* d_info, void* stream);
 
+/* Work-queue form of gbmv_chem_newton_async (no counterpart in the reference): the launch's
+ * one-warp blocks take 32-cell chunks from the device counter *d_queue until every cell is
+ * taken, so several launches -- on different streams of one graph -- can share one pass over
+ * the cells: for example a narrow persistent launch beside the WENO sweep of the stage and a
+ * wide one after the sweep that drains what is left.  The caller zeroes *d_queue before the
+ * first launch that shares it.  blocks_per_sm: 0 = a deep grid (as many blocks as fit), n > 0
+ * = n resident one-warp blocks per SM.  Every cell's f and x are those of
+ * gbmv_chem_newton_async bit for bit, whichever launch computes it. */
+int gbmv_chem_newton_queue_async(gbmv_chem c, double t, const double* y, double* f, double* x,
+                                 double gamma, double time_units, int lu_precision, int refine,
+                                 unsigned long long* d_queue, int blocks_per_sm, int* d_info,
+                                 void* stream);
+
 /* Products with the chemistry Jacobian of gbmv_chem_jac (J = time_units * df/dy at the
  * temperature state of the last gbmv_chem_rhs, entries rounded exactly as gbmv_chem_jac
  * writes them) without forming it: gbmv_chem_jvp jv = J dy (the matrix-free Jacobian action

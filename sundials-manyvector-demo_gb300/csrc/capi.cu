@@ -531,6 +531,21 @@ int gbmv_chem_newton_async(gbmv_chem c, double t, const double* y, double* f, do
                      refine, d_info, (cudaStream_t)stream, c->newton_bps);
 }
 
+int gbmv_chem_newton_queue_async(gbmv_chem c, double t, const double* y, double* f, double* x,
+                                 double gamma, double time_units, int lu_precision, int refine,
+                                 unsigned long long* d_queue, int blocks_per_sm, int* d_info,
+                                 void* stream) {
+  (void)t;
+  if (!c || !y || !f || !x || !d_info || !d_queue || refine < 0 || refine > 8 ||
+      blocks_per_sm < 0 || blocks_per_sm > 32 ||
+      (lu_precision != GBMV_FP64 && lu_precision != GBMV_MIXED)) {
+    set_error("bad chem_newton_queue arguments");
+    return GBMV_EINVAL;
+  }
+  return chem_newton(c->P, c->S, c->n, y, f, x, gamma, time_units, lu_precision == GBMV_MIXED,
+                     refine, d_info, (cudaStream_t)stream, blocks_per_sm, nullptr, d_queue);
+}
+
 }  // extern "C"
 
 // synchronous fused Newton (b null: gbmv_chem_newton; b set: its implicit-stage form)

@@ -48,9 +48,11 @@ int mri_forcing(long ncell, const ForcingSet& F, int nf, const DevFields6& wdot,
 
 // fused source + Jacobian + Newton matrix + LU solve (chem_newton.cu)
 // b: null, or the implicit-stage right-hand side base: x = (I - gamma J)^{-1} (b + gamma f)
+// queue: null (a grid-stride sweep) or a caller-zeroed cell counter shared by launches
 int chem_newton(const ChemParams& P, const ChemState& S, long n, const double* y, double* f,
                 double* x, double gamma, double tunit, int lu_fp32, int refine, int* d_info,
-                cudaStream_t s, int blocks_per_sm = 0, const double* b = nullptr);
+                cudaStream_t s, int blocks_per_sm = 0, const double* b = nullptr,
+                unsigned long long* queue = nullptr);
 
 // The stiffly accurate ESDIRK the persistent DIRK runs (explicit first stage, one diagonal
 // value gamma, b = last row of a): stage i of s solves z_i = y + h sum_{j<i} a_ij K_j

@@ -128,6 +128,9 @@ SIGNATURES = [
                                          C.c_double, C.c_int, C.c_int, _VP]),
     ("gbmv_chem_newton_async", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double, C.c_double,
                                          C.c_int, C.c_int, _VP, _VP]),
+    ("gbmv_chem_newton_queue_async", C.c_int, [_VP, C.c_double, _VP, _VP, _VP, C.c_double,
+                                               C.c_double, C.c_int, C.c_int, _VP, C.c_int, _VP,
+                                               _VP]),
     ("gbmv_dirk_opts_default", None, [C.POINTER(_DirkOpts)]),
     ("gbmv_chem_dirk_evolve", C.c_int, [_VP, C.c_double, C.c_double, _VP, C.c_double,
                                         C.POINTER(_DirkOpts), _VP, _VP]),
@@ -591,6 +594,21 @@ def chem_newton_async(chem: Chem, t, y, f, x, gamma, time_units, info, lu_precis
                                                 gamma, time_units, lu_precision, refine,
                                                 info.data_ptr(), _stream_ptr(stream)),
                   "gbmv_chem_newton_async")
+
+
+def chem_newton_queue_async(chem: Chem, t, y, f, x, gamma, time_units, info, queue,
+                            blocks_per_sm=0, lu_precision=FP64, refine=4, stream=None):
+    """gbmv_chem_newton_queue_async: the fused Newton over 32-cell chunks taken from `queue`
+    (a zeroed CUDA int64 tensor of one element, shared by the launches that split the cells)."""
+    import torch
+    if queue.dtype != torch.int64 or not queue.is_cuda or queue.numel() < 1:
+        raise GbmvError("queue must be a CUDA int64 tensor")
+    return _check(load().gbmv_chem_newton_queue_async(chem.c, t, _dev_ptr(y), _dev_ptr(f),
+                                                      _dev_ptr(x), gamma, time_units,
+                                                      lu_precision, refine, queue.data_ptr(),
+                                                      blocks_per_sm, info.data_ptr(),
+                                                      _stream_ptr(stream)),
+                  "gbmv_chem_newton_queue_async")
 
 
 def ffast(hydro: Hydro, chem: Chem, t, w, wdot, time_units, forcing=(), tshift=0.0, tscale=1.0,

@@ -71,3 +71,38 @@ def test_newton_autotune_keeps_results_and_state(cuda, tables):
     assert c.newton_iteration(0.0, z, f2, x2, 1e-4, 1e11, lu_precision=gbmv.MIXED) == 0
     torch.cuda.synchronize()
     assert torch.equal(f1, f2) and torch.equal(x1, x2)
+
+
+@pytest.mark.parametrize("lu", ["fp64", "mixed"])
+def test_newton_queue_launches_share_one_pass(cuda, tables, lu):
+    """gbmv_chem_newton_queue_async: a narrow launch on a second stream and a full-width one on
+    the first, sharing one chunk counter, compute every cell exactly as one plain launch does
+    (f, x and the carried temperature), on a cell count that leaves a partial last chunk."""
+    torch = cuda
+    import gbmv
+    n = 20000 + 13
+    prec = gbmv.MIXED if lu == "mixed" else gbmv.FP64
+    y, _ = W.primordial(n, seed=W.SEED_BASE + 802)
+    c = gbmv.Chem(n, tables)
+    c.set_scale(torch.from_numpy(y.reshape(-1).copy()).cuda())
+    z = torch.ones(10 * n, dtype=torch.float64, device="cuda")
+    ts0 = c.state("Ts").clone()
+    f1, x1 = torch.empty_like(z), torch.empty_like(z)
+    assert c.newton_iteration(0.0, z, f1, x1, 1e-4, 1e11, lu_precision=prec) == 0
+    ts1 = c.state("Ts").clone()
+    c.state("Ts").copy_(ts0)
+    f2, x2 = torch.full_like(z, np.nan), torch.full_like(z, np.nan)
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    queue = torch.zeros(1, dtype=torch.int64, device="cuda")
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    gbmv.chem_newton_queue_async(c, 0.0, z, f2, x2, 1e-4, 1e11, info, queue, 2,
+                                 lu_precision=prec, refine=2, stream=side)
+    gbmv.chem_newton_queue_async(c, 0.0, z, f2, x2, 1e-4, 1e11, info, queue, 0,
+                                 lu_precision=prec, refine=2)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    assert int(info.item()) == 0
+    assert int(queue.item()) >= n
+    assert torch.equal(f1, f2) and torch.equal(x1, x2)
+    assert torch.equal(c.state("Ts"), ts1)
