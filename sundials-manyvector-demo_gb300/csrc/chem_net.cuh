@@ -93,14 +93,9 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
 // basin where the two FP64 iterations restore full accuracy (quadratic convergence), so the
 // result matches chem_temperature's to rounding whenever the reference's ten iterations
 // converge.  From the carried temperature of a nearby state (successive stages, Newton
-// iterates) one FP32 iteration usually suffices.  adaptive (the fused Newton): when the FP32
-// stage stopped early, one FP64 iteration instead of two -- from a start within ~1e-10 T it
-// leaves ~1e-14 T (measured: the fused step's Newton 5.45 -> 5.11 ms at 128^3, its update
-// 6.9e-10 -> 1.3e-9 from the FP64 path); a stage that used all its FP32 iterations still
-// gets two.
+// iterates) one FP32 iteration usually suffices.
 __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, const double (&y)[10],
-                                                       double& Ts, double& dTs_ge, int nfloat,
-                                                       bool adaptive = false) {
+                                                       double& Ts, double& dTs_ge, int nfloat) {
   const float kb = 1.3806504e-16f, mh = 1.67e-24f, gm1 = 1.5f;
   const float H2_1 = (float)y[0], H2_2 = (float)y[1], H_1 = (float)y[2], H_2 = (float)y[3],
               H_m0 = (float)y[4], He_1 = (float)y[5], He_2 = (float)y[6], He_3 = (float)y[7],
@@ -110,7 +105,6 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
   const float kdm = kb / (density * mh);
   const float lb = P.lbf, idbin = P.idbinf, dbin = P.dbinf;
   float T = (float)Ts;
-  bool early = false;
 #pragma unroll 1
   for (int it = 0; it < nfloat; ++it) {
     const float logT = logf(T);
@@ -131,12 +125,8 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
     const float dge = kdm * T * nsum - ge;
     const float dT = dge / dge_dT;
     T = T - dT;
-    if (fabsf(dT) <= 1e-5f * T) {
-      early = true;
-      break;
-    }
+    if (fabsf(dT) <= 1e-5f * T) break;
   }
-  const int nfp64 = (adaptive && early) ? 1 : 10 - nfloat;
   Ts = (double)T;
   // remaining iterations (and dT/dge) in FP64: exactly chem_temperature's loop body
   const double kbd = 1.3806504e-16, mhd = 1.67e-24, gm1d = 1.0 / (5.e0 / 3.e0 - 1);
@@ -150,7 +140,7 @@ __device__ __forceinline__ void chem_temperature_mixed(const ChemParams& P, cons
   const double kdmd = kbd / dmh;
   double Tc = Ts, Tnew = Ts, dge_dTd = 0.0;
 #pragma unroll 1
-  for (int it = 0; it < nfp64; ++it) {
+  for (int it = nfloat; it < 10; ++it) {
     Tc = Ts;
     double t1, t2;
     const double logT = log(Ts);
