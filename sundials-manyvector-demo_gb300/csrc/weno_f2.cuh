@@ -135,16 +135,38 @@ __global__ void __launch_bounds__(128, MINB)
     o[1 + DIR] = o1;
 #pragma unroll
     for (int v = 0; v < 5; ++v) F[v * nfaces + f] = make_float2(o[v].hi, o[v].lo);
+    if constexpr (MINB <= kF2FastMinB) {
+      // two species per pass, two independent dependency chains (GBMV_MIXED 128^3 RHS 5.84 ->
+      // 5.66 ms); under the shared register budget the extra live values spill, so that
+      // budget keeps one species per pass (concurrent stage 8.46 against 8.30 ms)
+      static_assert(NCHEM % 2 == 0, "tracers are reconstructed two at a time");
 #pragma unroll 1
-    for (int c = 0; c < NCHEM; ++c) {
-      f2 cv[6];
+      for (int c = 0; c < NCHEM; c += 2) {
+        f2 cv[6], cw[6];
 #pragma unroll
-      for (int l = 0; l < 6; ++l) {
-        const float2 t = __ldg(Q2 + (kQ2Base + c) * n + cell[l]);
-        cv[l] = nall[l] ? f2(-t.x, -t.y) : f2(t.x, t.y);
+        for (int l = 0; l < 6; ++l) {
+          const float2 t = __ldg(Q2 + (kQ2Base + c) * n + cell[l]);
+          const float2 u = __ldg(Q2 + (kQ2Base + c + 1) * n + cell[l]);
+          cv[l] = nall[l] ? f2(-t.x, -t.y) : f2(t.x, t.y);
+          cw[l] = nall[l] ? f2(-u.x, -u.y) : f2(u.x, u.y);
+        }
+        f2 r, q;
+        tracer_face_flux_f2v_x2<WV>(S, cv, cw, r, q);
+        F[(5 + c) * nfaces + f] = make_float2(r.hi, r.lo);
+        F[(6 + c) * nfaces + f] = make_float2(q.hi, q.lo);
       }
-      const f2 r = tracer_face_flux_f2v<WV>(S, cv);
-      F[(5 + c) * nfaces + f] = make_float2(r.hi, r.lo);
+    } else {
+#pragma unroll 1
+      for (int c = 0; c < NCHEM; ++c) {
+        f2 cv[6];
+#pragma unroll
+        for (int l = 0; l < 6; ++l) {
+          const float2 t = __ldg(Q2 + (kQ2Base + c) * n + cell[l]);
+          cv[l] = nall[l] ? f2(-t.x, -t.y) : f2(t.x, t.y);
+        }
+        const f2 r = tracer_face_flux_f2v<WV>(S, cv);
+        F[(5 + c) * nfaces + f] = make_float2(r.hi, r.lo);
+      }
     }
   }
 }

@@ -218,7 +218,7 @@ __device__ __forceinline__ T weno_pick(T f0, T f1, T f2_, T f3, T f4) {
 // smoothness indicators map onto each other under the reversal) -- so one instruction stream
 // serves both.  Lane x returns exactly weno_side_f2<true>'s value; lane y the minus side's
 // value up to the rounding of the mirrored evaluation order.
-static __device__ __noinline__ f2v weno_plus_f2v(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
+__device__ __forceinline__ f2v weno_plus_f2v_body(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
   const f2v D01 = f0 - f1, D12 = f1 - f2_, D23 = f2_ - f3, D34 = f3 - f4;
   const f2v dA = D23 - D34, dB = D12 - D23, dC = D01 - D12;  // second differences
   const f2v eA = dA + f2v_scale(D23, 2.f), eB = D12 + D23, eC = dC - f2v_scale(D12, 2.f);
@@ -236,7 +236,7 @@ static __device__ __noinline__ f2v weno_plus_f2v(f2v f0, f2v f1, f2v f2_, f2v f3
   return (tA * qA + tB * qB + tC * qC) / (tA + tB + tC);
 }
 // the correction form of weno_side_f2d (species fields of GBMV_MIXED_FAST), paired
-static __device__ __noinline__ f2v weno_plus_f2dv(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
+__device__ __forceinline__ f2v weno_plus_f2dv_body(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
   const float2 D01 = (f0 - f1).to_float(), D12 = (f1 - f2_).to_float(),
                D23 = (f2_ - f3).to_float(), D34 = (f3 - f4).to_float();
   const float2 dA = sub2(D23, D34), dB = sub2(D12, D23), dC = sub2(D01, D12);
@@ -261,6 +261,32 @@ static __device__ __noinline__ f2v weno_plus_f2dv(f2v f0, f2v f1, f2v f2_, f2v f
   const float2 corr = make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
   return f2_ + f2v(corr, make_float2(0.f, 0.f));
 }
+// One out-of-line copy of each serves every reconstruction of a face (the kernel stays inside
+// the instruction cache); the x2 forms take two independent reconstructions at once, two
+// dependency chains the scheduler interleaves.
+static __device__ __noinline__ f2v weno_plus_f2v(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
+  return weno_plus_f2v_body(f0, f1, f2_, f3, f4);
+}
+static __device__ __noinline__ f2v weno_plus_f2dv(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4) {
+  return weno_plus_f2dv_body(f0, f1, f2_, f3, f4);
+}
+struct f2v2 {
+  f2v a, b;
+};
+template <int WV>
+static __device__ __noinline__ f2v2 weno_plus_x2(f2v a0, f2v a1, f2v a2, f2v a3, f2v a4,
+                                                 f2v b0, f2v b1, f2v b2, f2v b3, f2v b4) {
+  f2v2 r;
+  if constexpr (WV == 1) {
+    r.a = weno_plus_f2dv_body(a0, a1, a2, a3, a4);
+    r.b = weno_plus_f2dv_body(b0, b1, b2, b3, b4);
+  } else {
+    r.a = weno_plus_f2v_body(a0, a1, a2, a3, a4);
+    r.b = weno_plus_f2v_body(b0, b1, b2, b3, b4);
+  }
+  return r;
+}
+
 // both sides of a face: lane x the plus side from f0..f4, lane y the minus side whose stencil
 // g0..g4 is held reversed (f0.y = g4, ..., f4.y = g0); values beyond 1e18 in magnitude (where
 // float squares would overflow) go to the per-side FP64 fallback
@@ -279,6 +305,22 @@ __device__ __forceinline__ f2v weno_pair(f2v f0, f2v f1, f2v f2_, f2v f3, f2v f4
   const f2 rx = weno_side_f2_fallback<true>(f0.x(), f1.x(), f2_.x(), f3.x(), f4.x());
   const f2 ry = weno_side_f2_fallback<false>(f4.y(), f3.y(), f2_.y(), f1.y(), f0.y());
   return f2v(rx, ry);
+}
+
+__device__ __forceinline__ float f2v_absmax(f2v a) {
+  return fmaxf(fabsf(a.hi.x), fabsf(a.hi.y));
+}
+template <int WV>
+__device__ __forceinline__ f2v2 weno_pair_x2(f2v a0, f2v a1, f2v a2, f2v a3, f2v a4, f2v b0,
+                                             f2v b1, f2v b2, f2v b3, f2v b4) {
+  float mx = fmaxf(fmaxf(f2v_absmax(a0), f2v_absmax(a1)), fmaxf(f2v_absmax(a2), f2v_absmax(a3)));
+  mx = fmaxf(mx, fmaxf(fmaxf(f2v_absmax(a4), f2v_absmax(b0)), fmaxf(f2v_absmax(b1), f2v_absmax(b2))));
+  mx = fmaxf(mx, fmaxf(f2v_absmax(b3), f2v_absmax(b4)));
+  if (mx < 1e18f) return weno_plus_x2<WV>(a0, a1, a2, a3, a4, b0, b1, b2, b3, b4);
+  f2v2 r;
+  r.a = weno_pair<WV>(a0, a1, a2, a3, a4);
+  r.b = weno_pair<WV>(b0, b1, b2, b3, b4);
+  return r;
 }
 
 // Face-local data shared by the fluid and tracer parts.
@@ -477,6 +519,22 @@ __device__ __forceinline__ void fluid_face_flux_f2v(const f2 (&W)[6][5], double 
   out[2] = v * ff[0] + ff[1] + v * ff[3] + v * ff[4];
   out[3] = ww * ff[0] + ff[2] + ww * ff[3] + ww * ff[4];
   out[4] = (H - u * c) * ff[0] + v * ff[1] + ww * ff[2] + (half * qsq) * ff[3] + (H + u * c) * ff[4];
+}
+
+// Two species at once (two independent reconstruction chains)
+template <int WV>
+__device__ __forceinline__ void tracer_face_flux_f2v_x2(const FaceState<f2>& S, const f2 (&cv)[6],
+                                                        const f2 (&cw)[6], f2& rv, f2& rw) {
+  f2v a[5], b[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const f2v h(S.hp[k], S.hm[5 - k]);
+    a[k] = f2v(cv[k], cv[5 - k]) * h;
+    b[k] = f2v(cw[k], cw[5 - k]) * h;
+  }
+  const f2v2 r = weno_pair_x2<WV>(a[0], a[1], a[2], a[3], a[4], b[0], b[1], b[2], b[3], b[4]);
+  rv = r.a.x() + r.a.y();
+  rw = r.b.x() + r.b.y();
 }
 
 // Float-float tracer part with both sides paired: pair k holds c_k hp_k (lane x) and
