@@ -316,6 +316,10 @@ typedef struct {
                         passes, or no cell is left to start; then they set up together.  1 =
                         every cell sets up at once.  Every cell runs the same computation
                         whatever the value: only the interleaving changes (default 8) */
+  int order;         /* 1: cells are taken largest initial derivative first (||F(z0)|| in the
+                        WRMS norm, in quarter-decade buckets), so the costliest cells start
+                        early and few lanes idle at the end; 0: in index order.  Every cell's
+                        result is the same either way (default 1) */
 } gbmv_dirk_opts;
 
 /* Fill *o with the defaults above (rtol 1e-6, atol 1e-10). */

@@ -99,6 +99,8 @@ struct gbmv_chem_s {
   long dirk_k_lanes = 0;
   double* dirk_retry = nullptr;        // FP32 DIRK's second pass: start state, Ts, cell list
   DirkRetry retry{};
+  int* dirk_order_buf = nullptr;       // DIRK cost order: buckets, counts, ordered cell list
+  DirkOrder order{};
   int newton_bps = 0;                  // fused Newton: resident blocks per SM (0 = default)
 };
 
@@ -465,6 +467,7 @@ int gbmv_chem_destroy(gbmv_chem c) {
   cudaFree(c->d_info);
   cudaFree(c->dirk_k);
   cudaFree(c->dirk_retry);
+  cudaFree(c->dirk_order_buf);
   delete c;
   return GBMV_OK;
 }
@@ -612,6 +615,7 @@ void gbmv_dirk_opts_default(gbmv_dirk_opts* o) {
   o->block = 0;
   o->table = 0;
   o->setup_batch = 8;
+  o->order = 1;
 }
 
 // The DIRK table of the options (0: ARK437L2SA_DIRK_7_3_4, the reference's chemistry inputs'
@@ -679,6 +683,25 @@ static int dirk_store(gbmv_chem c, DirkOpts* O, cudaStream_t s) {
     c->retry.list = reinterpret_cast<int*>(c->dirk_retry + 12 * n);
     c->retry.count = c->retry.list + n;
   }
+  if (!c->dirk_order_buf) {  // the cost order's buckets, counts and cell list
+    if (capturing(s)) {
+      set_error("the first DIRK call allocates its buffers: make it before any capture");
+      return GBMV_EINVAL;
+    }
+    const long n = c->n;
+    const size_t ints = (size_t)n + 2 * kDirkOrderBuckets + 1 + ((size_t)n + 3) / 4;
+    if (cudaMalloc(&c->dirk_order_buf, sizeof(int) * ints) != cudaSuccess) {
+      cudaGetLastError();
+      c->dirk_order_buf = nullptr;
+      set_error("device allocation of the DIRK order buffers failed");
+      return GBMV_ENOMEM;
+    }
+    c->order.list = c->dirk_order_buf;
+    c->order.hist = c->order.list + n;
+    c->order.offset = c->order.hist + kDirkOrderBuckets;
+    c->order.count = c->order.offset + kDirkOrderBuckets;
+    c->order.bucket = reinterpret_cast<unsigned char*>(c->order.count + 1);
+  }
   return GBMV_OK;
 }
 
@@ -689,9 +712,10 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
       o->maxnef < 1 || o->maxncf < 1 || o->refine < 0 || o->refine > 8 ||
       (o->precision != GBMV_FP64 && o->precision != GBMV_MIXED) ||
       (o->block != 0 && o->block != 32 && o->block != 64 && o->block != 128) ||
-      o->setup_batch < 1 || o->setup_batch > 32 || !(tout > t0) || !(tunit > 0.0)) {
+      o->setup_batch < 1 || o->setup_batch > 32 || (o->order != 0 && o->order != 1) ||
+      !(tout > t0) || !(tunit > 0.0)) {
     set_error("bad DIRK options (tolerances > 0, growth >= 1, hmax >= 0, counts >= 1, refine 0-8, "
-              "block 0/32/64/128, setup_batch 1-32, tout > t0, time_units > 0)");
+              "block 0/32/64/128, setup_batch 1-32, order 0/1, tout > t0, time_units > 0)");
     return GBMV_EINVAL;
   }
   O->t0 = t0;
@@ -714,6 +738,7 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
   O->maxncf = o->maxncf;
   O->refine = o->precision == GBMV_MIXED ? o->refine : 0;
   O->setup_batch = o->setup_batch;
+  O->order = o->order;
   O->mixed_temp = o->precision == GBMV_MIXED;
   O->nforcing = 0;
   O->tshift = 0.0;
@@ -735,7 +760,11 @@ static int ck(cudaError_t e, const char* where) {
 }
 
 // Block-size autotuner: integrates a sample of the cells (the first min(n, 65536), their
-// temperature state saved and restored) once per candidate and keeps the fastest.
+// temperature state saved and restored) once per candidate, 32 and 64 threads, and keeps the
+// fastest.  (128 is accepted as an explicit option but not a candidate: on the 64^3
+// static-chemistry run it measured 2.49 s against 2.27-2.30 s for 32 and 64 in the FP64 form
+// and no better in the mixed one, while a sample run -- under two cells per lane, so mostly
+// its slowest cells -- cannot tell them apart.)
 static int dirk_autotune(gbmv_chem c, const double* y, const DirkOpts& O, int mixed,
                          cudaStream_t s) {
   const long ns = c->n < 65536 ? c->n : 65536;
@@ -754,8 +783,8 @@ static int dirk_autotune(gbmv_chem c, const double* y, const DirkOpts& O, int mi
                                            cudaMemcpyDeviceToDevice, s), "autotune save");
   if (!rc) rc = ck(cudaMemcpyAsync(tsave + ns, c->S.dTs_ge, sizeof(double) * ns,
                                            cudaMemcpyDeviceToDevice, s), "autotune save");
-  const int cand[3] = {32, 64, 128};
-  for (int k = 0; k < 3 && !rc; ++k) {
+  const int cand[2] = {32, 64};
+  for (int k = 0; k < 2 && !rc; ++k) {
     rc = ck(cudaMemcpyAsync(ybuf, y, sizeof(double) * 10 * ns, cudaMemcpyDeviceToDevice, s),
                     "autotune sample");
     if (!rc) rc = ck(cudaMemcpyAsync(c->S.Ts, tsave, sizeof(double) * ns,
@@ -765,7 +794,7 @@ static int dirk_autotune(gbmv_chem c, const double* y, const DirkOpts& O, int mi
     if (!rc) rc = ck(cudaEventRecord(e0, s), "autotune event");
     if (rc) break;
     const int r = chem_dirk(c->P, c->S, ns, ybuf, O, mixed, cand[k], c->d_next, nullptr,
-                            c->d_info, s);  // failures of the sample land in a scratch word
+                            c->d_info, s, nullptr, &c->order);  // failures: a scratch word
     if (r == GBMV_EUNSUPPORTED) continue;  // does not fit on an SM
     if (r) { rc = r; break; }
     rc = ck(cudaEventRecord(e1, s), "autotune event");
@@ -812,7 +841,7 @@ static int dirk_launch(gbmv_chem c, double t0, double tout, double* y, double ti
     block = c->dirk_block[mixed];
   }
   rc = chem_dirk(c->P, c->S, c->n, y, O, mixed, block, c->d_next, stats, d_nfail, s,
-                 &c->retry);
+                 &c->retry, &c->order);
   if (rc == GBMV_EUNSUPPORTED) set_error("DIRK block of %d threads does not fit on an SM", block);
   return rc;
 }
@@ -1148,7 +1177,7 @@ static int mri_fast_launch(gbmv_hydro h, gbmv_chem c, double t0, double tout, do
     if (rc) return rc;
   }
   return chem_dirk(c->P, c->S, c->n, w[5], O, mixed, block, c->d_next, stats, d_nfail, s,
-                   &c->retry);
+                   &c->retry, &c->order);
 }
 
 int gbmv_mri_fast_evolve(gbmv_hydro h, gbmv_chem c, double t0, double tout, double* const* w,

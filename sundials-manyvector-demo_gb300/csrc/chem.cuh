@@ -79,6 +79,7 @@ struct DirkOpts {
   int maxcor, max_steps, msbp, maxnef, maxncf;
   int refine;      // FP32 LU: refinement steps per Newton solve
   int setup_batch; // waiting lanes of a warp that trigger its matrix setups (1: no waiting)
+  int order;       // 1: cells taken largest initial derivative first (DirkOrder), 0: by index
   int mixed_temp;  // temperature iterations 1-8 in FP32
   // MRI forcing added to F: sum_i tau^i fz[i] (chemistry components, 10 per cell),
   // tau = (t - tshift) / tscale
@@ -109,12 +110,23 @@ struct DirkRetry {
   int* list;    // n: failed cells of the FP32 pass
   int* count;   // 1
 };
+// Buffers of the cost order: a bucket per cell (kDirkOrderBuckets, 4 per decade of the cell's
+// initial WRMS derivative size, largest first), the bucket counts and offsets, the ordered
+// cell list and its length.
+constexpr int kDirkOrderBuckets = 64;
+struct DirkOrder {
+  unsigned char* bucket;  // n
+  int* hist;              // kDirkOrderBuckets
+  int* offset;            // kDirkOrderBuckets
+  int* count;             // 1
+  int* list;              // n
+};
 constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
                                // matrix setups, Jacobians (= setups), F evaluations, failed
 // retry: null, or (FP32 form without refinement) the buffers of the FP64 second pass
 int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const DirkOpts& O,
               int lu_fp32, int block, unsigned long long* d_next, int* stats, int* d_nfail,
-              cudaStream_t s, const DirkRetry* retry = nullptr);
+              cudaStream_t s, const DirkRetry* retry = nullptr, const DirkOrder* order = nullptr);
 // Largest number of lanes (threads) any launch shape of chem_dirk runs on this device: the
 // stage store must hold kstore_lanes >= this many lanes.
 long chem_dirk_max_lanes();

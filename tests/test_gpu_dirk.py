@@ -111,7 +111,7 @@ def test_dirk_block_sizes_bitwise_equal_and_autotune(cuda, tables):
         else:
             assert np.array_equal(z, ref[0]) and np.array_equal(st, ref[1]), b
     z, st, nf, c = _gpu_run(torch, tables, scale, tout, precision=1, block=0, **OPTS)
-    assert c.dirk_block(gbmv.MIXED) in (32, 64, 128)
+    assert c.dirk_block(gbmv.MIXED) in (32, 64)
     assert c.dirk_block(gbmv.FP64) == 0
     assert np.array_equal(z, ref[0]) and np.array_equal(st, ref[1])
 
@@ -135,6 +135,27 @@ def test_dirk_setup_batching_bitwise_equal(cuda, tables, precision):
         else:
             assert np.array_equal(z, ref[0]) and np.array_equal(st, ref[1]), sb
             assert np.array_equal(Ts, ref[2]), sb
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_dirk_cost_order_bitwise_equal(cuda, tables, precision):
+    """Taking the cells largest initial derivative first (order 1, the default) instead of by
+    index changes only which lane integrates which cell when: every cell's state, temperature
+    and counters are identical."""
+    torch = cuda
+    n, tout = 6000, 2e-4
+    scale = _cells(n, W.SEED_BASE + 506)
+    ref = None
+    for order in (0, 1):
+        z, st, nf, c = _gpu_run(torch, tables, scale, tout, precision=precision, block=64,
+                                order=order, **OPTS)
+        Ts = c.state("Ts").cpu().numpy()
+        assert nf == 0
+        if ref is None:
+            ref = (z, st, Ts)
+        else:
+            assert np.array_equal(z, ref[0]) and np.array_equal(st, ref[1])
+            assert np.array_equal(Ts, ref[2])
 
 
 def test_dirk_every_cell_retired_once_and_histogram(cuda, tables):
@@ -174,7 +195,7 @@ def test_dirk_options_rejected(cuda, tables):
     z = torch.ones(160, dtype=torch.float64, device="cuda")
     for bad in (dict(rtol=0.0), dict(block=48), dict(refine=9), dict(precision=3),
                 dict(maxcor=0), dict(table=13), dict(table=104 + 1000), dict(table=8),
-                dict(setup_batch=0), dict(setup_batch=33)):
+                dict(setup_batch=0), dict(setup_batch=33), dict(order=2)):
         with pytest.raises(gbmv.GbmvError):
             c.dirk_evolve(0.0, 1e-3, z, TU, **bad)
     with pytest.raises(gbmv.GbmvError):
