@@ -819,6 +819,24 @@ def run_weno(torch, gbmv, grids, steps=3, warmup=2, parity=True):
 SOD_TABLE = 3  # ARKODE's default order-4 ERK (input_sod.txt: order = 4)
 
 
+def sod_errors(yg, shape, x, t=0.2, gamma=1.4):
+    """L-infinity and RMS errors of the five conserved fields against the exact Riemann
+    solution over the whole grid, as the reference's Sod output_diagnostics forms them
+    (src/sod.cpp:385-469: rho, mx, my, mz, et)."""
+    import integrate as I
+    r, u, p = I.sod_exact(x, t, gamma)
+    exact = [r, r * u, 0.0 * r, 0.0 * r, p / (gamma - 1.0) + 0.5 * r * u * u]
+    names = ["rho", "mx", "my", "mz", "et"]
+    linf, rms = {}, {}
+    for v, (nm, e) in enumerate(zip(names, exact)):
+        d = np.abs(yg[v].reshape(shape) - e[None, None, :])
+        linf[nm] = float(f"{float(d.max()):.3e}")
+        rms[nm] = float(f"{float(np.sqrt(np.mean(d * d))):.3e}")
+    return {"linf": linf, "rms": rms,
+            "note": "shocks and contacts are smeared over a few cells, so the L-infinity errors "
+                    "are of the jump's size there; the RMS errors carry the convergence"}
+
+
 def run_sod(torch, gbmv, with_cpu):
     """Sod shock tube 128x3x3 (reflecting x, periodic y,z, gamma 1.4) to t_f = 0.2 with the
     adaptive ERK of the Sod inputs (order 4: ARKODE's Zonneveld 5-3-4, PID controller; rtol
@@ -884,7 +902,8 @@ def run_sod(torch, gbmv, with_cpu):
            "host_loop": {"s_to_tf": round(dt_loop, 3), "steps": stl.steps,
                          "note": "integrate.erk_evolve: one host synchronisation per step"},
            "graph_vs_host_loop_maxnorm_diff": float(f"{max(float(np.max(np.abs(yg[v] - yl.cpu().numpy()[v]))) / max(float(np.max(np.abs(yl.cpu().numpy()[v]))), 1e-300) for v in range(5)):.3e}"),
-           "l1_density_err_vs_exact": float(f"{np.mean(np.abs(rho - r)):.3e}")}
+           "l1_density_err_vs_exact": float(f"{np.mean(np.abs(rho - r)):.3e}"),
+           "vs_exact": sod_errors(yg, shape, x)}
     if with_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle_py as O
