@@ -329,8 +329,8 @@ void gbmv_dirk_opts_default(gbmv_dirk_opts* o);
  * gbmv_chem_rhs) from t0 to tout with the adaptive ESDIRK of opts->table and modified Newton
  * on per-cell 10x10 systems, each cell on its own step sequence, in one persistent launch
  * that retires finished cells and pulls new ones.  In the GBMV_MIXED form the cells whose
- * FP32 pass fails are integrated again from their start state by a second, FP64 launch over
- * just those cells (counted by gbmv_chem_dirk_retried).  It replaces the fast-stage
+ * FP32 pass fails are integrated again from their start state by a second launch with the
+ * FP64 factor over just those cells (counted by gbmv_chem_dirk_retried).  It replaces the fast-stage
  * integration of the chemistry drivers: ARKStep DIRK + Jfast/Jimpl + the block solver
  * (src/primordial_ode_main.cpp) and the rank-local MRI inner stepper's evolve
  * (src/multirate_chem_hydro_main.cpp:1114-1224), with per-cell instead of rank-wide step
@@ -376,9 +376,10 @@ int gbmv_mri_fast_evolve_async(gbmv_hydro h, gbmv_chem c, double t0, double tout
 
 /* The GBMV_MIXED DIRK (refine 0) runs two passes: every cell in FP32-LU arithmetic, then the
  * cells that pass could not finish (Newton iterations that keep failing on an FP32 factor too
- * poor for the block) again from their start state in FP64, so they get exactly the FP64
- * form's result.  This returns how many cells the last GBMV_MIXED call on the handle sent to
- * the FP64 pass, and copies up to max_cells of their indices (host) into cells (may be NULL).
+ * poor for the block) again from their start state with the FP64 factor (and the mixed
+ * temperature solve, within ~1e-16 of the FP64 form's), so they end where the FP64 form ends
+ * them to rounding.  This returns how many cells the last GBMV_MIXED call on the handle sent to
+ * the second pass, and copies up to max_cells of their indices (host) into cells (may be NULL).
  * Synchronous. */
 int gbmv_chem_dirk_retried(gbmv_chem c, int* cells, int max_cells, void* stream);
 

@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         st[7] = failed ? 1 : 0;
       }
       if (failed) {
-        if (O.list_out) O.list_out[atomicAdd(O.list_out_n, 1)] = (int)i;  // retried in FP64
+        if (O.list_out) O.list_out[atomicAdd(O.list_out_n, 1)] = (int)i;  // second pass
         else atomicAdd(nfail, 1);
       }
       i = -1;
@@ -788,9 +788,9 @@ int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const 
   if (!retry)
     return launch_dirk_bs<float, false>(block, P, S, n, y, O, d_next, stats, d_nfail, nsm, s);
   // FP32 pass over every cell, its start state kept; a cell it cannot finish (its Newton
-  // iterations keep failing on an FP32 factor too poor for the block) is listed, and an FP64
-  // pass integrates the listed cells again from their start state.  Both passes are
-  // asynchronous launches; the second finds an empty list when nothing failed.
+  // iterations keep failing on an FP32 factor too poor for the block) is listed, and a pass
+  // with the FP64 factor integrates the listed cells again from their start state.  Both
+  // passes are asynchronous launches; the second finds an empty list when nothing failed.
   GBMV_CUDA_TRY(cudaMemcpyAsync(retry->y0, y, sizeof(double) * 10 * n, cudaMemcpyDeviceToDevice,
                                 s));
   GBMV_CUDA_TRY(cudaMemcpyAsync(retry->ts0, S.Ts, sizeof(double) * n, cudaMemcpyDeviceToDevice,
@@ -809,7 +809,11 @@ int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const 
   Of.list_in_n = retry->count;
   Of.y_init = retry->y0;
   Of.Ts_init = retry->ts0;
-  Of.mixed_temp = 0;
+  // the retried cells keep the mixed temperature solve (8 FP32 + 2 FP64 iterations, the FP64
+  // form's temperature to ~1e-16) with the FP64 factor: a handful of hard cells, one lane each,
+  // whose pass is latency-bound by its F evaluations -- the ten FP64 temperature iterations
+  // were 70 % of them (retry pass 210 -> 95 ms, 64^3 call 1.31 -> 1.19 s)
+  Of.mixed_temp = 1;
   return launch_dirk<double, false, 64>(P, S, n, y, Of, d_next, stats, d_nfail, nsm, s);
 }
 
