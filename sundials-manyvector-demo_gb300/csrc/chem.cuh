@@ -121,6 +121,7 @@ struct DirkOrder {
   int* count;             // 1
   int* list;              // n
 };
+constexpr int kDirkFp32MaxNcf = 5;  // the mixed DIRK's FP32 pass: Newton failures per step
 constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
                                // matrix setups, Jacobians (= setups), F evaluations, failed
 // retry: null, or (FP32 form without refinement) the buffers of the FP64 second pass

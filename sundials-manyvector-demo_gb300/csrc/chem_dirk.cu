@@ -64,7 +64,7 @@ __device__ __forceinline__ void dirk_F(const ChemParams& P, const ChemState& S, 
 #pragma unroll
   for (int s = 0; s < 10; ++s) ya[s] = X[s * BS] * S.scale[j + s];
   if (mixed_temp)
-    chem_temperature_mixed(P, ya, Ts, dTs, 8);
+    chem_temperature_mixed(P, ya, Ts, dTs, 9);  // up to 9 FP32 + 1 FP64 iteration
   else
     chem_temperature(P, ya, Ts, dTs);
   double k[kNRates], dk[kNRates];
@@ -801,6 +801,13 @@ int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const 
   DirkOpts Om = O;
   Om.list_out = retry->list;
   Om.list_out_n = retry->count;
+  // The FP32 pass gives a cell up after kDirkFp32MaxNcf Newton failures in one step (the
+  // caller's maxncf applies in the second pass).  With the mixed F's single FP64 temperature
+  // iteration the FP32 pass is faster per cell, but the few cells whose FP32 factor keeps
+  // failing would otherwise crawl on in tiny steps and become the launch's tail (64^3: FP32
+  // pass alone 1.78 s with the caller's 10; 1.14 s for both passes at 5, 195 cells retried;
+  // 1.18 s at 2 and 3)
+  Om.maxncf = O.maxncf < kDirkFp32MaxNcf ? O.maxncf : kDirkFp32MaxNcf;
   int rc = launch_dirk_bs<float, false>(block, P, S, n, y, Om, d_next, stats, d_nfail, nsm, s);
   if (rc) return rc;
   GBMV_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), s));

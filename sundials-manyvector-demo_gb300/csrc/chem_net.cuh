@@ -88,7 +88,10 @@ __device__ __forceinline__ void chem_temperature(const ChemParams& P, const doub
 
 // The same Newton solve with up to `nfloat` iterations in FP32 (table lookups on float copies
 // of the four adiabatic-index tables, value and slope per bin, rounded once at setup exactly
-// as the iterations would round the FP64 entries) and two in FP64.  The FP32 stage stops early
+// as the iterations would round the FP64 entries) and 10 - nfloat in FP64 (the fused Newton
+// 8 + 2, which keeps the carried temperature within ~1e-16 of the FP64 form's; the DIRK's F
+// evaluations 9 + 1, ~1e-10 near a table bin edge, far inside the integration tolerance,
+// where Newton converges only linearly).  The FP32 stage stops early
 // once its step is below 1e-5 T: Newton's error after such a step is ~1e-10 T, inside the
 // basin where the two FP64 iterations restore full accuracy (quadratic convergence), so the
 // result matches chem_temperature's to rounding whenever the reference's ten iterations
