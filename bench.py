@@ -189,11 +189,19 @@ class FusedStep:
                 self.tuned["sweeps"] = "shared"
                 if concurrent == "queue":
                     self.queue = torch.zeros(1, dtype=torch.int64, device="cuda")
-                if newton_bps is None:  # the Newton's resident blocks per SM, by timing the
-                    # two-branch graph (the state is restored after each trial)
-                    trials = {b: self._graph_ms(b) for b in NEWTON_BPS_CANDIDATES}
-                    newton_bps = min(trials, key=trials.get)
-                    self.tuned["newton_blocks_per_sm_trials_ms"] = trials
+                if newton_bps is None:  # the Newton's resident blocks per SM and the sweeps'
+                    # threads per block, by timing the two-branch graph (the state is restored
+                    # after each trial)
+                    trials = {}
+                    for st in SWEEP_THREADS_CANDIDATES:
+                        self.hydro.set_sweep_threads(self.precision, st)
+                        for b in NEWTON_BPS_CANDIDATES:
+                            trials[f"{st}x{b}"] = self._graph_ms(b)
+                    best = min(trials, key=trials.get)
+                    st, newton_bps = (int(v) for v in best.split("x"))
+                    self.hydro.set_sweep_threads(self.precision, st)
+                    self.tuned["sweep_threads"] = st
+                    self.tuned["trials_ms (sweep threads x newton blocks per SM)"] = trials
                 self.tuned["newton_blocks_per_sm"] = newton_bps
                 self._set_narrow(newton_bps)
             self.graph = self._capture()
@@ -1016,7 +1024,8 @@ def run_mri(torch, gbmv, n):
     return out
 
 
-NEWTON_BPS_CANDIDATES = (2, 3, 4, 5, 6)  # the concurrent stage's Newton blocks per SM, timed
+NEWTON_BPS_CANDIDATES = (3, 4, 5)  # the concurrent stage's Newton blocks per SM, timed
+SWEEP_THREADS_CANDIDATES = (64, 128)  # and its sweeps' threads per block
 
 
 IMEX_OPTS = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, safety=0.99, bias=2.0,

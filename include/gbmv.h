@@ -134,6 +134,12 @@ int gbmv_hydro_autotune(gbmv_hydro h, const double* const* w, int precision, int
 #define GBMV_SWEEPS_SHARED 1
 int gbmv_hydro_set_sweep_budget(gbmv_hydro h, int budget);
 
+/* Threads per block of the face sweeps of `precision` on this handle: 32, 64 or 128, or 0 for
+ * the size-based default -- what gbmv_hydro_autotune picks, set by a caller that tunes a
+ * composition of its own (for example the sweeps beside the chemistry Newton).  Results do not
+ * depend on it.  Returns 0 or GBMV_EINVAL. */
+int gbmv_hydro_set_sweep_threads(gbmv_hydro h, int precision, int threads);
+
 /* stability (src/utilities.cpp:483-528): dt_stab = cfl * min(dx,dy,dz) / max(|mx/rho| + c),
  * including the reference's use of |mx/rho| for all three directions.  *dt_stab is host. */
 int gbmv_stability(gbmv_hydro h, const double* const* w, double cfl, double* dt_stab,

@@ -336,6 +336,16 @@ int gbmv_hydro_autotune(gbmv_hydro h, const double* const* w, int precision, int
   return GBMV_OK;
 }
 
+int gbmv_hydro_set_sweep_threads(gbmv_hydro h, int precision, int threads) {
+  if (!h || precision < GBMV_FP64 || precision > GBMV_MIXED_FAST ||
+      (threads != 0 && threads != 32 && threads != 64 && threads != 128)) {
+    set_error("null handle, unknown precision or threads not 0/32/64/128");
+    return GBMV_EINVAL;
+  }
+  h->sweep_threads[precision] = threads;
+  return GBMV_OK;
+}
+
 int gbmv_hydro_set_sweep_budget(gbmv_hydro h, int budget) {
   if (!h || (budget != GBMV_SWEEPS_ALONE && budget != GBMV_SWEEPS_SHARED)) {
     set_error("null handle or unknown sweep budget (GBMV_SWEEPS_ALONE, GBMV_SWEEPS_SHARED)");

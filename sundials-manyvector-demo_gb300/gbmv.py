@@ -88,6 +88,7 @@ SIGNATURES = [
     ("gbmv_stability", C.c_int, [_VP, C.POINTER(_VP), C.c_double, _P, _VP]),
     ("gbmv_hydro_autotune", C.c_int, [_VP, C.POINTER(_VP), C.c_int, C.POINTER(C.c_int), _VP]),
     ("gbmv_hydro_set_sweep_budget", C.c_int, [_VP, C.c_int]),
+    ("gbmv_hydro_set_sweep_threads", C.c_int, [_VP, C.c_int, C.c_int]),
     ("gbmv_chem_newton_autotune", C.c_int, [_VP, _VP, C.c_double, C.c_double, C.c_int, C.c_int,
                                             C.POINTER(C.c_int), _VP]),
     ("gbmv_pack1d", C.c_int, [_VP, C.POINTER(_VP), C.c_int, _VP, _VP]),
@@ -298,6 +299,11 @@ class Hydro:
         _check(load().gbmv_hydro_set_sweep_budget(self.h, SWEEPS_SHARED if shared
                                                   else SWEEPS_ALONE),
                "gbmv_hydro_set_sweep_budget")
+
+    def set_sweep_threads(self, precision, threads) -> None:
+        """gbmv_hydro_set_sweep_threads: the face sweeps' threads per block (0 = default)."""
+        _check(load().gbmv_hydro_set_sweep_threads(self.h, precision, threads),
+               "gbmv_hydro_set_sweep_threads")
 
     def kink_mask(self, w, dw, eps, mask, stream=None):
         """gbmv_feuler_kink_mask into `mask` (CUDA uint8 tensor of ncells): 1 where a central

@@ -48,7 +48,14 @@ def test_sweep_budget_keeps_results(cuda):
             assert h.fEuler(0.0, w, b, prec) == 0
             torch.cuda.synchronize()
             assert all(torch.equal(x, y) for x, y in zip(a, b)), (nchem, prec)
+            for threads in (32, 64):  # the caller-set launch shape, likewise
+                h.set_sweep_threads(prec, threads)
+                assert h.fEuler(0.0, w, b, prec) == 0
+                torch.cuda.synchronize()
+                assert all(torch.equal(x, y) for x, y in zip(a, b)), (nchem, prec, threads)
+            h.set_sweep_threads(prec, 0)
     assert gbmv.load().gbmv_hydro_set_sweep_budget(h.h, 2) == -101  # GBMV_EINVAL
+    assert gbmv.load().gbmv_hydro_set_sweep_threads(h.h, gbmv.MIXED_FAST, 96) == -101
 
 
 def test_newton_autotune_keeps_results_and_state(cuda, tables):
