@@ -75,7 +75,8 @@ def parse():
                    help="differentiation measurement on ad_n^3 x 9 fields (0 = skip)")
     p.add_argument("--dirk-only", action="store_true",
                    help="run only the DIRK measurement (prints its object)")
-    p.add_argument("--dirk-form", default="both", choices=["both", "fp64", "mixed"])
+    p.add_argument("--dirk-form", default="all",
+                   choices=["all", "fp64", "mixed", "fp64_deduce", "mixed_deduce"])
     return p.parse_args()
 
 
@@ -951,7 +952,8 @@ MRI_FAST = dict(rtol=1e-6, atol=1e-10, maxcor=10, nlscoef=0.01, itable=112)
 def run_mri(torch, gbmv, n):
     """Multirate chemistry-hydrodynamics to t_f = MRI_STEPS * MRI_H on the chem_hydro state
     (integrate.mri_evolve: WENO slow stages, persistent batched DIRK fast stages) with the
-    reference's default third-order MIS-KW3 coupling in the FP64 and the mixed form, and the
+    reference's default third-order MIS-KW3 coupling in the FP64 and the mixed form (the
+    latter also with the fast DIRK's intermediate stage derivatives deduced), and the
     second-order MRI-GARK-ERK22b coupling in the mixed form; time-to-t_f and max-normalised
     differences per field."""
     import h5tables
@@ -966,9 +968,11 @@ def run_mri(torch, gbmv, n):
                         "atol 1e-10; slow chemistry tendency added unconverted, as the "
                         "reference"), "forms": {}}
     finals = {}
-    for name, prec, table in (("fp64", gbmv.FP64, integrate.MRI_KW3),
-                              ("mixed", gbmv.MIXED, integrate.MRI_KW3),
-                              ("mixed_erk22b", gbmv.MIXED, integrate.MRI_ERK22B)):
+    for name, prec, table, extra in (("fp64", gbmv.FP64, integrate.MRI_KW3, {}),
+                                     ("mixed", gbmv.MIXED, integrate.MRI_KW3, {}),
+                                     ("mixed_deduce", gbmv.MIXED, integrate.MRI_KW3,
+                                      {"deduce": 1}),
+                                     ("mixed_erk22b", gbmv.MIXED, integrate.MRI_ERK22B, {})):
         hy = gbmv.Hydro((n, n, n), 10, wl["bc"], wl["gamma"])
         c = gbmv.Chem(n ** 3, tables)
         c.set_scale(torch.from_numpy(wl["scale"].reshape(-1).copy()).cuda())
@@ -976,7 +980,7 @@ def run_mri(torch, gbmv, n):
         # every slow step one CUDA graph (integrate.GraphMRI): the first step runs eagerly
         # (allocations, the DIRK block autotuner) and the graph is captured, outside the timed
         # region; then the state goes back to the start and all steps replay the graph
-        gm = integrate.GraphMRI(gbmv, hy, c, w, MRI_H, eu, tu, table, prec, **MRI_FAST)
+        gm = integrate.GraphMRI(gbmv, hy, c, w, MRI_H, eu, tu, table, prec, **MRI_FAST, **extra)
         gm.evolve(0.0, MRI_H)
         for x, f in zip(w, wl["fields"]):
             x.copy_(torch.from_numpy(np.ascontiguousarray(f)))
@@ -1024,13 +1028,16 @@ def run_mri(torch, gbmv, n):
         "reference_s": round(time.perf_counter() - t0, 3),
         "reference_failed_cells": r.fast_failed_cells,
         "fp64_maxnorm_err": errs(finals["fp64"], ref),
-        "mixed_maxnorm_err": errs(finals["mixed"], ref)}
+        "mixed_maxnorm_err": errs(finals["mixed"], ref),
+        "mixed_deduce_maxnorm_err": errs(finals["mixed_deduce"], ref)}
     del hy, c, w, gm
     torch.cuda.empty_cache()
     # the coupling's own contribution (second- against third-order MRI at the same slow step)
     out["erk22b_vs_kw3_maxnorm_diff"] = errs(finals["mixed_erk22b"], finals["mixed"])
     out["speedup_mixed_vs_fp64"] = round(out["forms"]["fp64"]["s_to_tf"] /
                                          out["forms"]["mixed"]["s_to_tf"], 3)
+    out["speedup_mixed_deduce_vs_fp64"] = round(out["forms"]["fp64"]["s_to_tf"] /
+                                                out["forms"]["mixed_deduce"]["s_to_tf"], 3)
     return out
 
 
@@ -1259,10 +1266,12 @@ def _dirk_summary(st):
             "f_evals_mean": round(float(st[:, 6].mean()), 2), "failed": int(st[:, 7].sum())}
 
 
-def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
+def run_dirk(torch, gbmv, n1, with_cpu, forms="all"):
     """Static primordial chemistry on n1^3 cells integrated to DIRK_TOUT by the persistent
     batched DIRK kernel, FP64 form and mixed form (equilibrated FP32 LU, FP32 temperature
-    iterations); per-cell Newton-iteration histograms; oracle port timed on a sample."""
+    iterations), each with the intermediate stage derivatives evaluated (ARKODE's default)
+    and deduced from the stage equations (`_deduce`); per-cell Newton-iteration histograms;
+    every form against a tight-tolerance solution; oracle port timed on a sample."""
     import h5tables
     import workloads as W
     tables = h5tables.load_table_block(TABLES)
@@ -1276,8 +1285,9 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
                         f"t in [0, {DIRK_TOUT}] x 1e11 s"),
            "cells": n, "tout": DIRK_TOUT, "table": DIRK_TABLE, "forms": {}}
     finals = {}
-    for name, prec in (("fp64", gbmv.FP64), ("mixed", gbmv.MIXED)):
-        if forms not in ("both", name):
+    for name, prec, deduce in (("fp64", gbmv.FP64, 0), ("mixed", gbmv.MIXED, 0),
+                               ("fp64_deduce", gbmv.FP64, 1), ("mixed_deduce", gbmv.MIXED, 1)):
+        if forms not in ("all", name):
             continue
         c = gbmv.Chem(n, tables)
         c.set_scale(scale)
@@ -1285,7 +1295,8 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
         st = torch.zeros(8 * n, dtype=torch.int32, device="cuda")
         # warm-up call over the full interval: the block-size autotuner times its candidates
         # on this call's work, which must be representative of the timed one
-        c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, precision=prec, table=DIRK_TABLE, **DIRK_OPTS)
+        c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, precision=prec, table=DIRK_TABLE, deduce=deduce,
+                      **DIRK_OPTS)
         z.fill_(1.0)
         c.state("Ts").fill_(1000.0)
         torch.cuda.synchronize()
@@ -1294,7 +1305,7 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
         with ClockSampler(0) as clk:
             e0.record(s)
             nf = c.dirk_evolve(0.0, DIRK_TOUT, z, 1e11, stats=st, precision=prec,
-                               table=DIRK_TABLE, **DIRK_OPTS)
+                               table=DIRK_TABLE, deduce=deduce, **DIRK_OPTS)
             e1.record(s)
             torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -1304,9 +1315,15 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
                               "unit": "Mcells/s (cells integrated to tout per second)",
                               "block": c.dirk_block(prec), "failed_cells": int(nf),
                               "clocks": clk.summary(), **_dirk_summary(stn)}
+        if prec == gbmv.MIXED:  # cells the FP32 pass left to the FP64-factor pass, their cost
+            rc = c.dirk_retried()
+            out["forms"][name]["second_pass"] = {
+                "cells": int(rc.size),
+                "newton_iters_max": int(stn[rc, 1].max()) if rc.size else 0,
+                "f_evals_max": int(stn[rc, 6].max()) if rc.size else 0}
         del c
         torch.cuda.empty_cache()
-    if len(finals) == 2:
+    if "mixed" in finals and "fp64" in finals:
         a, b = finals["mixed"], finals["fp64"]
         e = np.abs(a - b) / (np.abs(b) + DIRK_OPTS["atol"] / DIRK_OPTS["rtol"])
         out["mixed_vs_fp64_relerr"] = {"median": float(f"{np.median(e):.3e}"),
@@ -1314,6 +1331,10 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
                                        "max": float(f"{e.max():.3e}")}
         out["speedup_mixed_vs_fp64"] = round(out["forms"]["fp64"]["ms"] /
                                              out["forms"]["mixed"]["ms"], 3)
+    for name in ("fp64_deduce", "mixed_deduce"):
+        if name in finals and "fp64" in finals:
+            out[f"speedup_{name}_vs_fp64"] = round(out["forms"]["fp64"]["ms"] /
+                                                   out["forms"][name]["ms"], 3)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as O
     # both forms against a tight-tolerance FP64 solution (the oracle at rtol 1e-10) on a sample
@@ -1334,11 +1355,36 @@ def run_dirk(torch, gbmv, n1, with_cpu, forms="both"):
         tight[f"{name}_relerr"] = {"median": float(f"{np.median(e):.3e}"),
                                    "p99": float(f"{np.percentile(e, 99):.3e}"),
                                    "max": float(f"{e.max():.3e}")}
-    if len(finals) == 2:
+    if "mixed" in finals and "fp64" in finals:
         d = (np.abs(finals["mixed"][:ns_t] - finals["fp64"][:ns_t]) /
              (np.abs(finals["fp64"][:ns_t]) + floor)).max(axis=1)
         tight["mixed_vs_fp64_relerr_max"] = float(f"{d.max():.3e}")
     out["vs_tight_tolerance_solution"] = tight
+    if len(finals) >= 2:
+        # the cells where the forms disagree most (over all cells), against the same tight
+        # solution: which form a large disagreement comes from
+        names = list(finals)
+        base = finals[names[0]]
+        dis = np.zeros(n)
+        for name in names[1:]:
+            dis = np.maximum(dis, (np.abs(finals[name] - base) / (np.abs(base) + floor)).max(axis=1))
+        nh = 32
+        idx = np.sort(np.argsort(dis)[-nh:])
+        t0 = time.perf_counter()
+        oc = O.Chem(tables, y[idx].reshape(-1))
+        zh, _, nfh = oc.dirk_evolve(np.ones(10 * nh), 0.0, DIRK_TOUT, 1e11, rtol=1e-10,
+                                    atol=1e-14, maxcor=10, nlscoef=0.01, max_steps=500000,
+                                    table=DIRK_TABLE)
+        zh = zh.reshape(nh, 10)
+        hard = {"sample": f"the {nh} cells of largest disagreement between the forms (largest "
+                          f"{dis.max():.3e}, smallest {dis[idx].min():.3e}, against {names[0]})",
+                "reference_failed_cells": int(nfh),
+                "oracle_s": round(time.perf_counter() - t0, 2)}
+        for name, z in finals.items():
+            e = (np.abs(z[idx] - zh) / (np.abs(zh) + floor)).max(axis=1)
+            hard[f"{name}_relerr"] = {"median": float(f"{np.median(e):.3e}"),
+                                      "max": float(f"{e.max():.3e}")}
+        out["vs_tight_tolerance_solution_hardest"] = hard
     if with_cpu:
         ns = 256
         oc = O.Chem(tables, y[:ns].reshape(-1))

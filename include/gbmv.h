@@ -326,6 +326,15 @@ typedef struct {
                         WRMS norm, in quarter-decade buckets), so the costliest cells start
                         early and few lanes idle at the end; 0: in index order.  Every cell's
                         result is the same either way (default 1) */
+  int deduce;        /* 1: the derivative of every converged intermediate stage is deduced
+                        from its stage equation, K_i = (z_i - base_i) / (h gamma), instead of
+                        evaluating F(z_i) (ARKODE's ARKStepSetDeduceImplicitRhs; a Newton error
+                        enters K_i as itself over h gamma rather than multiplied by the stiff
+                        Jacobian); the last stage is still evaluated, since F(z_s) = F(y_{n+1})
+                        is the next step's first stage.  In the GBMV_MIXED form the FP32 pass
+                        also hands a cell to the FP64-factor pass after 8 Newton failures in
+                        all (a deduced derivative carries the FP32 factor's inexact
+                        corrections).  0: every stage evaluated, ARKODE's default (default 0) */
 } gbmv_dirk_opts;
 
 /* Fill *o with the defaults above (rtol 1e-6, atol 1e-10). */

@@ -802,8 +802,13 @@ long orc_chem_dirk_evolve(const orc_chem* c, long n, double* y, const double* sc
           delp = del;
         }
         if (conv && st < ns - 1) {
-          dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, KS[st]);
-          ++nfe;
+          if (O->deduce) { /* ARKODE's deduced implicit RHS: no F evaluation */
+            const double rg = 1.0 / gam; /* as the GPU kernel: one reciprocal, ten products */
+            for (int s = 0; s < 10; ++s) KS[st][s] = (Z[s] - Bv[s]) * rg;
+          } else {
+            dirk_F(c, Z, sc, isc, md, imd, cie, h2, O, i, tst, &Tsc, &dTsc, KS[st]);
+            ++nfe;
+          }
         }
       }
       if (!conv) {

@@ -103,6 +103,9 @@ typedef struct {
   double c[7];
   double a[7][7];
   double e[7];
+  /* 1: the derivative of each converged intermediate stage from its stage equation,
+   * K_i = (z_i - base_i) / (h gamma), instead of F(z_i) (gbmv_dirk_opts.deduce) */
+  int deduce;
 } orc_dirk_opts;
 
 /* Per-cell adaptive ESDIRK integration (the table in O) of dz/dt = tunit * f_chem(z) (scaled

@@ -54,7 +54,7 @@ class OrcDirkOpts(C.Structure):
                                        "nforcing")] + \
                [("tshift", C.c_double), ("tscale", C.c_double), ("fz", _P * 8),
                 ("s", C.c_int), ("p", C.c_int), ("gamma", C.c_double), ("c", C.c_double * 7),
-                ("a", (C.c_double * 7) * 7), ("e", C.c_double * 7)]
+                ("a", (C.c_double * 7) * 7), ("e", C.c_double * 7), ("deduce", C.c_int)]
 
 
 def _q(a, b):
@@ -105,7 +105,7 @@ DIRK_TABLES = _dirk_tables()
 # defaults of gbmv_dirk_opts_default (include/gbmv.h)
 DIRK_DEFAULTS = dict(rtol=1e-6, atol=1e-10, nlscoef=0.1, h0=0.0, safety=0.9, dgmax=0.2,
                      growth=20.0, etamx1=10000.0, hmax=0.0, maxcor=3, max_steps=5000, msbp=20,
-                     maxnef=7, maxncf=10)
+                     maxnef=7, maxncf=10, deduce=0)
 
 
 def _ptr(a: np.ndarray):

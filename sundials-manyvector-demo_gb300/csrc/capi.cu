@@ -626,6 +626,7 @@ void gbmv_dirk_opts_default(gbmv_dirk_opts* o) {
   o->table = 0;
   o->setup_batch = 8;
   o->order = 1;
+  o->deduce = 0;
 }
 
 // The DIRK table of the options (0: ARK437L2SA_DIRK_7_3_4, the reference's chemistry inputs'
@@ -723,9 +724,10 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
       (o->precision != GBMV_FP64 && o->precision != GBMV_MIXED) ||
       (o->block != 0 && o->block != 32 && o->block != 64 && o->block != 128) ||
       o->setup_batch < 1 || o->setup_batch > 32 || (o->order != 0 && o->order != 1) ||
-      !(tout > t0) || !(tunit > 0.0)) {
+      (o->deduce != 0 && o->deduce != 1) || !(tout > t0) || !(tunit > 0.0)) {
     set_error("bad DIRK options (tolerances > 0, growth >= 1, hmax >= 0, counts >= 1, refine 0-8, "
-              "block 0/32/64/128, setup_batch 1-32, order 0/1, tout > t0, time_units > 0)");
+              "block 0/32/64/128, setup_batch 1-32, order 0/1, deduce 0/1, tout > t0, "
+              "time_units > 0)");
     return GBMV_EINVAL;
   }
   O->t0 = t0;
@@ -749,6 +751,8 @@ static int dirk_opts(const gbmv_dirk_opts* o, double t0, double tout, double tun
   O->refine = o->precision == GBMV_MIXED ? o->refine : 0;
   O->setup_batch = o->setup_batch;
   O->order = o->order;
+  O->deduce = o->deduce;
+  O->maxncf_total = 0;
   O->mixed_temp = o->precision == GBMV_MIXED;
   O->nforcing = 0;
   O->tshift = 0.0;

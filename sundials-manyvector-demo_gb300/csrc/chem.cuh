@@ -80,7 +80,9 @@ struct DirkOpts {
   int refine;      // FP32 LU: refinement steps per Newton solve
   int setup_batch; // waiting lanes of a warp that trigger its matrix setups (1: no waiting)
   int order;       // 1: cells taken largest initial derivative first (DirkOrder), 0: by index
-  int mixed_temp;  // temperature iterations 1-8 in FP32
+  int deduce;      // 1: intermediate stage derivatives from the stage equation, not F
+  int maxncf_total;  // Newton failures of a cell before it counts as failed (0: no limit)
+  int mixed_temp;  // F evaluations' temperature solve: up to 9 FP32 iterations + 1 FP64
   // MRI forcing added to F: sum_i tau^i fz[i] (chemistry components, 10 per cell),
   // tau = (t - tshift) / tscale
   int nforcing;
@@ -122,6 +124,7 @@ struct DirkOrder {
   int* list;              // n
 };
 constexpr int kDirkFp32MaxNcf = 5;  // the mixed DIRK's FP32 pass: Newton failures per step
+constexpr int kDirkFp32MaxNcfTotal = 8;  // and per cell, with deduced stage derivatives
 constexpr int kDirkStats = 8;  // per cell: steps, Newton iters, error fails, Newton fails,
                                // matrix setups, Jacobians (= setups), F evaluations, failed
 // retry: null, or (FP32 form without refinement) the buffers of the FP64 second pass

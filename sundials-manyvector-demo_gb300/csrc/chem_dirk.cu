@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
           if (info) {  // singular Newton matrix: a recoverable failure, cut the step and retry
             ++ncf_s;
             ++c_ncf;
-            if (ncf_s >= O.maxncf) {
+            if (ncf_s >= O.maxncf || (O.maxncf_total > 0 && c_ncf >= O.maxncf_total)) {
               retire = failed = true;
             } else {
               h *= 0.25;
@@ -490,14 +490,26 @@ __global__ void __launch_bounds__(BS) chem_dirk_kernel(ChemParams P, ChemState S
         ++c_nni;
         if (m > 1) crate = fmax(0.3 * crate, del / delp);
         const double dcon = fmin(crate, 1.0) * del / O.nlscoef;
-        if (dcon <= 1.0) {
+        if (dcon <= 1.0 && O.deduce && stage < ns - 1) {
+          // converged intermediate stage, derivative deduced from the stage equation:
+          // K_stage = (z - base) / (h gamma), no F evaluation; next stage in this pass.  One
+          // reciprocal and ten products: nearly every pass of a warp has a lane deducing, and
+          // ten FP64 divisions there cost as much FP64-pipe time as the F evaluations saved
+          const double rg = 1.0 / gam;
+#pragma unroll
+          for (int s = 0; s < 10; ++s)
+            KG[((stage - 1) * 10 + s) * kst] = (Z[s * BS] - B[s * BS]) * rg;
+          ++stage;
+          dirk_stage_base<BS>(O, stage, h, Y, K1, KG, kst, B);
+          m = 0;
+        } else if (dcon <= 1.0) {
           phase = kPhStage;
         } else if ((m > 1 && del > 2.3 * delp) || m >= O.maxcor || !(del == del)) {
           // Newton failure: with a matrix from an earlier step set up a current one at the
           // same h, else cut the step
           ++ncf_s;
           ++c_ncf;
-          if (ncf_s >= O.maxncf) {
+          if (ncf_s >= O.maxncf || (O.maxncf_total > 0 && c_ncf >= O.maxncf_total)) {
             retire = failed = true;
           } else {
             if (jcur) h *= 0.25;
@@ -808,6 +820,13 @@ int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const 
   // pass alone 1.78 s with the caller's 10; 1.14 s for both passes at 5, 195 cells retried;
   // 1.18 s at 2 and 3)
   Om.maxncf = O.maxncf < kDirkFp32MaxNcf ? O.maxncf : kDirkFp32MaxNcf;
+  // With deduced stage derivatives the FP32 factor's inexact corrections enter the next
+  // stages' bases, and on the few blocks whose species span ~50 decades that shows as repeated
+  // Newton failures (64^3: two cells with 10 and 14 over the run, against 0-1 for every other
+  // form, ending 2e-3 and 3e-2 from a tight-tolerance solution; with the FP64 factor 4e-5 and
+  // 1.4e-4, as the evaluated forms).  So the FP32 pass also gives up a cell after
+  // kDirkFp32MaxNcfTotal Newton failures in all, and the FP64 factor integrates it
+  Om.maxncf_total = O.deduce ? kDirkFp32MaxNcfTotal : 0;
   int rc = launch_dirk_bs<float, false>(block, P, S, n, y, Om, d_next, stats, d_nfail, nsm, s);
   if (rc) return rc;
   GBMV_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), s));
@@ -816,9 +835,9 @@ int chem_dirk(const ChemParams& P, const ChemState& S, long n, double* y, const 
   Of.list_in_n = retry->count;
   Of.y_init = retry->y0;
   Of.Ts_init = retry->ts0;
-  // the retried cells keep the mixed temperature solve (8 FP32 + 2 FP64 iterations, the FP64
-  // form's temperature to ~1e-16) with the FP64 factor: a handful of hard cells, one lane each,
-  // whose pass is latency-bound by its F evaluations -- the ten FP64 temperature iterations
+  // the retried cells keep the mixed temperature solve (up to 9 FP32 + 1 FP64 iterations)
+  // with the FP64 factor: a few hundred hard cells, one lane each, whose pass is
+  // latency-bound by its F evaluations -- the ten FP64 temperature iterations of the FP64 form
   // were 70 % of them (retry pass 210 -> 95 ms, 64^3 call 1.31 -> 1.19 s)
   Of.mixed_temp = 1;
   return launch_dirk<double, false, 64>(P, S, n, y, Of, d_next, stats, d_nfail, nsm, s);

@@ -46,7 +46,7 @@ class _DirkOpts(C.Structure):
                                           "growth", "etamx1", "hmax")] + \
                [(k, C.c_int) for k in ("maxcor", "max_steps", "msbp", "maxnef", "maxncf",
                                        "precision", "refine", "block", "table",
-                                       "setup_batch", "order")]
+                                       "setup_batch", "order", "deduce")]
 
 
 MAX_STAGES = 7

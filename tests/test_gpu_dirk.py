@@ -44,25 +44,32 @@ def _relerr(a, b, floor):
     return np.abs(a - b) / (np.abs(b) + floor)
 
 
-@pytest.mark.parametrize("table", [112, 102])
-def test_dirk_fp64_matches_oracle(cuda, tables, table):
-    """Both ESDIRK tables (112 = ARK4(3)7L[2]SA, the inputs' itable; 102 = TR-BDF2)."""
+@pytest.mark.parametrize("table,deduce", [(112, 0), (102, 0), (112, 1)])
+def test_dirk_fp64_matches_oracle(cuda, tables, table, deduce):
+    """Both ESDIRK tables (112 = ARK4(3)7L[2]SA, the inputs' itable; 102 = TR-BDF2), and the
+    intermediate stage derivatives evaluated (ARKODE's default) or deduced."""
     n, tout = 256, 1e-3
     scale = _cells(n, W.SEED_BASE + 500)
     zg, sg, nfg, _ = _gpu_run(cuda, tables, scale, tout, precision=0, block=64, table=table,
-                              **OPTS)
+                              deduce=deduce, **OPTS)
     oc = O.Chem(tables, scale)
-    zo, so, nfo = oc.dirk_evolve(np.ones(10 * n), 0.0, tout, TU, table=table, **OPTS)
+    zo, so, nfo = oc.dirk_evolve(np.ones(10 * n), 0.0, tout, TU, table=table, deduce=deduce,
+                                 **OPTS)
     zo = zo.reshape(n, 10)
     assert nfg == nfo == 0
     same = np.all(sg[:, :7] == so[:, :7], axis=1)
-    assert same.mean() >= 0.7, same.mean()  # identical step/iteration/setup counts
     err = _relerr(zg, zo, OPTS["atol"] / OPTS["rtol"]).max(axis=1)
+    got = (same.mean(), np.median(err[same]), np.max(err[same]), np.max(err))
+    assert same.mean() >= 0.7, got  # identical step/iteration/setup counts
     # identical decisions: rounding-level agreement (a few stiff cells amplify libm-versus-CUDA
-    # rounding of the rates over hundreds of steps to ~1e-8)
-    assert np.median(err[same]) <= 1e-11, np.median(err[same])
-    assert np.max(err[same]) <= 1e-6, np.max(err[same])
-    assert np.max(err) <= 1e-3, np.max(err)  # decision flips: within the integration error
+    # rounding of the rates over hundreds of steps to ~1e-8).  Equal totals do not mean equal
+    # per-stage iteration counts, and a deduced stage derivative carries its stage's Newton
+    # error (up to nlscoef x the tolerance) into the next stage's base, so with deduce = 1 a
+    # cell whose iterations split differently between its stages parts at that level (median
+    # 1.1e-11, largest 4.3e-6 measured)
+    assert np.median(err[same]) <= (3e-11 if deduce else 1e-11), got
+    assert np.max(err[same]) <= (1e-5 if deduce else 1e-6), got
+    assert np.max(err) <= 1e-3, got  # decision flips: within the integration error
 
 
 def test_dirk_mixed_accuracy_matches_fp64(cuda, tables):
@@ -93,6 +100,15 @@ def test_dirk_mixed_accuracy_matches_fp64(cuda, tables):
     erf = _relerr(zrf, zt, floor)
     assert np.median(erf) <= 2.0 * np.median(e64) + 1e-9
     assert srf[:, 1].mean() <= 1.1 * s64[:, 1].mean()
+    # intermediate stage derivatives deduced from the stage equations: same accuracy, fewer F
+    zdd, sdd, nfdd, _ = _gpu_run(cuda, tables, scale, tout, precision=1, deduce=1, block=64,
+                                 **OPTS)
+    assert nfdd == 0
+    edd = _relerr(zdd, zt, floor)
+    assert np.median(edd) <= 2.0 * np.median(e64) + 1e-9, (np.median(edd), np.median(e64))
+    assert np.max(edd) <= 2.0 * np.max(e64) + 1e-6, (np.max(edd), np.max(e64))
+    assert sdd[:, 6].sum() < 0.9 * smx[:, 6].sum()
+    assert sdd[:, 1].mean() <= 1.1 * s64[:, 1].mean()
 
 
 def test_dirk_block_sizes_bitwise_equal_and_autotune(cuda, tables):
@@ -195,17 +211,19 @@ def test_dirk_options_rejected(cuda, tables):
     z = torch.ones(160, dtype=torch.float64, device="cuda")
     for bad in (dict(rtol=0.0), dict(block=48), dict(refine=9), dict(precision=3),
                 dict(maxcor=0), dict(table=13), dict(table=104 + 1000), dict(table=8),
-                dict(setup_batch=0), dict(setup_batch=33), dict(order=2)):
+                dict(setup_batch=0), dict(setup_batch=33), dict(order=2), dict(deduce=2)):
         with pytest.raises(gbmv.GbmvError):
             c.dirk_evolve(0.0, 1e-3, z, TU, **bad)
     with pytest.raises(gbmv.GbmvError):
         c.dirk_evolve(1.0, 0.5, z, TU)   # tout must exceed t0
 
 
-def test_mri_fast_evolve_with_forcing(cuda, tables):
+@pytest.mark.parametrize("deduce", [0, 1])
+def test_mri_fast_evolve_with_forcing(cuda, tables, deduce):
     """RankLocalStepper_Evolve counterpart: chemistry by the DIRK with the forcing's chemistry
     component in its right-hand side (against the oracle's forced integration), fluid
-    components by the forcing polynomial's exact integral."""
+    components by the forcing polynomial's exact integral; intermediate stage derivatives
+    evaluated or deduced (a deduced one includes the forcing through the stage equation)."""
     torch = cuda
     import gbmv
     wl = W.chem_hydro(shape=(8, 6, 5))
@@ -221,7 +239,7 @@ def test_mri_fast_evolve_with_forcing(cuda, tables):
     t0, tout, tshift, tscale = 0.2, 0.2 + 1e-4, 0.15, 1e-3
     st = torch.zeros(8 * n, dtype=torch.int32, device="cuda")
     nf = gbmv.mri_fast_evolve(h, c, t0, tout, w, TU, forcing, tshift, tscale, stats=st,
-                              precision=0, block=64, **OPTS)
+                              precision=0, block=64, deduce=deduce, **OPTS)
     torch.cuda.synchronize()
     assert nf == 0
     tau0, tau1 = (t0 - tshift) / tscale, (tout - tshift) / tscale
@@ -232,7 +250,7 @@ def test_mri_fast_evolve_with_forcing(cuda, tables):
     oc = O.Chem(tables, wl["scale"].reshape(-1))
     zo, so, nfo = oc.dirk_evolve(wl["fields"][5].reshape(-1), t0, tout, TU,
                                  forcing=[fv[5] for fv in fh], tshift=tshift, tscale=tscale,
-                                 **OPTS)
+                                 deduce=deduce, **OPTS)
     assert nfo == 0
     zg = w[5].cpu().numpy().reshape(n, 10)
     zo = zo.reshape(n, 10)
@@ -240,7 +258,7 @@ def test_mri_fast_evolve_with_forcing(cuda, tables):
     same = np.all(sg[:, :7] == so[:, :7], axis=1)
     assert same.mean() >= 0.75
     err = _relerr(zg, zo, OPTS["atol"] / OPTS["rtol"]).max(axis=1)
-    assert np.median(err[same]) <= 1e-11 and np.max(err) <= 1e-3
+    assert np.median(err[same]) <= (3e-11 if deduce else 1e-11) and np.max(err) <= 1e-3
     # the forcing changed the chemistry: an unforced run lands elsewhere
     oc2 = O.Chem(tables, wl["scale"].reshape(-1))
     zu, _, _ = oc2.dirk_evolve(wl["fields"][5].reshape(-1), t0, tout, TU, **OPTS)
